@@ -1,0 +1,362 @@
+"""Benchmark: batched Newton-Raphson power flow on one GB300.
+
+Workload (one "step" = one batched solve): the 2,000-bus synthetic meshed
+grid (1 slack, 300 PV, 1,699 PQ, 2,799 branches), 4,096 scenarios with
+every bus load x lognormal(0, 0.15) and PV generation rebalanced, flat
+start, tol 1e-8 pu, <= 20 iterations.  Headline = the mixed-precision path
+(FP32 refactor/solve, FP64 mismatch/update); the plain FP64 GPU path is
+timed in the same run.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference]
+
+Prints one JSON line (rank 0).  `value` = solves/s with inputs resident in
+HBM; `e2e` = the same through the host-buffer C-ABI call (host<->device
+copies inside the timed region).  The working set (>1 GB of factors) is far
+larger than L2, and L2 is also flushed (256 MB write) between steps.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import subprocess
+import sys
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+WORKLOAD = dict(grid="case2000", scenarios=4096, sigma=0.15, seed=2024, tol=1e-8, max_iter=20)
+METRIC = "PF solves/s on 1 GB300 at <=1e-8 pu mismatch, mixed vs FP64; p50/p99 latency"
+
+
+def _env_int(name, default):
+    try:
+        return int(os.environ.get(name, default))
+    except ValueError:
+        return default
+
+
+def _peaks():
+    path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(path):
+        with open(path) as fh:
+            d = json.load(fh)
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+class ClockSampler:
+    """nvidia-smi clocks / throttle reasons sampled during the timed region."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index: int):
+        self.index = index
+        self.proc = None
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.index), f"--query-gpu={self.Q}",
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except Exception:
+            self.proc = None
+
+    def stop(self):
+        if self.proc is None:
+            return None
+        time.sleep(0.25)
+        self.proc.terminate()
+        try:
+            out, _ = self.proc.communicate(timeout=5)
+        except Exception:
+            self.proc.kill()
+            out = ""
+        sm, mx, reasons = [], 0.0, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in out.strip().splitlines():
+            f = [x.strip() for x in line.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                mx = max(mx, float(f[2]))
+            except ValueError:
+                continue
+            for nm, v in zip(names, f[5:9]):
+                if v.lower() == "active":
+                    reasons.add(nm)
+        if not sm:
+            return None
+        return {"sm_mhz": float(np.median(sm)), "sm_max_mhz": mx, "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def make_inputs():
+    from gridoxide_gb300 import grids as G
+    g = G.config_grid(WORKLOAD["grid"])
+    yb = G.build_ybus(g)
+    p, q = G.load_scenarios(g, WORKLOAD["scenarios"], WORKLOAD["sigma"], WORKLOAD["seed"])
+    return g, yb, p, q
+
+
+def algorithmic_bytes(info: dict, n_bus: int, w: int) -> dict:
+    """Compulsory HBM bytes per scenario-iteration for each kernel."""
+    N, nU, nJ = n_bus, info["n_u"], info["nnz_j"]
+    nLU = info["nnz_l"] + info["nnz_u"] + info["n_u"]
+    return {
+        "mismatch": 16 * N + 16 * N + 8 * nU,
+        "fill": 16 * N + 16 * N + w * nJ,
+        "refactor": w * nJ + w * nLU,
+        "solve": w * nLU + 8 * nU + w * nU,
+    }
+
+
+def read_traffic(kernel: str):
+    """DRAM bytes per scenario of one launch of `kernel`, from the committed
+    ncu summary (profiles/), or None."""
+    path = os.path.join(ROOT, "profiles", "dram_traffic_per_scenario.txt")
+    if not os.path.exists(path):
+        return None
+    with open(path) as fh:
+        for line in fh:
+            f = line.split()
+            if len(f) >= 2 and f[0] == kernel:
+                try:
+                    return float(f[1])
+                except ValueError:
+                    return None
+    return None
+
+
+def cpu_baseline(g, yb, p, q, sample: int, threads: int):
+    """The oracle port (C restatement of BatchSolver + KLU) on host cores."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle as O
+    from gridoxide_gb300 import solver as S
+    O.build(ref=False) if not os.path.exists(O.LIB) else None
+    jac = O.Jacobian(yb, g.bus_type)
+    Ap, Ai, _ = jac.csc_pattern()
+    topo = O.Topology(yb, g.bus_type, *S.analyze(jac.n_u, Ap, Ai))
+    topo.batch_solve(p[:threads], q[:threads], g.vm, g.va, threads=threads)  # warm-up
+    t0 = time.perf_counter()
+    res = topo.batch_solve(p[:sample], q[:sample], g.vm, g.va, tol=WORKLOAD["tol"],
+                           max_iter=WORKLOAD["max_iter"], threads=threads)
+    dt = time.perf_counter() - t0
+    return sample / dt, dt, res
+
+
+def run_reference_arm(args):
+    rank = _env_int("RANK", 0)
+    if rank != 0:
+        return
+    g, yb, p, q = make_inputs()
+    threads = os.cpu_count() or 1
+    sample = 512
+    vals = []
+    for _ in range(args.warmup):
+        cpu_baseline(g, yb, p, q, min(sample, 64), threads)
+    for _ in range(args.steps):
+        v, dt, _ = cpu_baseline(g, yb, p, q, sample, threads)
+        vals.append(v)
+    value = float(np.median(vals))
+    line = {
+        "impl": "reference", "metric": METRIC, "value": value, "unit": "solves/s",
+        "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": 1000.0 * sample / value, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": {"workload": f"{WORKLOAD['grid']} x {WORKLOAD['scenarios']} scenarios "
+                               f"(sample of {sample} per step)", **WORKLOAD},
+        "cpu_baseline": {"value": value, "unit": "solves/s", "cores": threads, "kind": "port",
+                         "sample": f"{sample} scenarios of the workload per step"},
+        "e2e": {"value": value, "unit": "solves/s", "h2d_bytes_per_step": 0,
+                "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    args.warmup = max(args.warmup, 3)
+    if args.impl == "reference":
+        run_reference_arm(args)
+        return
+
+    import torch
+    import gridoxide_gb300 as gox
+
+    world = _env_int("WORLD_SIZE", 1)
+    rank = _env_int("RANK", 0)
+    local = _env_int("LOCAL_RANK", 0)
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    gox.build.build()
+
+    g, yb, p, q = make_inputs()
+    B, N = p.shape
+    topo = gox.Topology(yb, g.bus_type)
+    topo.set_timing(True)
+    stream = torch.cuda.Stream(device=dev)
+    tp = torch.from_numpy(p).to(dev)
+    tq = torch.from_numpy(q).to(dev)
+    tvm0 = torch.from_numpy(g.vm).to(dev)
+    tva0 = torch.from_numpy(g.va).to(dev)
+    ovm = torch.empty((B, N), dtype=torch.float64, device=dev)
+    ova = torch.empty_like(ovm)
+    oit = torch.empty(B, dtype=torch.int32, device=dev)
+    ost = torch.empty(B, dtype=torch.int32, device=dev)
+    omm = torch.empty(B, dtype=torch.float64, device=dev)
+    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=dev)
+    torch.cuda.synchronize()
+
+    def step(precision):
+        topo.solve_device(tp, tq, tvm0, tva0, ovm, ova, oit, ost, omm, tol=WORKLOAD["tol"],
+                          max_iter=WORKLOAD["max_iter"], precision=precision, stream=stream)
+
+    def timed(precision, steps, clocks=None):
+        ms, kern, launches = [], {"mismatch": 0.0, "fill": 0.0, "refactor": 0.0, "solve": 0.0}, 0
+        iters_run = []
+        if world > 1:
+            torch.distributed.barrier()
+        torch.cuda.synchronize()
+        if clocks:
+            clocks.start()
+        for _ in range(steps):
+            flush.zero_()
+            torch.cuda.synchronize()
+            e0 = torch.cuda.Event(enable_timing=True)
+            e1 = torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            step(precision)
+            e1.record(stream)
+            e1.synchronize()
+            ms.append(e0.elapsed_time(e1))
+            t = topo.last_timing()
+            kern["mismatch"] += t["mismatch_ms"]
+            kern["fill"] += t["fill_ms"]
+            kern["refactor"] += t["refactor_ms"]
+            kern["solve"] += t["solve_ms"]
+            iters_run.append(int(t["iterations"]))
+            launches += topo.last_launches()
+        torch.cuda.synchronize()
+        cl = clocks.stop() if clocks else None
+        if world > 1:
+            torch.distributed.barrier()
+        return np.array(ms), kern, launches, iters_run, cl
+
+    for _ in range(args.warmup):
+        step(gox.GOX_PRECISION_MIXED)
+        step(gox.GOX_PRECISION_FP64)
+    torch.cuda.synchronize()
+    # correctness of the timed configuration
+    its = oit.cpu().numpy()
+    sts = ost.cpu().numpy()
+    mm = omm.cpu().numpy()
+
+    clocks = ClockSampler(local)
+    ms_mx, kern_mx, launches_mx, iters_mx, cl = timed(gox.GOX_PRECISION_MIXED, args.steps, clocks)
+    st_mx = ost.cpu().numpy().copy()
+    mm_mx = omm.cpu().numpy().copy()
+    it_mx = oit.cpu().numpy().copy()
+    ms_64, kern_64, launches_64, iters_64, _ = timed(gox.GOX_PRECISION_FP64,
+                                                     max(3, args.steps // 2))
+    it_64 = oit.cpu().numpy().copy()
+
+    total_ms = float(ms_mx.sum())
+    if world > 1:
+        t = torch.tensor([total_ms], device=dev)
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        total_ms = float(t.item())
+    value = world * B * args.steps / (total_ms / 1000.0)
+    fp64_value = B * len(ms_64) / (ms_64.sum() / 1000.0)
+
+    # e2e through the host-buffer C-ABI call (pinned host memory)
+    hp = torch.from_numpy(p).pin_memory().numpy()
+    hq = torch.from_numpy(q).pin_memory().numpy()
+    e2e_ms = []
+    for k in range(max(3, args.steps // 2)):
+        t0 = time.perf_counter()
+        topo.solve(hp, hq, g.vm, g.va, tol=WORKLOAD["tol"], max_iter=WORKLOAD["max_iter"],
+                   precision=gox.GOX_PRECISION_MIXED)
+        e2e_ms.append(1000.0 * (time.perf_counter() - t0))
+    e2e_value = B / (np.median(e2e_ms) / 1000.0)
+    h2d = 2 * B * N * 8 + 2 * N * 8
+    d2h = 2 * B * N * 8 + B * (4 + 4 + 8)
+
+    # roofline of the dominant kernel (mixed path)
+    info = topo.info()
+    abytes = algorithmic_bytes(info, N, 4)
+    dom = max(kern_mx, key=lambda k: kern_mx[k])
+    n_launch = sum(iters_mx) if dom != "mismatch" else sum(iters_mx) + args.steps
+    per_launch_bytes = abytes[dom] * B
+    avg_launch_ms = kern_mx[dom] / max(n_launch, 1)
+    achieved = per_launch_bytes / (avg_launch_ms / 1000.0) / 1e9
+    peak, peak_kind = _peaks()
+    traffic = read_traffic(dom)
+    roof = {"bound": "hbm", "kernel": dom, "achieved": round(achieved, 1), "peak": peak,
+            "unit": "GB/s", "frac": round(achieved / peak, 4), "peak_source": peak_kind,
+            "traffic": None if traffic is None else traffic * B,
+            "algorithmic_bytes_per_launch": per_launch_bytes,
+            "avg_launch_ms": round(avg_launch_ms, 4)}
+    kernels = {}
+    for k in kern_mx:
+        nl = sum(iters_mx) + (args.steps if k == "mismatch" else 0)
+        t_ms = kern_mx[k] / max(nl, 1)
+        kernels[k] = {"ms_per_launch": round(t_ms, 4),
+                      "GB/s": round(abytes[k] * B / (t_ms / 1000.0) / 1e9, 1) if t_ms > 0 else None,
+                      "share": round(kern_mx[k] / max(sum(kern_mx.values()), 1e-9), 3)}
+
+    line = {
+        "metric": METRIC, "value": round(value, 1), "unit": "solves/s", "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": round(float(np.mean(ms_mx)), 4), "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32 LU/solve + f64 mismatch",
+        "data": "synthetic",
+        "config": {"workload": "case2000 x 4096 scenarios, lognormal(0,0.15) loads, flat start, "
+                               "mixed precision", "l2": "inputs > L2 and 256 MB flush per step",
+                   "parallelism": f"replicas x{world}", **WORKLOAD},
+        "latency_ms": {"p50": round(float(np.percentile(ms_mx, 50)), 4),
+                       "p99": round(float(np.percentile(ms_mx, 99)), 4)},
+        "fp64": {"value": round(fp64_value, 1), "unit": "solves/s",
+                 "ms_per_step": round(float(np.mean(ms_64)), 4),
+                 "iterations_hist": np.bincount(it_64).tolist()},
+        "mixed_over_fp64": round(value / world / fp64_value, 3),
+        "iterations_hist": np.bincount(it_mx).tolist(),
+        "converged": int(np.sum(st_mx == 0)), "max_mismatch": float(mm_mx.max()),
+        "e2e": {"value": round(e2e_value, 1), "unit": "solves/s", "h2d_bytes_per_step": h2d,
+                "d2h_bytes_per_step": d2h},
+        "gpu_launches": int(launches_mx),
+        "roofline": roof,
+        "kernels": kernels,
+        "clocks": cl,
+    }
+    if rank == 0 and not args.no_cpu_baseline:
+        threads = os.cpu_count() or 1
+        sample = 512
+        v, dt, _ = cpu_baseline(g, yb, p, q, sample, threads)
+        line["cpu_baseline"] = {"value": round(v, 1), "unit": "solves/s", "cores": threads,
+                                "kind": "port",
+                                "sample": f"{sample} scenarios of the workload ({dt:.1f} s)"}
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    if world > 1:
+        torch.distributed.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

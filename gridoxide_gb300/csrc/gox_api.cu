@@ -1,0 +1,996 @@
+// extern "C" layer and device engine of the GB300 batched power-flow
+// library.  See include/gridoxide_gb300.h for the contract of each entry
+// point and the reference interface it replaces.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <functional>
+#include <cstdio>
+#include <cstring>
+#include <memory>
+#include <new>
+#include <stdexcept>
+#include <string>
+#include <vector>
+
+#include "../../include/gridoxide_gb300.h"
+#include "gox_engine.hpp"
+#include "gox_kernels.cuh"
+
+namespace gox {
+
+struct CudaError : std::runtime_error {
+  using std::runtime_error::runtime_error;
+};
+
+#define GOX_CK(x)                                                                          \
+  do {                                                                                     \
+    cudaError_t e_ = (x);                                                                  \
+    if (e_ != cudaSuccess)                                                                 \
+      throw CudaError(std::string(#x) + ": " + cudaGetErrorString(e_));                    \
+  } while (0)
+
+// Owning device allocation.
+struct DevMem {
+  void* p = nullptr;
+  size_t bytes = 0;
+  DevMem() = default;
+  DevMem(const DevMem&) = delete;
+  DevMem& operator=(const DevMem&) = delete;
+  ~DevMem() { release(); }
+  void release() {
+    if (p) cudaFree(p);
+    p = nullptr;
+    bytes = 0;
+  }
+  void ensure(size_t b) {
+    if (b <= bytes && p) return;
+    release();
+    if (b == 0) b = 16;
+    cudaError_t e = cudaMalloc(&p, b);
+    if (e == cudaErrorMemoryAllocation) {
+      cudaGetLastError();
+      throw std::bad_alloc();
+    }
+    GOX_CK(e);
+    bytes = b;
+  }
+  template <typename T>
+  T* as() const { return reinterpret_cast<T*>(p); }
+};
+
+template <typename T>
+static void upload(DevMem& m, const std::vector<T>& v) {
+  m.ensure(sizeof(T) * std::max<size_t>(v.size(), 1));
+  if (!v.empty()) GOX_CK(cudaMemcpy(m.p, v.data(), sizeof(T) * v.size(), cudaMemcpyHostToDevice));
+}
+
+// ---------------------------------------------------------------------------
+// Layout kernels: row-major [B][N] <-> scenario-interleaved [G][N][32].
+
+__global__ void k_scatter_rows(const double* __restrict__ src, int B, int N, int stride,
+                               double* __restrict__ dst, int G) {
+  // dst[(g*N + i)*32 + l] = src[s*stride + i], s = min(32g + l, B-1)
+  size_t total = (size_t)G * N * 32;
+  for (size_t t = blockIdx.x * (size_t)blockDim.x + threadIdx.x; t < total;
+       t += (size_t)gridDim.x * blockDim.x) {
+    int l = (int)(t & 31);
+    size_t gi = t >> 5;
+    int i = (int)(gi % N);
+    int g = (int)(gi / N);
+    int s = min(g * 32 + l, B - 1);
+    dst[t] = src[(size_t)s * stride + i];
+  }
+}
+
+__global__ void k_gather_rows(const double* __restrict__ src, int B, int N, int G,
+                              double* __restrict__ dst) {
+  size_t total = (size_t)B * N;
+  for (size_t t = blockIdx.x * (size_t)blockDim.x + threadIdx.x; t < total;
+       t += (size_t)gridDim.x * blockDim.x) {
+    int s = (int)(t / N);
+    int i = (int)(t % N);
+    int g = s >> 5, l = s & 31;
+    dst[t] = src[((size_t)g * N + i) * 32 + l];
+  }
+}
+
+__global__ void k_init_scen(int B, int G, int32_t* status, int32_t* iters, int32_t* sing,
+                            int32_t* piv, double* maxmis) {
+  int s = blockIdx.x * blockDim.x + threadIdx.x;
+  if (s >= G * 32) return;
+  status[s] = (s < B) ? ST_RUNNING : ST_UNUSED;
+  iters[s] = 0;
+  sing[s] = 0;
+  piv[s] = 0;
+  maxmis[s] = 0.0;
+}
+
+// Outage slots -> branch buses; validates the slots.  err[0] set on a bad slot.
+__global__ void k_outage_prep(int B, int G, const int32_t* slot_in, const double* dre_in,
+                              const double* dim_in, const int32_t* yp, const int32_t* yi, int n,
+                              int nnz, int32_t* o_slot, double* o_dre, double* o_dim,
+                              int32_t* o_bf, int32_t* o_bt, int32_t* err) {
+  int s = blockIdx.x * blockDim.x + threadIdx.x;
+  if (s >= G * 32) return;
+  int src = min(s, B - 1);
+  bool use = (s < B) && slot_in[4 * src] >= 0;
+  int sl[4];
+  for (int c = 0; c < 4; c++) sl[c] = use ? slot_in[4 * src + c] : -1;
+  int bf = -1, bt = -1;
+  if (use) {
+    for (int c = 0; c < 4; c++)
+      if (sl[c] < 0 || sl[c] >= nnz) { atomicExch(err, 1); use = false; }
+  }
+  if (use) {
+    // row of a slot: binary search in the row pointers
+    auto row_of = [&](int sp) {
+      int lo = 0, hi = n - 1;
+      while (lo < hi) {
+        int mid = (lo + hi + 1) >> 1;
+        if (yp[mid] <= sp) lo = mid; else hi = mid - 1;
+      }
+      return lo;
+    };
+    bf = row_of(sl[0]);
+    bt = row_of(sl[3]);
+    // (ff, ft, tf, tt) must be (f,f), (f,t), (t,f), (t,t)
+    if (yi[sl[0]] != bf || yi[sl[3]] != bt || row_of(sl[1]) != bf || yi[sl[1]] != bt ||
+        row_of(sl[2]) != bt || yi[sl[2]] != bf) {
+      atomicExch(err, 1);
+      use = false;
+      bf = bt = -1;
+    }
+  }
+  o_bf[s] = use ? bf : -1;
+  o_bt[s] = use ? bt : -1;
+  for (int c = 0; c < 4; c++) {
+    o_slot[4 * s + c] = use ? sl[c] : -1;
+    o_dre[4 * s + c] = use ? dre_in[4 * src + c] : 0.0;
+    o_dim[4 * s + c] = use ? dim_in[4 * src + c] : 0.0;
+  }
+}
+
+__global__ void k_unpack_scen(int B, const int32_t* st_in, const int32_t* it_in,
+                              const double* mm_in, const double* hist_in, int max_iter,
+                              int32_t* st, int32_t* it, double* mm, double* hist) {
+  int s = blockIdx.x * blockDim.x + threadIdx.x;
+  if (s >= B) return;
+  st[s] = st_in[s];
+  it[s] = it_in[s];
+  mm[s] = mm_in[s];
+  if (hist)
+    for (int k = 0; k < max_iter; k++) hist[(size_t)s * max_iter + k] = hist_in[(size_t)s * max_iter + k];
+}
+
+// ---------------------------------------------------------------------------
+
+struct DevSchedule {
+  DevMem yp, yi, yre, yim, bus_rowP, bus_rowQ, bus_colA, bus_colV, a_kind, a_bi, a_bk, a_yslot,
+      a_dst, lev_ptr, lev_cols, c_base, c_ulen, c_llen, c_abeg, op_ptr, op_slot, op_pos, ph_ptr,
+      ph_rows, ph_kind, fw_ptr, fw_slot, fw_col, bw_ptr, bw_slot, bw_col, diag_slot;
+  SchedDev d{};
+
+  void load(const Schedule& sc, const std::vector<int32_t>& yp_h, const std::vector<int32_t>& yi_h,
+            const std::vector<double>& yre_h, const std::vector<double>& yim_h) {
+    upload(yp, yp_h); upload(yi, yi_h); upload(yre, yre_h); upload(yim, yim_h);
+    upload(bus_rowP, sc.bus_rowP); upload(bus_rowQ, sc.bus_rowQ);
+    upload(bus_colA, sc.bus_colA); upload(bus_colV, sc.bus_colV);
+    upload(a_kind, sc.a_kind); upload(a_bi, sc.a_bi); upload(a_bk, sc.a_bk);
+    upload(a_yslot, sc.a_yslot); upload(a_dst, sc.a_dst);
+    upload(lev_ptr, sc.lev_ptr); upload(lev_cols, sc.lev_cols); upload(c_base, sc.c_base);
+    upload(c_ulen, sc.c_ulen); upload(c_llen, sc.c_llen); upload(c_abeg, sc.c_abeg);
+    upload(op_ptr, sc.op_ptr); upload(op_slot, sc.op_slot); upload(op_pos, sc.op_pos);
+    upload(ph_ptr, sc.ph_ptr); upload(ph_rows, sc.ph_rows); upload(ph_kind, sc.ph_kind);
+    upload(fw_ptr, sc.fw_ptr); upload(fw_slot, sc.fw_slot); upload(fw_col, sc.fw_col);
+    upload(bw_ptr, sc.bw_ptr); upload(bw_slot, sc.bw_slot); upload(bw_col, sc.bw_col);
+    upload(diag_slot, sc.diag_slot);
+    d.n_bus = sc.n_bus; d.n_u = sc.n_u; d.n_a = sc.n_a; d.n_slots = sc.n_slots;
+    d.n_off = std::max(sc.n_off, 1); d.n_levels = sc.n_levels; d.n_phases = sc.n_phases;
+    d.nnz_y = (int)yi_h.size();
+    d.yp = yp.as<int32_t>(); d.yi = yi.as<int32_t>(); d.yre = yre.as<double>(); d.yim = yim.as<double>();
+    d.bus_rowP = bus_rowP.as<int32_t>(); d.bus_rowQ = bus_rowQ.as<int32_t>();
+    d.bus_colA = bus_colA.as<int32_t>(); d.bus_colV = bus_colV.as<int32_t>();
+    d.a_kind = a_kind.as<int32_t>(); d.a_bi = a_bi.as<int32_t>(); d.a_bk = a_bk.as<int32_t>();
+    d.a_yslot = a_yslot.as<int32_t>(); d.a_dst = a_dst.as<int32_t>();
+    d.lev_ptr = lev_ptr.as<int32_t>(); d.lev_cols = lev_cols.as<int32_t>();
+    d.c_base = c_base.as<int32_t>(); d.c_ulen = c_ulen.as<int32_t>(); d.c_llen = c_llen.as<int32_t>();
+    d.c_abeg = c_abeg.as<int32_t>(); d.op_ptr = op_ptr.as<int32_t>();
+    d.op_slot = op_slot.as<int32_t>(); d.op_pos = op_pos.as<uint32_t>();
+    d.ph_ptr = ph_ptr.as<int32_t>(); d.ph_rows = ph_rows.as<int32_t>(); d.ph_kind = ph_kind.as<int32_t>();
+    d.fw_ptr = fw_ptr.as<int32_t>(); d.fw_slot = fw_slot.as<int32_t>(); d.fw_col = fw_col.as<int32_t>();
+    d.bw_ptr = bw_ptr.as<int32_t>(); d.bw_slot = bw_slot.as<int32_t>(); d.bw_col = bw_col.as<int32_t>();
+    d.diag_slot = diag_slot.as<int32_t>();
+  }
+};
+
+// Device buffers of one batch (capacity in groups of 32 scenarios).
+struct DevBatch {
+  int G = 0, prec = -1, max_iter = 0;
+  DevMem vm, va, e, f, psp, qsp, eT, fT, ivT, pT, qT, jbuf, lu, off, rhs, sol;
+  DevMem status, iters, sing, piv, maxmis, hist, gact, nactive, err;
+  DevMem o_slot, o_bf, o_bt, o_dre, o_dim;
+  DevMem in_stage, out_stage;  // host I/O staging (row-major)
+
+  void ensure(const SchedDev& S, int G_, int prec_, int max_iter_, bool want_hist) {
+    const size_t nb = (size_t)G_ * S.n_bus * 32, w = prec_ == GOX_PRECISION_FP64 ? 8 : 4;
+    vm.ensure(nb * 8); va.ensure(nb * 8); e.ensure(nb * 8); f.ensure(nb * 8);
+    psp.ensure(nb * 8); qsp.ensure(nb * 8);
+    eT.ensure(nb * w); fT.ensure(nb * w); ivT.ensure(nb * w); pT.ensure(nb * w); qT.ensure(nb * w);
+    jbuf.ensure((size_t)G_ * S.n_a * 32 * w);
+    lu.ensure((size_t)G_ * S.n_slots * 32 * w);
+    off.ensure((size_t)G_ * S.n_off * 32 * w);
+    rhs.ensure((size_t)G_ * S.n_u * 32 * w);
+    sol.ensure((size_t)G_ * S.n_u * 32 * w);
+    const size_t ns = (size_t)G_ * 32;
+    status.ensure(ns * 4); iters.ensure(ns * 4); sing.ensure(ns * 4); piv.ensure(ns * 4);
+    maxmis.ensure(ns * 8);
+    if (want_hist) hist.ensure(ns * std::max(max_iter_, 1) * 8);
+    gact.ensure((size_t)G_ * 4); nactive.ensure(16); err.ensure(16);
+    o_slot.ensure(ns * 16); o_bf.ensure(ns * 4); o_bt.ensure(ns * 4);
+    o_dre.ensure(ns * 32); o_dim.ensure(ns * 32);
+    G = G_; prec = prec_; max_iter = max_iter_;
+  }
+
+  BatchDev view(bool want_hist, bool outage, double tol) {
+    BatchDev D{};
+    D.G = G; D.max_iter = max_iter; D.tol = tol;
+    D.vm = vm.as<double>(); D.va = va.as<double>(); D.e = e.as<double>(); D.f = f.as<double>();
+    D.psp = psp.as<double>(); D.qsp = qsp.as<double>();
+    D.eT = eT.p; D.fT = fT.p; D.ivT = ivT.p; D.pT = pT.p; D.qT = qT.p;
+    D.jbuf = jbuf.p; D.lu = lu.p; D.off = off.p; D.rhs = rhs.p; D.sol = sol.p;
+    D.status = status.as<int32_t>(); D.iters = iters.as<int32_t>(); D.sing = sing.as<int32_t>();
+    D.piv_flag = piv.as<int32_t>(); D.maxmis = maxmis.as<double>();
+    D.hist = want_hist ? hist.as<double>() : nullptr;
+    D.gact = gact.as<int32_t>(); D.nactive = nactive.as<int32_t>();
+    D.o_slot = outage ? o_slot.as<int32_t>() : nullptr;
+    D.o_bf = outage ? o_bf.as<int32_t>() : nullptr;
+    D.o_bt = outage ? o_bt.as<int32_t>() : nullptr;
+    D.o_dre = outage ? o_dre.as<double>() : nullptr;
+    D.o_dim = outage ? o_dim.as<double>() : nullptr;
+    D.piv_tol = prec == GOX_PRECISION_MIXED ? 1e-6f : 0.0f;
+    return D;
+  }
+};
+
+static int grid1d(size_t n, int threads = 256) {
+  size_t b = (n + threads - 1) / threads;
+  return (int)std::min<size_t>(std::max<size_t>(b, 1), 152 * 32);
+}
+
+static constexpr int kWarps = 8;  // warps per CTA of the group kernels
+
+struct Timing {
+  bool on = false;
+  double iters = 0, total = 0, k1 = 0, k2 = 0, k3 = 0, k4 = 0;
+};
+
+// Launches one NR iteration's kernels for precision T.
+template <typename T>
+struct Iter {
+  static void mismatch(const SchedDev& S, const BatchDev& D, int it, int mode, bool outage,
+                       cudaStream_t st) {
+    dim3 grid(D.G), block(32 * kWarps);
+    if (outage) k_mismatch<T, true><<<grid, block, 0, st>>>(S, D, it, mode);
+    else k_mismatch<T, false><<<grid, block, 0, st>>>(S, D, it, mode);
+  }
+  static void fill(const SchedDev& S, const BatchDev& D, bool outage, cudaStream_t st) {
+    const int per_warp = 32;
+    int warps = (S.n_a + per_warp - 1) / per_warp;
+    dim3 grid((warps + kWarps - 1) / kWarps, D.G), block(32 * kWarps);
+    if (outage) k_fill<T, true><<<grid, block, 0, st>>>(S, D, per_warp);
+    else k_fill<T, false><<<grid, block, 0, st>>>(S, D, per_warp);
+  }
+  static int stage_cap(const SchedDev& S, int max_collen) {
+    size_t budget = 200 * 1024;  // dynamic shared memory per CTA
+    int cap = (int)(budget / ((size_t)kWarps * 32 * sizeof(T)));
+    return std::max(1, std::min(cap, max_collen));
+  }
+  static void refactor(const SchedDev& S, const BatchDev& D, int cap, cudaStream_t st) {
+    size_t smem = (size_t)kWarps * cap * 32 * sizeof(T);
+    GOX_CK(cudaFuncSetAttribute(k_refactor<T>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                (int)std::max<size_t>(smem, 1)));
+    k_refactor<T><<<D.G, 32 * kWarps, smem, st>>>(S, D, cap);
+  }
+  static void solve(const SchedDev& S, const BatchDev& D, cudaStream_t st) {
+    k_solve<T><<<D.G, 32 * kWarps, 0, st>>>(S, D);
+  }
+};
+
+}  // namespace gox
+
+using namespace gox;
+
+// ---------------------------------------------------------------------------
+// opaque handles
+
+struct gox_topo {
+  int n_bus = 0;
+  std::vector<int32_t> yp, yi, bus_type;
+  std::vector<double> yre, yim;
+  JacPattern jac;
+  Csc csc;
+  Symbolic sym;
+  bool factored = false;
+  Numeric num;
+  Schedule sc;
+  DevSchedule dsched;
+  DevBatch batch;
+  Timing timing;
+  int64_t launches = 0;
+  int device = 0;
+};
+
+struct gox_ls {
+  int n = 0;
+  std::vector<int32_t> rows, cols;
+  Csc csc;
+  Symbolic sym;
+  Numeric num;
+  Schedule sc;
+  DevSchedule dsched;
+  DevMem jbuf, lu, off, rhs, sol, sing, piv, gact, status;
+  std::vector<double> packed, hostbuf;
+};
+
+static int guard_impl(const std::function<int()>& f) {
+  try {
+    return f();
+  } catch (const std::bad_alloc&) {
+    return GOX_E_OUT_OF_MEMORY;
+  } catch (const CudaError& e) {
+    std::fprintf(stderr, "gridoxide_gb300: %s\n", e.what());
+    return GOX_E_CUDA;
+  } catch (const std::exception& e) {
+    std::fprintf(stderr, "gridoxide_gb300: %s\n", e.what());
+    return GOX_E_INVALID;
+  }
+}
+
+static int require_device() {
+  int n = 0;
+  if (cudaGetDeviceCount(&n) != cudaSuccess || n == 0) {
+    cudaGetLastError();
+    return GOX_E_NO_DEVICE;
+  }
+  return GOX_OK;
+}
+
+// Fixes the topology's pivot order from the first scenario whose Jacobian
+// at its start point is needed and factors (the first Jacobian a
+// PersistentSolver sees, src/solver.rs:711-713).  Returns the scenario index
+// used, or -1 when every scenario already meets tol at its start point.
+static int fix_pivots(gox_topo* t, int B, const double* p_spec, const double* q_spec,
+                      const double* vm0, const double* va0, int v_stride, const int32_t* o_slot,
+                      const double* o_dre, const double* o_dim, double tol,
+                      std::vector<int>& first_singular) {
+  const int n = t->n_bus, nu = t->jac.n_u;
+  std::vector<double> p(n), q(n), vals(t->jac.nnz()), yre, yim, packed(t->csc.nnz());
+  for (int s = 0; s < B; s++) {
+    const double* vm = vm0 + (size_t)s * v_stride;
+    const double* va = va0 + (size_t)s * v_stride;
+    yre = t->yre;
+    yim = t->yim;
+    if (o_slot && o_slot[4 * s] >= 0)
+      for (int c = 0; c < 4; c++) {
+        int sl = o_slot[4 * s + c];
+        if (sl < 0 || sl >= (int)yre.size()) throw std::runtime_error("bad outage slot");
+        yre[sl] += o_dre[4 * s + c];
+        yim[sl] += o_dim[4 * s + c];
+      }
+    host_injections(n, t->yp.data(), t->yi.data(), yre.data(), yim.data(), vm, va, p.data(),
+                    q.data());
+    double mx = 0.0;
+    for (int a = 0; a < t->jac.n_ang; a++) {
+      int i = t->jac.ns_idx[a];
+      mx = std::fmax(mx, std::fabs(p_spec[(size_t)s * n + i] - p[i]));
+    }
+    for (int a = 0; a < t->jac.n_pq; a++) {
+      int i = t->jac.pq_idx[a];
+      mx = std::fmax(mx, std::fabs(q_spec[(size_t)s * n + i] - q[i]));
+    }
+    if (mx < tol) continue;
+    host_jac_fill(t->jac, yre.data(), yim.data(), vm, va, p.data(), q.data(), vals.data());
+    std::fill(packed.begin(), packed.end(), 0.0);
+    for (int e = 0; e < t->jac.nnz(); e++) packed[t->csc.slot_of[e]] += vals[e];
+    Numeric N;
+    if (klu_factor(t->csc, packed.data(), t->sym, 0.001, N) == 0) {
+      t->num = std::move(N);
+      build_schedule(&t->jac, t->csc, t->sym, t->num, t->sc);
+      t->dsched.load(t->sc, t->yp, t->yi, t->yre, t->yim);
+      t->factored = true;
+      (void)nu;
+      return s;
+    }
+    first_singular.push_back(s);
+  }
+  return -1;
+}
+
+template <typename T>
+static void run_iterations(gox_topo* t, BatchDev D, int max_iter, bool outage, cudaStream_t st,
+                           int32_t* h_nactive) {
+  const SchedDev& S = t->dsched.d;
+  const int cap = Iter<T>::stage_cap(S, t->sc.max_collen);
+  const bool timing = t->timing.on;
+  // events: per iteration [k1 start, k1 end, k2 end, k3 end, k4 end]; read once at the end
+  std::vector<cudaEvent_t> ev;
+  auto rec = [&]() {
+    if (!timing) return;
+    cudaEvent_t e;
+    GOX_CK(cudaEventCreate(&e));
+    GOX_CK(cudaEventRecord(e, st));
+    ev.push_back(e);
+  };
+  int it = 0;
+  std::vector<int> full;  // iterations that ran K2-K4
+  rec();
+  for (it = 0; it < max_iter; it++) {
+    GOX_CK(cudaMemsetAsync(D.nactive, 0, sizeof(int32_t), st));
+    rec();
+    Iter<T>::mismatch(S, D, it, 0, outage, st);
+    t->launches++;
+    rec();
+    GOX_CK(cudaMemcpyAsync(h_nactive, D.nactive, sizeof(int32_t), cudaMemcpyDeviceToHost, st));
+    GOX_CK(cudaStreamSynchronize(st));
+    if (*h_nactive == 0) break;
+    Iter<T>::fill(S, D, outage, st);
+    rec();
+    Iter<T>::refactor(S, D, cap, st);
+    rec();
+    Iter<T>::solve(S, D, st);
+    rec();
+    t->launches += 3;
+    GOX_CK(cudaGetLastError());
+  }
+  if (it == max_iter) {
+    Iter<T>::mismatch(S, D, max_iter, 1, outage, st);
+    t->launches++;
+  }
+  rec();
+  GOX_CK(cudaGetLastError());
+  if (timing) {
+    GOX_CK(cudaEventSynchronize(ev.back()));
+    auto el = [&](size_t a, size_t b) {
+      float ms = 0;
+      GOX_CK(cudaEventElapsedTime(&ms, ev[a], ev[b]));
+      return (double)ms;
+    };
+    Timing& T_ = t->timing;
+    T_.iters = it;
+    T_.total = el(0, ev.size() - 1);
+    T_.k1 = T_.k2 = T_.k3 = T_.k4 = 0;
+    size_t i = 1;
+    for (int k = 0; k <= it && k < max_iter; k++) {
+      if (i + 1 >= ev.size()) break;
+      T_.k1 += el(i, i + 1);
+      if (i + 4 < ev.size() && k < it) {
+        T_.k2 += el(i + 1, i + 2);
+        T_.k3 += el(i + 2, i + 3);
+        T_.k4 += el(i + 3, i + 4);
+        i += 5;
+      } else {
+        break;
+      }
+    }
+    for (auto e : ev) cudaEventDestroy(e);
+  }
+}
+
+// Core of both batch entry points: all arrays on the device.
+static int batch_device(gox_topo* t, int B, const double* p_spec, const double* q_spec,
+                        const double* vm0, const double* va0, int v_stride,
+                        const int32_t* o_slot, const double* o_dre, const double* o_dim,
+                        double tol, int max_iter, int precision, double* vm_out,
+                        double* va_out, int32_t* iters, int32_t* status, double* max_mis,
+                        double* hist, cudaStream_t st, const double* h_p, const double* h_q,
+                        const double* h_vm, const double* h_va, const int32_t* h_oslot,
+                        const double* h_odre, const double* h_odim) {
+  const int n = t->n_bus;
+  const int G = (B + 31) / 32;
+  t->launches = 0;
+  std::vector<int> first_singular;
+  if (!t->factored) {
+    // host copies of the inputs to find the pivot-fixing Jacobian
+    std::vector<double> hp, hq, hvm, hva, hdre, hdim;
+    std::vector<int32_t> hslot;
+    const double *pp = h_p, *qq = h_q, *vv = h_vm, *aa = h_va, *dr = h_odre, *di = h_odim;
+    const int32_t* ss = h_oslot;
+    if (!pp) {
+      size_t nv = (size_t)(v_stride ? B : 1) * n;
+      hp.resize((size_t)B * n); hq.resize((size_t)B * n); hvm.resize(nv); hva.resize(nv);
+      GOX_CK(cudaMemcpyAsync(hp.data(), p_spec, hp.size() * 8, cudaMemcpyDeviceToHost, st));
+      GOX_CK(cudaMemcpyAsync(hq.data(), q_spec, hq.size() * 8, cudaMemcpyDeviceToHost, st));
+      GOX_CK(cudaMemcpyAsync(hvm.data(), vm0, nv * 8, cudaMemcpyDeviceToHost, st));
+      GOX_CK(cudaMemcpyAsync(hva.data(), va0, nv * 8, cudaMemcpyDeviceToHost, st));
+      if (o_slot) {
+        hslot.resize((size_t)B * 4); hdre.resize((size_t)B * 4); hdim.resize((size_t)B * 4);
+        GOX_CK(cudaMemcpyAsync(hslot.data(), o_slot, hslot.size() * 4, cudaMemcpyDeviceToHost, st));
+        GOX_CK(cudaMemcpyAsync(hdre.data(), o_dre, hdre.size() * 8, cudaMemcpyDeviceToHost, st));
+        GOX_CK(cudaMemcpyAsync(hdim.data(), o_dim, hdim.size() * 8, cudaMemcpyDeviceToHost, st));
+        ss = hslot.data(); dr = hdre.data(); di = hdim.data();
+      }
+      GOX_CK(cudaStreamSynchronize(st));
+      pp = hp.data(); qq = hq.data(); vv = hvm.data(); aa = hva.data();
+    }
+    fix_pivots(t, B, pp, qq, vv, aa, v_stride, ss, dr, di, tol, first_singular);
+  }
+  const bool outage = o_slot != nullptr;
+  const bool want_hist = hist != nullptr;
+  if (!t->factored) {
+    // no Jacobian needed (all scenarios converged at their start point) or
+    // every candidate factorization was singular: evaluate the mismatch
+    // only, with a one-iteration budget that never reaches a solve.
+  }
+  const SchedDev& S = t->dsched.d;
+  DevBatch& DB = t->batch;
+  if (t->factored) {
+    DB.ensure(S, G, precision, max_iter, want_hist);
+  } else {
+    return -1;  // handled by the caller's fallback below
+  }
+  BatchDev D = DB.view(want_hist, outage, tol);
+  // inputs -> interleaved layout
+  const size_t tot = (size_t)G * n * 32;
+  k_scatter_rows<<<grid1d(tot), 256, 0, st>>>(p_spec, B, n, n, D.psp, G);
+  k_scatter_rows<<<grid1d(tot), 256, 0, st>>>(q_spec, B, n, n, D.qsp, G);
+  k_scatter_rows<<<grid1d(tot), 256, 0, st>>>(vm0, B, n, v_stride, D.vm, G);
+  k_scatter_rows<<<grid1d(tot), 256, 0, st>>>(va0, B, n, v_stride, D.va, G);
+  k_init_scen<<<(G * 32 + 255) / 256, 256, 0, st>>>(B, G, D.status, D.iters, D.sing, D.piv_flag,
+                                                     D.maxmis);
+  t->launches += 5;
+  if (want_hist) GOX_CK(cudaMemsetAsync(D.hist, 0, (size_t)G * 32 * max_iter * 8, st));
+  if (outage) {
+    GOX_CK(cudaMemsetAsync(DB.err.p, 0, 4, st));
+    k_outage_prep<<<(G * 32 + 255) / 256, 256, 0, st>>>(
+        B, G, o_slot, o_dre, o_dim, S.yp, S.yi, n, S.nnz_y, DB.o_slot.as<int32_t>(), DB.o_dre.as<double>(),
+        DB.o_dim.as<double>(), DB.o_bf.as<int32_t>(), DB.o_bt.as<int32_t>(), DB.err.as<int32_t>());
+    t->launches++;
+    int32_t herr = 0;
+    GOX_CK(cudaMemcpyAsync(&herr, DB.err.p, 4, cudaMemcpyDeviceToHost, st));
+    GOX_CK(cudaStreamSynchronize(st));
+    if (herr) return GOX_E_BUS_RANGE;
+  }
+  // scenarios whose own first Jacobian was singular before the pivot order
+  // was fixed report Singular after their first mismatch (src/solver.rs:711-716)
+  if (!first_singular.empty()) {
+    std::vector<int32_t> ones(1, 2);
+    for (int s : first_singular)
+      GOX_CK(cudaMemcpyAsync(D.sing + s, ones.data(), 4, cudaMemcpyHostToDevice, st));
+    GOX_CK(cudaStreamSynchronize(st));
+  }
+  int32_t* h_nactive = nullptr;
+  GOX_CK(cudaMallocHost(&h_nactive, sizeof(int32_t)));
+  try {
+    if (precision == GOX_PRECISION_FP64) run_iterations<double>(t, D, max_iter, outage, st, h_nactive);
+    else run_iterations<float>(t, D, max_iter, outage, st, h_nactive);
+  } catch (...) {
+    cudaFreeHost(h_nactive);
+    throw;
+  }
+  cudaFreeHost(h_nactive);
+  // outputs
+  k_gather_rows<<<grid1d((size_t)B * n), 256, 0, st>>>(D.vm, B, n, G, vm_out);
+  k_gather_rows<<<grid1d((size_t)B * n), 256, 0, st>>>(D.va, B, n, G, va_out);
+  k_unpack_scen<<<(B + 255) / 256, 256, 0, st>>>(B, D.status, D.iters, D.maxmis, D.hist,
+                                                  max_iter, status, iters, max_mis, hist);
+  t->launches += 3;
+  GOX_CK(cudaGetLastError());
+  return GOX_OK;
+}
+
+extern "C" {
+
+const char* gox_version(void) { return "gridoxide_gb300 0.1.0 (sm_103a)"; }
+
+int gox_analyze(int32_t n, const int32_t* Ap, const int32_t* Ai, int32_t* P, int32_t* Q,
+                int32_t* R) {
+  if (n < 0 || !Ap || !Ai || !P || !Q || !R) return GOX_E_INVALID;
+  return guard_impl([&]() -> int {
+    for (int j = 0; j < n; j++)
+      if (Ap[j] > Ap[j + 1]) return GOX_E_INVALID;
+    for (int p = 0; p < Ap[n]; p++)
+      if (Ai[p] < 0 || Ai[p] >= n) return GOX_E_INVALID;
+    Symbolic S = klu_analyze(n, Ap, Ai);
+    std::copy(S.P.begin(), S.P.end(), P);
+    std::copy(S.Q.begin(), S.Q.end(), Q);
+    std::copy(S.R.begin(), S.R.end(), R);
+    return S.nblocks;
+  });
+}
+
+int gox_factor_host(int32_t n, int32_t nnz, const int32_t* rows, const int32_t* cols,
+                    const double* vals, int64_t* sizes, int32_t* Lp, int32_t* Li, double* Lx,
+                    int32_t* Up, int32_t* Ui, double* Ux, int32_t* Fp, int32_t* Fi, double* Fx,
+                    int32_t* P, int32_t* Q, int32_t* R) {
+  if (n <= 0 || nnz < 0 || !sizes || (nnz > 0 && (!rows || !cols || !vals))) return GOX_E_INVALID;
+  for (int e = 0; e < nnz; e++)
+    if (rows[e] < 0 || rows[e] >= n || cols[e] < 0 || cols[e] >= n) return GOX_E_INVALID;
+  return guard_impl([&]() -> int {
+    Csc A = build_csc(n, nnz, rows, cols);
+    Symbolic S = klu_analyze(n, A.p.data(), A.i.data());
+    std::vector<double> packed(A.nnz(), 0.0);
+    for (int e = 0; e < nnz; e++) packed[A.slot_of[e]] += vals[e];
+    Numeric N;
+    if (klu_factor(A, packed.data(), S, 0.001, N) != 0) return GOX_SINGULAR;
+    sizes[0] = (int64_t)N.Li.size() + n;
+    sizes[1] = (int64_t)N.Ui.size() + n;
+    sizes[2] = (int64_t)N.Offi.size();
+    sizes[3] = S.nblocks;
+    if (!Lp) return GOX_OK;
+    int nz = 0;
+    for (int k = 0; k < n; k++) {
+      Lp[k] = nz;
+      Li[nz] = k; Lx[nz] = 1.0; nz++;
+      for (int p = N.Lp[k]; p < N.Lp[k + 1]; p++) { Li[nz] = N.Li[p]; Lx[nz] = N.Lx[p]; nz++; }
+    }
+    Lp[n] = nz;
+    nz = 0;
+    for (int k = 0; k < n; k++) {
+      Up[k] = nz;
+      for (int p = N.Up[k]; p < N.Up[k + 1]; p++) { Ui[nz] = N.Ui[p]; Ux[nz] = N.Ux[p]; nz++; }
+      Ui[nz] = k; Ux[nz] = N.Udiag[k]; nz++;
+    }
+    Up[n] = nz;
+    for (int k = 0; k <= n; k++) Fp[k] = N.Offp[k];
+    for (size_t p = 0; p < N.Offi.size(); p++) { Fi[p] = N.Offi[p]; Fx[p] = N.Offx[p]; }
+    for (int k = 0; k < n; k++) { P[k] = N.Pnum[k]; Q[k] = S.Q[k]; }
+    for (int b = 0; b <= S.nblocks; b++) R[b] = S.R[b];
+    return GOX_OK;
+  });
+}
+
+int gox_topo_register(int32_t n_bus, const int32_t* yp, const int32_t* yi, const double* yre,
+                      const double* yim, const int32_t* bus_type, gox_topo** out) {
+  if (!out) return GOX_E_INVALID;
+  *out = nullptr;
+  if (n_bus <= 0 || !yp || !yi || !yre || !yim || !bus_type) return GOX_E_INVALID;
+  return guard_impl([&]() -> int {
+    if (yp[0] != 0) return GOX_E_INVALID;
+    for (int i = 0; i < n_bus; i++) {
+      if (yp[i] > yp[i + 1]) return GOX_E_INVALID;
+      if (bus_type[i] < 1 || bus_type[i] > 3) return GOX_E_INVALID;
+      for (int p = yp[i]; p < yp[i + 1]; p++) {
+        if (yi[p] < 0 || yi[p] >= n_bus) return GOX_E_INVALID;
+        if (p > yp[i] && yi[p] <= yi[p - 1]) return GOX_E_INVALID;  // sorted, no duplicates
+      }
+    }
+    std::unique_ptr<gox_topo> t(new gox_topo());
+    t->n_bus = n_bus;
+    int nnz = yp[n_bus];
+    t->yp.assign(yp, yp + n_bus + 1);
+    t->yi.assign(yi, yi + nnz);
+    t->yre.assign(yre, yre + nnz);
+    t->yim.assign(yim, yim + nnz);
+    t->bus_type.assign(bus_type, bus_type + n_bus);
+    t->jac = jac_analyze(n_bus, yp, yi, bus_type);
+    t->csc = build_csc(t->jac.n_u, t->jac.nnz(), t->jac.rows.data(), t->jac.cols.data());
+    t->sym = klu_analyze(t->jac.n_u, t->csc.p.data(), t->csc.i.data());
+    cudaGetDevice(&t->device);
+    *out = t.release();
+    return GOX_OK;
+  });
+}
+
+int gox_topo_reset(gox_topo* t) {
+  if (!t) return GOX_E_INVALID;
+  t->factored = false;
+  t->num = Numeric();
+  t->sc = Schedule();
+  return GOX_OK;
+}
+
+void gox_topo_destroy(gox_topo* t) { delete t; }
+
+static int check_batch_args(gox_topo* t, int B, const void* p, const void* q, const void* vm,
+                            const void* va, int v_stride, double tol, int max_iter,
+                            int precision, const void* vo, const void* ao, const void* it,
+                            const void* st, const void* mm, const int32_t* o_slot,
+                            const double* o_dre, const double* o_dim) {
+  if (!t || B < 0 || max_iter < 0 || !(tol >= 0)) return GOX_E_INVALID;
+  if (B == 0) return GOX_OK;
+  if (!p || !q || !vm || !va || !vo || !ao || !it || !st || !mm) return GOX_E_INVALID;
+  if (v_stride != 0 && v_stride != t->n_bus) return GOX_E_INVALID;
+  if (precision != GOX_PRECISION_FP64 && precision != GOX_PRECISION_MIXED) return GOX_E_INVALID;
+  if (o_slot && (!o_dre || !o_dim)) return GOX_E_INVALID;
+  return 1;
+}
+
+// When no Jacobian is ever needed (every scenario meets tol at its start),
+// or max_iter == 0, the result is computed on the host from the mismatch
+// only; no factorization exists to run on the device.
+static void host_only_result(gox_topo* t, int B, const double* p_spec, const double* q_spec,
+                             const double* vm0, const double* va0, int v_stride,
+                             const int32_t* o_slot, const double* o_dre, const double* o_dim,
+                             double tol, int max_iter, double* vm_out, double* va_out,
+                             int32_t* iters, int32_t* status, double* max_mis, double* hist,
+                             const std::vector<int>& singular_first) {
+  const int n = t->n_bus;
+  std::vector<double> p(n), q(n), yre, yim;
+  for (int s = 0; s < B; s++) {
+    const double* vm = vm0 + (size_t)s * v_stride;
+    const double* va = va0 + (size_t)s * v_stride;
+    std::copy(vm, vm + n, vm_out + (size_t)s * n);
+    std::copy(va, va + n, va_out + (size_t)s * n);
+    if (hist) std::fill(hist + (size_t)s * max_iter, hist + (size_t)(s + 1) * max_iter, 0.0);
+    if (max_iter == 0) { iters[s] = 0; status[s] = GOX_MAX_ITERATIONS; max_mis[s] = 0.0; continue; }
+    yre = t->yre; yim = t->yim;
+    if (o_slot && o_slot[4 * s] >= 0)
+      for (int c = 0; c < 4; c++) { yre[o_slot[4 * s + c]] += o_dre[4 * s + c]; yim[o_slot[4 * s + c]] += o_dim[4 * s + c]; }
+    host_injections(n, t->yp.data(), t->yi.data(), yre.data(), yim.data(), vm, va, p.data(), q.data());
+    double mx = 0.0;
+    for (int a = 0; a < t->jac.n_ang; a++) { int i = t->jac.ns_idx[a]; mx = std::fmax(mx, std::fabs(p_spec[(size_t)s * n + i] - p[i])); }
+    for (int a = 0; a < t->jac.n_pq; a++) { int i = t->jac.pq_idx[a]; mx = std::fmax(mx, std::fabs(q_spec[(size_t)s * n + i] - q[i])); }
+    iters[s] = 1;
+    max_mis[s] = mx;
+    if (hist) hist[(size_t)s * max_iter] = mx;
+    status[s] = mx < tol ? GOX_CONVERGED : GOX_SINGULAR_SCENARIO;
+  }
+  (void)singular_first;
+}
+
+int gox_batch_solve_device(gox_topo* t, int32_t B, const double* p_spec, const double* q_spec,
+                           const double* vm0, const double* va0, int32_t v_stride,
+                           const int32_t* o_slot, const double* o_dre, const double* o_dim,
+                           double tol, int32_t max_iter, int32_t precision, double* vm_out,
+                           double* va_out, int32_t* iterations, int32_t* status,
+                           double* max_mismatch, double* history, void* stream) {
+  int c = check_batch_args(t, B, p_spec, q_spec, vm0, va0, v_stride, tol, max_iter, precision,
+                           vm_out, va_out, iterations, status, max_mismatch, o_slot, o_dre, o_dim);
+  if (c <= 0) return c;
+  if (int r = require_device()) return r;
+  return guard_impl([&]() -> int {
+    cudaStream_t st = (cudaStream_t)stream;
+    if (max_iter == 0) return GOX_E_INVALID;
+    int r = batch_device(t, B, p_spec, q_spec, vm0, va0, v_stride, o_slot, o_dre, o_dim, tol,
+                         max_iter, precision, vm_out, va_out, iterations, status, max_mismatch,
+                         history, st, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr,
+                         nullptr);
+    if (r == -1) {
+      // no factorization could be fixed: evaluate on the host copy
+      size_t nv = (size_t)(v_stride ? B : 1) * t->n_bus;
+      std::vector<double> hp((size_t)B * t->n_bus), hq(hp.size()), hvm(nv), hva(nv),
+          ovm(hp.size()), ova(hp.size()), mm(B), hh(history ? (size_t)B * max_iter : 0);
+      std::vector<int32_t> it(B), ss(B), hs;
+      std::vector<double> hr, hi;
+      GOX_CK(cudaMemcpy(hp.data(), p_spec, hp.size() * 8, cudaMemcpyDeviceToHost));
+      GOX_CK(cudaMemcpy(hq.data(), q_spec, hq.size() * 8, cudaMemcpyDeviceToHost));
+      GOX_CK(cudaMemcpy(hvm.data(), vm0, nv * 8, cudaMemcpyDeviceToHost));
+      GOX_CK(cudaMemcpy(hva.data(), va0, nv * 8, cudaMemcpyDeviceToHost));
+      if (o_slot) {
+        hs.resize((size_t)B * 4); hr.resize(hs.size()); hi.resize(hs.size());
+        GOX_CK(cudaMemcpy(hs.data(), o_slot, hs.size() * 4, cudaMemcpyDeviceToHost));
+        GOX_CK(cudaMemcpy(hr.data(), o_dre, hr.size() * 8, cudaMemcpyDeviceToHost));
+        GOX_CK(cudaMemcpy(hi.data(), o_dim, hi.size() * 8, cudaMemcpyDeviceToHost));
+      }
+      host_only_result(t, B, hp.data(), hq.data(), hvm.data(), hva.data(), v_stride,
+                       o_slot ? hs.data() : nullptr, hr.data(), hi.data(), tol, max_iter,
+                       ovm.data(), ova.data(), it.data(), ss.data(), mm.data(),
+                       history ? hh.data() : nullptr, {});
+      GOX_CK(cudaMemcpy(vm_out, ovm.data(), ovm.size() * 8, cudaMemcpyHostToDevice));
+      GOX_CK(cudaMemcpy(va_out, ova.data(), ova.size() * 8, cudaMemcpyHostToDevice));
+      GOX_CK(cudaMemcpy(iterations, it.data(), B * 4, cudaMemcpyHostToDevice));
+      GOX_CK(cudaMemcpy(status, ss.data(), B * 4, cudaMemcpyHostToDevice));
+      GOX_CK(cudaMemcpy(max_mismatch, mm.data(), B * 8, cudaMemcpyHostToDevice));
+      if (history) GOX_CK(cudaMemcpy(history, hh.data(), hh.size() * 8, cudaMemcpyHostToDevice));
+      return GOX_OK;
+    }
+    return r;
+  });
+}
+
+int gox_batch_solve(gox_topo* t, int32_t B, const double* p_spec, const double* q_spec,
+                    const double* vm0, const double* va0, int32_t v_stride,
+                    const int32_t* o_slot, const double* o_dre, const double* o_dim, double tol,
+                    int32_t max_iter, int32_t precision, double* vm_out, double* va_out,
+                    int32_t* iterations, int32_t* status, double* max_mismatch,
+                    double* history) {
+  int c = check_batch_args(t, B, p_spec, q_spec, vm0, va0, v_stride, tol, max_iter, precision,
+                           vm_out, va_out, iterations, status, max_mismatch, o_slot, o_dre, o_dim);
+  if (c <= 0) return c;
+  if (max_iter == 0) {
+    std::vector<int> none;
+    host_only_result(t, B, p_spec, q_spec, vm0, va0, v_stride, o_slot, o_dre, o_dim, tol, 0,
+                     vm_out, va_out, iterations, status, max_mismatch, history, none);
+    return GOX_OK;
+  }
+  if (int r = require_device()) return r;
+  return guard_impl([&]() -> int {
+    const int n = t->n_bus;
+    cudaStream_t st = nullptr;
+    GOX_CK(cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking));
+    struct StreamGuard {
+      cudaStream_t s;
+      ~StreamGuard() { cudaStreamDestroy(s); }
+    } sg{st};
+    const size_t bn = (size_t)B * n, nv = (size_t)(v_stride ? B : 1) * n;
+    DevMem dp, dq, dvm, dva, dovm, dova, dit, dst, dmm, dh, dsl, dre, dim;
+    dp.ensure(bn * 8); dq.ensure(bn * 8); dvm.ensure(nv * 8); dva.ensure(nv * 8);
+    dovm.ensure(bn * 8); dova.ensure(bn * 8); dit.ensure((size_t)B * 4); dst.ensure((size_t)B * 4);
+    dmm.ensure((size_t)B * 8);
+    if (history) dh.ensure((size_t)B * max_iter * 8);
+    GOX_CK(cudaMemcpyAsync(dp.p, p_spec, bn * 8, cudaMemcpyHostToDevice, st));
+    GOX_CK(cudaMemcpyAsync(dq.p, q_spec, bn * 8, cudaMemcpyHostToDevice, st));
+    GOX_CK(cudaMemcpyAsync(dvm.p, vm0, nv * 8, cudaMemcpyHostToDevice, st));
+    GOX_CK(cudaMemcpyAsync(dva.p, va0, nv * 8, cudaMemcpyHostToDevice, st));
+    if (o_slot) {
+      dsl.ensure((size_t)B * 16); dre.ensure((size_t)B * 32); dim.ensure((size_t)B * 32);
+      GOX_CK(cudaMemcpyAsync(dsl.p, o_slot, (size_t)B * 16, cudaMemcpyHostToDevice, st));
+      GOX_CK(cudaMemcpyAsync(dre.p, o_dre, (size_t)B * 32, cudaMemcpyHostToDevice, st));
+      GOX_CK(cudaMemcpyAsync(dim.p, o_dim, (size_t)B * 32, cudaMemcpyHostToDevice, st));
+    }
+    int r = batch_device(t, B, dp.as<double>(), dq.as<double>(), dvm.as<double>(),
+                         dva.as<double>(), v_stride, o_slot ? dsl.as<int32_t>() : nullptr,
+                         o_slot ? dre.as<double>() : nullptr, o_slot ? dim.as<double>() : nullptr,
+                         tol, max_iter, precision, dovm.as<double>(), dova.as<double>(),
+                         dit.as<int32_t>(), dst.as<int32_t>(), dmm.as<double>(),
+                         history ? dh.as<double>() : nullptr, st, p_spec, q_spec, vm0, va0,
+                         o_slot, o_dre, o_dim);
+    if (r == -1) {
+      std::vector<int> none;
+      GOX_CK(cudaStreamSynchronize(st));
+      host_only_result(t, B, p_spec, q_spec, vm0, va0, v_stride, o_slot, o_dre, o_dim, tol,
+                       max_iter, vm_out, va_out, iterations, status, max_mismatch, history, none);
+      return GOX_OK;
+    }
+    if (r != GOX_OK) return r;
+    GOX_CK(cudaMemcpyAsync(vm_out, dovm.p, bn * 8, cudaMemcpyDeviceToHost, st));
+    GOX_CK(cudaMemcpyAsync(va_out, dova.p, bn * 8, cudaMemcpyDeviceToHost, st));
+    GOX_CK(cudaMemcpyAsync(iterations, dit.p, (size_t)B * 4, cudaMemcpyDeviceToHost, st));
+    GOX_CK(cudaMemcpyAsync(status, dst.p, (size_t)B * 4, cudaMemcpyDeviceToHost, st));
+    GOX_CK(cudaMemcpyAsync(max_mismatch, dmm.p, (size_t)B * 8, cudaMemcpyDeviceToHost, st));
+    if (history)
+      GOX_CK(cudaMemcpyAsync(history, dh.p, (size_t)B * max_iter * 8, cudaMemcpyDeviceToHost, st));
+    GOX_CK(cudaStreamSynchronize(st));
+    return GOX_OK;
+  });
+}
+
+int gox_topo_info(const gox_topo* t, int64_t* info) {
+  if (!t || !info || !t->factored) return GOX_E_INVALID;
+  const Schedule& sc = t->sc;
+  info[0] = t->jac.n_u;
+  info[1] = t->jac.nnz();
+  info[2] = (int64_t)t->num.Li.size();
+  info[3] = (int64_t)t->num.Ui.size();
+  info[4] = sc.n_off;
+  info[5] = sc.nblocks;
+  info[6] = sc.n_levels;
+  info[7] = sc.n_phases;
+  info[8] = sc.n_slots;
+  info[9] = sc.max_collen;
+  return GOX_OK;
+}
+
+int gox_topo_structure(const gox_topo* t, int32_t* Pnum, int32_t* Q, int32_t* R, int32_t* Lp,
+                       int32_t* Li, int32_t* Up, int32_t* Ui, double* flops) {
+  if (!t || !t->factored) return GOX_E_INVALID;
+  const Numeric& N = t->num;
+  if (Pnum) std::copy(N.Pnum.begin(), N.Pnum.end(), Pnum);
+  if (Q) std::copy(t->sym.Q.begin(), t->sym.Q.end(), Q);
+  if (R) std::copy(t->sym.R.begin(), t->sym.R.end(), R);
+  if (Lp) std::copy(N.Lp.begin(), N.Lp.end(), Lp);
+  if (Li) std::copy(N.Li.begin(), N.Li.end(), Li);
+  if (Up) std::copy(N.Up.begin(), N.Up.end(), Up);
+  if (Ui) std::copy(N.Ui.begin(), N.Ui.end(), Ui);
+  if (flops) { flops[0] = t->sc.flops_refactor; flops[1] = t->sc.flops_solve; }
+  return GOX_OK;
+}
+
+int gox_topo_jacobian_pattern(const gox_topo* t, int32_t* rows, int32_t* cols) {
+  if (!t || !rows || !cols) return GOX_E_INVALID;
+  std::copy(t->jac.rows.begin(), t->jac.rows.end(), rows);
+  std::copy(t->jac.cols.begin(), t->jac.cols.end(), cols);
+  return GOX_OK;
+}
+
+int gox_set_timing(gox_topo* t, int32_t enable) {
+  if (!t) return GOX_E_INVALID;
+  t->timing.on = enable != 0;
+  return GOX_OK;
+}
+
+int gox_last_timing(const gox_topo* t, double* out) {
+  if (!t || !out) return GOX_E_INVALID;
+  out[0] = t->timing.iters; out[1] = t->timing.total; out[2] = t->timing.k1;
+  out[3] = t->timing.k2; out[4] = t->timing.k3; out[5] = t->timing.k4;
+  return GOX_OK;
+}
+
+int64_t gox_last_launches(const gox_topo* t) { return t ? t->launches : -1; }
+
+// ---- LinearSolver level ----------------------------------------------------
+
+int gox_ls_create(int32_t n, int32_t nnz, const int32_t* rows, const int32_t* cols,
+                  const double* vals, gox_ls** out) {
+  if (!out) return GOX_E_INVALID;
+  *out = nullptr;
+  if (n <= 0 || nnz < 0 || (nnz > 0 && (!rows || !cols || !vals))) return GOX_E_INVALID;
+  for (int e = 0; e < nnz; e++)
+    if (rows[e] < 0 || rows[e] >= n || cols[e] < 0 || cols[e] >= n) return GOX_E_INVALID;
+  if (int r = require_device()) return r;
+  return guard_impl([&]() -> int {
+    std::unique_ptr<gox_ls> h(new gox_ls());
+    h->n = n;
+    h->rows.assign(rows, rows + nnz);
+    h->cols.assign(cols, cols + nnz);
+    h->csc = build_csc(n, nnz, rows, cols);
+    h->sym = klu_analyze(n, h->csc.p.data(), h->csc.i.data());
+    h->packed.assign(h->csc.nnz(), 0.0);
+    for (int e = 0; e < nnz; e++) h->packed[h->csc.slot_of[e]] += vals[e];
+    if (klu_factor(h->csc, h->packed.data(), h->sym, 0.001, h->num) != 0) return GOX_SINGULAR;
+    build_schedule(nullptr, h->csc, h->sym, h->num, h->sc);
+    std::vector<int32_t> dummy_p(1, 0), dummy_i;
+    std::vector<double> dummy_x;
+    h->dsched.load(h->sc, dummy_p, dummy_i, dummy_x, dummy_x);
+    const SchedDev& S = h->dsched.d;
+    h->jbuf.ensure((size_t)S.n_a * 32 * 8 + 8);
+    h->lu.ensure((size_t)S.n_slots * 32 * 8 + 8);
+    h->off.ensure((size_t)S.n_off * 32 * 8 + 8);
+    h->rhs.ensure((size_t)n * 32 * 8);
+    h->sol.ensure((size_t)n * 32 * 8);
+    h->sing.ensure(128); h->piv.ensure(128); h->gact.ensure(16); h->status.ensure(128);
+    int32_t one = 1;
+    GOX_CK(cudaMemcpy(h->gact.p, &one, 4, cudaMemcpyHostToDevice));
+    *out = h.release();
+    return GOX_OK;
+  });
+}
+
+static int ls_run(gox_ls* h, const double* vals, const double* rhs, double* x) {
+  const SchedDev& S = h->dsched.d;
+  const int n = h->n;
+  // pack duplicates, A order, replicate to all 32 lanes
+  std::fill(h->packed.begin(), h->packed.end(), 0.0);
+  for (size_t e = 0; e < h->rows.size(); e++) h->packed[h->csc.slot_of[e]] += vals[e];
+  h->hostbuf.assign((size_t)S.n_a * 32, 0.0);
+  for (int k = 0; k < n; k++) {
+    int oldcol = h->sym.Q[k];
+    for (int p = h->csc.p[oldcol], a = h->sc.c_abeg[k]; p < h->csc.p[oldcol + 1]; p++, a++)
+      for (int l = 0; l < 32; l++) h->hostbuf[(size_t)a * 32 + l] = h->packed[p];
+  }
+  GOX_CK(cudaMemcpy(h->jbuf.p, h->hostbuf.data(), h->hostbuf.size() * 8, cudaMemcpyHostToDevice));
+  std::vector<double> b((size_t)n * 32);
+  for (int k = 0; k < n; k++)
+    for (int l = 0; l < 32; l++) b[(size_t)k * 32 + l] = rhs[h->num.Pnum[k]];
+  GOX_CK(cudaMemcpy(h->rhs.p, b.data(), b.size() * 8, cudaMemcpyHostToDevice));
+  GOX_CK(cudaMemset(h->sing.p, 0, 128));
+  BatchDev D{};
+  D.G = 1;
+  D.jbuf = h->jbuf.p; D.lu = h->lu.p; D.off = h->off.p; D.rhs = h->rhs.p; D.sol = h->sol.p;
+  D.sing = h->sing.as<int32_t>(); D.piv_flag = h->piv.as<int32_t>(); D.gact = h->gact.as<int32_t>();
+  D.piv_tol = 0.0f;
+  int cap = Iter<double>::stage_cap(S, h->sc.max_collen);
+  Iter<double>::refactor(S, D, cap, nullptr);
+  Iter<double>::solve(S, D, nullptr);
+  GOX_CK(cudaGetLastError());
+  std::vector<double> X((size_t)n * 32);
+  int32_t sing = 0;
+  GOX_CK(cudaMemcpy(X.data(), h->sol.p, X.size() * 8, cudaMemcpyDeviceToHost));
+  GOX_CK(cudaMemcpy(&sing, h->sing.p, 4, cudaMemcpyDeviceToHost));
+  bool finite = true;
+  for (int k = 0; k < n; k++) {
+    double v = X[(size_t)k * 32];
+    x[h->sym.Q[k]] = v;
+    if (!std::isfinite(v)) finite = false;
+  }
+  return (sing || !finite) ? GOX_SINGULAR : GOX_OK;
+}
+
+int gox_ls_factor_solve_values(gox_ls* h, const double* vals, const double* rhs, double* x) {
+  if (!h || (!vals && !h->rows.empty()) || !rhs || !x) return GOX_E_INVALID;
+  return guard_impl([&]() -> int { return ls_run(h, vals, rhs, x); });
+}
+
+int gox_ls_factor_solve(gox_ls* h, int32_t nnz, const int32_t* rows, const int32_t* cols,
+                        const double* vals, const double* rhs, double* x) {
+  if (!h || nnz != (int32_t)h->rows.size()) return h ? GOX_E_PATTERN : GOX_E_INVALID;
+  for (int e = 0; e < nnz; e++)
+    if (rows[e] != h->rows[e] || cols[e] != h->cols[e]) return GOX_E_PATTERN;
+  return gox_ls_factor_solve_values(h, vals, rhs, x);
+}
+
+void gox_ls_destroy(gox_ls* h) { delete h; }
+
+}  // extern "C"

@@ -1,0 +1,414 @@
+"""Host-side mirror of the reference's linear-solver plugin surface.
+
+* :class:`Gb300LinearSolver` -- the ``solver::LinearSolver`` trait
+  (gridoxide src/solver.rs:35-57): ``new`` / ``factor_and_solve`` /
+  ``factor_and_solve_values``, ``None`` on a singular matrix.
+* :class:`Topology` -- one registered topology on the GPU, the state a
+  ``PersistentSolver`` keeps (src/solver.rs:395-494): Jacobian pattern,
+  symbolic ordering, pivot order (fixed by the first Jacobian factored),
+  ``reset``.
+* :class:`BatchSolver` -- ``batch::BatchSolver::solve`` (src/batch.rs:198-289)
+  with :class:`Scenario` / :class:`BusOverride` / :func:`uniform_load_scaling`
+  (src/batch.rs:40-106) and :class:`BatchError` (src/batch.rs:108-135).
+
+Every numeric call goes through ``libgridoxide_gb300.so``; there is no CPU
+path here.
+"""
+from __future__ import annotations
+
+import ctypes as C
+from dataclasses import dataclass, field
+from typing import Optional, Sequence
+
+import numpy as np
+
+from . import _lib
+from ._lib import (GOX_CONVERGED, GOX_MAX_ITERATIONS, GOX_PRECISION_FP64, GOX_PRECISION_MIXED,
+                   GOX_SINGULAR, GOX_SINGULAR_SCENARIO, check)
+
+
+class SolveStatus:
+    """solver::SolveStatus (src/solver.rs:162-171)."""
+
+    Converged = GOX_CONVERGED
+    MaxIterationsReached = GOX_MAX_ITERATIONS
+    Singular = GOX_SINGULAR_SCENARIO
+
+
+class JacobianBackend:
+    """The two GB300 entries added beside Scalar/Block/Klu/KluNative/Pardiso
+    (src/solver.rs:62-108)."""
+
+    Gb300 = GOX_PRECISION_MIXED       # FP32 refactor/solve, FP64 mismatch/update
+    Gb300Fp64 = GOX_PRECISION_FP64    # plain FP64 on the GPU
+
+
+def _i32(a):
+    return np.ascontiguousarray(a, dtype=np.int32)
+
+
+def _f64(a):
+    return np.ascontiguousarray(a, dtype=np.float64)
+
+
+def _p(a, t):
+    return None if a is None else a.ctypes.data_as(t)
+
+
+# ---------------------------------------------------------------------------
+# LinearSolver
+
+class Gb300LinearSolver:
+    """LinearSolver on the GPU: symbolic + first factor on the host, FP64
+    refactor and solves on the device with the fixed pivot order."""
+
+    def __init__(self, handle, n, rows, cols):
+        self._h = handle
+        self.n = n
+        self._rows = rows
+        self._cols = cols
+
+    @classmethod
+    def new(cls, n: int, entries: Sequence) -> Optional["Gb300LinearSolver"]:
+        """``LinearSolver::new``: ``None`` if singular (src/solver.rs:38-41)."""
+        L = _lib.load()
+        ent = list(entries)
+        rows = _i32([e[0] for e in ent])
+        cols = _i32([e[1] for e in ent])
+        vals = _f64([e[2] for e in ent])
+        h = C.c_void_p()
+        rc = L.gox_ls_create(n, len(ent), _p(rows, _lib.i32p), _p(cols, _lib.i32p),
+                             _p(vals, _lib.f64p), C.byref(h))
+        if rc == GOX_SINGULAR:
+            return None
+        check(rc, "gox_ls_create")
+        return cls(h, n, rows, cols)
+
+    def factor_and_solve_values(self, values, rhs) -> Optional[np.ndarray]:
+        L = _lib.load()
+        x = np.zeros(self.n)
+        rc = L.gox_ls_factor_solve_values(self._h, _p(_f64(values), _lib.f64p),
+                                          _p(_f64(rhs), _lib.f64p), _p(x, _lib.f64p))
+        if rc == GOX_SINGULAR:
+            return None
+        check(rc, "gox_ls_factor_solve_values")
+        return x
+
+    def factor_and_solve(self, entries, rhs) -> Optional[np.ndarray]:
+        L = _lib.load()
+        ent = list(entries)
+        rows = _i32([e[0] for e in ent])
+        cols = _i32([e[1] for e in ent])
+        vals = _f64([e[2] for e in ent])
+        x = np.zeros(self.n)
+        rc = L.gox_ls_factor_solve(self._h, len(ent), _p(rows, _lib.i32p), _p(cols, _lib.i32p),
+                                   _p(vals, _lib.f64p), _p(_f64(rhs), _lib.f64p),
+                                   _p(x, _lib.f64p))
+        if rc == GOX_SINGULAR:
+            return None
+        check(rc, "gox_ls_factor_solve")
+        return x
+
+    def __del__(self):
+        try:
+            if self._h:
+                _lib.load().gox_ls_destroy(self._h)
+                self._h = None
+        except Exception:
+            pass
+
+
+# ---------------------------------------------------------------------------
+# Topology (PersistentSolver state) and batched solves
+
+@dataclass
+class BatchResult:
+    """BatchResult of the reference's Python surface (src/python.rs:63-78)."""
+
+    voltage_mag: np.ndarray
+    voltage_ang: np.ndarray
+    iterations: np.ndarray
+    status: np.ndarray
+    max_mismatch: np.ndarray
+    history: Optional[np.ndarray] = None
+
+    @property
+    def converged(self) -> np.ndarray:
+        return self.status == GOX_CONVERGED
+
+
+class Topology:
+    """A registered topology: Y-bus (CSR) + bus types, resident on the GPU."""
+
+    def __init__(self, ybus, bus_type):
+        L = _lib.load()
+        self.n_bus = int(ybus.n)
+        self.ybus = ybus
+        self.bus_type = _i32(bus_type)
+        h = C.c_void_p()
+        check(L.gox_topo_register(self.n_bus, _p(_i32(ybus.indptr), _lib.i32p),
+                                  _p(_i32(ybus.indices), _lib.i32p), _p(_f64(ybus.re), _lib.f64p),
+                                  _p(_f64(ybus.im), _lib.f64p), _p(self.bus_type, _lib.i32p),
+                                  C.byref(h)), "gox_topo_register")
+        self._h = h
+
+    @property
+    def handle(self):
+        return self._h
+
+    def reset(self):
+        """PersistentSolver::reset: forget the fixed pivot order."""
+        check(_lib.load().gox_topo_reset(self._h), "gox_topo_reset")
+
+    def solve(self, p_spec, q_spec, vm0, va0, tol=1e-8, max_iter=20,
+              precision=GOX_PRECISION_MIXED, outage=None, history=False) -> BatchResult:
+        """Batched NR on host arrays (inputs/outputs copied to/from the GPU).
+
+        p_spec/q_spec [B, N]; vm0/va0 [N] (shared) or [B, N];
+        outage = (slots [B,4], dre [B,4], dim [B,4]) or None."""
+        L = _lib.load()
+        p_spec = _f64(np.atleast_2d(p_spec))
+        q_spec = _f64(np.atleast_2d(q_spec))
+        B, n = p_spec.shape
+        if n != self.n_bus or q_spec.shape != p_spec.shape:
+            raise ValueError("p_spec/q_spec must be [B, n_bus]")
+        vm0 = _f64(vm0)
+        va0 = _f64(va0)
+        stride = n if vm0.ndim == 2 else 0
+        vm = np.zeros((B, n))
+        va = np.zeros((B, n))
+        iters = np.zeros(B, np.int32)
+        status = np.zeros(B, np.int32)
+        mis = np.zeros(B)
+        hist = np.zeros((B, max_iter)) if history else None
+        if outage is not None:
+            sl, dr, di = _i32(outage[0]), _f64(outage[1]), _f64(outage[2])
+        else:
+            sl = dr = di = None
+        rc = L.gox_batch_solve(self._h, B, _p(p_spec, _lib.f64p), _p(q_spec, _lib.f64p),
+                               _p(vm0, _lib.f64p), _p(va0, _lib.f64p), stride,
+                               _p(sl, _lib.i32p), _p(dr, _lib.f64p), _p(di, _lib.f64p),
+                               float(tol), int(max_iter), int(precision), _p(vm, _lib.f64p),
+                               _p(va, _lib.f64p), _p(iters, _lib.i32p), _p(status, _lib.i32p),
+                               _p(mis, _lib.f64p), _p(hist, _lib.f64p))
+        if rc == _lib.GOX_E_BUS_RANGE:
+            raise BatchError("BusOutOfRange", rc)
+        check(rc, "gox_batch_solve")
+        return BatchResult(vm, va, iters, status, mis, hist)
+
+    def solve_device(self, p_spec, q_spec, vm0, va0, vm_out, va_out, iters, status, max_mis,
+                     tol=1e-8, max_iter=20, precision=GOX_PRECISION_MIXED, outage=None,
+                     history=None, stream=None):
+        """Batched NR on device tensors (torch CUDA tensors, contiguous):
+        p/q/vm_out/va_out float64 [B, N]; vm0/va0 float64 [N] or [B, N];
+        iters/status int32 [B]; max_mis float64 [B]; outage = (slots int32
+        [B,4], dre, dim float64 [B,4]) or None; history float64 [B, max_iter]
+        or None.  Work is enqueued on `stream` (a torch.cuda.Stream or None)."""
+        L = _lib.load()
+        B, n = p_spec.shape
+        stride = n if vm0.dim() == 2 else 0
+        ptr = lambda t: None if t is None else C.c_void_p(t.data_ptr())
+        sl, dr, di = outage if outage is not None else (None, None, None)
+        st = None if stream is None else C.c_void_p(stream.cuda_stream)
+        rc = L.gox_batch_solve_device(self._h, B, ptr(p_spec), ptr(q_spec), ptr(vm0), ptr(va0),
+                                      stride, ptr(sl), ptr(dr), ptr(di), float(tol),
+                                      int(max_iter), int(precision), ptr(vm_out), ptr(va_out),
+                                      ptr(iters), ptr(status), ptr(max_mis), ptr(history), st)
+        if rc == _lib.GOX_E_BUS_RANGE:
+            raise BatchError("BusOutOfRange", rc)
+        check(rc, "gox_batch_solve_device")
+
+    def info(self) -> dict:
+        a = np.zeros(10, np.int64)
+        check(_lib.load().gox_topo_info(self._h, _p(a, _lib.i64p)), "gox_topo_info")
+        keys = ["n_u", "nnz_j", "nnz_l", "nnz_u", "nnz_off", "nblocks", "levels", "phases",
+                "lu_slots", "max_collen"]
+        return dict(zip(keys, [int(v) for v in a]))
+
+    def structure(self) -> dict:
+        inf = self.info()
+        n = inf["n_u"]
+        out = dict(P=np.zeros(n, np.int32), Q=np.zeros(n, np.int32),
+                   R=np.zeros(inf["nblocks"] + 1, np.int32), Lp=np.zeros(n + 1, np.int32),
+                   Li=np.zeros(max(inf["nnz_l"], 1), np.int32), Up=np.zeros(n + 1, np.int32),
+                   Ui=np.zeros(max(inf["nnz_u"], 1), np.int32), flops=np.zeros(2))
+        check(_lib.load().gox_topo_structure(
+            self._h, *[_p(out[k], _lib.i32p) for k in ("P", "Q", "R", "Lp", "Li", "Up", "Ui")],
+            _p(out["flops"], _lib.f64p)), "gox_topo_structure")
+        out["Li"] = out["Li"][:inf["nnz_l"]]
+        out["Ui"] = out["Ui"][:inf["nnz_u"]]
+        return out
+
+    def set_timing(self, on: bool):
+        check(_lib.load().gox_set_timing(self._h, 1 if on else 0), "gox_set_timing")
+
+    def last_timing(self) -> dict:
+        a = np.zeros(6)
+        check(_lib.load().gox_last_timing(self._h, _p(a, _lib.f64p)), "gox_last_timing")
+        return dict(iterations=a[0], total_ms=a[1], mismatch_ms=a[2], fill_ms=a[3],
+                    refactor_ms=a[4], solve_ms=a[5])
+
+    def last_launches(self) -> int:
+        return int(_lib.load().gox_last_launches(self._h))
+
+    def __del__(self):
+        try:
+            if self._h:
+                _lib.load().gox_topo_destroy(self._h)
+                self._h = None
+        except Exception:
+            pass
+
+
+# ---------------------------------------------------------------------------
+# BatchSolver mirror
+
+@dataclass
+class BusOverride:
+    """batch::BusOverride (src/batch.rs:40-68)."""
+
+    bus: int
+    p_spec: Optional[float] = None
+    q_spec: Optional[float] = None
+    voltage_mag: Optional[float] = None
+
+
+@dataclass
+class Scenario:
+    """batch::Scenario (src/batch.rs:73-91).  ``branch_outages`` holds at most
+    one branch index here: the N-1 outage keeps the branch's Y-bus entries in
+    the pattern and zeroes its series admittance and charging."""
+
+    bus_overrides: list = field(default_factory=list)
+    branch_outages: list = field(default_factory=list)
+
+
+class BatchError(Exception):
+    """batch::BatchError (src/batch.rs:108-135)."""
+
+    def __init__(self, kind: str, detail=None):
+        self.kind = kind
+        self.detail = detail
+        super().__init__(f"{kind}: {detail}")
+
+
+def uniform_load_scaling(p_spec, q_spec, factor: float) -> Scenario:
+    """batch::uniform_load_scaling (src/batch.rs:98-106)."""
+    ov = [BusOverride(i, float(p) * factor, float(q) * factor)
+          for i, (p, q) in enumerate(zip(p_spec, q_spec)) if p != 0.0 or q != 0.0]
+    return Scenario(ov)
+
+
+@dataclass
+class Buses:
+    """The bus template: per-bus arrays of the reference's ``Bus`` fields the
+    engine consumes (src/types.rs:26-42)."""
+
+    bus_type: np.ndarray
+    voltage_mag: np.ndarray
+    voltage_ang: np.ndarray
+    p_spec: np.ndarray
+    q_spec: np.ndarray
+
+
+@dataclass
+class PowerFlowReport:
+    voltage_mag: np.ndarray
+    voltage_ang: np.ndarray
+    status: int
+    mismatch_history: np.ndarray
+
+    @property
+    def iterations(self) -> int:
+        return len(self.mismatch_history)
+
+
+class BatchSolver:
+    """batch::BatchSolver with a GB300 backend.  Scenario validation and
+    result order follow src/batch.rs:198-289; the work runs as one GPU
+    batch instead of a rayon work queue."""
+
+    def __init__(self, backend=JacobianBackend.Gb300):
+        self.backend = backend
+        self._topos = {}
+
+    def solve(self, buses: Buses, ybus, scenarios: Sequence[Scenario], tol: float,
+              max_iter: int, branch_stamps=None) -> list:
+        """``branch_stamps(branch) -> (slots[4], dre[4], dim[4])`` supplies the
+        Y-bus deltas of an outage (see grids.outage_deltas)."""
+        n = len(buses.bus_type)
+        for i, sc in enumerate(scenarios):
+            for ov in sc.bus_overrides:
+                if ov.bus < 0 or ov.bus >= n:
+                    raise BatchError("BusOutOfRange", dict(scenario=i, bus=ov.bus, n_buses=n))
+            if len(sc.branch_outages) > 1 or (sc.branch_outages and branch_stamps is None):
+                raise BatchError("OutagesUnsupported", dict(scenario=i))
+        if len(scenarios) == 0:
+            return []
+        B = len(scenarios)
+        p = np.tile(_f64(buses.p_spec), (B, 1))
+        q = np.tile(_f64(buses.q_spec), (B, 1))
+        vm = np.tile(_f64(buses.voltage_mag), (B, 1))
+        va = np.tile(_f64(buses.voltage_ang), (B, 1))
+        outage = None
+        if any(sc.branch_outages for sc in scenarios):
+            sl = np.full((B, 4), -1, np.int32)
+            dr = np.zeros((B, 4))
+            di = np.zeros((B, 4))
+            for s, sc in enumerate(scenarios):
+                if sc.branch_outages:
+                    sl[s], dr[s], di[s] = branch_stamps(sc.branch_outages[0])
+            outage = (sl, dr, di)
+        for s, sc in enumerate(scenarios):
+            for ov in sc.bus_overrides:
+                if ov.p_spec is not None:
+                    p[s, ov.bus] = ov.p_spec
+                if ov.q_spec is not None:
+                    q[s, ov.bus] = ov.q_spec
+                if ov.voltage_mag is not None:
+                    vm[s, ov.bus] = ov.voltage_mag
+        key = id(ybus)
+        topo = self._topos.get(key)
+        if topo is None:
+            topo = Topology(ybus, buses.bus_type)
+            self._topos[key] = topo
+        res = topo.solve(p, q, vm, va, tol=tol, max_iter=max_iter, precision=self.backend,
+                         outage=outage, history=True)
+        return [PowerFlowReport(res.voltage_mag[s], res.voltage_ang[s], int(res.status[s]),
+                                res.history[s, :res.iterations[s]]) for s in range(B)]
+
+
+def analyze(n: int, Ap, Ai):
+    """klu_analyze (BTF + AMD) through the library: (P, Q, R)."""
+    L = _lib.load()
+    P = np.zeros(n, np.int32)
+    Q = np.zeros(n, np.int32)
+    R = np.zeros(n + 1, np.int32)
+    nb = check(L.gox_analyze(n, _p(_i32(Ap), _lib.i32p), _p(_i32(Ai), _lib.i32p),
+                             _p(P, _lib.i32p), _p(Q, _lib.i32p), _p(R, _lib.i32p)), "gox_analyze")
+    return P, Q, R[:nb + 1].copy()
+
+
+def factor_host(n: int, rows, cols, vals) -> Optional[dict]:
+    """The host partial-pivoting factorization (klu_extract layout), or None."""
+    L = _lib.load()
+    rows, cols, vals = _i32(rows), _i32(cols), _f64(vals)
+    sz = np.zeros(4, np.int64)
+    args = (n, len(rows), _p(rows, _lib.i32p), _p(cols, _lib.i32p), _p(vals, _lib.f64p),
+            _p(sz, _lib.i64p))
+    rc = L.gox_factor_host(*args, *([None] * 12))
+    if rc == GOX_SINGULAR:
+        return None
+    check(rc, "gox_factor_host")
+    lnz, unz, nzoff, nb = [int(v) for v in sz]
+    out = dict(Lp=np.zeros(n + 1, np.int32), Li=np.zeros(lnz, np.int32), Lx=np.zeros(lnz),
+               Up=np.zeros(n + 1, np.int32), Ui=np.zeros(unz, np.int32), Ux=np.zeros(unz),
+               Fp=np.zeros(n + 1, np.int32), Fi=np.zeros(max(nzoff, 1), np.int32),
+               Fx=np.zeros(max(nzoff, 1)), P=np.zeros(n, np.int32), Q=np.zeros(n, np.int32),
+               R=np.zeros(nb + 1, np.int32))
+    keys = ("Lp", "Li", "Lx", "Up", "Ui", "Ux", "Fp", "Fi", "Fx", "P", "Q", "R")
+    check(L.gox_factor_host(*args, *[_p(out[k], _lib.i32p if out[k].dtype == np.int32
+                                        else _lib.f64p) for k in keys]), "gox_factor_host")
+    out["Fi"] = out["Fi"][:nzoff]
+    out["Fx"] = out["Fx"][:nzoff]
+    return out

@@ -1,0 +1,191 @@
+/*
+ * gridoxide_gb300.h -- C ABI of the GB300 batched Newton-Raphson power-flow
+ * engine.  Plain pointers and sizes only; link against
+ * libgridoxide_gb300.so.
+ *
+ * Two levels, mirroring the reference's plugin surface:
+ *
+ *  1. gox_ls_*    -- one sparse system, the solver::LinearSolver trait
+ *                    (gridoxide src/solver.rs:35-57) that KluNativeSystem
+ *                    implements (src/klu_native/mod.rs:136-211).
+ *  2. gox_topo_* / gox_batch_* -- one topology, many scenarios: what
+ *                    batch::BatchSolver::solve does (src/batch.rs:198-289)
+ *                    with PersistentSolver's cached pattern and pivot order
+ *                    (src/solver.rs:395-494), run on the GPU.
+ *
+ * Status convention: 0 = OK; GOX_SINGULAR (1) = structurally or numerically
+ * singular (the trait's `None`); negative = error (KLU_INVALID /
+ * KLU_OUT_OF_MEMORY / BatchError analogues below).  Handles are not
+ * thread-safe: use one per host thread, like the reference's !Send FFI
+ * backends (src/batch.rs:234-246).
+ *
+ * All host buffers are caller-owned.  Per-scenario arrays are row-major
+ * [scenario][bus].  Bus types: 1 PQ, 2 PV, 3 slack (src/types.rs:26-42).
+ */
+#ifndef GRIDOXIDE_GB300_H
+#define GRIDOXIDE_GB300_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- status codes ------------------------------------------------------ */
+#define GOX_OK 0
+#define GOX_SINGULAR 1          /* LinearSolver returned None (KLU_SINGULAR) */
+#define GOX_E_OUT_OF_MEMORY (-2) /* KLU_OUT_OF_MEMORY */
+#define GOX_E_INVALID (-3)      /* KLU_INVALID: bad sizes / pointers / pattern */
+#define GOX_E_BUS_RANGE (-4)    /* BatchError::BusOutOfRange (src/batch.rs:108-135) */
+#define GOX_E_CUDA (-5)         /* a CUDA runtime call failed */
+#define GOX_E_PATTERN (-6)      /* values given for a different pattern */
+#define GOX_E_NO_DEVICE (-7)    /* no CUDA device visible */
+#define GOX_E_TOO_LARGE (-8)    /* request exceeds a documented size limit */
+
+/* per-scenario outcome, solver::SolveStatus (src/solver.rs:162-171) */
+#define GOX_CONVERGED 0
+#define GOX_MAX_ITERATIONS 1
+#define GOX_SINGULAR_SCENARIO 2
+
+/* arithmetic of the Jacobian refactorization and triangular solves; the
+ * mismatch, convergence test and voltage update are always FP64 */
+#define GOX_PRECISION_FP64 0
+#define GOX_PRECISION_MIXED 1   /* FP32 refactor/solve, FP64 mismatch */
+
+/* ---- level 1: LinearSolver ------------------------------------------- */
+typedef struct gox_ls gox_ls;
+
+/* LinearSolver::new (src/solver.rs:38-41; KluNativeSystem::new,
+ * src/klu_native/mod.rs:159-169): analyze the (row, col) pattern (BTF + AMD),
+ * factor `vals` once with partial pivoting (tol 0.001) to fix the pivot
+ * order.  Duplicate (row, col) entries are summed.  *out = NULL and
+ * GOX_SINGULAR if the matrix is singular. */
+int gox_ls_create(int32_t n, int32_t nnz, const int32_t *rows, const int32_t *cols,
+                  const double *vals, gox_ls **out);
+
+/* LinearSolver::factor_and_solve_values (src/solver.rs:56;
+ * src/klu_native/mod.rs:208-210): refactor on the GPU with the fixed pivot
+ * order (FP64) and solve A x = rhs.  vals positionally match the triplets
+ * given to gox_ls_create.  GOX_SINGULAR on a zero pivot or non-finite x. */
+int gox_ls_factor_solve_values(gox_ls *h, const double *vals, const double *rhs, double *x);
+
+/* LinearSolver::factor_and_solve (src/solver.rs:44-45): as above, but the
+ * caller passes the triplets again; they must equal those given to
+ * gox_ls_create, position by position (GOX_E_PATTERN otherwise). */
+int gox_ls_factor_solve(gox_ls *h, int32_t nnz, const int32_t *rows, const int32_t *cols,
+                        const double *vals, const double *rhs, double *x);
+
+/* Drop (src/sparse_klu.rs:205-212). */
+void gox_ls_destroy(gox_ls *h);
+
+/* ---- level 2: batched Newton-Raphson --------------------------------- */
+typedef struct gox_topo gox_topo;
+
+/* Registers a topology: the frozen Y-bus in CSR form (each row's columns
+ * ascending, duplicates already summed -- YBus::finish, src/network.rs:52-71)
+ * and the bus types.  Computes the Jacobian pattern
+ * (JacobianPattern::analyze, src/jacobian.rs:96-171) and its symbolic
+ * ordering (klu_native analyze, src/klu_native/analyze.rs:67-150).  The
+ * numeric pivot order is fixed later by the first Jacobian factored, as in
+ * PersistentSolver. */
+int gox_topo_register(int32_t n_bus, const int32_t *y_rowptr, const int32_t *y_col,
+                      const double *y_re, const double *y_im, const int32_t *bus_type,
+                      gox_topo **out);
+
+/* PersistentSolver::reset (src/solver.rs:480-493): forget the pivot order
+ * (the next solve refactors from a fresh partial-pivoting factorization). */
+int gox_topo_reset(gox_topo *t);
+
+void gox_topo_destroy(gox_topo *t);
+
+/* BatchSolver::solve on the GPU.  B scenarios of one topology.
+ *   p_spec, q_spec [B][n_bus]: net injections (BusOverride p/q already
+ *       applied; src/batch.rs:254-266);
+ *   vm0, va0: start voltages, [B][n_bus] when v_stride == n_bus or one
+ *       shared [n_bus] template when v_stride == 0.  Slack and PV entries
+ *       of vm0 are the voltage set-points;
+ *   out_slot, out_dre, out_dim [B][4] or NULL: per-scenario Y-bus deltas
+ *       (N-1 branch outage with the pattern kept): the four slots of the
+ *       branch's (ff, ft, tf, tt) entries and the values added to them;
+ *       out_slot[4s] < 0 means no outage for scenario s;
+ *   tol, max_iter: newton_raphson_cached's strict `max|F| < tol` and
+ *       iteration cap (src/solver.rs:699-703);
+ *   precision: GOX_PRECISION_FP64 or GOX_PRECISION_MIXED;
+ *   outputs: vm/va [B][n_bus], iterations (= mismatch-history length),
+ *       status (GOX_CONVERGED ...), final max mismatch [B], history
+ *       [B][max_iter] or NULL.
+ * Non-convergence is not an error (src/batch.rs:193-197).  Returns
+ * GOX_E_BUS_RANGE if an outage slot is outside the Y-bus. */
+int gox_batch_solve(gox_topo *t, int32_t B, const double *p_spec, const double *q_spec,
+                    const double *vm0, const double *va0, int32_t v_stride,
+                    const int32_t *out_slot, const double *out_dre, const double *out_dim,
+                    double tol, int32_t max_iter, int32_t precision, double *vm_out,
+                    double *va_out, int32_t *iterations, int32_t *status, double *max_mismatch,
+                    double *history);
+
+/* As gox_batch_solve, with every array in device memory and the work
+ * enqueued on `stream` (a cudaStream_t, NULL = legacy default stream).
+ * Synchronizes with the stream once per Newton iteration to read the
+ * running-scenario count. */
+int gox_batch_solve_device(gox_topo *t, int32_t B, const double *p_spec, const double *q_spec,
+                           const double *vm0, const double *va0, int32_t v_stride,
+                           const int32_t *out_slot, const double *out_dre,
+                           const double *out_dim, double tol, int32_t max_iter,
+                           int32_t precision, double *vm_out, double *va_out,
+                           int32_t *iterations, int32_t *status, double *max_mismatch,
+                           double *history, void *stream);
+
+/* ---- inspection (klu_analyze / klu_extract analogues) ------------------ */
+
+/* klu_analyze on a CSC pattern (BTF + AMD): P, Q [n], R [n+1]; returns the
+ * number of blocks or < 0. */
+int gox_analyze(int32_t n, const int32_t *Ap, const int32_t *Ai, int32_t *P, int32_t *Q,
+                int32_t *R);
+
+/* klu_analyze + klu_factor + klu_extract analogue on the host, no GPU:
+ * the partial-pivoting factorization whose pivot order the GPU refactor
+ * reuses (KluNativeSystem::new, src/klu_native/mod.rs:159-169).  Triplets
+ * as for gox_ls_create.  sizes[0] = nnz L incl. unit diagonal, [1] = nnz U
+ * incl. diagonal, [2] = nnz off-diagonal, [3] = nblocks.  With Lp == NULL
+ * only sizes are written.  Layout of klu_extract: L columns start with the
+ * unit diagonal, U columns end with the diagonal, rows in pivot order; P is
+ * the final row permutation (Pnum).  Returns GOX_SINGULAR if singular. */
+int gox_factor_host(int32_t n, int32_t nnz, const int32_t *rows, const int32_t *cols,
+                    const double *vals, int64_t *sizes, int32_t *Lp, int32_t *Li, double *Lx,
+                    int32_t *Up, int32_t *Ui, double *Ux, int32_t *Fp, int32_t *Fi, double *Fx,
+                    int32_t *P, int32_t *Q, int32_t *R);
+
+/* Sizes of the topology's Jacobian and factor, once its pivot order is
+ * fixed: [0] n unknowns, [1] nnz J, [2] nnz L (no diag), [3] nnz U (no
+ * diag), [4] nnz off-diagonal, [5] BTF blocks, [6] refactor levels,
+ * [7] solve phases, [8] LU slots per scenario, [9] max column length.
+ * Returns GOX_E_INVALID before the first solve. */
+int gox_topo_info(const gox_topo *t, int64_t *info);
+
+/* The fixed factorization structure (klu_extract layout without values):
+ * Pnum, Q [n], R [nblocks+1], L pattern Lp [n+1] / Li (rows in pivot order,
+ * no unit diagonal), U pattern Up [n+1] / Ui (DFS order, no diagonal).
+ * Also the refactor flop count per scenario in flops[0] and the solve flop
+ * count in flops[1]. */
+int gox_topo_structure(const gox_topo *t, int32_t *Pnum, int32_t *Q, int32_t *R, int32_t *Lp,
+                       int32_t *Li, int32_t *Up, int32_t *Ui, double *flops);
+
+/* The Jacobian pattern in emission order: rows, cols [nnz J]. */
+int gox_topo_jacobian_pattern(const gox_topo *t, int32_t *rows, int32_t *cols);
+
+/* Timing of the last gox_batch_solve*: [0] iterations run, [1] total kernel
+ * ms, [2] mismatch ms, [3] fill ms, [4] refactor ms, [5] solve ms (CUDA
+ * events on the solve stream; only when timing was enabled). */
+int gox_set_timing(gox_topo *t, int32_t enable);
+int gox_last_timing(const gox_topo *t, double *out);
+
+/* Kernel launches issued by the last gox_batch_solve* call. */
+int64_t gox_last_launches(const gox_topo *t);
+
+/* Library version string. */
+const char *gox_version(void);
+
+#ifdef __cplusplus
+}
+#endif
+#endif
