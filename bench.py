@@ -188,7 +188,14 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--grid", default=WORKLOAD["grid"], help="profiling: another grid")
+    ap.add_argument("--scenarios", type=int, default=WORKLOAD["scenarios"],
+                    help="profiling: a smaller batch")
+    ap.add_argument("--quick", action="store_true",
+                    help="profiling: mixed-precision steps only (no FP64, e2e, CPU legs)")
     args = ap.parse_args()
+    WORKLOAD["grid"] = args.grid
+    WORKLOAD["scenarios"] = args.scenarios
     args.warmup = max(args.warmup, 3)
     if args.impl == "reference":
         run_reference_arm(args)
@@ -261,7 +268,8 @@ def main():
 
     for _ in range(args.warmup):
         step(gox.GOX_PRECISION_MIXED)
-        step(gox.GOX_PRECISION_FP64)
+        if not args.quick:
+            step(gox.GOX_PRECISION_FP64)
     torch.cuda.synchronize()
     # correctness of the timed configuration
     its = oit.cpu().numpy()
@@ -273,6 +281,10 @@ def main():
     st_mx = ost.cpu().numpy().copy()
     mm_mx = omm.cpu().numpy().copy()
     it_mx = oit.cpu().numpy().copy()
+    if args.quick:
+        print(json.dumps({"quick": True, "ms_per_step": float(np.mean(ms_mx)),
+                          "kernels_ms": kern_mx, "iterations": iters_mx}), flush=True)
+        return
     ms_64, kern_64, launches_64, iters_64, _ = timed(gox.GOX_PRECISION_FP64,
                                                      max(3, args.steps // 2))
     it_64 = oit.cpu().numpy().copy()

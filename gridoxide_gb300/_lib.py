@@ -20,6 +20,7 @@ GOX_E_CUDA = -5
 GOX_E_PATTERN = -6
 GOX_E_NO_DEVICE = -7
 GOX_E_TOO_LARGE = -8
+GOX_E_DEVICE_WAIT = -9
 
 GOX_CONVERGED = 0
 GOX_MAX_ITERATIONS = 1
@@ -36,6 +37,7 @@ ERRORS = {
     GOX_E_PATTERN: "values given for a different pattern",
     GOX_E_NO_DEVICE: "no CUDA device visible",
     GOX_E_TOO_LARGE: "request exceeds a size limit",
+    GOX_E_DEVICE_WAIT: "a bounded device wait gave up",
 }
 
 
@@ -68,6 +70,9 @@ SIGNATURES = {
     "gox_analyze": (C.c_int, [C.c_int32, i32p, i32p, i32p, i32p, i32p]),
     "gox_factor_host": (C.c_int, [C.c_int32, C.c_int32, i32p, i32p, f64p, i64p, i32p, i32p, f64p,
                                   i32p, i32p, f64p, i32p, i32p, f64p, i32p, i32p, i32p]),
+    "gox_topo_prepare": (C.c_int, [vp, C.c_int32, f64p, f64p, f64p, f64p, C.c_int32, i32p, f64p,
+                                   f64p, C.c_double]),
+    "gox_topo_emulate_step": (C.c_int, [vp, f64p, f64p, f64p]),
     "gox_topo_info": (C.c_int, [vp, i64p]),
     "gox_topo_structure": (C.c_int, [vp, i32p, i32p, i32p, i32p, i32p, i32p, i32p, f64p]),
     "gox_topo_jacobian_pattern": (C.c_int, [vp, i32p, i32p]),

@@ -97,7 +97,7 @@ __global__ void k_gather_rows(const double* __restrict__ src, int B, int N, int 
 }
 
 __global__ void k_init_scen(int B, int G, int32_t* status, int32_t* iters, int32_t* sing,
-                            int32_t* piv, double* maxmis) {
+                            int32_t* piv, double* maxmis, unsigned long long* maxacc) {
   int s = blockIdx.x * blockDim.x + threadIdx.x;
   if (s >= G * 32) return;
   status[s] = (s < B) ? ST_RUNNING : ST_UNUSED;
@@ -105,6 +105,7 @@ __global__ void k_init_scen(int B, int G, int32_t* status, int32_t* iters, int32
   sing[s] = 0;
   piv[s] = 0;
   maxmis[s] = 0.0;
+  maxacc[s] = 0ull;
 }
 
 // Outage slots -> branch buses; validates the slots.  err[0] set on a bad slot.
@@ -168,9 +169,11 @@ __global__ void k_unpack_scen(int B, const int32_t* st_in, const int32_t* it_in,
 
 struct DevSchedule {
   DevMem yp, yi, yre, yim, bus_rowP, bus_rowQ, bus_colA, bus_colV, a_kind, a_bi, a_bk, a_yslot,
-      a_dst, lev_ptr, lev_cols, c_base, c_ulen, c_llen, c_abeg, op_ptr, op_slot, op_pos, ph_ptr,
-      ph_rows, ph_kind, fw_ptr, fw_slot, fw_col, bw_ptr, bw_slot, bw_col, diag_slot;
+      a_dst, lev_ptr, lev_cols, c_base, c_ulen, c_llen, c_abeg, c_aend, op_ptr, op_slot, op_pos, ph_ptr,
+      ph_rows, ph_kind, fw_ptr, fw_slot, fw_col, bw_ptr, bw_slot, bw_col, diag_slot, bt_ptr, bt_cnt,
+      pk_off, pk, slot_a, off_a;
   SchedDev d{};
+  int max_collen = 0, max_ops = 0, max_pk = 0, max_head = 0, max_fw = 0;
 
   void load(const Schedule& sc, const std::vector<int32_t>& yp_h, const std::vector<int32_t>& yi_h,
             const std::vector<double>& yre_h, const std::vector<double>& yim_h) {
@@ -181,14 +184,25 @@ struct DevSchedule {
     upload(a_yslot, sc.a_yslot); upload(a_dst, sc.a_dst);
     upload(lev_ptr, sc.lev_ptr); upload(lev_cols, sc.lev_cols); upload(c_base, sc.c_base);
     upload(c_ulen, sc.c_ulen); upload(c_llen, sc.c_llen); upload(c_abeg, sc.c_abeg);
+    upload(c_aend, sc.c_aend);
     upload(op_ptr, sc.op_ptr); upload(op_slot, sc.op_slot); upload(op_pos, sc.op_pos);
     upload(ph_ptr, sc.ph_ptr); upload(ph_rows, sc.ph_rows); upload(ph_kind, sc.ph_kind);
     upload(fw_ptr, sc.fw_ptr); upload(fw_slot, sc.fw_slot); upload(fw_col, sc.fw_col);
     upload(bw_ptr, sc.bw_ptr); upload(bw_slot, sc.bw_slot); upload(bw_col, sc.bw_col);
     upload(diag_slot, sc.diag_slot);
+    upload(bt_ptr, sc.bt_ptr); upload(bt_cnt, sc.bt_cnt);
+    upload(pk_off, sc.pk_off); upload(pk, sc.pk);
+    upload(slot_a, sc.slot_a); upload(off_a, sc.off_a);
+    d.slot_a = slot_a.as<int32_t>(); d.off_a = off_a.as<int32_t>();
+    d.n_off_real = sc.n_off;
+    d.bt_ptr = bt_ptr.as<int32_t>(); d.bt_cnt = bt_cnt.as<uint8_t>();
+    d.pk_off = pk_off.as<int32_t>(); d.pk = pk.as<int32_t>();
+    max_collen = sc.max_collen; max_ops = sc.max_ops; max_pk = sc.max_pk;
+    max_head = sc.max_head; max_fw = sc.max_fw;
     d.n_bus = sc.n_bus; d.n_u = sc.n_u; d.n_a = sc.n_a; d.n_slots = sc.n_slots;
     d.n_off = std::max(sc.n_off, 1); d.n_levels = sc.n_levels; d.n_phases = sc.n_phases;
     d.nnz_y = (int)yi_h.size();
+    d.fuse_fwd = sc.fuse_fwd ? 1 : 0;
     d.yp = yp.as<int32_t>(); d.yi = yi.as<int32_t>(); d.yre = yre.as<double>(); d.yim = yim.as<double>();
     d.bus_rowP = bus_rowP.as<int32_t>(); d.bus_rowQ = bus_rowQ.as<int32_t>();
     d.bus_colA = bus_colA.as<int32_t>(); d.bus_colV = bus_colV.as<int32_t>();
@@ -196,7 +210,7 @@ struct DevSchedule {
     d.a_yslot = a_yslot.as<int32_t>(); d.a_dst = a_dst.as<int32_t>();
     d.lev_ptr = lev_ptr.as<int32_t>(); d.lev_cols = lev_cols.as<int32_t>();
     d.c_base = c_base.as<int32_t>(); d.c_ulen = c_ulen.as<int32_t>(); d.c_llen = c_llen.as<int32_t>();
-    d.c_abeg = c_abeg.as<int32_t>(); d.op_ptr = op_ptr.as<int32_t>();
+    d.c_abeg = c_abeg.as<int32_t>(); d.c_aend = c_aend.as<int32_t>(); d.op_ptr = op_ptr.as<int32_t>();
     d.op_slot = op_slot.as<int32_t>(); d.op_pos = op_pos.as<uint32_t>();
     d.ph_ptr = ph_ptr.as<int32_t>(); d.ph_rows = ph_rows.as<int32_t>(); d.ph_kind = ph_kind.as<int32_t>();
     d.fw_ptr = fw_ptr.as<int32_t>(); d.fw_slot = fw_slot.as<int32_t>(); d.fw_col = fw_col.as<int32_t>();
@@ -209,7 +223,7 @@ struct DevSchedule {
 struct DevBatch {
   int G = 0, prec = -1, max_iter = 0;
   DevMem vm, va, e, f, psp, qsp, eT, fT, ivT, pT, qT, jbuf, lu, off, rhs, sol;
-  DevMem status, iters, sing, piv, maxmis, hist, gact, nactive, err;
+  DevMem status, iters, sing, piv, maxmis, maxacc, hist, gact, nactive, err;
   DevMem o_slot, o_bf, o_bt, o_dre, o_dim;
   DevMem in_stage, out_stage;  // host I/O staging (row-major)
 
@@ -226,6 +240,7 @@ struct DevBatch {
     const size_t ns = (size_t)G_ * 32;
     status.ensure(ns * 4); iters.ensure(ns * 4); sing.ensure(ns * 4); piv.ensure(ns * 4);
     maxmis.ensure(ns * 8);
+    maxacc.ensure(ns * 8);
     if (want_hist) hist.ensure(ns * std::max(max_iter_, 1) * 8);
     gact.ensure((size_t)G_ * 4); nactive.ensure(16); err.ensure(16);
     o_slot.ensure(ns * 16); o_bf.ensure(ns * 4); o_bt.ensure(ns * 4);
@@ -242,6 +257,7 @@ struct DevBatch {
     D.jbuf = jbuf.p; D.lu = lu.p; D.off = off.p; D.rhs = rhs.p; D.sol = sol.p;
     D.status = status.as<int32_t>(); D.iters = iters.as<int32_t>(); D.sing = sing.as<int32_t>();
     D.piv_flag = piv.as<int32_t>(); D.maxmis = maxmis.as<double>();
+    D.maxacc = maxacc.as<unsigned long long>();
     D.hist = want_hist ? hist.as<double>() : nullptr;
     D.gact = gact.as<int32_t>(); D.nactive = nactive.as<int32_t>();
     D.o_slot = outage ? o_slot.as<int32_t>() : nullptr;
@@ -250,6 +266,7 @@ struct DevBatch {
     D.o_dre = outage ? o_dre.as<double>() : nullptr;
     D.o_dim = outage ? o_dim.as<double>() : nullptr;
     D.piv_tol = prec == GOX_PRECISION_MIXED ? 1e-6f : 0.0f;
+    D.err = err.as<int32_t>() + 1;
     return D;
   }
 };
@@ -269,29 +286,64 @@ struct Timing {
 // Launches one NR iteration's kernels for precision T.
 template <typename T>
 struct Iter {
-  static void mismatch(const SchedDev& S, const BatchDev& D, int it, int mode, bool outage,
-                       cudaStream_t st) {
-    dim3 grid(D.G), block(32 * kWarps);
-    if (outage) k_mismatch<T, true><<<grid, block, 0, st>>>(S, D, it, mode);
-    else k_mismatch<T, false><<<grid, block, 0, st>>>(S, D, it, mode);
+  // K5 + K1: update, injections / mismatch, decision.  Returns launches.
+  static int mismatch(const SchedDev& S, const BatchDev& D, int it, int mode, bool outage,
+                      cudaStream_t st) {
+    constexpr int BPW = 4;
+    dim3 gu((S.n_bus + 7) / 8, D.G);
+    k_update<T><<<gu, 256, 0, st>>>(S, D, it, mode);
+    if (mode == 0) {
+      dim3 gi((S.n_bus + 8 * BPW - 1) / (8 * BPW), D.G);
+      if (outage) k_inject<T, true, BPW><<<gi, 256, 0, st>>>(S, D, it);
+      else k_inject<T, false, BPW><<<gi, 256, 0, st>>>(S, D, it);
+    }
+    k_decide<<<D.G, 32, 0, st>>>(D, it, mode);
+    return mode == 0 ? 3 : 2;
   }
   static void fill(const SchedDev& S, const BatchDev& D, bool outage, cudaStream_t st) {
     const int per_warp = 32;
-    int warps = (S.n_a + per_warp - 1) / per_warp;
+    int warps = (S.n_slots + S.n_off_real + per_warp - 1) / per_warp;
     dim3 grid((warps + kWarps - 1) / kWarps, D.G), block(32 * kWarps);
     if (outage) k_fill<T, true><<<grid, block, 0, st>>>(S, D, per_warp);
     else k_fill<T, false><<<grid, block, 0, st>>>(S, D, per_warp);
   }
-  static int stage_cap(const SchedDev& S, int max_collen) {
-    size_t budget = 200 * 1024;  // dynamic shared memory per CTA
-    int cap = (int)(budget / ((size_t)kWarps * 32 * sizeof(T)));
-    return std::max(1, std::min(cap, max_collen));
+  // Launch shape of the refactor: warps per CTA and the per-warp shared
+  // memory slices (packet double buffer, stage, update window, data window),
+  // within ~220 KB per CTA.
+  struct Plan { int nw, cap, opcap, pkcap, dcap; size_t smem; };
+  // Windows first, warps second: a column whose updates overflow the
+  // update window pays a synchronous round trip per refill, which costs far
+  // more than the extra warps gain on wide levels.
+  static Plan plan(const DevSchedule& ds) {
+    const size_t budget = 220 * 1024;
+    Plan p{};
+    auto per_warp = [&](const Plan& q) {
+      size_t b = (size_t)2 * q.pkcap * 4 + (size_t)q.opcap * 8 +
+                 ((size_t)q.cap + q.opcap + q.dcap) * 32 * sizeof(T);
+      return (b + 127) & ~(size_t)127;
+    };
+    const int head = (ds.max_head + 3) & ~3;
+    for (int nw : {8, 6, 4}) {
+      p.nw = nw;
+      p.cap = std::max(8, std::min(ds.max_collen, sizeof(T) == 4 ? 96 : 72));
+      p.opcap = std::max(8, std::min(ds.max_ops, sizeof(T) == 4 ? 128 : 64));
+      p.pkcap = std::max(head, std::min((ds.max_pk + 3) & ~3, 512));
+      p.dcap = std::max(4, std::min(2 * ds.max_fw + 1, 40));
+      while ((size_t)nw * per_warp(p) > budget && p.pkcap > std::max(head, 256))
+        p.pkcap = std::max(head, p.pkcap - 64);
+      while ((size_t)nw * per_warp(p) > budget && p.dcap > 24) p.dcap -= 4;
+      while ((size_t)nw * per_warp(p) > budget && p.opcap > 48) p.opcap -= 8;
+      while ((size_t)nw * per_warp(p) > budget && p.cap > std::min(ds.max_collen, 48)) p.cap -= 8;
+      p.smem = (size_t)nw * per_warp(p);
+      if (p.smem <= budget) return p;
+    }
+    return p;
   }
-  static void refactor(const SchedDev& S, const BatchDev& D, int cap, cudaStream_t st) {
-    size_t smem = (size_t)kWarps * cap * 32 * sizeof(T);
+  static void refactor(const DevSchedule& ds, const BatchDev& D, cudaStream_t st) {
+    const Plan p = plan(ds);
     GOX_CK(cudaFuncSetAttribute(k_refactor<T>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                (int)std::max<size_t>(smem, 1)));
-    k_refactor<T><<<D.G, 32 * kWarps, smem, st>>>(S, D, cap);
+                                (int)p.smem));
+    k_refactor<T><<<D.G, 32 * p.nw, p.smem, st>>>(ds.d, D, p.cap, p.opcap, p.pkcap, p.dcap);
   }
   static void solve(const SchedDev& S, const BatchDev& D, cudaStream_t st) {
     k_solve<T><<<D.G, 32 * kWarps, 0, st>>>(S, D);
@@ -312,7 +364,7 @@ struct gox_topo {
   JacPattern jac;
   Csc csc;
   Symbolic sym;
-  bool factored = false;
+  bool factored = false, uploaded = false;
   Numeric num;
   Schedule sc;
   DevSchedule dsched;
@@ -398,8 +450,8 @@ static int fix_pivots(gox_topo* t, int B, const double* p_spec, const double* q_
     if (klu_factor(t->csc, packed.data(), t->sym, 0.001, N) == 0) {
       t->num = std::move(N);
       build_schedule(&t->jac, t->csc, t->sym, t->num, t->sc);
-      t->dsched.load(t->sc, t->yp, t->yi, t->yre, t->yim);
       t->factored = true;
+      t->uploaded = false;
       (void)nu;
       return s;
     }
@@ -412,7 +464,6 @@ template <typename T>
 static void run_iterations(gox_topo* t, BatchDev D, int max_iter, bool outage, cudaStream_t st,
                            int32_t* h_nactive) {
   const SchedDev& S = t->dsched.d;
-  const int cap = Iter<T>::stage_cap(S, t->sc.max_collen);
   const bool timing = t->timing.on;
   // events: per iteration [k1 start, k1 end, k2 end, k3 end, k4 end]; read once at the end
   std::vector<cudaEvent_t> ev;
@@ -429,25 +480,21 @@ static void run_iterations(gox_topo* t, BatchDev D, int max_iter, bool outage, c
   for (it = 0; it < max_iter; it++) {
     GOX_CK(cudaMemsetAsync(D.nactive, 0, sizeof(int32_t), st));
     rec();
-    Iter<T>::mismatch(S, D, it, 0, outage, st);
-    t->launches++;
+    t->launches += Iter<T>::mismatch(S, D, it, 0, outage, st);
     rec();
     GOX_CK(cudaMemcpyAsync(h_nactive, D.nactive, sizeof(int32_t), cudaMemcpyDeviceToHost, st));
     GOX_CK(cudaStreamSynchronize(st));
     if (*h_nactive == 0) break;
     Iter<T>::fill(S, D, outage, st);
     rec();
-    Iter<T>::refactor(S, D, cap, st);
+    Iter<T>::refactor(t->dsched, D, st);
     rec();
     Iter<T>::solve(S, D, st);
     rec();
     t->launches += 3;
     GOX_CK(cudaGetLastError());
   }
-  if (it == max_iter) {
-    Iter<T>::mismatch(S, D, max_iter, 1, outage, st);
-    t->launches++;
-  }
+  if (it == max_iter) t->launches += Iter<T>::mismatch(S, D, max_iter, 1, outage, st);
   rec();
   GOX_CK(cudaGetLastError());
   if (timing) {
@@ -523,6 +570,10 @@ static int batch_device(gox_topo* t, int B, const double* p_spec, const double* 
     // every candidate factorization was singular: evaluate the mismatch
     // only, with a one-iteration budget that never reaches a solve.
   }
+  if (t->factored && !t->uploaded) {
+    t->dsched.load(t->sc, t->yp, t->yi, t->yre, t->yim);
+    t->uploaded = true;
+  }
   const SchedDev& S = t->dsched.d;
   DevBatch& DB = t->batch;
   if (t->factored) {
@@ -538,7 +589,7 @@ static int batch_device(gox_topo* t, int B, const double* p_spec, const double* 
   k_scatter_rows<<<grid1d(tot), 256, 0, st>>>(vm0, B, n, v_stride, D.vm, G);
   k_scatter_rows<<<grid1d(tot), 256, 0, st>>>(va0, B, n, v_stride, D.va, G);
   k_init_scen<<<(G * 32 + 255) / 256, 256, 0, st>>>(B, G, D.status, D.iters, D.sing, D.piv_flag,
-                                                     D.maxmis);
+                                                     D.maxmis, D.maxacc);
   t->launches += 5;
   if (want_hist) GOX_CK(cudaMemsetAsync(D.hist, 0, (size_t)G * 32 * max_iter * 8, st));
   if (outage) {
@@ -560,6 +611,7 @@ static int batch_device(gox_topo* t, int B, const double* p_spec, const double* 
       GOX_CK(cudaMemcpyAsync(D.sing + s, ones.data(), 4, cudaMemcpyHostToDevice, st));
     GOX_CK(cudaStreamSynchronize(st));
   }
+  GOX_CK(cudaMemsetAsync(DB.err.p, 0, 16, st));
   int32_t* h_nactive = nullptr;
   GOX_CK(cudaMallocHost(&h_nactive, sizeof(int32_t)));
   try {
@@ -570,6 +622,12 @@ static int batch_device(gox_topo* t, int B, const double* p_spec, const double* 
     throw;
   }
   cudaFreeHost(h_nactive);
+  {
+    int32_t herr[2] = {0, 0};
+    GOX_CK(cudaMemcpyAsync(herr, DB.err.p, 8, cudaMemcpyDeviceToHost, st));
+    GOX_CK(cudaStreamSynchronize(st));
+    if (herr[1]) return GOX_E_DEVICE_WAIT;
+  }
   // outputs
   k_gather_rows<<<grid1d((size_t)B * n), 256, 0, st>>>(D.vm, B, n, G, vm_out);
   k_gather_rows<<<grid1d((size_t)B * n), 256, 0, st>>>(D.va, B, n, G, va_out);
@@ -676,6 +734,7 @@ int gox_topo_register(int32_t n_bus, const int32_t* yp, const int32_t* yi, const
 int gox_topo_reset(gox_topo* t) {
   if (!t) return GOX_E_INVALID;
   t->factored = false;
+  t->uploaded = false;
   t->num = Numeric();
   t->sc = Schedule();
   return GOX_OK;
@@ -847,6 +906,93 @@ int gox_batch_solve(gox_topo* t, int32_t B, const double* p_spec, const double* 
   });
 }
 
+int gox_topo_prepare(gox_topo* t, int32_t B, const double* p_spec, const double* q_spec,
+                     const double* vm0, const double* va0, int32_t v_stride,
+                     const int32_t* o_slot, const double* o_dre, const double* o_dim, double tol) {
+  if (!t || B <= 0 || !p_spec || !q_spec || !vm0 || !va0 || !(tol >= 0)) return GOX_E_INVALID;
+  if (v_stride != 0 && v_stride != t->n_bus) return GOX_E_INVALID;
+  if (o_slot && (!o_dre || !o_dim)) return GOX_E_INVALID;
+  return guard_impl([&]() -> int {
+    if (t->factored) return GOX_OK;
+    std::vector<int> first_singular;
+    int s = fix_pivots(t, B, p_spec, q_spec, vm0, va0, v_stride, o_slot, o_dre, o_dim, tol,
+                       first_singular);
+    return s < 0 ? GOX_SINGULAR : GOX_OK;
+  });
+}
+
+// Host mirror of k_refactor (+ fused forward) and k_solve for one scenario:
+// same batches, stage positions, phases and term lists, FP64.
+int gox_topo_emulate_step(const gox_topo* t, const double* jac_vals, const double* rhs,
+                          double* dx) {
+  if (!t || !t->factored || !jac_vals || !rhs || !dx) return GOX_E_INVALID;
+  return guard_impl([&]() -> int {
+    const Schedule& sc = t->sc;
+    const int n = sc.n_u;
+    std::vector<double> lu(sc.n_slots, 0.0), off(std::max(sc.n_off, 1), 0.0), X(n, 0.0),
+        b(n), st(sc.max_collen);
+    for (int u = 0; u < n; u++) b[t->num.Pinv[u]] = rhs[u];
+    // A values in consumption order
+    std::vector<double> packed(t->csc.nnz(), 0.0);
+    for (int e = 0; e < t->jac.nnz(); e++) packed[t->csc.slot_of[e]] += jac_vals[e];
+    bool bad = false;
+    for (int lv = 0; lv < sc.n_levels; lv++) {
+      for (int q = sc.lev_ptr[lv]; q < sc.lev_ptr[lv + 1]; q++) {
+        const int k = sc.lev_cols[q];
+        const int ulen = sc.c_ulen[k], llen = sc.c_llen[k], len = ulen + 1 + llen;
+        for (int p = 0; p < len; p++) {
+          const int a = sc.slot_a[sc.c_base[k] + p];
+          st[p] = a >= 0 ? packed[sc.a_csc[a]] : 0.0;
+        }
+        for (int a = sc.c_abeg[k]; a < sc.c_aend[k]; a++)
+          if (sc.a_dst[a] < 0) off[-sc.a_dst[a] - 1] = packed[sc.a_csc[a]];
+        int o = sc.op_ptr[k];
+        for (int bt = sc.bt_ptr[k]; bt < sc.bt_ptr[k + 1]; bt++) {
+          const int cnt = sc.bt_cnt[bt];
+          double xd[kMaxBatch], xu[kMaxBatch];
+          for (int c = 0; c < cnt; c++) {
+            xd[c] = st[sc.op_pos[o + c] & 0xffff];
+            xu[c] = st[sc.op_pos[o + c] >> 16];
+          }
+          for (int c = 0; c < cnt; c++) st[sc.op_pos[o + c] & 0xffff] = xd[c] - lu[sc.op_slot[o + c]] * xu[c];
+          o += cnt;
+        }
+        const double piv = st[ulen];
+        if (piv == 0.0) bad = true;
+        const double inv = 1.0 / piv;
+        for (int p = 0; p <= ulen; p++) lu[sc.c_base[k] + p] = st[p];
+        for (int p = ulen + 1; p < len; p++) lu[sc.c_base[k] + p] = st[p] * inv;
+        if (sc.fuse_fwd) {
+          double y = b[k];
+          for (int tt = sc.fw_ptr[k]; tt < sc.fw_ptr[k + 1]; tt++) y -= lu[sc.fw_slot[tt]] * X[sc.fw_col[tt]];
+          X[k] = y;
+        }
+      }
+    }
+    for (int ph = 0; ph < sc.n_phases; ph++) {
+      for (int q = sc.ph_ptr[ph]; q < sc.ph_ptr[ph + 1]; q++) {
+        const int k = sc.ph_rows[q];
+        if (sc.ph_kind[ph] == 0) {
+          double v = b[k];
+          for (int tt = sc.fw_ptr[k]; tt < sc.fw_ptr[k + 1]; tt++) {
+            const int sl = sc.fw_slot[tt];
+            v -= (sl >= 0 ? lu[sl] : off[-sl - 1]) * X[sc.fw_col[tt]];
+          }
+          X[k] = v;
+        } else {
+          double v = X[k];
+          for (int tt = sc.bw_ptr[k]; tt < sc.bw_ptr[k + 1]; tt++) v -= lu[sc.bw_slot[tt]] * X[sc.bw_col[tt]];
+          v = v / lu[sc.diag_slot[k]];
+          if (!std::isfinite(v)) bad = true;
+          X[k] = v;
+        }
+      }
+    }
+    for (int k = 0; k < n; k++) dx[t->sym.Q[k]] = X[k];
+    return bad ? GOX_SINGULAR : GOX_OK;
+  });
+}
+
 int gox_topo_info(const gox_topo* t, int64_t* info) {
   if (!t || !info || !t->factored) return GOX_E_INVALID;
   const Schedule& sc = t->sc;
@@ -944,13 +1090,20 @@ static int ls_run(gox_ls* h, const double* vals, const double* rhs, double* x) {
   // pack duplicates, A order, replicate to all 32 lanes
   std::fill(h->packed.begin(), h->packed.end(), 0.0);
   for (size_t e = 0; e < h->rows.size(); e++) h->packed[h->csc.slot_of[e]] += vals[e];
-  h->hostbuf.assign((size_t)S.n_a * 32, 0.0);
-  for (int k = 0; k < n; k++) {
-    int oldcol = h->sym.Q[k];
-    for (int p = h->csc.p[oldcol], a = h->sc.c_abeg[k]; p < h->csc.p[oldcol + 1]; p++, a++)
-      for (int l = 0; l < 32; l++) h->hostbuf[(size_t)a * 32 + l] = h->packed[p];
+  // A values in the factor's layout (zeros at fill-in), replicated to 32 lanes
+  h->hostbuf.assign((size_t)S.n_slots * 32, 0.0);
+  for (int x = 0; x < S.n_slots; x++) {
+    const int a = h->sc.slot_a[x];
+    if (a >= 0)
+      for (int l = 0; l < 32; l++) h->hostbuf[(size_t)x * 32 + l] = h->packed[h->sc.a_csc[a]];
   }
-  GOX_CK(cudaMemcpy(h->jbuf.p, h->hostbuf.data(), h->hostbuf.size() * 8, cudaMemcpyHostToDevice));
+  GOX_CK(cudaMemcpy(h->lu.p, h->hostbuf.data(), h->hostbuf.size() * 8, cudaMemcpyHostToDevice));
+  if (h->sc.n_off > 0) {
+    std::vector<double> ob((size_t)h->sc.n_off * 32, 0.0);
+    for (int x = 0; x < h->sc.n_off; x++)
+      for (int l = 0; l < 32; l++) ob[(size_t)x * 32 + l] = h->packed[h->sc.a_csc[h->sc.off_a[x]]];
+    GOX_CK(cudaMemcpy(h->off.p, ob.data(), ob.size() * 8, cudaMemcpyHostToDevice));
+  }
   std::vector<double> b((size_t)n * 32);
   for (int k = 0; k < n; k++)
     for (int l = 0; l < 32; l++) b[(size_t)k * 32 + l] = rhs[h->num.Pnum[k]];
@@ -961,10 +1114,14 @@ static int ls_run(gox_ls* h, const double* vals, const double* rhs, double* x) {
   D.jbuf = h->jbuf.p; D.lu = h->lu.p; D.off = h->off.p; D.rhs = h->rhs.p; D.sol = h->sol.p;
   D.sing = h->sing.as<int32_t>(); D.piv_flag = h->piv.as<int32_t>(); D.gact = h->gact.as<int32_t>();
   D.piv_tol = 0.0f;
-  int cap = Iter<double>::stage_cap(S, h->sc.max_collen);
-  Iter<double>::refactor(S, D, cap, nullptr);
+  D.err = h->status.as<int32_t>() + 8;
+  GOX_CK(cudaMemset(h->status.p, 0, 128));
+  Iter<double>::refactor(h->dsched, D, nullptr);
   Iter<double>::solve(S, D, nullptr);
   GOX_CK(cudaGetLastError());
+  int32_t werr = 0;
+  GOX_CK(cudaMemcpy(&werr, h->status.as<int32_t>() + 8, 4, cudaMemcpyDeviceToHost));
+  if (werr) return GOX_E_DEVICE_WAIT;
   std::vector<double> X((size_t)n * 32);
   int32_t sing = 0;
   GOX_CK(cudaMemcpy(X.data(), h->sol.p, X.size() * 8, cudaMemcpyDeviceToHost));

@@ -218,6 +218,35 @@ class Topology:
             raise BatchError("BusOutOfRange", rc)
         check(rc, "gox_batch_solve_device")
 
+    def prepare(self, p_spec, q_spec, vm0, va0, tol=1e-8, outage=None):
+        """Fix the pivot order on the host (no GPU needed); see gox_topo_prepare."""
+        L = _lib.load()
+        p_spec = _f64(np.atleast_2d(p_spec))
+        q_spec = _f64(np.atleast_2d(q_spec))
+        vm0, va0 = _f64(vm0), _f64(va0)
+        stride = self.n_bus if vm0.ndim == 2 else 0
+        sl, dr, di = (None, None, None) if outage is None else (
+            _i32(outage[0]), _f64(outage[1]), _f64(outage[2]))
+        rc = L.gox_topo_prepare(self._h, p_spec.shape[0], _p(p_spec, _lib.f64p),
+                                _p(q_spec, _lib.f64p), _p(vm0, _lib.f64p), _p(va0, _lib.f64p),
+                                stride, _p(sl, _lib.i32p), _p(dr, _lib.f64p), _p(di, _lib.f64p),
+                                float(tol))
+        if rc == GOX_SINGULAR:
+            return False
+        check(rc, "gox_topo_prepare")
+        return True
+
+    def emulate_step(self, jac_vals, rhs) -> Optional[np.ndarray]:
+        """Host FP64 mirror of the device refactor + solve schedule."""
+        L = _lib.load()
+        dx = np.zeros(len(rhs))
+        rc = L.gox_topo_emulate_step(self._h, _p(_f64(jac_vals), _lib.f64p),
+                                     _p(_f64(rhs), _lib.f64p), _p(dx, _lib.f64p))
+        if rc == GOX_SINGULAR:
+            return None
+        check(rc, "gox_topo_emulate_step")
+        return dx
+
     def info(self) -> dict:
         a = np.zeros(10, np.int64)
         check(_lib.load().gox_topo_info(self._h, _p(a, _lib.i64p)), "gox_topo_info")

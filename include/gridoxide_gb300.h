@@ -41,6 +41,7 @@ extern "C" {
 #define GOX_E_PATTERN (-6)      /* values given for a different pattern */
 #define GOX_E_NO_DEVICE (-7)    /* no CUDA device visible */
 #define GOX_E_TOO_LARGE (-8)    /* request exceeds a documented size limit */
+#define GOX_E_DEVICE_WAIT (-9)  /* a bounded wait inside a kernel gave up; results invalid */
 
 /* per-scenario outcome, solver::SolveStatus (src/solver.rs:162-171) */
 #define GOX_CONVERGED 0
@@ -134,6 +135,24 @@ int gox_batch_solve_device(gox_topo *t, int32_t B, const double *p_spec, const d
                            int32_t precision, double *vm_out, double *va_out,
                            int32_t *iterations, int32_t *status, double *max_mismatch,
                            double *history, void *stream);
+
+/* Fixes the topology's pivot order on the host, without a GPU: the first
+ * scenario whose start point misses `tol` has its Jacobian factored with
+ * partial pivoting (KluNativeSystem::new on the first Jacobian a
+ * PersistentSolver sees, src/solver.rs:711-713).  Arguments as for
+ * gox_batch_solve.  A later gox_batch_solve* reuses this order.  Returns
+ * GOX_SINGULAR if no scenario's Jacobian factors. */
+int gox_topo_prepare(gox_topo *t, int32_t B, const double *p_spec, const double *q_spec,
+                     const double *vm0, const double *va0, int32_t v_stride,
+                     const int32_t *out_slot, const double *out_dre, const double *out_dim,
+                     double tol);
+
+/* Host mirror of the device refactor + substitution schedule for one
+ * scenario, in FP64: Jacobian values in emission order, right-hand side in
+ * unknown order, solution dx in unknown order.  Needs a fixed pivot order.
+ * Returns GOX_SINGULAR on a zero pivot or non-finite dx. */
+int gox_topo_emulate_step(const gox_topo *t, const double *jac_vals, const double *rhs,
+                          double *dx);
 
 /* ---- inspection (klu_analyze / klu_extract analogues) ------------------ */
 
