@@ -58,6 +58,7 @@ SIGNATURES = {
     "gox_ls_factor_solve_values": (C.c_int, [vp, f64p, f64p, f64p]),
     "gox_ls_factor_solve": (C.c_int, [vp, C.c_int32, i32p, i32p, f64p, f64p, f64p]),
     "gox_ls_destroy": (None, [vp]),
+    "gox_ls_factor_solve_values_static": (C.c_int, [vp, f64p, f64p, f64p]),
     "gox_topo_register": (C.c_int, [C.c_int32, i32p, i32p, f64p, f64p, i32p, C.POINTER(vp)]),
     "gox_topo_reset": (C.c_int, [vp]),
     "gox_topo_destroy": (None, [vp]),

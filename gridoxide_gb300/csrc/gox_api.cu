@@ -9,6 +9,7 @@
 #include <cstdio>
 #include <cstring>
 #include <memory>
+#include <mutex>
 #include <new>
 #include <stdexcept>
 #include <string>
@@ -1151,3 +1152,132 @@ int gox_ls_factor_solve(gox_ls* h, int32_t nnz, const int32_t* rows, const int32
 void gox_ls_destroy(gox_ls* h) { delete h; }
 
 }  // extern "C"
+
+// ---- static-scratch LinearSolver variant --------------------------------------
+// The scratch of gox_ls_factor_solve_values_static: one fixed device array per
+// process (per device), so the call never allocates.  Host code must not take
+// its address directly (that is a host-side stand-in); it asks the runtime
+// for the device address once per device and passes that to the kernels.
+namespace gox {
+static __device__ __align__(256) unsigned char g_static_scratch[GOX_STATIC_SCRATCH_BYTES];
+static void* g_static_addr[256];
+static std::mutex g_static_mu;
+
+static int static_scratch(void** out) {
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 256) {
+    cudaGetLastError();
+    return GOX_E_CUDA;
+  }
+  std::lock_guard<std::mutex> lk(g_static_mu);
+  if (!g_static_addr[dev]) {
+    void* p = nullptr;
+    cudaError_t e = cudaGetSymbolAddress(&p, g_static_scratch);
+    if (e != cudaSuccess || !p) {
+      cudaGetLastError();
+      return GOX_E_CUDA;
+    }
+    g_static_addr[dev] = p;
+  }
+  *out = g_static_addr[dev];
+  return GOX_OK;
+}
+
+// Builds the factor's starting image (A values in the LU layout, zeros at
+// fill-in, replicated to the 32 lanes), the permuted right-hand side, and
+// clears the flags.
+__global__ void k_static_prepare(SchedDev S, const double* packed, const int32_t* acsc,
+                                 const double* rhs_raw, const int32_t* pnum, int n, double* lu,
+                                 double* off, double* rhsb, int32_t* flags) {
+  const size_t total = ((size_t)S.n_slots + (size_t)S.n_off_real + (size_t)n) * 32u;
+  for (size_t t = blockIdx.x * (size_t)blockDim.x + threadIdx.x; t < total;
+       t += (size_t)gridDim.x * blockDim.x) {
+    const size_t e = t >> 5;
+    if (e < (size_t)S.n_slots) {
+      const int a = S.slot_a[e];
+      lu[t] = a >= 0 ? packed[acsc[a]] : 0.0;
+    } else if (e < (size_t)S.n_slots + S.n_off_real) {
+      const size_t o = e - S.n_slots;
+      off[o * 32 + (t & 31)] = packed[acsc[S.off_a[o]]];
+    } else {
+      const size_t k = e - S.n_slots - S.n_off_real;
+      rhsb[k * 32 + (t & 31)] = rhs_raw[pnum[k]];
+    }
+  }
+  if (blockIdx.x == 0 && threadIdx.x < 128) flags[threadIdx.x] = (threadIdx.x == 64) ? 1 : 0;
+}
+
+// x[Q[k]] = X[k] (lane 0), flagging non-finite values.
+__global__ void k_static_finish(const double* sol, const int32_t* qperm, int n, double* xout,
+                                int32_t* flags) {
+  for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < n; k += gridDim.x * blockDim.x) {
+    const double v = sol[(size_t)k * 32];
+    xout[qperm[k]] = v;
+    if (!isfinite(v)) flags[96] = 1;
+  }
+}
+}  // namespace gox
+
+extern "C" int gox_ls_factor_solve_values_static(gox_ls* h, const double* vals,
+                                                 const double* rhs, double* x) {
+  if (!h || (!vals && !h->rows.empty()) || !rhs || !x) return GOX_E_INVALID;
+  return guard_impl([&]() -> int {
+    const SchedDev& S = h->dsched.d;
+    const int n = h->n;
+    // carve the fixed array: 256-byte aligned regions
+    size_t off = 0;
+    auto take = [&](size_t bytes) {
+      size_t o = off;
+      off += (bytes + 255) & ~(size_t)255;
+      return o;
+    };
+    const size_t o_lu = take((size_t)S.n_slots * 32 * 8);
+    const size_t o_off = take((size_t)std::max(S.n_off_real, 1) * 32 * 8);
+    const size_t o_rhs = take((size_t)n * 32 * 8);
+    const size_t o_sol = take((size_t)n * 32 * 8);
+    const size_t o_pk = take((size_t)h->csc.nnz() * 8);
+    const size_t o_acsc = take((size_t)S.n_a * 4);
+    const size_t o_rraw = take((size_t)n * 8);
+    const size_t o_pnum = take((size_t)n * 4);
+    const size_t o_q = take((size_t)n * 4);
+    const size_t o_x = take((size_t)n * 8);
+    const size_t o_fl = take(128 * 4);
+    if (off > (size_t)GOX_STATIC_SCRATCH_BYTES) return GOX_E_TOO_LARGE;
+    void* base = nullptr;
+    if (int r = static_scratch(&base)) return r;
+    unsigned char* B = static_cast<unsigned char*>(base);
+    // values of the CSC slots (duplicates summed), as gox_ls_factor_solve_values
+    std::fill(h->packed.begin(), h->packed.end(), 0.0);
+    for (size_t e = 0; e < h->rows.size(); e++) h->packed[h->csc.slot_of[e]] += vals[e];
+    GOX_CK(cudaMemcpy(B + o_pk, h->packed.data(), h->packed.size() * 8, cudaMemcpyHostToDevice));
+    GOX_CK(cudaMemcpy(B + o_acsc, h->sc.a_csc.data(), (size_t)S.n_a * 4, cudaMemcpyHostToDevice));
+    GOX_CK(cudaMemcpy(B + o_rraw, rhs, (size_t)n * 8, cudaMemcpyHostToDevice));
+    GOX_CK(cudaMemcpy(B + o_pnum, h->num.Pnum.data(), (size_t)n * 4, cudaMemcpyHostToDevice));
+    GOX_CK(cudaMemcpy(B + o_q, h->sym.Q.data(), (size_t)n * 4, cudaMemcpyHostToDevice));
+    int32_t* flags = reinterpret_cast<int32_t*>(B + o_fl);  // [0,32) sing [32,64) piv [64] gact [96] non-finite [100..] wait errors
+    const size_t work = ((size_t)S.n_slots + S.n_off_real + n) * 32;
+    k_static_prepare<<<grid1d(work), 256>>>(S, reinterpret_cast<double*>(B + o_pk),
+                                            reinterpret_cast<int32_t*>(B + o_acsc),
+                                            reinterpret_cast<double*>(B + o_rraw),
+                                            reinterpret_cast<int32_t*>(B + o_pnum), n,
+                                            reinterpret_cast<double*>(B + o_lu),
+                                            reinterpret_cast<double*>(B + o_off),
+                                            reinterpret_cast<double*>(B + o_rhs), flags);
+    BatchDev D{};
+    D.G = 1;
+    D.lu = B + o_lu; D.off = B + o_off; D.rhs = B + o_rhs; D.sol = B + o_sol;
+    D.sing = flags; D.piv_flag = flags + 32; D.gact = flags + 64; D.err = flags + 100;
+    D.piv_tol = 0.0f;
+    Iter<double>::refactor(h->dsched, D, nullptr);
+    Iter<double>::solve(S, D, nullptr);
+    k_static_finish<<<grid1d((size_t)n), 256>>>(reinterpret_cast<double*>(B + o_sol),
+                                                reinterpret_cast<int32_t*>(B + o_q), n,
+                                                reinterpret_cast<double*>(B + o_x), flags);
+    GOX_CK(cudaGetLastError());
+    int32_t hf[128];
+    GOX_CK(cudaMemcpy(hf, flags, sizeof(hf), cudaMemcpyDeviceToHost));
+    GOX_CK(cudaMemcpy(x, B + o_x, (size_t)n * 8, cudaMemcpyDeviceToHost));
+    if (hf[100]) return GOX_E_DEVICE_WAIT;
+    return (hf[0] || hf[96]) ? GOX_SINGULAR : GOX_OK;
+  });
+}

@@ -94,6 +94,21 @@ class Gb300LinearSolver:
         check(rc, "gox_ls_factor_solve_values")
         return x
 
+    def factor_and_solve_values_static(self, values, rhs) -> Optional[np.ndarray]:
+        """As factor_and_solve_values, allocating no device memory: for callers
+        that cannot allocate at solve time (inside a stream capture, under an
+        allocator that owns all device memory, or in a latency-critical loop).
+        Its scratch is a fixed array inside the library, shared by every call
+        (serialize calls; see gox_ls_factor_solve_values_static)."""
+        L = _lib.load()
+        x = np.zeros(self.n)
+        rc = L.gox_ls_factor_solve_values_static(self._h, _p(_f64(values), _lib.f64p),
+                                                 _p(_f64(rhs), _lib.f64p), _p(x, _lib.f64p))
+        if rc == GOX_SINGULAR:
+            return None
+        check(rc, "gox_ls_factor_solve_values_static")
+        return x
+
     def factor_and_solve(self, entries, rhs) -> Optional[np.ndarray]:
         L = _lib.load()
         ent = list(entries)
