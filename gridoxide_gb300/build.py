@@ -15,7 +15,7 @@ CSRC = os.path.join(HERE, "csrc")
 OUT = os.path.join(HERE, "libgridoxide_gb300.so")
 OBJ = os.path.join(HERE, "_build")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
-SOURCES = ["gox_symbolic.cpp", "gox_engine.cpp", "gox_api.cu"]
+SOURCES = ["gox_symbolic.cpp", "gox_engine.cpp", "gox_stream.cpp", "gox_api.cu"]
 
 
 def _nvcc() -> str:

@@ -17,6 +17,7 @@
 
 #include "../../include/gridoxide_gb300.h"
 #include "gox_engine.hpp"
+#include "gox_stream.hpp"
 #include "gox_kernels.cuh"
 
 namespace gox {
@@ -175,6 +176,28 @@ struct DevSchedule {
       pk_off, pk, slot_a, off_a;
   SchedDev d{};
   int max_collen = 0, max_ops = 0, max_pk = 0, max_head = 0, max_fw = 0;
+  // refactor command streams, FP32 and FP64 plans
+  DevMem sw[2], sc0[2], snc[2];
+  StreamDev st[2]{};
+  int st_nw[2] = {0, 0};
+  size_t st_smem[2] = {0, 0};
+
+  void load_streams(const Stream& s32, const Stream& s64) {
+    const Stream* ss[2] = {&s32, &s64};
+    for (int i = 0; i < 2; i++) {
+      upload(sw[i], ss[i]->words);
+      upload(sc0[i], ss[i]->chunk0);
+      upload(snc[i], ss[i]->nchunks);
+      st[i].words = sw[i].as<int32_t>();
+      st[i].chunk0 = sc0[i].as<int32_t>();
+      st[i].nchunks = snc[i].as<int32_t>();
+      st[i].ring_rows = ss[i]->plan.ring_rows;
+      st[i].chunk_words = ss[i]->plan.chunk_words;
+      st[i].n_bars = ss[i]->n_bars;
+      st_nw[i] = ss[i]->plan.nw;
+      st_smem[i] = stream_smem_bytes(ss[i]->plan);
+    }
+  }
 
   void load(const Schedule& sc, const std::vector<int32_t>& yp_h, const std::vector<int32_t>& yi_h,
             const std::vector<double>& yre_h, const std::vector<double>& yim_h) {
@@ -279,6 +302,27 @@ static int grid1d(size_t n, int threads = 256) {
 
 static constexpr int kWarps = 8;  // warps per CTA of the group kernels
 
+// Dynamic shared memory the refactor may use per CTA (of 227 KB).
+static constexpr size_t kRefactorSmem = 225 * 1024;
+
+// Compiles the refactor streams of a schedule for both precisions.
+static void make_streams(const Schedule& sc, Stream& s32, Stream& s64) {
+  std::string why;
+  if (!choose_stream(sc, 4, kRefactorSmem, s32, why))
+    throw std::runtime_error("refactor schedule (FP32): " + why);
+  if (!choose_stream(sc, 8, kRefactorSmem, s64, why))
+    throw std::runtime_error("refactor schedule (FP64): " + why);
+  // every stream runs once through the checking host interpreter before a
+  // GPU sees it (indices, copies waited for, no cross-warp conflicts)
+  std::vector<double> lu(sc.n_slots, 1.0), rhs(sc.n_u, 0.0), X;
+  bool sing = false;
+  for (const Stream* s : {&s32, &s64}) {
+    std::fill(lu.begin(), lu.end(), 1.0);
+    const std::string e = run_stream_host(sc, *s, lu, rhs, X, sing);
+    if (!e.empty()) throw std::runtime_error("refactor stream check: " + e);
+  }
+}
+
 struct Timing {
   bool on = false;
   double iters = 0, total = 0, k1 = 0, k2 = 0, k3 = 0, k4 = 0;
@@ -308,43 +352,11 @@ struct Iter {
     if (outage) k_fill<T, true><<<grid, block, 0, st>>>(S, D, per_warp);
     else k_fill<T, false><<<grid, block, 0, st>>>(S, D, per_warp);
   }
-  // Launch shape of the refactor: warps per CTA and the per-warp shared
-  // memory slices (packet double buffer, stage, update window, data window),
-  // within ~220 KB per CTA.
-  struct Plan { int nw, cap, opcap, pkcap, dcap; size_t smem; };
-  // Windows first, warps second: a column whose updates overflow the
-  // update window pays a synchronous round trip per refill, which costs far
-  // more than the extra warps gain on wide levels.
-  static Plan plan(const DevSchedule& ds) {
-    const size_t budget = 220 * 1024;
-    Plan p{};
-    auto per_warp = [&](const Plan& q) {
-      size_t b = (size_t)2 * q.pkcap * 4 + (size_t)q.opcap * 8 +
-                 ((size_t)q.cap + q.opcap + q.dcap) * 32 * sizeof(T);
-      return (b + 127) & ~(size_t)127;
-    };
-    const int head = (ds.max_head + 3) & ~3;
-    for (int nw : {8, 6, 4}) {
-      p.nw = nw;
-      p.cap = std::max(8, std::min(ds.max_collen, sizeof(T) == 4 ? 96 : 72));
-      p.opcap = std::max(8, std::min(ds.max_ops, sizeof(T) == 4 ? 128 : 64));
-      p.pkcap = std::max(head, std::min((ds.max_pk + 3) & ~3, 512));
-      p.dcap = std::max(4, std::min(2 * ds.max_fw + 1, 40));
-      while ((size_t)nw * per_warp(p) > budget && p.pkcap > std::max(head, 256))
-        p.pkcap = std::max(head, p.pkcap - 64);
-      while ((size_t)nw * per_warp(p) > budget && p.dcap > 24) p.dcap -= 4;
-      while ((size_t)nw * per_warp(p) > budget && p.opcap > 48) p.opcap -= 8;
-      while ((size_t)nw * per_warp(p) > budget && p.cap > std::min(ds.max_collen, 48)) p.cap -= 8;
-      p.smem = (size_t)nw * per_warp(p);
-      if (p.smem <= budget) return p;
-    }
-    return p;
-  }
   static void refactor(const DevSchedule& ds, const BatchDev& D, cudaStream_t st) {
-    const Plan p = plan(ds);
+    const int i = sizeof(T) == 4 ? 0 : 1;
     GOX_CK(cudaFuncSetAttribute(k_refactor<T>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                (int)p.smem));
-    k_refactor<T><<<D.G, 32 * p.nw, p.smem, st>>>(ds.d, D, p.cap, p.opcap, p.pkcap, p.dcap);
+                                (int)ds.st_smem[i]));
+    k_refactor<T><<<D.G, 32 * ds.st_nw[i], ds.st_smem[i], st>>>(ds.st[i], ds.d, D);
   }
   static void solve(const SchedDev& S, const BatchDev& D, cudaStream_t st) {
     k_solve<T><<<D.G, 32 * kWarps, 0, st>>>(S, D);
@@ -368,6 +380,7 @@ struct gox_topo {
   bool factored = false, uploaded = false;
   Numeric num;
   Schedule sc;
+  Stream s32, s64;
   DevSchedule dsched;
   DevBatch batch;
   Timing timing;
@@ -382,6 +395,7 @@ struct gox_ls {
   Symbolic sym;
   Numeric num;
   Schedule sc;
+  Stream s32, s64;
   DevSchedule dsched;
   DevMem jbuf, lu, off, rhs, sol, sing, piv, gact, status;
   std::vector<double> packed, hostbuf;
@@ -451,6 +465,7 @@ static int fix_pivots(gox_topo* t, int B, const double* p_spec, const double* q_
     if (klu_factor(t->csc, packed.data(), t->sym, 0.001, N) == 0) {
       t->num = std::move(N);
       build_schedule(&t->jac, t->csc, t->sym, t->num, t->sc);
+      make_streams(t->sc, t->s32, t->s64);
       t->factored = true;
       t->uploaded = false;
       (void)nu;
@@ -573,6 +588,7 @@ static int batch_device(gox_topo* t, int B, const double* p_spec, const double* 
   }
   if (t->factored && !t->uploaded) {
     t->dsched.load(t->sc, t->yp, t->yi, t->yre, t->yim);
+    t->dsched.load_streams(t->s32, t->s64);
     t->uploaded = true;
   }
   const SchedDev& S = t->dsched.d;
@@ -937,39 +953,22 @@ int gox_topo_emulate_step(const gox_topo* t, const double* jac_vals, const doubl
     std::vector<double> packed(t->csc.nnz(), 0.0);
     for (int e = 0; e < t->jac.nnz(); e++) packed[t->csc.slot_of[e]] += jac_vals[e];
     bool bad = false;
-    for (int lv = 0; lv < sc.n_levels; lv++) {
-      for (int q = sc.lev_ptr[lv]; q < sc.lev_ptr[lv + 1]; q++) {
-        const int k = sc.lev_cols[q];
-        const int ulen = sc.c_ulen[k], llen = sc.c_llen[k], len = ulen + 1 + llen;
-        for (int p = 0; p < len; p++) {
-          const int a = sc.slot_a[sc.c_base[k] + p];
-          st[p] = a >= 0 ? packed[sc.a_csc[a]] : 0.0;
-        }
-        for (int a = sc.c_abeg[k]; a < sc.c_aend[k]; a++)
-          if (sc.a_dst[a] < 0) off[-sc.a_dst[a] - 1] = packed[sc.a_csc[a]];
-        int o = sc.op_ptr[k];
-        for (int bt = sc.bt_ptr[k]; bt < sc.bt_ptr[k + 1]; bt++) {
-          const int cnt = sc.bt_cnt[bt];
-          double xd[kMaxBatch], xu[kMaxBatch];
-          for (int c = 0; c < cnt; c++) {
-            xd[c] = st[sc.op_pos[o + c] & 0xffff];
-            xu[c] = st[sc.op_pos[o + c] >> 16];
-          }
-          for (int c = 0; c < cnt; c++) st[sc.op_pos[o + c] & 0xffff] = xd[c] - lu[sc.op_slot[o + c]] * xu[c];
-          o += cnt;
-        }
-        const double piv = st[ulen];
-        if (piv == 0.0) bad = true;
-        const double inv = 1.0 / piv;
-        for (int p = 0; p <= ulen; p++) lu[sc.c_base[k] + p] = st[p];
-        for (int p = ulen + 1; p < len; p++) lu[sc.c_base[k] + p] = st[p] * inv;
-        if (sc.fuse_fwd) {
-          double y = b[k];
-          for (int tt = sc.fw_ptr[k]; tt < sc.fw_ptr[k + 1]; tt++) y -= lu[sc.fw_slot[tt]] * X[sc.fw_col[tt]];
-          X[k] = y;
-        }
-      }
-    }
+    // the factor's starting image (A values, zeros at fill-in), then the
+    // refactor streams of both precisions run by the host interpreter:
+    // both must pass every check and give the same factor
+    for (int x = 0; x < sc.n_slots; x++) lu[x] = sc.slot_a[x] >= 0 ? packed[sc.a_csc[sc.slot_a[x]]] : 0.0;
+    for (int a = 0; a < sc.n_a; a++)
+      if (sc.a_dst[a] < 0) off[-sc.a_dst[a] - 1] = packed[sc.a_csc[a]];
+    std::vector<double> lu64 = lu, X64;
+    bool sing32 = false, sing64 = false;
+    std::string e32 = run_stream_host(sc, t->s32, lu, b, X, sing32);
+    if (!e32.empty()) throw std::runtime_error("FP32 refactor stream: " + e32);
+    std::string e64 = run_stream_host(sc, t->s64, lu64, b, X64, sing64);
+    if (!e64.empty()) throw std::runtime_error("FP64 refactor stream: " + e64);
+    for (int x = 0; x < sc.n_slots; x++)
+      if (!(lu[x] == lu64[x]) && !(std::isnan(lu[x]) && std::isnan(lu64[x])))
+        throw std::runtime_error("the two refactor streams disagree");
+    bad = sing32;
     for (int ph = 0; ph < sc.n_phases; ph++) {
       for (int q = sc.ph_ptr[ph]; q < sc.ph_ptr[ph + 1]; q++) {
         const int k = sc.ph_rows[q];
@@ -1007,6 +1006,13 @@ int gox_topo_info(const gox_topo* t, int64_t* info) {
   info[7] = sc.n_phases;
   info[8] = sc.n_slots;
   info[9] = sc.max_collen;
+  const Stream& a = t->s32;
+  const Stream& b = t->s64;
+  info[10] = a.plan.nw; info[11] = a.plan.ring_rows; info[12] = (int64_t)a.est_cycles;
+  info[13] = a.rows_resident; info[14] = a.rows_gathered; info[15] = a.rows_prefetched;
+  info[16] = a.rows_late; info[17] = a.rows_jit; info[18] = a.n_steps; info[19] = a.n_waits;
+  info[20] = b.plan.nw; info[21] = b.plan.ring_rows; info[22] = (int64_t)b.est_cycles;
+  info[23] = b.rows_resident;
   return GOX_OK;
 }
 
@@ -1068,9 +1074,11 @@ int gox_ls_create(int32_t n, int32_t nnz, const int32_t* rows, const int32_t* co
     for (int e = 0; e < nnz; e++) h->packed[h->csc.slot_of[e]] += vals[e];
     if (klu_factor(h->csc, h->packed.data(), h->sym, 0.001, h->num) != 0) return GOX_SINGULAR;
     build_schedule(nullptr, h->csc, h->sym, h->num, h->sc);
+    make_streams(h->sc, h->s32, h->s64);
     std::vector<int32_t> dummy_p(1, 0), dummy_i;
     std::vector<double> dummy_x;
     h->dsched.load(h->sc, dummy_p, dummy_i, dummy_x, dummy_x);
+    h->dsched.load_streams(h->s32, h->s64);
     const SchedDev& S = h->dsched.d;
     h->jbuf.ensure((size_t)S.n_a * 32 * 8 + 8);
     h->lu.ensure((size_t)S.n_slots * 32 * 8 + 8);

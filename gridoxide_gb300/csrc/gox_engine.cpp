@@ -177,6 +177,9 @@ void build_schedule(const JacPattern* Jp, const Csc& A, const Symbolic& S, const
   //             d (batches load before they store) but not precede it
   sc.op_ptr.assign(n + 1, 0);
   sc.bt_ptr.assign(n + 1, 0);
+  sc.col_level = level;
+  sc.cu_ptr.assign(n + 1, 0);
+  sc.cu_dptr.assign(1, 0);
   std::vector<int32_t> lastw(sc.max_collen + 1, -1), maxr(sc.max_collen + 1, -1);
   struct Op { int32_t dst, up, slot, lev; };
   std::vector<Op> ops;
@@ -193,7 +196,10 @@ void build_schedule(const JacPattern* Jp, const Csc& A, const Symbolic& S, const
         int d = pos_of[N.Li[N.Lp[j] + t]];
         if (d < 0 || d <= p) throw std::runtime_error("update outside the column pattern");
         ops.push_back({d, p, lslot(j, t), 0});
+        sc.cu_dst.push_back(d);
       }
+      sc.cu_j.push_back(j);
+      sc.cu_dptr.push_back((int32_t)sc.cu_dst.size());
       sc.flops_refactor += 2.0 * sc.c_llen[j];
     }
     sc.flops_refactor += llen;
@@ -224,6 +230,7 @@ void build_schedule(const JacPattern* Jp, const Csc& A, const Symbolic& S, const
       }
     }
     sc.op_ptr[k + 1] = (int)sc.op_slot.size();
+    sc.cu_ptr[k + 1] = (int)sc.cu_j.size();
     sc.bt_ptr[k + 1] = (int)sc.bt_cnt.size();
     sc.max_ops = std::max(sc.max_ops, (int)ops.size());
     sc.max_batches = std::max(sc.max_batches, sc.bt_ptr[k + 1] - sc.bt_ptr[k]);

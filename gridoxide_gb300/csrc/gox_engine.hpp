@@ -61,6 +61,11 @@ struct Schedule {
   // fill recipe in LU layout: per LU slot the A entry it starts from (-1 =
   // fill-in, starts at zero); off-diagonal A entries separately
   std::vector<int32_t> slot_a, off_a;
+  // left-looking updates per column, in KLU's order: for column k the U
+  // entries p = 0 .. ulen-1 (stage row p holds U(j, k), j = cu_j[cu_ptr[k] + p]);
+  // U entry e updates the stage rows cu_dst[cu_dptr[e] ..] with the rows of
+  // L(:, j) in stored order.  col_level: dependency level of each column.
+  std::vector<int32_t> cu_ptr, cu_j, cu_dptr, cu_dst, col_level;
   int max_pk = 0;    // largest packet, int32 words
   int max_head = 0;  // largest packet without its update descriptors
   int max_ops = 0, max_batches = 0, max_fw = 0;

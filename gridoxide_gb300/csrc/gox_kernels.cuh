@@ -21,6 +21,8 @@
 #include <cstdint>
 #include <cuda_runtime.h>
 
+#include "gox_stream.hpp"
+
 namespace gox {
 
 enum : int { ST_RUNNING = -1, ST_CONVERGED = 0, ST_MAXITER = 1, ST_SINGULAR = 2, ST_UNUSED = 3 };
@@ -288,23 +290,6 @@ __global__ void __launch_bounds__(256) k_fill(SchedDev S, BatchDev D, int per_wa
   }
 }
 
-// Per-lane asynchronous copies global -> shared (cp.async, 4 or 8 bytes).
-__device__ __forceinline__ void cp_async4(void* smem, const void* gmem) {
-  unsigned sa = (unsigned)__cvta_generic_to_shared(smem);
-  asm volatile("cp.async.ca.shared.global [%0], [%1], 4;\n" ::"r"(sa), "l"(gmem) : "memory");
-}
-__device__ __forceinline__ void cp_async8(void* smem, const void* gmem) {
-  unsigned sa = (unsigned)__cvta_generic_to_shared(smem);
-  asm volatile("cp.async.ca.shared.global [%0], [%1], 8;\n" ::"r"(sa), "l"(gmem) : "memory");
-}
-__device__ __forceinline__ void cp_async_commit_wait() {
-  asm volatile("cp.async.commit_group;\ncp.async.wait_group 0;\n" ::: "memory");
-}
-template <typename T>
-__device__ __forceinline__ void cp_async_t(T* smem, const T* gmem) {
-  if (sizeof(T) == 8) cp_async8(smem, gmem); else cp_async4(smem, gmem);
-}
-
 // Bulk (TMA) copy global -> shared with mbarrier completion, and a bounded
 // wait on it: after kSpinLimit polls the wait gives up and reports false.
 constexpr int kSpinLimit = 1 << 22;
@@ -334,226 +319,271 @@ __device__ __forceinline__ bool mbar_wait(uint64_t* bar, unsigned parity) {
   return false;
 }
 
-// The next column (index into lev_cols) this warp takes after column q,
-// or -1: columns of a level are dealt round-robin to the warps.
-__device__ __forceinline__ int next_task(const SchedDev& S, int lv, int q, int warp, int nw) {
-  if (q + nw < __ldg(S.lev_ptr + lv + 1)) return q + nw;
-  for (int l = lv + 1; l < S.n_levels; l++) {
-    const int c = __ldg(S.lev_ptr + l) + warp;
-    if (c < __ldg(S.lev_ptr + l + 1)) return c;
-  }
-  return -1;
-}
-
-// One batch of N independent updates on the stage: all loads, then the
-// FMAs, then the stores (no op of a batch touches an entry another writes).
-template <typename T, int N>
-__device__ __forceinline__ void run_batch(T* stl, const T* opvl, const int32_t* desc) {
-  int dd[N];
-  T xd[N], xu[N], lv[N];
-#pragma unroll
-  for (int t = 0; t < N; t++) {
-    const uint32_t ps = (uint32_t)desc[2 * t + 1];
-    dd[t] = (int)(ps & 0xffffu);
-    xd[t] = stl[dd[t]];
-    xu[t] = stl[ps >> 16];
-    lv[t] = opvl[t * 32];
-  }
-#pragma unroll
-  for (int t = 0; t < N; t++) stl[dd[t]] = xd[t] - lv[t] * xu[t];
-}
-
-// K3: refactor.  One CTA per group of 32 scenarios; the columns of each
-// dependency level are dealt round-robin to the warps; __syncthreads
-// between levels.  Per warp, in shared memory:
-//   pkt[2][pkcap]  its current and next column packet (TMA bulk copies)
-//   stage[cap][32] the column: [U (topological order) | diagonal | L],
-//                  initialised by one TMA bulk copy of the A values and
-//                  zeros the fill kernel left in the factor's layout
-//   opv[opcap][32] the L(i, j) values its updates read (cp.async)
-//   opd[opcap][2]  their descriptors when the packet could not hold them
-//   dat[dcap][32]  forward-substitution terms and b_k
-// Updates run as hazard-free batches dispatched to exact-size code.  With
-// S.fuse_fwd the forward substitution y_k = b_k - sum_j L(k, j) y_j runs in
-// the same sweep.
+// Shared-memory accesses by 32-bit shared address (the ring and the stage
+// are addressed by row numbers computed at run time).
 template <typename T>
-__global__ void __launch_bounds__(256) k_refactor(SchedDev S, BatchDev D, int cap, int opcap,
-                                                  int pkcap, int dcap) {
+__device__ __forceinline__ T lds(uint32_t a);
+template <>
+__device__ __forceinline__ float lds<float>(uint32_t a) {
+  float v;
+  asm volatile("ld.shared.f32 %0, [%1];\n" : "=f"(v) : "r"(a));
+  return v;
+}
+template <>
+__device__ __forceinline__ double lds<double>(uint32_t a) {
+  double v;
+  asm volatile("ld.shared.f64 %0, [%1];\n" : "=d"(v) : "r"(a));
+  return v;
+}
+__device__ __forceinline__ void sts(uint32_t a, float v) {
+  asm volatile("st.shared.f32 [%0], %1;\n" ::"r"(a), "f"(v) : "memory");
+}
+__device__ __forceinline__ void sts(uint32_t a, double v) {
+  asm volatile("st.shared.f64 [%0], %1;\n" ::"r"(a), "d"(v) : "memory");
+}
+__device__ __forceinline__ void cp_async16(uint32_t smem, const void* gmem) {
+  asm volatile("cp.async.ca.shared.global [%0], [%1], 16;\n" ::"r"(smem), "l"(gmem) : "memory");
+}
+__device__ __forceinline__ void cp_async_wait_n(int n) {
+  switch (n) {
+    case 0: asm volatile("cp.async.wait_group 0;\n" ::: "memory"); break;
+    case 1: asm volatile("cp.async.wait_group 1;\n" ::: "memory"); break;
+    case 2: asm volatile("cp.async.wait_group 2;\n" ::: "memory"); break;
+    case 3: asm volatile("cp.async.wait_group 3;\n" ::: "memory"); break;
+    case 4: asm volatile("cp.async.wait_group 4;\n" ::: "memory"); break;
+    case 5: asm volatile("cp.async.wait_group 5;\n" ::: "memory"); break;
+    case 6: asm volatile("cp.async.wait_group 6;\n" ::: "memory"); break;
+    default: asm volatile("cp.async.wait_group 7;\n" ::: "memory"); break;
+  }
+}
+
+// Correctly rounded reciprocal (the same value as 1 / x).
+__device__ __forceinline__ float rcp_rn(float x) { return __frcp_rn(x); }
+__device__ __forceinline__ double rcp_rn(double x) { return __drcp_rn(x); }
+
+// The refactor's command streams on the device (built on the host: one
+// stream per warp, in chunks of chunk_words words).
+struct StreamDev {
+  const int32_t* words;
+  const int32_t* chunk0;
+  const int32_t* nchunks;
+  int ring_rows, chunk_words, n_bars;
+};
+
+// K3: refactor, the interpreter of the per-warp command streams.  One CTA
+// per group of 32 scenarios (lane = scenario).  Shared memory: per warp two
+// stream chunks (TMA bulk copies, mbarrier completion, bounded waits), then
+// the rings of all warps as one space of rows of 32 values.  The host has
+// placed every value: a column's stage block holds [column rows | y | b];
+// update runs L(:, j) are read either from a copy in the warp's ring or
+// straight from the producing column's block.  Commands (see the stream
+// compiler for encodings): GATHER (cp.async 16 B per lane), WAIT, STEPS
+// (up to 9 updates stage[d] -= L(d, j) * stage[j] each, loads of a step
+// before its stores, the next step's descriptor loaded ahead), FWD (forward
+// substitution terms), FINISH (pivot, scale L, write the column back, y_k),
+// BAR, NEXT, END.  A bounded
+// wait that gives up, or a malformed command, sets the error flag; the warp
+// then drains its copies and still takes every remaining barrier.
+template <typename T>
+__global__ void __launch_bounds__(256) k_refactor(StreamDev P, SchedDev S, BatchDev D) {
   const int g = blockIdx.x;
   if (!D.gact[g]) return;
   extern __shared__ __align__(128) unsigned char smem_raw[];
-  __shared__ __align__(8) uint64_t mbar[8][3];
+  __shared__ __align__(8) uint64_t mbar[8][2];
   __shared__ int flags[2][32];
   __shared__ int timed_out;
+  constexpr uint32_t RB = 32u * sizeof(T);    // bytes per row
+  constexpr int RPI = 512 / (int)RB;          // rows per 16-byte-per-lane copy
+  constexpr int LPR = 32 / RPI;               // lanes per row in a copy
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
-  const size_t wbytes = (size_t)2 * pkcap * 4 + (size_t)opcap * 8 +
-                        ((size_t)cap + (size_t)opcap + (size_t)dcap) * 32 * sizeof(T);
-  unsigned char* wbase = smem_raw + (size_t)warp * ((wbytes + 127) & ~(size_t)127);
-  int32_t* pkb = reinterpret_cast<int32_t*>(wbase);
-  int32_t* opd = pkb + (size_t)2 * pkcap;
-  T* stage_w = reinterpret_cast<T*>(wbase + (size_t)2 * pkcap * 4 + (size_t)opcap * 8);
-  T* opv = stage_w + (size_t)cap * 32;
-  T* dat = opv + (size_t)opcap * 32;
+  const int CW = P.chunk_words;
+  int32_t* cbuf = reinterpret_cast<int32_t*>(smem_raw) + (size_t)warp * 2 * CW;
+  const uint32_t ring_s = smem_u32(smem_raw + (size_t)nw * 2 * CW * 4);
+  const uint32_t ring_lane = ring_s + (uint32_t)lane * sizeof(T);
   const int s = g * 32 + lane;
-  T* LU = (T*)D.lu;
-  T* X = (T*)D.sol;
-  const T* RHS = (const T*)D.rhs;
-  const size_t luG = (size_t)g * S.n_slots * 32u;
-  const size_t xG = (size_t)g * S.n_u * 32u;
-  T* LUg = LU + luG;
-  bool bad = false, tiny = false;
+  T* LUg = (T*)D.lu + (size_t)g * S.n_slots * 32u;
+  T* Xg = (T*)D.sol + (size_t)g * S.n_u * 32u;
+  const T* RHSg = (const T*)D.rhs + (size_t)g * S.n_u * 32u;
   const float ptol = D.piv_tol;
+  bool bad = false, tiny = false;
 
   if (threadIdx.x < 64) (&flags[0][0])[threadIdx.x] = 0;
   if (threadIdx.x == 0) timed_out = 0;
   if (lane == 0) {
     mbar_init(&mbar[warp][0]);
     mbar_init(&mbar[warp][1]);
-    mbar_init(&mbar[warp][2]);
   }
   asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
+  // the zero row (padding terms of the forward substitution read it)
+  if (warp == 0) sts(ring_lane + (uint32_t)(nw * P.ring_rows) * RB, (T)0);
   __syncthreads();
 
-  auto issue = [&](int q, int buf) {
-    const int off = __ldg(S.pk_off + q), sz = __ldg(S.pk_off + q + 1) - off;
-    const unsigned bytes = (unsigned)min(sz, pkcap) * 4u;
-    bulk_load(pkb + (size_t)buf * pkcap, S.pk + off, bytes, &mbar[warp][buf]);
-  };
-  int cur = 0;
-  unsigned parity[3] = {0u, 0u, 0u};
-  int first = -1;
-  for (int l = 0; l < S.n_levels && first < 0; l++) {
-    const int c = __ldg(S.lev_ptr + l) + warp;
-    if (c < __ldg(S.lev_ptr + l + 1)) first = c;
+  const int32_t* gw = P.words + (size_t)P.chunk0[warp] * CW;
+  const int nch = P.nchunks[warp];
+  if (lane == 0) {
+    bulk_load(cbuf, gw, (unsigned)CW * 4u, &mbar[warp][0]);
+    if (nch > 1) bulk_load(cbuf + CW, gw + CW, (unsigned)CW * 4u, &mbar[warp][1]);
   }
-  if (first >= 0 && lane == 0) issue(first, 0);
-
-  for (int lv = 0; lv < S.n_levels; lv++) {
-    const int q0 = __ldg(S.lev_ptr + lv), q1 = __ldg(S.lev_ptr + lv + 1);
-    for (int q = q0 + warp; q < q1; q += nw) {
-      bool ok = mbar_wait(&mbar[warp][cur], parity[cur]);
-      parity[cur] ^= 1u;
-      const int nq = next_task(S, lv, q, warp, nw);
-      if (nq >= 0 && lane == 0) issue(nq, cur ^ 1);
-      if (!ok) atomicExch(&timed_out, 1);
-      if (!ok || timed_out) { cur ^= 1; continue; }
-      const int32_t* pk = pkb + (size_t)cur * pkcap;
-      const int psz = __ldg(S.pk_off + q + 1) - __ldg(S.pk_off + q);
-      const int k = pk[0], base = pk[1], ulen = pk[2], llen = pk[3];
-      const int nA = pk[4], nops = pk[5], nbt = pk[6], nfw = pk[7], ob = pk[9];
-      const int len = ulen + 1 + llen;
-      const int32_t* fwp = pk + 12 + nA;
-      const int32_t* btw = fwp + 2 * nfw;
-      const int ops_at = 12 + nA + 2 * nfw + ((nbt + 3) >> 2);
-      const bool ops_in_pk = (ops_at + 2 * nops) <= min(psz, pkcap);
-      const bool in_smem = len <= cap;
-      T* st = in_smem ? stage_w : (LUg + (size_t)base * 32u);
-      T* stl = st + lane;
-      // --- stage: one bulk copy of the column (A values / zeros)
-      if (in_smem && lane == 0)
-        bulk_load(stage_w, LUg + (size_t)base * 32u, (unsigned)len * 32u * sizeof(T), &mbar[warp][2]);
-      // --- forward terms and b_k, first window of update values (cp.async)
-      const bool in_dat = S.fuse_fwd && (2 * nfw + 1) <= dcap;
-      if (in_dat) {
-        for (int t = 0; t < nfw; t++) {
-          cp_async_t<T>(dat + t * 32 + lane, LUg + (size_t)fwp[2 * t] * 32u + lane);
-          cp_async_t<T>(dat + (nfw + t) * 32 + lane, X + xG + (size_t)fwp[2 * t + 1] * 32u + lane);
+  unsigned par0 = 0u, par1 = 0u;
+  bool ok = mbar_wait(&mbar[warp][0], par0);
+  par0 ^= 1u;
+  int chunk = 0, buf = 0, pc = 0, bars = 0;
+  const int32_t* cb = cbuf;
+  while (ok) {
+    const int32_t w0 = cb[pc];
+    switch (w0 & 15) {
+      case CMD_STEPS: {
+        // no branch inside a step: unused slots update the block's dummy row
+        const int m = (w0 >> 4) & 0xfff;
+        const uint32_t st_lane = ring_lane + (((uint32_t)w0) >> 16) * RB;
+        const int first = (pc + 1 + 3) & ~3;
+        const uint4* sd = reinterpret_cast<const uint4*>(cb + first);
+        uint4 d = sd[0];
+        for (int q = 0; q < m; q++) {
+          const uint4 dn = sd[q + 1];
+          const uint32_t la = ring_lane + (d.x & 0xffffu) * RB;
+          const T xj = lds<T>(st_lane + ((d.x >> 16) & 0x3ffu) * RB);
+          uint32_t da[kStepOps];
+          T xi[kStepOps], lv[kStepOps];
+#pragma unroll
+          for (int t = 0; t < kStepOps; t++) {
+            const uint32_t wd = t < 3 ? d.y : (t < 6 ? d.z : d.w);
+            da[t] = st_lane + ((wd >> (10 * (t % 3))) & 0x3ffu) * RB;
+          }
+#pragma unroll
+          for (int t = 0; t < kStepOps; t++) {
+            xi[t] = lds<T>(da[t]);
+            lv[t] = lds<T>(la + (uint32_t)t * RB);
+          }
+#pragma unroll
+          for (int t = 0; t < kStepOps; t++) sts(da[t], xi[t] - lv[t] * xj);
+          d = dn;
         }
-        cp_async_t<T>(dat + 2 * nfw * 32 + lane, RHS + xG + (size_t)k * 32u + lane);
+        pc = first + 4 * m;
+        break;
       }
-      int ochunk = min(nops, opcap);
-      const int32_t* dsrc = ops_in_pk ? pk + ops_at : opd;  // descriptors of the window
-      if (!ops_in_pk) {
-        // descriptors of the first window: lane-parallel coalesced loads
-        for (int t = lane; t < ochunk; t += 32) {
-          const uint32_t ps = __ldg(S.op_pos + ob + t);
-          opd[2 * t] = __ldg(S.op_slot + ob + t) * 32;
-          opd[2 * t + 1] = (int32_t)(((ps & 0xffffu) * 32u) | (((ps >> 16) * 32u) << 16));
+      case CMD_GATHER: {
+        // m is a multiple of RPI (padding copies land in the trash row);
+        // source rows: the factor image, then X, then the right-hand side
+        const int m = (w0 >> 4) & 0xffff;
+        const int sub = lane % LPR, rsel = lane / LPR;
+        for (int q0 = 0; q0 < m; q0 += RPI) {
+          const uint32_t rw = (uint32_t)cb[pc + 1 + q0 + rsel];
+          const uint32_t v = rw & 0x1fffffu;
+          const char* src = v < (uint32_t)S.n_slots ? (const char*)LUg + (size_t)v * RB
+                            : v < (uint32_t)(S.n_slots + S.n_u)
+                                ? (const char*)Xg + (size_t)(v - S.n_slots) * RB
+                                : (const char*)RHSg + (size_t)(v - S.n_slots - S.n_u) * RB;
+          cp_async16(ring_s + (rw >> 21) * RB + (uint32_t)sub * 16u, src + (size_t)sub * 16u);
         }
+        if ((w0 >> 23) & 1) asm volatile("cp.async.commit_group;\n" ::: "memory");
+        pc += 1 + m;
+        break;
+      }
+      case CMD_WAIT:
+        cp_async_wait_n((w0 >> 4) & 7);
         __syncwarp();
-      }
-      for (int t = 0; t < ochunk; t++) cp_async_t<T>(opv + t * 32 + lane, LUg + dsrc[2 * t] + lane);
-      asm volatile("cp.async.commit_group;\n" ::: "memory");
-      if (in_smem) {
-        if (!mbar_wait(&mbar[warp][2], parity[2])) atomicExch(&timed_out, 1);
-        parity[2] ^= 1u;
-      }
-      asm volatile("cp.async.wait_group 0;\n" ::: "memory");
-      __syncwarp();
-      // --- update batches
-      int o = 0, cbase = 0;
-      for (int b = 0; b < nbt; b++) {
-        const int cnt = (btw[b >> 2] >> (8 * (b & 3))) & 0xff;
-        if (o + cnt > cbase + ochunk) {  // refill the update window (long columns)
-          cbase = o;
-          ochunk = min(nops - o, opcap);
-          __syncwarp();
-          if (!ops_in_pk) {
-            for (int t = lane; t < ochunk; t += 32) {
-              const uint32_t ps = __ldg(S.op_pos + ob + o + t);
-              opd[2 * t] = __ldg(S.op_slot + ob + o + t) * 32;
-              opd[2 * t + 1] = (int32_t)(((ps & 0xffffu) * 32u) | (((ps >> 16) * 32u) << 16));
-            }
-            __syncwarp();
+        pc++;
+        break;
+      case CMD_FWD: {
+        // m is a multiple of 8 (padding terms read the zero row)
+        const int m = (w0 >> 4) & 0xffff;
+        const uint32_t w1 = (uint32_t)cb[pc + 1];
+        const uint32_t yrow = ring_lane + ((w1 & 0xffffu) + (w1 >> 16)) * RB;
+        T y = lds<T>(((w0 >> 20) & 1) ? yrow + RB : yrow);
+        for (int f0 = 0; f0 < m; f0 += 8) {
+          T a[8], b[8];
+#pragma unroll
+          for (int t = 0; t < 8; t++) {
+            const uint32_t fw = (uint32_t)cb[pc + 2 + f0 + t];
+            a[t] = lds<T>(ring_lane + (fw & 0xffffu) * RB);
+            b[t] = lds<T>(ring_lane + (fw >> 16) * RB);
           }
-          const int32_t* ds = ops_in_pk ? pk + ops_at + 2 * o : opd;
-          for (int t = 0; t < ochunk; t++) cp_async_t<T>(opv + t * 32 + lane, LUg + ds[2 * t] + lane);
-          cp_async_commit_wait();
-          __syncwarp();
+#pragma unroll
+          for (int t = 0; t < 8; t++) y -= a[t] * b[t];
         }
-        const int32_t* desc = ops_in_pk ? pk + ops_at + 2 * o : opd + 2 * (o - cbase);
-        const T* ov = opv + (o - cbase) * 32 + lane;
-        switch (cnt) {
-          case 1: run_batch<T, 1>(stl, ov, desc); break;
-          case 2: run_batch<T, 2>(stl, ov, desc); break;
-          case 3: run_batch<T, 3>(stl, ov, desc); break;
-          case 4: run_batch<T, 4>(stl, ov, desc); break;
-          case 5: run_batch<T, 5>(stl, ov, desc); break;
-          case 6: run_batch<T, 6>(stl, ov, desc); break;
-          case 7: run_batch<T, 7>(stl, ov, desc); break;
-          default: run_batch<T, 8>(stl, ov, desc); break;
-        }
-        o += cnt;
+        sts(yrow, y);
+        pc += 2 + m;
+        break;
       }
-      // --- pivot (static order), scale L, write back
-      const T piv = stl[ulen * 32];
-      if (piv == (T)0) bad = true;
-      if (ptol > 0.0f) {
+      case CMD_FINISH: {
+        // rows in blocks of 8, the last block clamped to the column's end
+        const int k = cb[pc + 1], base = cb[pc + 2];
+        const int ulen = cb[pc + 3] & 0xffff, llen = (cb[pc + 3] >> 16) & 0xffff;
+        const uint32_t st_lane = ring_lane + (uint32_t)cb[pc + 4] * RB;
+        const int len = ulen + 1 + llen;
+        const T piv = lds<T>(st_lane + (uint32_t)ulen * RB);
+        bad |= (piv == (T)0);
+        const T inv = rcp_rn(piv);
+        T* dst = LUg + (size_t)base * 32u + lane;
+        for (int p0 = 0; p0 <= ulen; p0 += 8) {
+          T v[8];
+#pragma unroll
+          for (int t = 0; t < 8; t++) v[t] = lds<T>(st_lane + (uint32_t)min(p0 + t, ulen) * RB);
+#pragma unroll
+          for (int t = 0; t < 8; t++) dst[(size_t)min(p0 + t, ulen) * 32u] = v[t];
+        }
         T colmax = fabs(piv);
-        for (int t = 0; t < llen; t++) colmax = fmax(colmax, fabs(stl[(ulen + 1 + t) * 32]));
-        if ((float)fabs(piv) < ptol * (float)colmax) tiny = true;
-      }
-      const T inv = (T)1 / piv;
-      T* dstl = LUg + (size_t)base * 32u + lane;
-      if (in_smem)
-        for (int p = 0; p <= ulen; p++) dstl[p * 32] = stl[p * 32];
-      for (int p = ulen + 1; p < len; p++) dstl[p * 32] = stl[p * 32] * inv;
-      if (S.fuse_fwd) {
-        T y;
-        if (in_dat) {
-          y = dat[2 * nfw * 32 + lane];
-          for (int t = 0; t < nfw; t++) y -= dat[t * 32 + lane] * dat[(nfw + t) * 32 + lane];
-        } else {
-          y = RHS[xG + (size_t)k * 32u + lane];
-          for (int t0 = 0; t0 < nfw; t0 += 16) {
-            T c[16], xv[16];
+        for (int p0 = ulen + 1; p0 < len; p0 += 8) {
+          T v[8];
 #pragma unroll
-            for (int t = 0; t < 16; t++)
-              if (t0 + t < nfw) {
-                c[t] = LUg[(size_t)fwp[2 * (t0 + t)] * 32u + lane];
-                xv[t] = X[xG + (size_t)fwp[2 * (t0 + t) + 1] * 32u + lane];
-              }
+          for (int t = 0; t < 8; t++) v[t] = lds<T>(st_lane + (uint32_t)min(p0 + t, len - 1) * RB);
 #pragma unroll
-            for (int t = 0; t < 16; t++)
-              if (t0 + t < nfw) y -= c[t] * xv[t];
+          for (int t = 0; t < 8; t++) colmax = fmax(colmax, fabs(v[t]));
+#pragma unroll
+          for (int t = 0; t < 8; t++) {
+            const int r = min(p0 + t, len - 1);
+            v[t] *= inv;
+            sts(st_lane + (uint32_t)r * RB, v[t]);
+            dst[(size_t)r * 32u] = v[t];
           }
         }
-        X[xG + (size_t)k * 32u + lane] = y;
+        tiny |= (ptol > 0.0f) && ((float)fabs(piv) < ptol * (float)colmax);
+        if (S.fuse_fwd) Xg[(size_t)k * 32u + lane] = lds<T>(st_lane + (uint32_t)len * RB);
+        pc += 5;
+        break;
       }
-      __syncwarp();
-      cur ^= 1;
+      case CMD_BAR:
+        __syncthreads();
+        bars++;
+        pc++;
+        break;
+      case CMD_NOP:
+        pc++;
+        break;
+      case CMD_NEXT:
+        __syncwarp();
+        if (lane == 0 && chunk + 2 < nch)
+          bulk_load(cbuf + (size_t)buf * CW, gw + (size_t)(chunk + 2) * CW, (unsigned)CW * 4u,
+                    &mbar[warp][buf]);
+        chunk++;
+        buf ^= 1;
+        if (chunk >= nch) {
+          ok = false;
+          break;
+        }
+        if (buf == 0) {
+          ok = mbar_wait(&mbar[warp][0], par0);
+          par0 ^= 1u;
+        } else {
+          ok = mbar_wait(&mbar[warp][1], par1);
+          par1 ^= 1u;
+        }
+        cb = cbuf + (size_t)buf * CW;
+        pc = 0;
+        break;
+      case CMD_END:
+        goto done;
+      default:
+        ok = false;
     }
-    __syncthreads();
+    if (pc >= CW) ok = false;  // a command ran past its chunk
+  }
+done:
+  if (!ok) {
+    if (lane == 0) atomicExch(&timed_out, 1);
+    asm volatile("cp.async.wait_all;\n" ::: "memory");
+    for (; bars < P.n_bars; bars++) __syncthreads();
   }
   if (bad) atomicOr(&flags[0][lane], 1);
   if (tiny) atomicOr(&flags[1][lane], 1);

@@ -1,0 +1,836 @@
+// Compiler of the refactor's per-warp command streams, and their host
+// interpreter (the CPU check of every stream before it reaches a GPU).
+#include "gox_stream.hpp"
+
+#include <algorithm>
+#include <cmath>
+#include <limits>
+#include <numeric>
+#include <stdexcept>
+
+namespace gox {
+
+size_t stream_smem_bytes(const StreamPlan& p) {
+  return (size_t)p.nw * 2 * p.chunk_words * 4 +
+         ((size_t)p.nw * p.ring_rows + kSpareRows) * 32 * p.elem;
+}
+
+namespace {
+
+constexpr int64_t kInf = std::numeric_limits<int64_t>::max();
+inline int64_t tmake(int level, int64_t pos) { return ((int64_t)level << 32) | pos; }
+inline int64_t tend(int level) { return ((int64_t)level << 32) | 0xffffffffLL; }
+inline int64_t tagof(int col, int rel) { return ((int64_t)col << 20) | rel; }
+
+enum { IT_LRUN = 0, IT_FWL = 1, IT_FWY = 2 };
+enum { ST_NONE = 0, ST_GATHERED = 1, ST_RESIDENT = 2 };
+constexpr int kPieceRows = 27;  // longest L run piece placed as one block
+
+// One value source of a column: a run of rows of another column's result.
+struct Item {
+  int kind = 0, j = 0;   // producer column
+  int src = 0;           // first source row (factor slot, or X row for y_j)
+  int rel = 0;           // first row within the producer's stage block
+  int nrows = 0;
+  int upos = -1;         // L runs: U entry p of the consuming column
+  int dfirst = 0;        // L runs: first op of U entry p this piece covers
+  int row = -1;          // absolute ring row once placed
+  int group = -1;        // commit group of its copy
+  int state = ST_NONE;
+  bool committed = false;
+};
+
+struct ColInfo {
+  int k = 0, level = 0, warp = -1, len = 0, brows = 0, nsteps = 0;
+  int block = -1;   // ring row (within its warp's ring) of the stage block
+  int group = -1;   // commit group of the stage copy
+  bool staged = false, committed = false;
+  double cost = 0;
+  std::vector<Item> items;  // consumption order: L-run pieces (U order), fw pairs
+};
+
+struct Emit {
+  std::vector<int32_t> w;
+  int cw;
+  size_t cstart = 0;
+  int64_t last_gather = -1;  // word index of the last GATHER header
+  explicit Emit(int cw_) : cw(cw_) {}
+  size_t room() const { return cstart + cw - 1 - w.size(); }  // last word: NEXT / END
+  void next_chunk() {
+    w.push_back(CMD_NEXT);
+    while (w.size() < cstart + cw) w.push_back(CMD_NOP);
+    cstart += cw;
+  }
+  void need(size_t n) {
+    if (room() < n) next_chunk();
+  }
+};
+
+struct Step {
+  uint32_t x, y, z, w;
+};
+
+struct Builder {
+  const Schedule& sc;
+  StreamPlan P;
+  int W, R, n;
+  std::vector<ColInfo> C;
+  std::vector<std::vector<int>> seq;
+  std::vector<int> seqpos;
+  std::vector<int64_t> busy, tag;
+  std::vector<int> cursor, ngroups, waited;
+  std::vector<int64_t> pos;
+  std::vector<Emit> em;
+  std::vector<std::vector<Item*>> uncommitted;
+  std::vector<std::vector<int>> uncommitted_cols;
+  std::vector<std::vector<std::pair<int, int>>> pend_rows;  // copies not yet emitted
+  std::vector<double> wcost;  // per warp, cycles in the current level (estimate)
+  std::vector<int> pinned;    // per warp, rows pinned in the current level
+  Stream* out;
+  std::string err;
+
+  Builder(const Schedule& s, const StreamPlan& p) : sc(s), P(p) {
+    W = p.nw;
+    R = p.ring_rows;
+    n = s.n_u;
+  }
+
+  int64_t now(int w, int L) { return tmake(L, pos[w]++); }
+
+  int alloc(int w, int m, int64_t t) {
+    if (m > R || m <= 0) return -1;
+    const int64_t* b = &busy[(size_t)w * R];
+    int run = 0;
+    for (int i = 0; i < 2 * R; i++) {
+      const int r = (cursor[w] + i) % R;
+      if (r == 0) run = 0;
+      if (b[r] < t) {
+        if (++run >= m) {
+          cursor[w] = (r + 1) % R;
+          return r - m + 1;
+        }
+      } else {
+        run = 0;
+      }
+    }
+    return -1;
+  }
+  void take(int w, int r0, int m, int64_t tg_col) {
+    for (int i = 0; i < m; i++) {
+      busy[(size_t)w * R + r0 + i] = kInf;
+      tag[(size_t)w * R + r0 + i] = tg_col >= 0 ? tagof((int)tg_col, i) : -1;
+    }
+  }
+  void release_abs(int row, int m, int64_t t) {
+    for (int i = 0; i < m; i++) busy[row + i] = t;
+  }
+
+  int rpi() const { return 512 / (32 * P.elem); }  // rows per 16-byte-per-lane copy
+  int zero_row() const { return W * R; }
+  int trash_row() const { return W * R + 1; }
+
+  // Source rows of the three arrays as one row space: the factor image,
+  // then the forward-substitution vector, then the right-hand side.
+  int vrow(int arr, int r) const {
+    return arr == ARR_LU ? r : arr == ARR_X ? sc.n_slots + r : sc.n_slots + n + r;
+  }
+  void emit_gather(int w, int arr, const std::vector<std::pair<int, int>>& rows) {
+    for (const auto& r : rows) pend_rows[w].push_back({vrow(arr, r.first), r.second});
+  }
+  // One GATHER command for every copy issued at this point.
+  void flush_gather(int w) {
+    std::vector<std::pair<int, int>>& rows = pend_rows[w];
+    if (rows.empty()) return;
+    Emit& e = em[w];
+    const size_t q = (size_t)rpi();
+    while (rows.size() % q) rows.push_back({0, trash_row()});
+    size_t i = 0;
+    while (i < rows.size()) {
+      if (e.room() < 1 + q) e.next_chunk();
+      size_t m = std::min(rows.size() - i, std::min<size_t>(e.room() - 1, 4092));
+      m -= m % q;
+      e.last_gather = (int64_t)e.w.size();
+      e.w.push_back(CMD_GATHER | (int32_t)(m << 4));
+      for (size_t t = 0; t < m; t++) {
+        const auto& r = rows[i + t];
+        e.w.push_back((int32_t)((uint32_t)r.first | ((uint32_t)r.second << 21)));
+      }
+      i += m;
+    }
+    rows.clear();
+    pos[w]++;
+  }
+  void commit(int w) {
+    Emit& e = em[w];
+    if (uncommitted[w].empty() && uncommitted_cols[w].empty()) return;
+    flush_gather(w);
+    if (e.last_gather < 0) throw std::logic_error("commit without a gather");
+    e.w[e.last_gather] |= (1 << 23);
+    const int g = ngroups[w]++;
+    out->n_groups++;
+    for (Item* it : uncommitted[w]) { it->group = g; it->committed = true; }
+    for (int ci : uncommitted_cols[w]) { C[ci].group = g; C[ci].committed = true; }
+    uncommitted[w].clear();
+    uncommitted_cols[w].clear();
+  }
+  void wait_for(int w, int g, int L, bool on_path) {
+    if (g < 0 || waited[w] >= g) return;
+    int m = ngroups[w] - 1 - g;
+    if (m < 0) throw std::logic_error("wait for an uncommitted group");
+    m = std::min(m, 7);
+    Emit& e = em[w];
+    e.need(1);
+    e.w.push_back(CMD_WAIT | (m << 4));
+    waited[w] = ngroups[w] - 1 - m;
+    out->n_waits++;
+    pos[w]++;
+    if (on_path) wcost[w] += 1200;
+    (void)L;
+  }
+
+  // Places a copy of item `it` (of a column run by warp w) in w's ring.
+  bool gather_item(int w, Item& it, int64_t t) {
+    const int r = alloc(w, it.nrows, t);
+    if (r < 0) return false;
+    take(w, r, it.nrows, -1);
+    it.row = w * R + r;
+    it.state = ST_GATHERED;
+    std::vector<std::pair<int, int>> rows;
+    for (int i = 0; i < it.nrows; i++) rows.push_back({it.src + i, it.row + i});
+    emit_gather(w, it.kind == IT_FWY ? ARR_X : ARR_LU, rows);
+    uncommitted[w].push_back(&it);
+    out->rows_gathered += it.nrows;
+    return true;
+  }
+
+  bool stage_col(int w, int ci, int64_t t) {
+    ColInfo& c = C[ci];
+    const int r = alloc(w, c.brows, t);
+    if (r < 0) return false;
+    take(w, r, c.brows, c.k);
+    c.block = r;
+    c.staged = true;
+    std::vector<std::pair<int, int>> rows;
+    const int base = sc.c_base[c.k];
+    for (int i = 0; i < c.len; i++) rows.push_back({base + i, w * R + r + i});
+    emit_gather(w, ARR_LU, rows);
+    if (sc.fuse_fwd) emit_gather(w, ARR_RHS, {{c.k, w * R + r + c.len + 1}});
+    uncommitted_cols[w].push_back(ci);
+    return true;
+  }
+
+  // Reads `it` in place from the producer's block when it is still there,
+  // pinning those rows through level L; at most half of a ring is pinned,
+  // so the warps keep room for their own copies.
+  bool try_resident(Item& it, int L) {
+    const ColInfo& pc = C[it.j];
+    if (pc.warp < 0 || pc.block < 0 || pc.level >= L) return false;
+    const size_t b = (size_t)pc.warp * R + pc.block + it.rel;
+    int fresh = 0;
+    for (int i = 0; i < it.nrows; i++) {
+      if (tag[b + i] != tagof(it.j, it.rel + i)) return false;
+      if (busy[b + i] < tend(L)) fresh++;
+    }
+    if (pinned[pc.warp] + fresh > R / 2) return false;
+    pinned[pc.warp] += fresh;
+    it.row = (int)b;
+    it.state = ST_RESIDENT;
+    for (int i = 0; i < it.nrows; i++) busy[b + i] = std::max(busy[b + i], tend(L));
+    out->rows_resident += it.nrows;
+    return true;
+  }
+
+  void flush_steps(int w, int stage_abs, std::vector<Step>& steps) {
+    Emit& e = em[w];
+    size_t i = 0;
+    while (i < steps.size()) {
+      // header word, steps from the next 4-word boundary, 4 words of
+      // over-read room
+      const size_t first = (e.w.size() + 1 + 3) & ~(size_t)3;
+      if (first + 4 + 4 > e.cstart + e.cw) {
+        e.next_chunk();
+        continue;
+      }
+      size_t m = std::min(steps.size() - i, (e.cstart + e.cw - first - 4) / 4);
+      m = std::min<size_t>(m, 4095);
+      e.w.push_back(CMD_STEPS | (int32_t)(m << 4) | (stage_abs << 16));
+      while (e.w.size() < first) e.w.push_back(0);
+      for (size_t q = 0; q < m; q++) {
+        const Step& s = steps[i + q];
+        e.w.push_back((int32_t)s.x); e.w.push_back((int32_t)s.y);
+        e.w.push_back((int32_t)s.z); e.w.push_back((int32_t)s.w);
+      }
+      i += m;
+    }
+    steps.clear();
+    pos[w]++;
+  }
+
+  void add_steps(const ColInfo& c, const Item& it, std::vector<Step>& steps) {
+    const int e = sc.cu_ptr[c.k] + it.upos;
+    const int d0 = sc.cu_dptr[e] + it.dfirst;
+    const uint32_t dummy = (uint32_t)(c.len + 2);
+    for (int o = 0; o < it.nrows; o += kStepOps) {
+      const int cnt = std::min(kStepOps, it.nrows - o);
+      Step s{};
+      s.x = (uint32_t)(it.row + o) | ((uint32_t)it.upos << 16) | ((uint32_t)cnt << 26);
+      uint32_t d[9];
+      for (int t = 0; t < 9; t++) d[t] = dummy;
+      for (int t = 0; t < cnt; t++) d[t] = (uint32_t)sc.cu_dst[d0 + o + t];
+      s.y = d[0] | (d[1] << 10) | (d[2] << 20);
+      s.z = d[3] | (d[4] << 10) | (d[5] << 20);
+      s.w = d[6] | (d[7] << 10) | (d[8] << 20);
+      steps.push_back(s);
+      out->n_steps++;
+    }
+  }
+
+  // Emits everything of column ci (warp w, level L).
+  bool run_col(int w, int ci, int L) {
+    ColInfo& c = C[ci];
+    int64_t t = now(w, L);
+    bool waited_late = false;
+    if (!c.staged) {
+      if (!stage_col(w, ci, t)) {
+        err = "no ring room for the stage block of column " + std::to_string(c.k);
+        return false;
+      }
+      waited_late = true;  // the stage copy was not issued ahead
+    }
+    for (Item& it : c.items)
+      if (it.state == ST_NONE && gather_item(w, it, t)) {
+        out->rows_late += it.nrows;
+        waited_late = true;
+      }
+    commit(w);
+    // the warp's next column: its stage block and every value finished before
+    // this level, issued now and waited for when that column starts
+    // (only when this column has every value placed: a prefetch must not
+    // take the room this column still needs)
+    bool placed = true;
+    for (const Item& it : c.items) placed = placed && it.state != ST_NONE;
+    const int sp = seqpos[ci];
+    if (placed && sp + 1 < (int)seq[w].size()) {
+      const int ni = seq[w][sp + 1];
+      ColInfo& nc = C[ni];
+      if (!nc.staged && stage_col(w, ni, t)) {
+        for (Item& it : nc.items) {
+          if (it.state != ST_NONE || C[it.j].level >= L) continue;
+          if (!gather_item(w, it, t)) break;
+          out->rows_prefetched += it.nrows;
+        }
+        commit(w);
+      }
+    }
+    int g = c.group;
+    for (const Item& it : c.items)
+      if (it.state == ST_GATHERED) g = std::max(g, it.group);
+    wait_for(w, g, L, waited_late);
+    // updates, fetching values that found no room just in time
+    std::vector<Step> steps;
+    std::vector<Item*> consumed;
+    const int stage_abs = w * R + c.block;
+    auto release_consumed = [&]() {
+      const int64_t tf = now(w, L);
+      for (Item* it : consumed) release_abs(it->row, it->nrows, tf);
+      consumed.clear();
+    };
+    auto jit = [&](size_t from) -> bool {
+      flush_steps(w, stage_abs, steps);
+      release_consumed();
+      const int64_t tj = now(w, L);
+      bool any = false;
+      for (size_t q = from; q < c.items.size(); q++) {
+        Item& it = c.items[q];
+        if (it.state != ST_NONE) continue;
+        if (!gather_item(w, it, tj)) break;
+        out->rows_jit += it.nrows;
+        any = true;
+      }
+      if (!any) return false;
+      commit(w);
+      int gg = -1;
+      for (size_t q = from; q < c.items.size(); q++)
+        if (c.items[q].state == ST_GATHERED) gg = std::max(gg, c.items[q].group);
+      wait_for(w, gg, L, true);
+      return true;
+    };
+    size_t q = 0;
+    for (; q < c.items.size() && c.items[q].kind == IT_LRUN; q++) {
+      Item& it = c.items[q];
+      if (it.state == ST_NONE && !jit(q)) {
+        err = "no ring room for an update run of column " + std::to_string(c.k);
+        return false;
+      }
+      add_steps(c, it, steps);
+      wcost[w] += 70.0 * ((it.nrows + kStepOps - 1) / kStepOps);
+      if (it.state == ST_GATHERED) consumed.push_back(&it);
+    }
+    flush_steps(w, stage_abs, steps);
+    release_consumed();
+    // forward substitution y_k = b_k - sum L(k, j) y_j, in order, in pieces
+    // whose values fit in the ring
+    Emit& e = em[w];
+    if (sc.fuse_fwd) {
+      size_t f = q;
+      bool first = true;
+      do {
+        if (f < c.items.size()) {
+          const size_t h = c.items[f].state == ST_NONE ? f : f + 1;
+          if (c.items[h].state == ST_NONE && !jit(h)) {
+            err = "no ring room for the forward terms of column " + std::to_string(c.k);
+            return false;
+          }
+        }
+        size_t f1 = f;
+        while (f1 < c.items.size() && c.items[f1].state != ST_NONE && c.items[f1 + 1].state != ST_NONE)
+          f1 += 2;
+        size_t a0 = f;
+        do {  // FWD commands over pairs a0 .. f1 (split at chunk ends)
+          e.need(2 + 8);
+          size_t m = std::min((f1 - a0) / 2, (e.room() - 2) & ~(size_t)7);
+          const size_t mp = (m + 7) & ~(size_t)7;
+          e.w.push_back(CMD_FWD | (int32_t)(mp << 4) | (first ? (1 << 20) : 0));
+          e.w.push_back(stage_abs | (c.len << 16));
+          for (size_t t = 0; t < m; t++) {
+            const Item& la = c.items[a0 + 2 * t];
+            const Item& ya = c.items[a0 + 2 * t + 1];
+            e.w.push_back(la.row | (ya.row << 16));
+          }
+          for (size_t t = m; t < mp; t++) e.w.push_back(zero_row() | (zero_row() << 16));
+          first = false;
+          a0 += 2 * m;
+        } while (a0 < f1);
+        pos[w]++;
+        const int64_t tr = now(w, L);
+        for (size_t t = f; t < f1; t++)
+          if (c.items[t].state == ST_GATHERED) release_abs(c.items[t].row, c.items[t].nrows, tr);
+        f = f1;
+      } while (f < c.items.size());
+    }
+    // finish
+    e.need(5);
+    e.w.push_back(CMD_FINISH);
+    e.w.push_back(c.k);
+    e.w.push_back(sc.c_base[c.k]);
+    e.w.push_back(sc.c_ulen[c.k] | (sc.c_llen[c.k] << 16));
+    e.w.push_back(stage_abs);
+    const int nfw = (int)(c.items.size() - q) / 2;
+    const int64_t tf = now(w, L);
+    release_abs(stage_abs, c.brows, tf);
+    wcost[w] += 80 + 4.0 * c.len + 8.0 * nfw;
+    return true;
+  }
+
+  bool build(Stream& st) {
+    out = &st;
+    st = Stream();
+    st.plan = P;
+    if (R <= 0 || W <= 0 || P.chunk_words % 4 || P.chunk_words < 64) {
+      err = "bad plan";
+      return false;
+    }
+    if (W * R + kSpareRows > kMaxRows) {
+      err = "ring rows exceed the 11-bit row fields";
+      return false;
+    }
+    if (sc.n_slots >= (1 << 21) || n >= (1 << 21)) {
+      err = "factor too large for 21-bit row fields";
+      return false;
+    }
+    // ---- columns and their value sources
+    C.assign(n, ColInfo());
+    for (int k = 0; k < n; k++) {
+      ColInfo& c = C[k];
+      c.k = k;
+      c.level = sc.col_level[k];
+      c.len = sc.c_ulen[k] + 1 + sc.c_llen[k];
+      c.brows = c.len + 3;
+      if (c.len >= 1024) {
+        err = "column too long for 10-bit stage rows";
+        return false;
+      }
+      if (c.brows > R) {
+        err = "column " + std::to_string(k) + " longer than the ring";
+        return false;
+      }
+      for (int p = 0; p < sc.c_ulen[k]; p++) {
+        const int e = sc.cu_ptr[k] + p;
+        const int j = sc.cu_j[e];
+        const int nl = sc.c_llen[j];
+        for (int d = 0; d < nl; d += kPieceRows) {
+          Item it;
+          it.kind = IT_LRUN;
+          it.j = j;
+          it.rel = sc.c_ulen[j] + 1 + d;
+          it.src = sc.c_base[j] + it.rel;
+          it.nrows = std::min(kPieceRows, nl - d);
+          it.upos = p;
+          it.dfirst = d;
+          c.items.push_back(it);
+          c.nsteps += (it.nrows + kStepOps - 1) / kStepOps;
+        }
+      }
+      if (sc.fuse_fwd) {
+        for (int tt = sc.fw_ptr[k]; tt < sc.fw_ptr[k + 1]; tt++) {
+          const int slot = sc.fw_slot[tt], j = sc.fw_col[tt];
+          if (slot < 0) {
+            err = "fused forward substitution with off-diagonal terms";
+            return false;
+          }
+          Item a;
+          a.kind = IT_FWL;
+          a.j = j;
+          a.src = slot;
+          a.rel = slot - sc.c_base[j];
+          a.nrows = 1;
+          Item b;
+          b.kind = IT_FWY;
+          b.j = j;
+          b.src = j;
+          b.rel = sc.c_ulen[j] + 1 + sc.c_llen[j];
+          b.nrows = 1;
+          c.items.push_back(a);
+          c.items.push_back(b);
+        }
+      }
+      c.cost = 40 + 70.0 * c.nsteps + 4.0 * c.len + 8.0 * (sc.fuse_fwd ? sc.fw_ptr[k + 1] - sc.fw_ptr[k] : 0);
+    }
+    // ---- columns to warps: per level, longest first to the least loaded
+    //      warp (ties: least total so far, which rotates single columns)
+    seq.assign(W, {});
+    seqpos.assign(n, 0);
+    std::vector<double> tot(W, 0.0);
+    for (int L = 0; L < sc.n_levels; L++) {
+      std::vector<int> cols(sc.lev_cols.begin() + sc.lev_ptr[L], sc.lev_cols.begin() + sc.lev_ptr[L + 1]);
+      std::stable_sort(cols.begin(), cols.end(), [&](int a, int b) { return C[a].cost > C[b].cost; });
+      std::vector<double> load(W, 0.0);
+      std::vector<std::vector<int>> mine(W);
+      for (int k : cols) {
+        int best = 0;
+        for (int w = 1; w < W; w++)
+          if (load[w] < load[best] || (load[w] == load[best] && tot[w] < tot[best])) best = w;
+        load[best] += C[k].cost;
+        tot[best] += C[k].cost;
+        C[k].warp = best;
+        mine[best].push_back(k);
+      }
+      for (int w = 0; w < W; w++)
+        for (int k : mine[w]) {
+          seqpos[k] = (int)seq[w].size();
+          seq[w].push_back(k);
+        }
+    }
+    // ---- simulate the warps level by level and emit
+    busy.assign((size_t)W * R, -1);
+    tag.assign((size_t)W * R, -1);
+    cursor.assign(W, 0);
+    ngroups.assign(W, 0);
+    waited.assign(W, -1);
+    pos.assign(W, 0);
+    em.assign(W, Emit(P.chunk_words));
+    uncommitted.assign(W, {});
+    uncommitted_cols.assign(W, {});
+    pend_rows.assign(W, {});
+    wcost.assign(W, 0.0);
+    pinned.assign(W, 0);
+    std::vector<int> wnext(W, 0);
+    for (int L = 0; L < sc.n_levels; L++) {
+      for (int w = 0; w < W; w++) { pos[w] = 0; pinned[w] = 0; }
+      // stage blocks the warps' previous columns could not issue ahead are
+      // placed first, before any value is pinned for reading in place
+      for (int w = 0; w < W; w++) {
+        const int q = wnext[w];
+        if (q < (int)seq[w].size() && C[seq[w][q]].level == L && !C[seq[w][q]].staged)
+          stage_col(w, seq[w][q], now(w, L));
+      }
+      // values finished at earlier levels that are still in some ring
+      for (int q = sc.lev_ptr[L]; q < sc.lev_ptr[L + 1]; q++) {
+        ColInfo& c = C[sc.lev_cols[q]];
+        for (Item& it : c.items)
+          if (it.state == ST_NONE) try_resident(it, L);
+      }
+      std::fill(wcost.begin(), wcost.end(), 0.0);
+      for (int w = 0; w < W; w++) {
+        while (wnext[w] < (int)seq[w].size() && C[seq[w][wnext[w]]].level == L) {
+          if (!run_col(w, seq[w][wnext[w]], L)) return false;
+          wnext[w]++;
+        }
+        em[w].need(1);
+        em[w].w.push_back(CMD_BAR);
+      }
+      st.est_cycles += *std::max_element(wcost.begin(), wcost.end()) + 120;
+    }
+    st.n_bars = sc.n_levels;
+    // ---- assemble
+    st.chunk0.assign(W, 0);
+    st.nchunks.assign(W, 0);
+    for (int w = 0; w < W; w++) {
+      Emit& e = em[w];
+      e.w.push_back(CMD_END);
+      while (e.w.size() < e.cstart + e.cw) e.w.push_back(CMD_NOP);
+      st.chunk0[w] = (int32_t)(st.words.size() / P.chunk_words);
+      st.nchunks[w] = (int32_t)(e.w.size() / P.chunk_words);
+      st.words.insert(st.words.end(), e.w.begin(), e.w.end());
+    }
+    return true;
+  }
+};
+
+}  // namespace
+
+bool build_stream(const Schedule& sc, const StreamPlan& plan, Stream& out, std::string& why) {
+  Builder b(sc, plan);
+  bool ok = false;
+  try {
+    ok = b.build(out);
+  } catch (const std::exception& e) {
+    b.err = e.what();
+    ok = false;
+  }
+  if (!ok) why = b.err;
+  return ok;
+}
+
+bool choose_stream(const Schedule& sc, int elem, size_t smem_budget, Stream& out,
+                   std::string& why) {
+  bool found = false;
+  std::string last;
+  for (int nw : {8, 6, 4, 3, 2, 1}) {
+    StreamPlan p;
+    p.elem = elem;
+    p.nw = nw;
+    p.chunk_words = 512;
+    const size_t fixed = (size_t)nw * 2 * p.chunk_words * 4 + (size_t)kSpareRows * 32 * elem;
+    if (fixed >= smem_budget) continue;
+    int r = (int)((smem_budget - fixed) / ((size_t)32 * elem) / nw);
+    r = std::min(r, (kMaxRows - kSpareRows) / nw);
+    if (r < 16) continue;
+    p.ring_rows = r;
+    Stream s;
+    std::string w;
+    if (!build_stream(sc, p, s, w)) {
+      last = w;
+      continue;
+    }
+    if (!found || s.est_cycles < out.est_cycles) {
+      out = std::move(s);
+      found = true;
+    }
+  }
+  if (!found) why = last.empty() ? "no plan fits the shared-memory budget" : last;
+  return found;
+}
+
+// ---------------------------------------------------------------------------
+// host interpreter
+
+std::string run_stream_host(const Schedule& sc, const Stream& st, std::vector<double>& lu,
+                            const std::vector<double>& rhs, std::vector<double>& X,
+                            bool& singular) {
+  const StreamPlan& P = st.plan;
+  const int W = P.nw, R = P.ring_rows, CW = P.chunk_words, n = sc.n_u;
+  const int rows = W * R + kSpareRows;
+  std::vector<double> ring(rows, 0.0);
+  const int zero_row = W * R, trash_row = W * R + 1;
+  std::vector<int> pend(rows, -1);  // commit group of a copy not yet waited for
+  std::vector<int> col_of_slot(sc.n_slots, -1);
+  for (int k = 0; k < n; k++)
+    for (int p = 0; p < sc.c_ulen[k] + 1 + sc.c_llen[k]; p++) col_of_slot[sc.c_base[k] + p] = k;
+  std::vector<int> colfin(n, -1), xfin(n, -1);
+  singular = false;
+  if ((int)lu.size() != sc.n_slots || (int)rhs.size() != n) return "buffer sizes";
+  X.assign(n, 0.0);
+  struct WS {
+    int chunk = 0, pc = 0, ng = 0, bars = 0;
+    bool done = false;
+    std::vector<int> pend_rows;
+  };
+  std::vector<WS> ws(W);
+  for (int w = 0; w < W; w++) ws[w].pc = st.chunk0[w] * CW;
+  auto fail = [&](int w, const std::string& m) {
+    return "warp " + std::to_string(w) + " word " + std::to_string(ws[w].pc) + ": " + m;
+  };
+  // per level: who touched which row
+  std::vector<int> wr_by(rows, -1), rd_by(rows, -1), stamp_w(rows, -1), stamp_r(rows, -1);
+  for (int L = 0; L <= st.n_bars; L++) {
+    for (int w = 0; w < W; w++) {
+      WS& s = ws[w];
+      if (s.done) continue;
+      std::string e;
+      auto in_ring = [&](int r) { return r >= 0 && r < W * R; };
+      auto note_w = [&](int r) -> bool {
+        if (stamp_w[r] == L && wr_by[r] != w) { e = "two warps write row " + std::to_string(r); return false; }
+        if (stamp_r[r] == L && rd_by[r] != w && rd_by[r] != -2) { e = "row " + std::to_string(r) + " written while another warp reads it"; return false; }
+        if (stamp_r[r] == L && rd_by[r] == -2) { e = "row " + std::to_string(r) + " written while other warps read it"; return false; }
+        stamp_w[r] = L;
+        wr_by[r] = w;
+        return true;
+      };
+      auto note_r = [&](int r) -> bool {
+        if (pend[r] >= 0) { e = "row " + std::to_string(r) + " read before its copy is waited for"; return false; }
+        if (stamp_w[r] == L && wr_by[r] != w) { e = "row " + std::to_string(r) + " read while another warp writes it"; return false; }
+        if (stamp_r[r] == L && rd_by[r] != w) rd_by[r] = -2;
+        else { stamp_r[r] = L; rd_by[r] = w; }
+        return true;
+      };
+      for (;;) {
+        if (s.pc < (st.chunk0[w] + s.chunk) * CW || s.pc >= (st.chunk0[w] + s.chunk + 1) * CW)
+          return fail(w, "ran past its chunk");
+        const int32_t w0 = st.words[s.pc];
+        const int op = w0 & 15;
+        if (op == CMD_NOP) { s.pc++; continue; }
+        if (op == CMD_NEXT) {
+          if (++s.chunk >= st.nchunks[w]) return fail(w, "NEXT past the last chunk");
+          s.pc = (st.chunk0[w] + s.chunk) * CW;
+          continue;
+        }
+        const int cend = (st.chunk0[w] + s.chunk + 1) * CW - 1;  // NEXT / END word
+        if (op == CMD_END) {
+          if (s.bars != st.n_bars) return fail(w, "END after a wrong number of barriers");
+          s.done = true;
+          break;
+        }
+        if (op == CMD_BAR) { s.pc++; s.bars++; break; }
+        if (op == CMD_GATHER) {
+          const int m = (w0 >> 4) & 0xffff, commit = (w0 >> 23) & 1;
+          if (s.pc + 1 + m > cend) return fail(w, "GATHER past its chunk");
+          if (m % (512 / (32 * P.elem))) return fail(w, "GATHER not padded");
+          for (int q = 0; q < m; q++) {
+            const uint32_t rw = (uint32_t)st.words[s.pc + 1 + q];
+            const int src = (int)(rw & 0x1fffff), dst = (int)(rw >> 21);
+            if (dst == trash_row && src == 0) continue;  // padding copy
+            if (dst < 0 || dst >= W * R || dst / R != w) return fail(w, "gather outside the warp's ring");
+            if (pend[dst] >= 0) return fail(w, "gather onto a row with a copy in flight");
+            double v;
+            int arr = ARR_LU, rsrc = src;
+            if (src >= sc.n_slots + n) { arr = ARR_RHS; rsrc = src - sc.n_slots - n; }
+            else if (src >= sc.n_slots) { arr = ARR_X; rsrc = src - sc.n_slots; }
+            const int srcv = src;
+            (void)srcv;
+            if (arr == ARR_LU) {
+              if (rsrc >= sc.n_slots) return fail(w, "factor row out of range");
+              const int col = col_of_slot[rsrc];
+              if (colfin[col] >= L) return fail(w, "copies a value finished in the same level");
+              v = lu[rsrc];
+            } else if (arr == ARR_X) {
+              if (xfin[rsrc] < 0 || xfin[rsrc] >= L) return fail(w, "copies y before it is final");
+              v = X[rsrc];
+            } else {
+              if (rsrc >= n) return fail(w, "rhs row out of range");
+              v = rhs[rsrc];
+            }
+            if (!note_w(dst)) return fail(w, e);
+            ring[dst] = v;
+            pend[dst] = s.ng;
+            s.pend_rows.push_back(dst);
+          }
+          if (commit) s.ng++;
+          s.pc += 1 + m;
+          continue;
+        }
+        if (op == CMD_WAIT) {
+          const int m = (w0 >> 4) & 7;
+          const int upto = s.ng - 1 - m;
+          std::vector<int> keep;
+          for (int r : s.pend_rows) {
+            if (pend[r] >= 0 && pend[r] <= upto) pend[r] = -1;
+            if (pend[r] >= 0) keep.push_back(r);
+          }
+          s.pend_rows.swap(keep);
+          s.pc++;
+          continue;
+        }
+        if (op == CMD_STEPS) {
+          const int m = (w0 >> 4) & 0xfff, S0 = (int)(((uint32_t)w0) >> 16);
+          const int first = (s.pc + 1 + 3) & ~3;
+          if (first + 4 * m + 4 > (st.chunk0[w] + s.chunk + 1) * CW) return fail(w, "STEPS past its chunk");
+          for (int q = 0; q < m; q++) {
+            const uint32_t* d = reinterpret_cast<const uint32_t*>(&st.words[first + 4 * q]);
+            const int lrow = (int)(d[0] & 0xffff), jp = (int)((d[0] >> 16) & 0x3ff), cnt = (int)(d[0] >> 26);
+            if (cnt < 1 || cnt > kStepOps) return fail(w, "bad step count");
+            if (lrow + kStepOps > rows) return fail(w, "step L rows out of range");
+            if (!in_ring(S0 + jp)) return fail(w, "step pivot row out of range");
+            if (!note_r(S0 + jp)) return fail(w, e);
+            const double xj = ring[S0 + jp];
+            uint32_t dw[3] = {d[1], d[2], d[3]};
+            for (int tt = cnt; tt < kStepOps; tt++) {
+              const int dr = S0 + (int)((dw[tt / 3] >> (10 * (tt % 3))) & 0x3ff);
+              if (!in_ring(dr)) return fail(w, "unused step slot outside the ring");
+            }
+            for (int tt = 0; tt < cnt; tt++) {
+              const int dr = S0 + (int)((dw[tt / 3] >> (10 * (tt % 3))) & 0x3ff);
+              if (!in_ring(dr) || !in_ring(lrow + tt)) return fail(w, "step row out of range");
+              if (dr == S0 + jp) return fail(w, "step writes its pivot row");
+              if (!note_r(lrow + tt) || !note_r(dr) || !note_w(dr)) return fail(w, e);
+              ring[dr] = ring[dr] - ring[lrow + tt] * xj;
+            }
+          }
+          s.pc = first + 4 * m;
+          continue;
+        }
+        if (op == CMD_FWD) {
+          const int m = (w0 >> 4) & 0xffff, first = (w0 >> 20) & 1;
+          const int S0 = st.words[s.pc + 1] & 0xffff, len = (st.words[s.pc + 1] >> 16) & 0xffff;
+          if (!sc.fuse_fwd) return fail(w, "FWD without fusion");
+          if (s.pc + 2 + m > cend) return fail(w, "FWD past its chunk");
+          if (m % 8) return fail(w, "FWD not padded");
+          if (!in_ring(S0 + len + 1)) return fail(w, "FWD rows out of range");
+          const int yr0 = S0 + len;
+          if (!note_r(first ? yr0 + 1 : yr0)) return fail(w, e);
+          double y = ring[first ? yr0 + 1 : yr0];
+          for (int f = 0; f < m; f++) {
+            const uint32_t fw = (uint32_t)st.words[s.pc + 2 + f];
+            const int lr = (int)(fw & 0xffff), yr = (int)(fw >> 16);
+            if (lr == zero_row && yr == zero_row) continue;  // padding term
+            if (!in_ring(lr) || !in_ring(yr)) return fail(w, "forward term row out of range");
+            if (!note_r(lr) || !note_r(yr)) return fail(w, e);
+            y -= ring[lr] * ring[yr];
+          }
+          if (!note_w(yr0)) return fail(w, e);
+          ring[yr0] = y;
+          s.pc += 2 + m;
+          continue;
+        }
+        if (op == CMD_FINISH) {
+          const int k = st.words[s.pc + 1], base = st.words[s.pc + 2];
+          const int ulen = st.words[s.pc + 3] & 0xffff, llen = (st.words[s.pc + 3] >> 16) & 0xffff;
+          const int S0 = st.words[s.pc + 4];
+          const int len = ulen + 1 + llen;
+          if (s.pc + 5 > cend) return fail(w, "FINISH past its chunk");
+          if (k < 0 || k >= n || base != sc.c_base[k] || ulen != sc.c_ulen[k] || llen != sc.c_llen[k])
+            return fail(w, "FINISH header does not match the column");
+          if (!in_ring(S0) || !in_ring(S0 + len + 2) || S0 / R != (S0 + len + 2) / R || S0 / R != w)
+            return fail(w, "stage block out of range");
+          for (int p = 0; p < len; p++)
+            if (!note_r(S0 + p)) return fail(w, e);
+          const double piv = ring[S0 + ulen];
+          if (piv == 0.0) singular = true;
+          const double inv = 1.0 / piv;
+          for (int p = 0; p <= ulen; p++) lu[base + p] = ring[S0 + p];
+          for (int p = ulen + 1; p < len; p++) {
+            if (!note_w(S0 + p)) return fail(w, e);
+            ring[S0 + p] = ring[S0 + p] * inv;
+            lu[base + p] = ring[S0 + p];
+          }
+          colfin[k] = L;
+          if (sc.fuse_fwd) {
+            if (!note_r(S0 + len)) return fail(w, e);
+            X[k] = ring[S0 + len];
+            xfin[k] = L;
+          }
+          s.pc += 5;
+          continue;
+        }
+        return fail(w, "bad opcode " + std::to_string(op));
+      }
+    }
+  }
+  for (int w = 0; w < W; w++)
+    if (!ws[w].done) return "warp " + std::to_string(w) + " did not reach END";
+  for (int k = 0; k < n; k++)
+    if (colfin[k] < 0) return "column " + std::to_string(k) + " never finished";
+  return "";
+}
+
+}  // namespace gox

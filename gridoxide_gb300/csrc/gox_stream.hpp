@@ -1,0 +1,117 @@
+// Per-warp command streams for the batched refactor.
+//
+// The refactor of one topology repeats the same sequence of operations for
+// every scenario and every Newton iteration, so all scheduling is done here,
+// once per topology, on the host: which warp of the refactor CTA takes which
+// column, where in the CTA's shared memory every value lives, which global
+// loads are issued a column ahead of their use, and which values are read
+// straight from the shared-memory block of the column that produced them
+// instead of being loaded again.  The result is, per warp, a list of
+// commands that the kernel interprets:
+//
+//   BAR                 __syncthreads (end of a dependency level)
+//   GATHER arr m rows   cp.async copies of m rows (one row = one value for
+//                       the 32 scenarios of a group) from the factor image,
+//                       the forward-substitution vector or the right-hand
+//                       side into ring rows; optionally commits the group
+//   WAIT n              cp.async.wait_group n, then __syncwarp
+//   STEPS m stage       m update steps on the column staged at `stage`
+//   FWD                 part of the forward substitution y_k = b_k -
+//                       sum L(k, j) y_j (terms in order, in pieces)
+//   FINISH              pivot, scale L, write the column back to the factor
+//                       and y_k to the forward-substitution vector
+//   NEXT                continue with the warp's next stream chunk
+//   END
+//
+// Shared memory: per warp two stream chunks (TMA bulk copies) and a ring of
+// rows; the rings of all warps form one row space, so a step may read the
+// L values of a column finished by any warp while its block is still there.
+#pragma once
+#include <cstdint>
+#include <string>
+#include <vector>
+
+#include "gox_engine.hpp"
+
+namespace gox {
+
+enum : int32_t {
+  CMD_NOP = 0,
+  CMD_BAR = 1,
+  CMD_GATHER = 2,
+  CMD_WAIT = 3,
+  CMD_STEPS = 4,
+  CMD_FINISH = 5,
+  CMD_NEXT = 6,
+  CMD_END = 7,
+  CMD_FWD = 8
+};
+enum : int32_t { ARR_LU = 0, ARR_X = 1, ARR_RHS = 2 };
+
+constexpr int kStepOps = 9;     // update ops per step (one L(:, j) run piece)
+// Rows after the rings of all warps: the zero row (padding terms of the
+// forward substitution read it), the trash row (padding copies land in it),
+// and rows the unused slots of a step may read.
+constexpr int kSpareRows = 12;
+constexpr int kMaxRows = 2048;  // ring rows of all warps (11-bit row fields)
+
+// Encodings (all little fields of 32-bit words):
+//   GATHER  w0 = op | m << 4 | commit << 23, then m words src_row | dst_row << 21;
+//           source rows number the factor image, then the forward-substitution
+//           vector, then the right-hand side as one row space; m is a multiple
+//           of the rows one 16-byte per-lane copy moves (4 FP32, 2 FP64),
+//           padded with copies of row 0 into the trash row
+//   WAIT    w0 = op | n << 4
+//   STEPS   w0 = op | m << 4 | stage_row << 16, then (from the next 16-byte
+//           boundary) m uint4 steps:
+//             x = l_row | j_pos << 16 | cnt << 26    (L values in rows l_row ..,
+//                                                     U(j, k) in stage row j_pos)
+//             y, z, w = 3 destination stage rows each (10 bits); a step
+//             always runs 9 updates, the unused ones on the block's dummy row
+//   FWD     w0 = op | m << 4 | first << 20, stage_row | len << 16, then m words
+//           l_row | y_row << 16 (L(k, j) and y_j): y = (first ? b : y) - sum;
+//           m is a multiple of 8, padded with terms on the zero row
+//   FINISH  w0 = op, k, base, ulen | llen << 16, stage_row; the stage block
+//           is [column rows | y | b | dummy]
+struct StreamPlan {
+  int elem = 4;             // bytes per value: 4 (FP32) or 8 (FP64)
+  int nw = 8;               // warps per CTA
+  int ring_rows = 0;        // ring rows per warp
+  int chunk_words = 512;    // stream chunk, 32-bit words (multiple of 4)
+};
+
+struct Stream {
+  StreamPlan plan;
+  std::vector<int32_t> words;            // all chunks; warp w owns chunks chunk0[w] ..
+  std::vector<int32_t> chunk0, nchunks;  // per warp
+  int n_bars = 0;
+  // statistics of the schedule
+  int64_t rows_gathered = 0, rows_prefetched = 0, rows_resident = 0, rows_late = 0;
+  int64_t rows_jit = 0, n_steps = 0, n_waits = 0, n_groups = 0;
+  double est_cycles = 0;  // rough critical-path estimate, used to choose a plan
+};
+
+// Shared memory (bytes) the refactor kernel needs for a plan.
+size_t stream_smem_bytes(const StreamPlan& plan);
+
+// Compiles the refactor of a schedule for a plan.  Returns false, with the
+// reason, when the plan cannot hold it (a column longer than the ring).
+bool build_stream(const Schedule& sc, const StreamPlan& plan, Stream& out, std::string& why);
+
+// Chooses the plan (warps, ring) within `smem_budget` bytes with the
+// lowest estimated critical path, and builds its stream.
+bool choose_stream(const Schedule& sc, int elem, size_t smem_budget, Stream& out,
+                   std::string& why);
+
+// Host interpreter of a stream for one scenario in FP64.  lu holds the A
+// image in the factor's layout on entry and the factor on exit; X receives
+// y_k (forward substitution) when the schedule fuses it.  Checks every
+// index, that no row is read before the copy into it is waited for, that
+// no copy reads a value before the level that finishes it, and that no two
+// warps touch a row within one level when one of them writes it.  Returns
+// an empty string, or the first violation.
+std::string run_stream_host(const Schedule& sc, const Stream& st, std::vector<double>& lu,
+                            const std::vector<double>& rhs, std::vector<double>& X,
+                            bool& singular);
+
+}  // namespace gox

@@ -201,8 +201,15 @@ int gox_factor_host(int32_t n, int32_t nnz, const int32_t *rows, const int32_t *
 /* Sizes of the topology's Jacobian and factor, once its pivot order is
  * fixed: [0] n unknowns, [1] nnz J, [2] nnz L (no diag), [3] nnz U (no
  * diag), [4] nnz off-diagonal, [5] BTF blocks, [6] refactor levels,
- * [7] solve phases, [8] LU slots per scenario, [9] max column length.
- * Returns GOX_E_INVALID before the first solve. */
+ * [7] solve phases, [8] LU slots per scenario, [9] max column length;
+ * refactor schedule of the FP32 plan: [10] warps per CTA, [11] ring rows
+ * per warp, [12] estimated critical path (cycles), [13] rows read in place
+ * from another column's shared-memory block, [14] rows copied from global
+ * memory, [15] of them issued a column ahead, [16] issued at the column's
+ * start, [17] issued just in time, [18] update steps, [19] waits; the FP64
+ * plan: [20] warps, [21] ring rows, [22] estimated cycles, [23] rows read
+ * in place.  info must hold 24 entries.  Returns GOX_E_INVALID before the
+ * first solve. */
 int gox_topo_info(const gox_topo *t, int64_t *info);
 
 /* The fixed factorization structure (klu_extract layout without values):
