@@ -1013,6 +1013,8 @@ int gox_topo_info(const gox_topo* t, int64_t* info) {
   info[16] = a.rows_late; info[17] = a.rows_jit; info[18] = a.n_steps; info[19] = a.n_waits;
   info[20] = b.plan.nw; info[21] = b.plan.ring_rows; info[22] = (int64_t)b.est_cycles;
   info[23] = b.rows_resident;
+  info[24] = a.n_column_cmds;
+  info[25] = (int64_t)a.words.size();
   return GOX_OK;
 }
 

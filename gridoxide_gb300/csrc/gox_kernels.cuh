@@ -370,31 +370,148 @@ struct StreamDev {
   int ring_rows, chunk_words, n_bars;
 };
 
+// Pieces of the refactor interpreter.  Every loop below runs over counts the
+// stream compiler padded (gather rows to 2 copies, steps to pairs, forward
+// terms to 8), so no branch depends on a value inside an iteration.
+template <typename T>
+struct Rf {
+  static constexpr uint32_t RB = 32u * sizeof(T);  // bytes per row
+  static constexpr int RPI = 512 / (int)RB;        // rows per 16-byte-per-lane copy
+  static constexpr int LPR = 32 / RPI;             // lanes per row in a copy
+
+  // m rows (multiple of 2 * RPI): words src_row | dst_row << 21 over the row
+  // space [factor image | X | right-hand side]
+  static __device__ __forceinline__ void gather(const int32_t* w, int m, uint32_t ring_s, int lane,
+                                                const T* LUg, const T* Xg, const T* RHSg,
+                                                int n_slots, int n_u) {
+    const int sub = lane % LPR, rsel = lane / LPR;
+    for (int q0 = 0; q0 < m; q0 += 2 * RPI) {
+#pragma unroll
+      for (int h = 0; h < 2; h++) {
+        const uint32_t rw = (uint32_t)w[q0 + h * RPI + rsel];
+        const uint32_t v = rw & 0x1fffffu;
+        const char* src = v < (uint32_t)n_slots ? (const char*)LUg + (size_t)v * RB
+                          : v < (uint32_t)(n_slots + n_u)
+                              ? (const char*)Xg + (size_t)(v - n_slots) * RB
+                              : (const char*)RHSg + (size_t)(v - n_slots - n_u) * RB;
+        cp_async16(ring_s + (rw >> 21) * RB + (uint32_t)sub * 16u, src + (size_t)sub * 16u);
+      }
+    }
+  }
+
+  static __device__ __forceinline__ void step(uint4 d, uint32_t st_lane, uint32_t ring_lane) {
+    const uint32_t la = ring_lane + (d.x & 0xffffu) * RB;
+    const T xj = lds<T>(st_lane + ((d.x >> 16) & 0x3ffu) * RB);
+    uint32_t da[kStepOps];
+    T xi[kStepOps], lv[kStepOps];
+#pragma unroll
+    for (int t = 0; t < kStepOps; t++) {
+      const uint32_t wd = t < 3 ? d.y : (t < 6 ? d.z : d.w);
+      da[t] = st_lane + ((wd >> (10 * (t % 3))) & 0x3ffu) * RB;
+    }
+#pragma unroll
+    for (int t = 0; t < kStepOps; t++) {
+      xi[t] = lds<T>(da[t]);
+      lv[t] = lds<T>(la + (uint32_t)t * RB);
+    }
+#pragma unroll
+    for (int t = 0; t < kStepOps; t++) sts(da[t], xi[t] - lv[t] * xj);
+  }
+
+  // m steps (even), uint4 each; the word after the last pair is readable
+  static __device__ __forceinline__ void steps(const uint4* sd, int m, uint32_t st_lane,
+                                               uint32_t ring_lane) {
+    uint4 d0 = sd[0], d1 = sd[1];
+    for (int q = 0; q < m; q += 2) {
+      const uint4 n0 = sd[q + 2], n1 = sd[q + 3];
+      step(d0, st_lane, ring_lane);
+      step(d1, st_lane, ring_lane);
+      d0 = n0;
+      d1 = n1;
+    }
+  }
+
+  // y = (first ? b : y) - sum L(k, j) y_j over m terms (multiple of 8)
+  static __device__ __forceinline__ void fwd(const int32_t* w, int m, bool first, uint32_t yrow,
+                                             uint32_t ring_lane) {
+    T y = lds<T>(first ? yrow + RB : yrow);
+    for (int f0 = 0; f0 < m; f0 += 8) {
+      T a[8], b[8];
+#pragma unroll
+      for (int t = 0; t < 8; t++) {
+        const uint32_t fw = (uint32_t)w[f0 + t];
+        a[t] = lds<T>(ring_lane + (fw & 0xffffu) * RB);
+        b[t] = lds<T>(ring_lane + (fw >> 16) * RB);
+      }
+#pragma unroll
+      for (int t = 0; t < 8; t++) y -= a[t] * b[t];
+    }
+    sts(yrow, y);
+  }
+
+  // pivot, scale L in place, write the column (and y_k) back; rows in
+  // blocks of 8, the last block clamped to the column's end
+  static __device__ __forceinline__ void finish(int k, int base, int ulen, int llen, uint32_t st_lane,
+                                                T* LUg, T* Xg, int lane, bool fuse, float ptol,
+                                                bool& bad, bool& tiny) {
+    const int len = ulen + 1 + llen;
+    const T piv = lds<T>(st_lane + (uint32_t)ulen * RB);
+    bad |= (piv == (T)0);
+    const T inv = rcp_rn(piv);
+    T* dst = LUg + (size_t)base * 32u + lane;
+    for (int p0 = 0; p0 <= ulen; p0 += 8) {
+      T v[8];
+#pragma unroll
+      for (int t = 0; t < 8; t++) v[t] = lds<T>(st_lane + (uint32_t)min(p0 + t, ulen) * RB);
+#pragma unroll
+      for (int t = 0; t < 8; t++) dst[(size_t)min(p0 + t, ulen) * 32u] = v[t];
+    }
+    T colmax = fabs(piv);
+    for (int p0 = ulen + 1; p0 < len; p0 += 8) {
+      T v[8];
+#pragma unroll
+      for (int t = 0; t < 8; t++) v[t] = lds<T>(st_lane + (uint32_t)min(p0 + t, len - 1) * RB);
+#pragma unroll
+      for (int t = 0; t < 8; t++) colmax = fmax(colmax, fabs(v[t]));
+#pragma unroll
+      for (int t = 0; t < 8; t++) {
+        const int r = min(p0 + t, len - 1);
+        v[t] *= inv;
+        sts(st_lane + (uint32_t)r * RB, v[t]);
+        dst[(size_t)r * 32u] = v[t];
+      }
+    }
+    tiny |= (ptol > 0.0f) && ((float)fabs(piv) < ptol * (float)colmax);
+    if (fuse) Xg[(size_t)k * 32u + lane] = lds<T>(st_lane + (uint32_t)len * RB);
+  }
+};
+
 // K3: refactor, the interpreter of the per-warp command streams.  One CTA
 // per group of 32 scenarios (lane = scenario).  Shared memory: per warp two
 // stream chunks (TMA bulk copies, mbarrier completion, bounded waits), then
-// the rings of all warps as one space of rows of 32 values.  The host has
-// placed every value: a column's stage block holds [column rows | y | b];
-// update runs L(:, j) are read either from a copy in the warp's ring or
-// straight from the producing column's block.  Commands (see the stream
-// compiler for encodings): GATHER (cp.async 16 B per lane), WAIT, STEPS
-// (up to 9 updates stage[d] -= L(d, j) * stage[j] each, loads of a step
-// before its stores, the next step's descriptor loaded ahead), FWD (forward
-// substitution terms), FINISH (pivot, scale L, write the column back, y_k),
-// BAR, NEXT, END.  A bounded
-// wait that gives up, or a malformed command, sets the error flag; the warp
-// then drains its copies and still takes every remaining barrier.
+// the rings of all warps as one space of rows of 32 values, then the zero
+// row, the trash row and spare rows.  The host has placed every value: a
+// column's stage block holds [column rows | y | b | dummy]; update runs
+// L(:, j) are read either from a copy in the warp's ring or straight from
+// the producing column's block.  The common case of a column is one COLUMN
+// command (copies for this column, copies issued ahead for the warp's next
+// column, wait, update steps, forward-substitution terms, finish, optional
+// level barrier); the single commands GATHER, WAIT, STEPS, FWD, FINISH,
+// BAR cover columns whose values are fetched in pieces.  Every branch is
+// per command or per loop trip; a step always performs 9 updates (unused
+// ones on the block's dummy row).  A bounded wait that gives up, or a
+// malformed command, sets the error flag; the warp then drains its copies
+// and still takes every remaining barrier.
 template <typename T>
 __global__ void __launch_bounds__(256) k_refactor(StreamDev P, SchedDev S, BatchDev D) {
+  using R = Rf<T>;
   const int g = blockIdx.x;
   if (!D.gact[g]) return;
   extern __shared__ __align__(128) unsigned char smem_raw[];
   __shared__ __align__(8) uint64_t mbar[8][2];
   __shared__ int flags[2][32];
   __shared__ int timed_out;
-  constexpr uint32_t RB = 32u * sizeof(T);    // bytes per row
-  constexpr int RPI = 512 / (int)RB;          // rows per 16-byte-per-lane copy
-  constexpr int LPR = 32 / RPI;               // lanes per row in a copy
+  constexpr uint32_t RB = R::RB;
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
   const int CW = P.chunk_words;
   int32_t* cbuf = reinterpret_cast<int32_t*>(smem_raw) + (size_t)warp * 2 * CW;
@@ -405,6 +522,7 @@ __global__ void __launch_bounds__(256) k_refactor(StreamDev P, SchedDev S, Batch
   T* Xg = (T*)D.sol + (size_t)g * S.n_u * 32u;
   const T* RHSg = (const T*)D.rhs + (size_t)g * S.n_u * 32u;
   const float ptol = D.piv_tol;
+  const bool fuse = S.fuse_fwd != 0;
   bool bad = false, tiny = false;
 
   if (threadIdx.x < 64) (&flags[0][0])[threadIdx.x] = 0;
@@ -431,151 +549,109 @@ __global__ void __launch_bounds__(256) k_refactor(StreamDev P, SchedDev S, Batch
   const int32_t* cb = cbuf;
   while (ok) {
     const int32_t w0 = cb[pc];
-    switch (w0 & 15) {
-      case CMD_STEPS: {
-        // no branch inside a step: unused slots update the block's dummy row
-        const int m = (w0 >> 4) & 0xfff;
-        const uint32_t st_lane = ring_lane + (((uint32_t)w0) >> 16) * RB;
-        const int first = (pc + 1 + 3) & ~3;
-        const uint4* sd = reinterpret_cast<const uint4*>(cb + first);
-        uint4 d = sd[0];
-        for (int q = 0; q < m; q++) {
-          const uint4 dn = sd[q + 1];
-          const uint32_t la = ring_lane + (d.x & 0xffffu) * RB;
-          const T xj = lds<T>(st_lane + ((d.x >> 16) & 0x3ffu) * RB);
-          uint32_t da[kStepOps];
-          T xi[kStepOps], lv[kStepOps];
-#pragma unroll
-          for (int t = 0; t < kStepOps; t++) {
-            const uint32_t wd = t < 3 ? d.y : (t < 6 ? d.z : d.w);
-            da[t] = st_lane + ((wd >> (10 * (t % 3))) & 0x3ffu) * RB;
-          }
-#pragma unroll
-          for (int t = 0; t < kStepOps; t++) {
-            xi[t] = lds<T>(da[t]);
-            lv[t] = lds<T>(la + (uint32_t)t * RB);
-          }
-#pragma unroll
-          for (int t = 0; t < kStepOps; t++) sts(da[t], xi[t] - lv[t] * xj);
-          d = dn;
-        }
-        pc = first + 4 * m;
-        break;
+    const int op = w0 & 15;
+    if (op == CMD_COLUMN) {
+      const int k = cb[pc + 1], base = cb[pc + 2], ul = cb[pc + 3];
+      const uint32_t h4 = (uint32_t)cb[pc + 4], h5 = (uint32_t)cb[pc + 5];
+      const int nfw = cb[pc + 6];
+      const uint32_t st_row = h4 & 0xffffu;
+      const int nlate = (int)(h4 >> 16), npref = (int)(h5 & 0xffffu), nst = (int)(h5 >> 16);
+      const int32_t* wl = cb + pc + 8;
+      if (nlate) {
+        R::gather(wl, nlate, ring_s, lane, LUg, Xg, RHSg, S.n_slots, S.n_u);
+        asm volatile("cp.async.commit_group;\n" ::: "memory");
       }
-      case CMD_GATHER: {
-        // m is a multiple of RPI (padding copies land in the trash row);
-        // source rows: the factor image, then X, then the right-hand side
-        const int m = (w0 >> 4) & 0xffff;
-        const int sub = lane % LPR, rsel = lane / LPR;
-        for (int q0 = 0; q0 < m; q0 += RPI) {
-          const uint32_t rw = (uint32_t)cb[pc + 1 + q0 + rsel];
-          const uint32_t v = rw & 0x1fffffu;
-          const char* src = v < (uint32_t)S.n_slots ? (const char*)LUg + (size_t)v * RB
-                            : v < (uint32_t)(S.n_slots + S.n_u)
-                                ? (const char*)Xg + (size_t)(v - S.n_slots) * RB
-                                : (const char*)RHSg + (size_t)(v - S.n_slots - S.n_u) * RB;
-          cp_async16(ring_s + (rw >> 21) * RB + (uint32_t)sub * 16u, src + (size_t)sub * 16u);
-        }
-        if ((w0 >> 23) & 1) asm volatile("cp.async.commit_group;\n" ::: "memory");
-        pc += 1 + m;
-        break;
+      if (npref) {
+        R::gather(wl + nlate, npref, ring_s, lane, LUg, Xg, RHSg, S.n_slots, S.n_u);
+        asm volatile("cp.async.commit_group;\n" ::: "memory");
       }
-      case CMD_WAIT:
+      if ((w0 >> 7) & 1) {
         cp_async_wait_n((w0 >> 4) & 7);
         __syncwarp();
-        pc++;
-        break;
-      case CMD_FWD: {
-        // m is a multiple of 8 (padding terms read the zero row)
-        const int m = (w0 >> 4) & 0xffff;
-        const uint32_t w1 = (uint32_t)cb[pc + 1];
-        const uint32_t yrow = ring_lane + ((w1 & 0xffffu) + (w1 >> 16)) * RB;
-        T y = lds<T>(((w0 >> 20) & 1) ? yrow + RB : yrow);
-        for (int f0 = 0; f0 < m; f0 += 8) {
-          T a[8], b[8];
-#pragma unroll
-          for (int t = 0; t < 8; t++) {
-            const uint32_t fw = (uint32_t)cb[pc + 2 + f0 + t];
-            a[t] = lds<T>(ring_lane + (fw & 0xffffu) * RB);
-            b[t] = lds<T>(ring_lane + (fw >> 16) * RB);
-          }
-#pragma unroll
-          for (int t = 0; t < 8; t++) y -= a[t] * b[t];
-        }
-        sts(yrow, y);
-        pc += 2 + m;
-        break;
       }
-      case CMD_FINISH: {
-        // rows in blocks of 8, the last block clamped to the column's end
-        const int k = cb[pc + 1], base = cb[pc + 2];
-        const int ulen = cb[pc + 3] & 0xffff, llen = (cb[pc + 3] >> 16) & 0xffff;
-        const uint32_t st_lane = ring_lane + (uint32_t)cb[pc + 4] * RB;
-        const int len = ulen + 1 + llen;
-        const T piv = lds<T>(st_lane + (uint32_t)ulen * RB);
-        bad |= (piv == (T)0);
-        const T inv = rcp_rn(piv);
-        T* dst = LUg + (size_t)base * 32u + lane;
-        for (int p0 = 0; p0 <= ulen; p0 += 8) {
-          T v[8];
-#pragma unroll
-          for (int t = 0; t < 8; t++) v[t] = lds<T>(st_lane + (uint32_t)min(p0 + t, ulen) * RB);
-#pragma unroll
-          for (int t = 0; t < 8; t++) dst[(size_t)min(p0 + t, ulen) * 32u] = v[t];
-        }
-        T colmax = fabs(piv);
-        for (int p0 = ulen + 1; p0 < len; p0 += 8) {
-          T v[8];
-#pragma unroll
-          for (int t = 0; t < 8; t++) v[t] = lds<T>(st_lane + (uint32_t)min(p0 + t, len - 1) * RB);
-#pragma unroll
-          for (int t = 0; t < 8; t++) colmax = fmax(colmax, fabs(v[t]));
-#pragma unroll
-          for (int t = 0; t < 8; t++) {
-            const int r = min(p0 + t, len - 1);
-            v[t] *= inv;
-            sts(st_lane + (uint32_t)r * RB, v[t]);
-            dst[(size_t)r * 32u] = v[t];
-          }
-        }
-        tiny |= (ptol > 0.0f) && ((float)fabs(piv) < ptol * (float)colmax);
-        if (S.fuse_fwd) Xg[(size_t)k * 32u + lane] = lds<T>(st_lane + (uint32_t)len * RB);
-        pc += 5;
-        break;
-      }
-      case CMD_BAR:
+      const int sw = (pc + 8 + nlate + npref + 3) & ~3;
+      const uint32_t st_lane = ring_lane + st_row * RB;
+      R::steps(reinterpret_cast<const uint4*>(cb + sw), nst, st_lane, ring_lane);
+      const int ulen = ul & 0xffff, llen = (ul >> 16) & 0xffff;
+      if (fuse)
+        R::fwd(cb + sw + 4 * nst, nfw, true, st_lane + (uint32_t)(ulen + 1 + llen) * RB, ring_lane);
+      R::finish(k, base, ulen, llen, st_lane, LUg, Xg, lane, fuse, ptol, bad, tiny);
+      pc = sw + 4 * nst + nfw;
+      if ((w0 >> 8) & 1) {
         __syncthreads();
         bars++;
-        pc++;
-        break;
-      case CMD_NOP:
-        pc++;
-        break;
-      case CMD_NEXT:
-        __syncwarp();
-        if (lane == 0 && chunk + 2 < nch)
-          bulk_load(cbuf + (size_t)buf * CW, gw + (size_t)(chunk + 2) * CW, (unsigned)CW * 4u,
-                    &mbar[warp][buf]);
-        chunk++;
-        buf ^= 1;
-        if (chunk >= nch) {
-          ok = false;
+      }
+    } else {
+      switch (op) {
+        case CMD_STEPS: {
+          const int m = (w0 >> 4) & 0xfff;
+          const int first = (pc + 1 + 3) & ~3;
+          R::steps(reinterpret_cast<const uint4*>(cb + first), m,
+                   ring_lane + (((uint32_t)w0) >> 16) * RB, ring_lane);
+          pc = first + 4 * m;
           break;
         }
-        if (buf == 0) {
-          ok = mbar_wait(&mbar[warp][0], par0);
-          par0 ^= 1u;
-        } else {
-          ok = mbar_wait(&mbar[warp][1], par1);
-          par1 ^= 1u;
+        case CMD_GATHER: {
+          const int m = (w0 >> 4) & 0xffff;
+          R::gather(cb + pc + 1, m, ring_s, lane, LUg, Xg, RHSg, S.n_slots, S.n_u);
+          if ((w0 >> 23) & 1) asm volatile("cp.async.commit_group;\n" ::: "memory");
+          pc += 1 + m;
+          break;
         }
-        cb = cbuf + (size_t)buf * CW;
-        pc = 0;
-        break;
-      case CMD_END:
-        goto done;
-      default:
-        ok = false;
+        case CMD_WAIT:
+          cp_async_wait_n((w0 >> 4) & 7);
+          __syncwarp();
+          pc++;
+          break;
+        case CMD_FWD: {
+          const int m = (w0 >> 4) & 0xffff;
+          const uint32_t w1 = (uint32_t)cb[pc + 1];
+          R::fwd(cb + pc + 2, m, (w0 >> 20) & 1,
+                 ring_lane + ((w1 & 0xffffu) + (w1 >> 16)) * RB, ring_lane);
+          pc += 2 + m;
+          break;
+        }
+        case CMD_FINISH: {
+          const int ulen = cb[pc + 3] & 0xffff, llen = (cb[pc + 3] >> 16) & 0xffff;
+          R::finish(cb[pc + 1], cb[pc + 2], ulen, llen, ring_lane + (uint32_t)cb[pc + 4] * RB, LUg,
+                    Xg, lane, fuse, ptol, bad, tiny);
+          pc += 5;
+          break;
+        }
+        case CMD_BAR:
+          __syncthreads();
+          bars++;
+          pc++;
+          break;
+        case CMD_NOP:
+          pc++;
+          break;
+        case CMD_NEXT:
+          __syncwarp();
+          if (lane == 0 && chunk + 2 < nch)
+            bulk_load(cbuf + (size_t)buf * CW, gw + (size_t)(chunk + 2) * CW, (unsigned)CW * 4u,
+                      &mbar[warp][buf]);
+          chunk++;
+          buf ^= 1;
+          if (chunk >= nch) {
+            ok = false;
+            break;
+          }
+          if (buf == 0) {
+            ok = mbar_wait(&mbar[warp][0], par0);
+            par0 ^= 1u;
+          } else {
+            ok = mbar_wait(&mbar[warp][1], par1);
+            par1 ^= 1u;
+          }
+          cb = cbuf + (size_t)buf * CW;
+          pc = 0;
+          break;
+        case CMD_END:
+          goto done;
+        default:
+          ok = false;
+      }
     }
     if (pc >= CW) ok = false;  // a command ran past its chunk
   }

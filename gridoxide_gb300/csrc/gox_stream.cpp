@@ -84,6 +84,7 @@ struct Builder {
   std::vector<std::vector<Item*>> uncommitted;
   std::vector<std::vector<int>> uncommitted_cols;
   std::vector<std::vector<std::pair<int, int>>> pend_rows;  // copies not yet emitted
+  std::vector<int64_t> last_colhdr, last_colend;           // the warp's last COLUMN command
   std::vector<double> wcost;  // per warp, cycles in the current level (estimate)
   std::vector<int> pinned;    // per warp, rows pinned in the current level
   Stream* out;
@@ -137,13 +138,30 @@ struct Builder {
   void emit_gather(int w, int arr, const std::vector<std::pair<int, int>>& rows) {
     for (const auto& r : rows) pend_rows[w].push_back({vrow(arr, r.first), r.second});
   }
+  // Pads a copy list to whole pairs of 16-byte-per-lane copies.
+  void pad_rows(std::vector<std::pair<int, int>>& rows) const {
+    const size_t q = 2 * (size_t)rpi();
+    while (rows.size() % q) rows.push_back({0, trash_row()});
+  }
+  // Gives the copies placed since the last group their commit group (-1 when
+  // there are none).
+  int new_group(int w) {
+    if (uncommitted[w].empty() && uncommitted_cols[w].empty()) return -1;
+    const int g = ngroups[w]++;
+    out->n_groups++;
+    for (Item* it : uncommitted[w]) { it->group = g; it->committed = true; }
+    for (int ci : uncommitted_cols[w]) { C[ci].group = g; C[ci].committed = true; }
+    uncommitted[w].clear();
+    uncommitted_cols[w].clear();
+    return g;
+  }
   // One GATHER command for every copy issued at this point.
   void flush_gather(int w) {
     std::vector<std::pair<int, int>>& rows = pend_rows[w];
     if (rows.empty()) return;
     Emit& e = em[w];
-    const size_t q = (size_t)rpi();
-    while (rows.size() % q) rows.push_back({0, trash_row()});
+    const size_t q = 2 * (size_t)rpi();
+    pad_rows(rows);
     size_t i = 0;
     while (i < rows.size()) {
       if (e.room() < 1 + q) e.next_chunk();
@@ -166,12 +184,7 @@ struct Builder {
     flush_gather(w);
     if (e.last_gather < 0) throw std::logic_error("commit without a gather");
     e.w[e.last_gather] |= (1 << 23);
-    const int g = ngroups[w]++;
-    out->n_groups++;
-    for (Item* it : uncommitted[w]) { it->group = g; it->committed = true; }
-    for (int ci : uncommitted_cols[w]) { C[ci].group = g; C[ci].committed = true; }
-    uncommitted[w].clear();
-    uncommitted_cols[w].clear();
+    new_group(w);
   }
   void wait_for(int w, int g, int L, bool on_path) {
     if (g < 0 || waited[w] >= g) return;
@@ -240,19 +253,29 @@ struct Builder {
     return true;
   }
 
-  void flush_steps(int w, int stage_abs, std::vector<Step>& steps) {
+  // A step that changes nothing the column reads: nine updates of the
+  // dummy row (pads step lists to pairs).
+  Step dummy_step(const ColInfo& c) const {
+    const uint32_t d = (uint32_t)(c.len + 2);
+    Step s{};
+    s.x = (uint32_t)zero_row();
+    s.y = s.z = s.w = d | (d << 10) | (d << 20);
+    return s;
+  }
+  void flush_steps(int w, int stage_abs, std::vector<Step>& steps, const ColInfo& c) {
     Emit& e = em[w];
+    if (steps.size() % 2) steps.push_back(dummy_step(c));
     size_t i = 0;
     while (i < steps.size()) {
-      // header word, steps from the next 4-word boundary, 4 words of
+      // header word, steps (pairs) from the next 4-word boundary, 8 words of
       // over-read room
       const size_t first = (e.w.size() + 1 + 3) & ~(size_t)3;
-      if (first + 4 + 4 > e.cstart + e.cw) {
+      if (first + 8 + 8 > e.cstart + e.cw) {
         e.next_chunk();
         continue;
       }
-      size_t m = std::min(steps.size() - i, (e.cstart + e.cw - first - 4) / 4);
-      m = std::min<size_t>(m, 4095);
+      size_t m = std::min(steps.size() - i, (e.cstart + e.cw - first - 8) / 4);
+      m = std::min<size_t>(m, 4094) & ~(size_t)1;
       e.w.push_back(CMD_STEPS | (int32_t)(m << 4) | (stage_abs << 16));
       while (e.w.size() < first) e.w.push_back(0);
       for (size_t q = 0; q < m; q++) {
@@ -285,6 +308,73 @@ struct Builder {
     }
   }
 
+  // The whole of column c as one COLUMN command, when every value is placed
+  // and the command fits in a stream chunk.  g: the last commit group the
+  // column's values arrive in.
+  bool column_cmd(int w, ColInfo& c, int L, std::vector<std::pair<int, int>>& late,
+                  std::vector<std::pair<int, int>>& pref, int g, bool on_path) {
+    pad_rows(late);
+    pad_rows(pref);
+    std::vector<Step> steps;
+    size_t q = 0;
+    for (; q < c.items.size() && c.items[q].kind == IT_LRUN; q++) add_steps(c, c.items[q], steps);
+    if (steps.size() % 2) steps.push_back(dummy_step(c));
+    std::vector<int32_t> fw;
+    if (sc.fuse_fwd) {
+      for (size_t f = q; f < c.items.size(); f += 2)
+        fw.push_back(c.items[f].row | (c.items[f + 1].row << 16));
+      while (fw.size() % 8) fw.push_back(zero_row() | (zero_row() << 16));
+    }
+    const size_t nl = late.size(), np = pref.size(), ns = steps.size(), nf = fw.size();
+    auto fits = [&](size_t at, size_t end) {
+      const size_t sw = (at + 8 + nl + np + 3) & ~(size_t)3;
+      return sw + 4 * ns + nf <= end - 1 && sw + 4 * ns + 8 <= end;
+    };
+    Emit& e = em[w];
+    if (!fits(0, (size_t)e.cw) || nl > 0xffff || np > 0xffff || ns > 0xffff) {
+      // the general form counts the steps again
+      for (size_t f = 0; f < q; f++)
+        out->n_steps -= (c.items[f].nrows + kStepOps - 1) / kStepOps;
+      return false;
+    }
+    if (!fits(e.w.size(), e.cstart + e.cw)) e.next_chunk();
+    int32_t w0 = CMD_COLUMN;
+    if (g >= 0 && waited[w] < g) {
+      const int m = std::min(ngroups[w] - 1 - g, 7);
+      w0 |= (m << 4) | (1 << 7);
+      waited[w] = ngroups[w] - 1 - m;
+      out->n_waits++;
+      if (on_path) wcost[w] += 1200;
+    }
+    const int stage_abs = w * R + c.block;
+    last_colhdr[w] = (int64_t)e.w.size();
+    e.w.push_back(w0);
+    e.w.push_back(c.k);
+    e.w.push_back(sc.c_base[c.k]);
+    e.w.push_back(sc.c_ulen[c.k] | (sc.c_llen[c.k] << 16));
+    e.w.push_back(stage_abs | (int32_t)(nl << 16));
+    e.w.push_back((int32_t)(np | (ns << 16)));
+    e.w.push_back((int32_t)nf);
+    e.w.push_back(0);
+    for (const auto& r : late) e.w.push_back((int32_t)((uint32_t)r.first | ((uint32_t)r.second << 21)));
+    for (const auto& r : pref) e.w.push_back((int32_t)((uint32_t)r.first | ((uint32_t)r.second << 21)));
+    while (e.w.size() % 4) e.w.push_back(0);
+    for (const Step& st : steps) {
+      e.w.push_back((int32_t)st.x); e.w.push_back((int32_t)st.y);
+      e.w.push_back((int32_t)st.z); e.w.push_back((int32_t)st.w);
+    }
+    for (int32_t x : fw) e.w.push_back(x);
+    last_colend[w] = (int64_t)e.w.size();
+    out->n_column_cmds++;
+    pos[w]++;
+    const int64_t tf = now(w, L);
+    for (const Item& it : c.items)
+      if (it.state == ST_GATHERED) release_abs(it.row, it.nrows, tf);
+    release_abs(stage_abs, c.brows, tf);
+    wcost[w] += 70.0 * ns + 80 + 4.0 * c.len + 8.0 * nf;
+    return true;
+  }
+
   // Emits everything of column ci (warp w, level L).
   bool run_col(int w, int ci, int L) {
     ColInfo& c = C[ci];
@@ -302,7 +392,9 @@ struct Builder {
         out->rows_late += it.nrows;
         waited_late = true;
       }
-    commit(w);
+    std::vector<std::pair<int, int>> late_rows, pref_rows;
+    late_rows.swap(pend_rows[w]);
+    new_group(w);
     // the warp's next column: its stage block and every value finished before
     // this level, issued now and waited for when that column starts
     // (only when this column has every value placed: a prefetch must not
@@ -319,12 +411,21 @@ struct Builder {
           if (!gather_item(w, it, t)) break;
           out->rows_prefetched += it.nrows;
         }
-        commit(w);
+        pref_rows.swap(pend_rows[w]);
+        new_group(w);
       }
     }
     int g = c.group;
     for (const Item& it : c.items)
       if (it.state == ST_GATHERED) g = std::max(g, it.group);
+    if (placed && column_cmd(w, c, L, late_rows, pref_rows, g, waited_late)) return true;
+    // the general form: single commands, values fetched in pieces as room allows
+    for (auto* rows : {&late_rows, &pref_rows}) {
+      if (rows->empty()) continue;
+      pend_rows[w].swap(*rows);
+      flush_gather(w);
+      em[w].w[em[w].last_gather] |= (1 << 23);
+    }
     wait_for(w, g, L, waited_late);
     // updates, fetching values that found no room just in time
     std::vector<Step> steps;
@@ -336,7 +437,7 @@ struct Builder {
       consumed.clear();
     };
     auto jit = [&](size_t from) -> bool {
-      flush_steps(w, stage_abs, steps);
+      flush_steps(w, stage_abs, steps, c);
       release_consumed();
       const int64_t tj = now(w, L);
       bool any = false;
@@ -366,7 +467,7 @@ struct Builder {
       wcost[w] += 70.0 * ((it.nrows + kStepOps - 1) / kStepOps);
       if (it.state == ST_GATHERED) consumed.push_back(&it);
     }
-    flush_steps(w, stage_abs, steps);
+    flush_steps(w, stage_abs, steps, c);
     release_consumed();
     // forward substitution y_k = b_k - sum L(k, j) y_j, in order, in pieces
     // whose values fit in the ring
@@ -532,6 +633,8 @@ struct Builder {
     uncommitted.assign(W, {});
     uncommitted_cols.assign(W, {});
     pend_rows.assign(W, {});
+    last_colhdr.assign(W, -1);
+    last_colend.assign(W, -1);
     wcost.assign(W, 0.0);
     pinned.assign(W, 0);
     std::vector<int> wnext(W, 0);
@@ -556,8 +659,14 @@ struct Builder {
           if (!run_col(w, seq[w][wnext[w]], L)) return false;
           wnext[w]++;
         }
-        em[w].need(1);
-        em[w].w.push_back(CMD_BAR);
+        Emit& e = em[w];
+        if (last_colhdr[w] >= 0 && last_colend[w] == (int64_t)e.w.size()) {
+          e.w[last_colhdr[w]] |= (1 << 8);  // the level's barrier rides on the last column
+        } else {
+          e.need(1);
+          e.w.push_back(CMD_BAR);
+        }
+        last_colhdr[w] = -1;
       }
       st.est_cycles += *std::max_element(wcost.begin(), wcost.end()) + 120;
     }
@@ -631,8 +740,9 @@ std::string run_stream_host(const Schedule& sc, const Stream& st, std::vector<do
   const StreamPlan& P = st.plan;
   const int W = P.nw, R = P.ring_rows, CW = P.chunk_words, n = sc.n_u;
   const int rows = W * R + kSpareRows;
-  std::vector<double> ring(rows, 0.0);
   const int zero_row = W * R, trash_row = W * R + 1;
+  const int rpi2 = 2 * (512 / (32 * P.elem));
+  std::vector<double> ring(rows, 0.0);
   std::vector<int> pend(rows, -1);  // commit group of a copy not yet waited for
   std::vector<int> col_of_slot(sc.n_slots, -1);
   for (int k = 0; k < n; k++)
@@ -648,21 +758,21 @@ std::string run_stream_host(const Schedule& sc, const Stream& st, std::vector<do
   };
   std::vector<WS> ws(W);
   for (int w = 0; w < W; w++) ws[w].pc = st.chunk0[w] * CW;
-  auto fail = [&](int w, const std::string& m) {
-    return "warp " + std::to_string(w) + " word " + std::to_string(ws[w].pc) + ": " + m;
-  };
   // per level: who touched which row
   std::vector<int> wr_by(rows, -1), rd_by(rows, -1), stamp_w(rows, -1), stamp_r(rows, -1);
   for (int L = 0; L <= st.n_bars; L++) {
     for (int w = 0; w < W; w++) {
       WS& s = ws[w];
-      if (s.done) continue;
+      if (s.done || s.bars > L) continue;  // finished, or already past this level's barrier
       std::string e;
+      auto fail = [&](const std::string& m) {
+        return "warp " + std::to_string(w) + " word " + std::to_string(s.pc) + ": " + m;
+      };
       auto in_ring = [&](int r) { return r >= 0 && r < W * R; };
       auto note_w = [&](int r) -> bool {
+        if (r == zero_row) { e = "writes the zero row"; return false; }
         if (stamp_w[r] == L && wr_by[r] != w) { e = "two warps write row " + std::to_string(r); return false; }
-        if (stamp_r[r] == L && rd_by[r] != w && rd_by[r] != -2) { e = "row " + std::to_string(r) + " written while another warp reads it"; return false; }
-        if (stamp_r[r] == L && rd_by[r] == -2) { e = "row " + std::to_string(r) + " written while other warps read it"; return false; }
+        if (stamp_r[r] == L && rd_by[r] != w) { e = "row " + std::to_string(r) + " written while another warp reads it"; return false; }
         stamp_w[r] = L;
         wr_by[r] = w;
         return true;
@@ -671,160 +781,203 @@ std::string run_stream_host(const Schedule& sc, const Stream& st, std::vector<do
         if (pend[r] >= 0) { e = "row " + std::to_string(r) + " read before its copy is waited for"; return false; }
         if (stamp_w[r] == L && wr_by[r] != w) { e = "row " + std::to_string(r) + " read while another warp writes it"; return false; }
         if (stamp_r[r] == L && rd_by[r] != w) rd_by[r] = -2;
-        else { stamp_r[r] = L; rd_by[r] = w; }
+        else if (stamp_r[r] != L) { stamp_r[r] = L; rd_by[r] = w; }
+        return true;
+      };
+      const int cbeg = (st.chunk0[w] + s.chunk) * CW;
+      auto gather = [&](int at, int m, bool commit) -> bool {
+        if (m % rpi2) { e = "gather list not padded"; return false; }
+        for (int q = 0; q < m; q++) {
+          const uint32_t rw = (uint32_t)st.words[at + q];
+          const int src = (int)(rw & 0x1fffff), dst = (int)(rw >> 21);
+          if (dst == trash_row && src == 0) continue;  // padding copy
+          if (dst < 0 || dst >= W * R || dst / R != w) { e = "gather outside the warp's ring"; return false; }
+          if (pend[dst] >= 0) { e = "gather onto a row with a copy in flight"; return false; }
+          double v;
+          if (src < sc.n_slots) {
+            const int col = col_of_slot[src];
+            if (colfin[col] >= L) { e = "copies a value finished in the same level"; return false; }
+            v = lu[src];
+          } else if (src < sc.n_slots + n) {
+            const int r = src - sc.n_slots;
+            if (xfin[r] < 0 || xfin[r] >= L) { e = "copies y before it is final"; return false; }
+            v = X[r];
+          } else if (src < sc.n_slots + 2 * n) {
+            v = rhs[src - sc.n_slots - n];
+          } else {
+            e = "source row out of range";
+            return false;
+          }
+          if (!note_w(dst)) return false;
+          ring[dst] = v;
+          pend[dst] = s.ng;
+          s.pend_rows.push_back(dst);
+        }
+        if (commit) s.ng++;
+        return true;
+      };
+      auto wait = [&](int m) {
+        const int upto = s.ng - 1 - m;
+        std::vector<int> keep;
+        for (int r : s.pend_rows) {
+          if (pend[r] >= 0 && pend[r] <= upto) pend[r] = -1;
+          if (pend[r] >= 0) keep.push_back(r);
+        }
+        s.pend_rows.swap(keep);
+      };
+      auto steps = [&](int first, int m, int S0) -> bool {
+        if (m % 2) { e = "odd step count"; return false; }
+        if (first + 4 * m + 8 > cbeg + CW) { e = "steps past the chunk"; return false; }
+        for (int q = 0; q < m; q++) {
+          const uint32_t* d = reinterpret_cast<const uint32_t*>(&st.words[first + 4 * q]);
+          const int lrow = (int)(d[0] & 0xffff), jp = (int)((d[0] >> 16) & 0x3ff), cnt = (int)(d[0] >> 26);
+          if (cnt > kStepOps) { e = "bad step count"; return false; }
+          if (lrow + kStepOps > rows) { e = "step L rows out of range"; return false; }
+          if (!in_ring(S0 + jp)) { e = "step pivot row out of range"; return false; }
+          const uint32_t dw[3] = {d[1], d[2], d[3]};
+          for (int tt = cnt; tt < kStepOps; tt++)
+            if (!in_ring(S0 + (int)((dw[tt / 3] >> (10 * (tt % 3))) & 0x3ff))) {
+              e = "unused step slot outside the ring";
+              return false;
+            }
+          if (cnt == 0) continue;  // padding step
+          if (!note_r(S0 + jp)) return false;
+          const double xj = ring[S0 + jp];
+          for (int tt = 0; tt < cnt; tt++) {
+            const int dr = S0 + (int)((dw[tt / 3] >> (10 * (tt % 3))) & 0x3ff);
+            if (!in_ring(dr) || !in_ring(lrow + tt)) { e = "step row out of range"; return false; }
+            if (dr == S0 + jp) { e = "step writes its pivot row"; return false; }
+            if (!note_r(lrow + tt) || !note_r(dr) || !note_w(dr)) return false;
+            ring[dr] = ring[dr] - ring[lrow + tt] * xj;
+          }
+        }
+        return true;
+      };
+      auto fwd = [&](int at, int m, bool first, int S0, int len) -> bool {
+        if (!sc.fuse_fwd) { e = "forward terms without fusion"; return false; }
+        if (m % 8) { e = "forward terms not padded"; return false; }
+        if (!in_ring(S0 + len + 1)) { e = "forward rows out of range"; return false; }
+        const int yr0 = S0 + len;
+        if (!note_r(first ? yr0 + 1 : yr0)) return false;
+        double y = ring[first ? yr0 + 1 : yr0];
+        for (int f = 0; f < m; f++) {
+          const uint32_t fw = (uint32_t)st.words[at + f];
+          const int lr = (int)(fw & 0xffff), yr = (int)(fw >> 16);
+          if (lr == zero_row && yr == zero_row) continue;  // padding term
+          if (!in_ring(lr) || !in_ring(yr)) { e = "forward term row out of range"; return false; }
+          if (!note_r(lr) || !note_r(yr)) return false;
+          y -= ring[lr] * ring[yr];
+        }
+        if (!note_w(yr0)) return false;
+        ring[yr0] = y;
+        return true;
+      };
+      auto finish = [&](int k, int base, int ulen, int llen, int S0) -> bool {
+        const int len = ulen + 1 + llen;
+        if (k < 0 || k >= n || base != sc.c_base[k] || ulen != sc.c_ulen[k] || llen != sc.c_llen[k]) {
+          e = "FINISH header does not match the column";
+          return false;
+        }
+        if (!in_ring(S0) || !in_ring(S0 + len + 2) || S0 / R != (S0 + len + 2) / R || S0 / R != w) {
+          e = "stage block out of range";
+          return false;
+        }
+        for (int p = 0; p < len; p++)
+          if (!note_r(S0 + p)) return false;
+        const double piv = ring[S0 + ulen];
+        if (piv == 0.0) singular = true;
+        const double inv = 1.0 / piv;
+        for (int p = 0; p <= ulen; p++) lu[base + p] = ring[S0 + p];
+        for (int p = ulen + 1; p < len; p++) {
+          if (!note_w(S0 + p)) return false;
+          ring[S0 + p] = ring[S0 + p] * inv;
+          lu[base + p] = ring[S0 + p];
+        }
+        colfin[k] = L;
+        if (sc.fuse_fwd) {
+          if (!note_r(S0 + len)) return false;
+          X[k] = ring[S0 + len];
+          xfin[k] = L;
+        }
         return true;
       };
       for (;;) {
-        if (s.pc < (st.chunk0[w] + s.chunk) * CW || s.pc >= (st.chunk0[w] + s.chunk + 1) * CW)
-          return fail(w, "ran past its chunk");
+        const int cend = (st.chunk0[w] + s.chunk + 1) * CW - 1;  // NEXT / END word
+        if (s.pc < cbeg || s.pc > cend) return fail("ran past its chunk");
         const int32_t w0 = st.words[s.pc];
         const int op = w0 & 15;
         if (op == CMD_NOP) { s.pc++; continue; }
         if (op == CMD_NEXT) {
-          if (++s.chunk >= st.nchunks[w]) return fail(w, "NEXT past the last chunk");
+          if (++s.chunk >= st.nchunks[w]) return fail("NEXT past the last chunk");
           s.pc = (st.chunk0[w] + s.chunk) * CW;
-          continue;
+          break;  // re-enter with the new chunk bounds
         }
-        const int cend = (st.chunk0[w] + s.chunk + 1) * CW - 1;  // NEXT / END word
         if (op == CMD_END) {
-          if (s.bars != st.n_bars) return fail(w, "END after a wrong number of barriers");
+          if (s.bars != st.n_bars) return fail("END after a wrong number of barriers");
           s.done = true;
           break;
         }
         if (op == CMD_BAR) { s.pc++; s.bars++; break; }
         if (op == CMD_GATHER) {
-          const int m = (w0 >> 4) & 0xffff, commit = (w0 >> 23) & 1;
-          if (s.pc + 1 + m > cend) return fail(w, "GATHER past its chunk");
-          if (m % (512 / (32 * P.elem))) return fail(w, "GATHER not padded");
-          for (int q = 0; q < m; q++) {
-            const uint32_t rw = (uint32_t)st.words[s.pc + 1 + q];
-            const int src = (int)(rw & 0x1fffff), dst = (int)(rw >> 21);
-            if (dst == trash_row && src == 0) continue;  // padding copy
-            if (dst < 0 || dst >= W * R || dst / R != w) return fail(w, "gather outside the warp's ring");
-            if (pend[dst] >= 0) return fail(w, "gather onto a row with a copy in flight");
-            double v;
-            int arr = ARR_LU, rsrc = src;
-            if (src >= sc.n_slots + n) { arr = ARR_RHS; rsrc = src - sc.n_slots - n; }
-            else if (src >= sc.n_slots) { arr = ARR_X; rsrc = src - sc.n_slots; }
-            const int srcv = src;
-            (void)srcv;
-            if (arr == ARR_LU) {
-              if (rsrc >= sc.n_slots) return fail(w, "factor row out of range");
-              const int col = col_of_slot[rsrc];
-              if (colfin[col] >= L) return fail(w, "copies a value finished in the same level");
-              v = lu[rsrc];
-            } else if (arr == ARR_X) {
-              if (xfin[rsrc] < 0 || xfin[rsrc] >= L) return fail(w, "copies y before it is final");
-              v = X[rsrc];
-            } else {
-              if (rsrc >= n) return fail(w, "rhs row out of range");
-              v = rhs[rsrc];
-            }
-            if (!note_w(dst)) return fail(w, e);
-            ring[dst] = v;
-            pend[dst] = s.ng;
-            s.pend_rows.push_back(dst);
-          }
-          if (commit) s.ng++;
+          const int m = (w0 >> 4) & 0xffff;
+          if (s.pc + 1 + m > cend) return fail("GATHER past its chunk");
+          if (!gather(s.pc + 1, m, (w0 >> 23) & 1)) return fail(e);
           s.pc += 1 + m;
           continue;
         }
-        if (op == CMD_WAIT) {
-          const int m = (w0 >> 4) & 7;
-          const int upto = s.ng - 1 - m;
-          std::vector<int> keep;
-          for (int r : s.pend_rows) {
-            if (pend[r] >= 0 && pend[r] <= upto) pend[r] = -1;
-            if (pend[r] >= 0) keep.push_back(r);
-          }
-          s.pend_rows.swap(keep);
-          s.pc++;
-          continue;
-        }
+        if (op == CMD_WAIT) { wait((w0 >> 4) & 7); s.pc++; continue; }
         if (op == CMD_STEPS) {
           const int m = (w0 >> 4) & 0xfff, S0 = (int)(((uint32_t)w0) >> 16);
           const int first = (s.pc + 1 + 3) & ~3;
-          if (first + 4 * m + 4 > (st.chunk0[w] + s.chunk + 1) * CW) return fail(w, "STEPS past its chunk");
-          for (int q = 0; q < m; q++) {
-            const uint32_t* d = reinterpret_cast<const uint32_t*>(&st.words[first + 4 * q]);
-            const int lrow = (int)(d[0] & 0xffff), jp = (int)((d[0] >> 16) & 0x3ff), cnt = (int)(d[0] >> 26);
-            if (cnt < 1 || cnt > kStepOps) return fail(w, "bad step count");
-            if (lrow + kStepOps > rows) return fail(w, "step L rows out of range");
-            if (!in_ring(S0 + jp)) return fail(w, "step pivot row out of range");
-            if (!note_r(S0 + jp)) return fail(w, e);
-            const double xj = ring[S0 + jp];
-            uint32_t dw[3] = {d[1], d[2], d[3]};
-            for (int tt = cnt; tt < kStepOps; tt++) {
-              const int dr = S0 + (int)((dw[tt / 3] >> (10 * (tt % 3))) & 0x3ff);
-              if (!in_ring(dr)) return fail(w, "unused step slot outside the ring");
-            }
-            for (int tt = 0; tt < cnt; tt++) {
-              const int dr = S0 + (int)((dw[tt / 3] >> (10 * (tt % 3))) & 0x3ff);
-              if (!in_ring(dr) || !in_ring(lrow + tt)) return fail(w, "step row out of range");
-              if (dr == S0 + jp) return fail(w, "step writes its pivot row");
-              if (!note_r(lrow + tt) || !note_r(dr) || !note_w(dr)) return fail(w, e);
-              ring[dr] = ring[dr] - ring[lrow + tt] * xj;
-            }
-          }
+          if (!steps(first, m, S0)) return fail(e);
           s.pc = first + 4 * m;
           continue;
         }
         if (op == CMD_FWD) {
-          const int m = (w0 >> 4) & 0xffff, first = (w0 >> 20) & 1;
+          const int m = (w0 >> 4) & 0xffff;
           const int S0 = st.words[s.pc + 1] & 0xffff, len = (st.words[s.pc + 1] >> 16) & 0xffff;
-          if (!sc.fuse_fwd) return fail(w, "FWD without fusion");
-          if (s.pc + 2 + m > cend) return fail(w, "FWD past its chunk");
-          if (m % 8) return fail(w, "FWD not padded");
-          if (!in_ring(S0 + len + 1)) return fail(w, "FWD rows out of range");
-          const int yr0 = S0 + len;
-          if (!note_r(first ? yr0 + 1 : yr0)) return fail(w, e);
-          double y = ring[first ? yr0 + 1 : yr0];
-          for (int f = 0; f < m; f++) {
-            const uint32_t fw = (uint32_t)st.words[s.pc + 2 + f];
-            const int lr = (int)(fw & 0xffff), yr = (int)(fw >> 16);
-            if (lr == zero_row && yr == zero_row) continue;  // padding term
-            if (!in_ring(lr) || !in_ring(yr)) return fail(w, "forward term row out of range");
-            if (!note_r(lr) || !note_r(yr)) return fail(w, e);
-            y -= ring[lr] * ring[yr];
-          }
-          if (!note_w(yr0)) return fail(w, e);
-          ring[yr0] = y;
+          if (s.pc + 2 + m > cend) return fail("FWD past its chunk");
+          if (!fwd(s.pc + 2, m, (w0 >> 20) & 1, S0, len)) return fail(e);
           s.pc += 2 + m;
           continue;
         }
         if (op == CMD_FINISH) {
-          const int k = st.words[s.pc + 1], base = st.words[s.pc + 2];
-          const int ulen = st.words[s.pc + 3] & 0xffff, llen = (st.words[s.pc + 3] >> 16) & 0xffff;
-          const int S0 = st.words[s.pc + 4];
-          const int len = ulen + 1 + llen;
-          if (s.pc + 5 > cend) return fail(w, "FINISH past its chunk");
-          if (k < 0 || k >= n || base != sc.c_base[k] || ulen != sc.c_ulen[k] || llen != sc.c_llen[k])
-            return fail(w, "FINISH header does not match the column");
-          if (!in_ring(S0) || !in_ring(S0 + len + 2) || S0 / R != (S0 + len + 2) / R || S0 / R != w)
-            return fail(w, "stage block out of range");
-          for (int p = 0; p < len; p++)
-            if (!note_r(S0 + p)) return fail(w, e);
-          const double piv = ring[S0 + ulen];
-          if (piv == 0.0) singular = true;
-          const double inv = 1.0 / piv;
-          for (int p = 0; p <= ulen; p++) lu[base + p] = ring[S0 + p];
-          for (int p = ulen + 1; p < len; p++) {
-            if (!note_w(S0 + p)) return fail(w, e);
-            ring[S0 + p] = ring[S0 + p] * inv;
-            lu[base + p] = ring[S0 + p];
-          }
-          colfin[k] = L;
-          if (sc.fuse_fwd) {
-            if (!note_r(S0 + len)) return fail(w, e);
-            X[k] = ring[S0 + len];
-            xfin[k] = L;
-          }
+          if (s.pc + 5 > cend) return fail("FINISH past its chunk");
+          const int ul = st.words[s.pc + 3];
+          if (!finish(st.words[s.pc + 1], st.words[s.pc + 2], ul & 0xffff, (ul >> 16) & 0xffff,
+                      st.words[s.pc + 4]))
+            return fail(e);
           s.pc += 5;
           continue;
         }
-        return fail(w, "bad opcode " + std::to_string(op));
+        if (op == CMD_COLUMN) {
+          if (s.pc + 8 > cend) return fail("COLUMN header past its chunk");
+          const int k = st.words[s.pc + 1], base = st.words[s.pc + 2], ul = st.words[s.pc + 3];
+          const uint32_t h4 = (uint32_t)st.words[s.pc + 4], h5 = (uint32_t)st.words[s.pc + 5];
+          const int nf = st.words[s.pc + 6];
+          const int S0 = (int)(h4 & 0xffff), nl = (int)(h4 >> 16), np = (int)(h5 & 0xffff), ns = (int)(h5 >> 16);
+          const int ulen = ul & 0xffff, llen = (ul >> 16) & 0xffff;
+          const int sw = (s.pc + 8 + nl + np + 3) & ~3;
+          if (sw + 4 * ns + nf > cend) return fail("COLUMN past its chunk");
+          if (nl && !gather(s.pc + 8, nl, true)) return fail(e);
+          if (np && !gather(s.pc + 8 + nl, np, true)) return fail(e);
+          if ((w0 >> 7) & 1) wait((w0 >> 4) & 7);
+          if (!steps(sw, ns, S0)) return fail(e);
+          if (sc.fuse_fwd && !fwd(sw + 4 * ns, nf, true, S0, ulen + 1 + llen)) return fail(e);
+          if (!sc.fuse_fwd && nf) return fail("forward terms without fusion");
+          if (!finish(k, base, ulen, llen, S0)) return fail(e);
+          s.pc = sw + 4 * ns + nf;
+          if ((w0 >> 8) & 1) { s.bars++; break; }
+          continue;
+        }
+        return fail("bad opcode " + std::to_string(op));
       }
     }
+    // warps that stopped at a chunk switch (NEXT) continue in this level
+    bool again = false;
+    for (int w = 0; w < W; w++)
+      if (!ws[w].done && ws[w].bars <= L) again = true;
+    if (again) L--;
   }
   for (int w = 0; w < W; w++)
     if (!ws[w].done) return "warp " + std::to_string(w) + " did not reach END";

@@ -9,6 +9,9 @@
 // instead of being loaded again.  The result is, per warp, a list of
 // commands that the kernel interprets:
 //
+//   COLUMN              all of one column (copies for it and for the
+//                       warp's next column, wait, steps, FWD, FINISH,
+//                       optionally BAR) in one command
 //   BAR                 __syncthreads (end of a dependency level)
 //   GATHER arr m rows   cp.async copies of m rows (one row = one value for
 //                       the 32 scenarios of a group) from the factor image,
@@ -44,7 +47,8 @@ enum : int32_t {
   CMD_FINISH = 5,
   CMD_NEXT = 6,
   CMD_END = 7,
-  CMD_FWD = 8
+  CMD_FWD = 8,
+  CMD_COLUMN = 9
 };
 enum : int32_t { ARR_LU = 0, ARR_X = 1, ARR_RHS = 2 };
 
@@ -73,6 +77,16 @@ constexpr int kMaxRows = 2048;  // ring rows of all warps (11-bit row fields)
 //           m is a multiple of 8, padded with terms on the zero row
 //   FINISH  w0 = op, k, base, ulen | llen << 16, stage_row; the stage block
 //           is [column rows | y | b | dummy]
+//   COLUMN  w0 = op | wait_n << 4 | do_wait << 7 | bar_after << 8, k, base,
+//           ulen | llen << 16, stage_row | nlate << 16, npref | nsteps << 16,
+//           nfw, 0; then nlate gather words (this column, one commit group),
+//           npref gather words (the warp's next column, one group), from the
+//           next 16-byte boundary nsteps steps, then nfw forward terms: the
+//           whole of one column in one command
+// Gather word counts are multiples of 2 copies (8 rows FP32, 4 FP64), step
+// counts are even, forward term counts multiples of 8 (padding as above);
+// 8 words after a command's last step stay inside its chunk (the step loop
+// reads the next pair ahead).
 struct StreamPlan {
   int elem = 4;             // bytes per value: 4 (FP32) or 8 (FP64)
   int nw = 8;               // warps per CTA
@@ -87,7 +101,7 @@ struct Stream {
   int n_bars = 0;
   // statistics of the schedule
   int64_t rows_gathered = 0, rows_prefetched = 0, rows_resident = 0, rows_late = 0;
-  int64_t rows_jit = 0, n_steps = 0, n_waits = 0, n_groups = 0;
+  int64_t rows_jit = 0, n_steps = 0, n_waits = 0, n_groups = 0, n_column_cmds = 0;
   double est_cycles = 0;  // rough critical-path estimate, used to choose a plan
 };
 
