@@ -80,6 +80,8 @@ SIGNATURES = {
     "gox_set_timing": (C.c_int, [vp, C.c_int32]),
     "gox_last_timing": (C.c_int, [vp, f64p]),
     "gox_last_launches": (C.c_int64, [vp]),
+    "gox_set_pivot_tolerance": (C.c_int, [vp, C.c_double]),
+    "gox_last_fallbacks": (C.c_int64, [vp]),
     "gox_version": (C.c_char_p, []),
 }
 

@@ -98,6 +98,28 @@ __global__ void k_gather_rows(const double* __restrict__ src, int B, int N, int 
   }
 }
 
+// dst row r = src row idx[r] (rows of `w` elements of 4 or 8 bytes), and back
+template <typename E>
+__global__ void k_take_rows(const E* __restrict__ src, int w, const int32_t* __restrict__ idx,
+                            int nr, E* __restrict__ dst) {
+  const size_t total = (size_t)nr * w;
+  for (size_t t = blockIdx.x * (size_t)blockDim.x + threadIdx.x; t < total;
+       t += (size_t)gridDim.x * blockDim.x) {
+    const size_t r = t / w, c = t % w;
+    dst[t] = src[(size_t)idx[r] * w + c];
+  }
+}
+template <typename E>
+__global__ void k_put_rows(const E* __restrict__ src, int w, const int32_t* __restrict__ idx,
+                           int nr, E* __restrict__ dst) {
+  const size_t total = (size_t)nr * w;
+  for (size_t t = blockIdx.x * (size_t)blockDim.x + threadIdx.x; t < total;
+       t += (size_t)gridDim.x * blockDim.x) {
+    const size_t r = t / w, c = t % w;
+    dst[(size_t)idx[r] * w + c] = src[t];
+  }
+}
+
 __global__ void k_init_scen(int B, int G, int32_t* status, int32_t* iters, int32_t* sing,
                             int32_t* piv, double* maxmis, unsigned long long* maxacc) {
   int s = blockIdx.x * blockDim.x + threadIdx.x;
@@ -272,7 +294,7 @@ struct DevBatch {
     G = G_; prec = prec_; max_iter = max_iter_;
   }
 
-  BatchDev view(bool want_hist, bool outage, double tol) {
+  BatchDev view(bool want_hist, bool outage, double tol, double piv_tol) {
     BatchDev D{};
     D.G = G; D.max_iter = max_iter; D.tol = tol;
     D.vm = vm.as<double>(); D.va = va.as<double>(); D.e = e.as<double>(); D.f = f.as<double>();
@@ -289,7 +311,7 @@ struct DevBatch {
     D.o_bt = outage ? o_bt.as<int32_t>() : nullptr;
     D.o_dre = outage ? o_dre.as<double>() : nullptr;
     D.o_dim = outage ? o_dim.as<double>() : nullptr;
-    D.piv_tol = prec == GOX_PRECISION_MIXED ? 1e-6f : 0.0f;
+    D.piv_tol = prec == GOX_PRECISION_MIXED ? (float)piv_tol : 0.0f;
     D.err = err.as<int32_t>() + 1;
     return D;
   }
@@ -386,6 +408,10 @@ struct gox_topo {
   Timing timing;
   int64_t launches = 0;
   int device = 0;
+  // mixed path: pivot-ratio threshold |u_kk| < piv_tol * max|L(:, k)| that
+  // sends a scenario to FP64, and how many the last batch sent
+  double piv_tol = 1e-6;
+  int64_t fallbacks = 0;
 };
 
 struct gox_ls {
@@ -598,7 +624,7 @@ static int batch_device(gox_topo* t, int B, const double* p_spec, const double* 
   } else {
     return -1;  // handled by the caller's fallback below
   }
-  BatchDev D = DB.view(want_hist, outage, tol);
+  BatchDev D = DB.view(want_hist, outage, tol, t->piv_tol);
   // inputs -> interleaved layout
   const size_t tot = (size_t)G * n * 32;
   k_scatter_rows<<<grid1d(tot), 256, 0, st>>>(p_spec, B, n, n, D.psp, G);
@@ -652,6 +678,75 @@ static int batch_device(gox_topo* t, int B, const double* p_spec, const double* 
                                                   max_iter, status, iters, max_mis, hist);
   t->launches += 3;
   GOX_CK(cudaGetLastError());
+  if (precision == GOX_PRECISION_MIXED) {
+    // Scenarios whose FP32 refactor met a pivot below piv_tol times its
+    // column's largest L entry are solved again, from their start point, on
+    // the FP64 path (the same pivot order, as the reference's FP64 refactor
+    // keeps it); their reports replace the mixed ones.
+    std::vector<int32_t> hpiv((size_t)G * 32, 0);
+    GOX_CK(cudaMemcpyAsync(hpiv.data(), D.piv_flag, hpiv.size() * 4, cudaMemcpyDeviceToHost, st));
+    GOX_CK(cudaStreamSynchronize(st));
+    std::vector<int32_t> idx;
+    for (int s = 0; s < B; s++)
+      if (hpiv[s]) idx.push_back(s);
+    t->fallbacks = (int64_t)idx.size();
+    if (!idx.empty()) {
+      const int Bf = (int)idx.size();
+      const int64_t launches0 = t->launches;
+      const Timing timing0 = t->timing;
+      DevMem didx, fp, fq, fvm, fva, fsl, fdr, fdi, ovm, ova, oit, ost, omm, ohi;
+      upload(didx, idx);
+      const int32_t* ix = didx.as<int32_t>();
+      const size_t rows = (size_t)Bf * n;
+      fp.ensure(rows * 8); fq.ensure(rows * 8);
+      k_take_rows<double><<<grid1d(rows), 256, 0, st>>>(p_spec, n, ix, Bf, fp.as<double>());
+      k_take_rows<double><<<grid1d(rows), 256, 0, st>>>(q_spec, n, ix, Bf, fq.as<double>());
+      const double* vmf = vm0;
+      const double* vaf = va0;
+      if (v_stride) {
+        fvm.ensure(rows * 8); fva.ensure(rows * 8);
+        k_take_rows<double><<<grid1d(rows), 256, 0, st>>>(vm0, v_stride, ix, Bf, fvm.as<double>());
+        k_take_rows<double><<<grid1d(rows), 256, 0, st>>>(va0, v_stride, ix, Bf, fva.as<double>());
+        vmf = fvm.as<double>();
+        vaf = fva.as<double>();
+      }
+      if (outage) {
+        fsl.ensure((size_t)Bf * 16); fdr.ensure((size_t)Bf * 32); fdi.ensure((size_t)Bf * 32);
+        k_take_rows<int32_t><<<grid1d((size_t)Bf * 4), 256, 0, st>>>(o_slot, 4, ix, Bf, fsl.as<int32_t>());
+        k_take_rows<double><<<grid1d((size_t)Bf * 4), 256, 0, st>>>(o_dre, 4, ix, Bf, fdr.as<double>());
+        k_take_rows<double><<<grid1d((size_t)Bf * 4), 256, 0, st>>>(o_dim, 4, ix, Bf, fdi.as<double>());
+      }
+      ovm.ensure(rows * 8); ova.ensure(rows * 8);
+      oit.ensure((size_t)Bf * 4); ost.ensure((size_t)Bf * 4); omm.ensure((size_t)Bf * 8);
+      if (want_hist) ohi.ensure((size_t)Bf * max_iter * 8);
+      const int rc = batch_device(
+          t, Bf, fp.as<double>(), fq.as<double>(), vmf, vaf, v_stride,
+          outage ? fsl.as<int32_t>() : nullptr, outage ? fdr.as<double>() : nullptr,
+          outage ? fdi.as<double>() : nullptr, tol, max_iter, GOX_PRECISION_FP64, ovm.as<double>(),
+          ova.as<double>(), oit.as<int32_t>(), ost.as<int32_t>(), omm.as<double>(),
+          want_hist ? ohi.as<double>() : nullptr, st, nullptr, nullptr, nullptr, nullptr, nullptr,
+          nullptr, nullptr);
+      if (rc != GOX_OK) return rc;
+      k_put_rows<double><<<grid1d(rows), 256, 0, st>>>(ovm.as<double>(), n, ix, Bf, vm_out);
+      k_put_rows<double><<<grid1d(rows), 256, 0, st>>>(ova.as<double>(), n, ix, Bf, va_out);
+      k_put_rows<int32_t><<<grid1d(Bf), 256, 0, st>>>(oit.as<int32_t>(), 1, ix, Bf, iters);
+      k_put_rows<int32_t><<<grid1d(Bf), 256, 0, st>>>(ost.as<int32_t>(), 1, ix, Bf, status);
+      k_put_rows<double><<<grid1d(Bf), 256, 0, st>>>(omm.as<double>(), 1, ix, Bf, max_mis);
+      if (want_hist)
+        k_put_rows<double><<<grid1d((size_t)Bf * max_iter), 256, 0, st>>>(ohi.as<double>(), max_iter,
+                                                                          ix, Bf, hist);
+      GOX_CK(cudaStreamSynchronize(st));
+      GOX_CK(cudaGetLastError());
+      t->launches += launches0 + 5 + (v_stride ? 2 : 0) + (outage ? 3 : 0) + (want_hist ? 1 : 0) + 2;
+      if (timing0.on) {
+        t->timing.total += timing0.total;
+        t->timing.k1 += timing0.k1; t->timing.k2 += timing0.k2;
+        t->timing.k3 += timing0.k3; t->timing.k4 += timing0.k4;
+        t->timing.iters = timing0.iters;
+      }
+      t->fallbacks = Bf;
+    }
+  }
   return GOX_OK;
 }
 
@@ -1054,6 +1149,14 @@ int gox_last_timing(const gox_topo* t, double* out) {
 }
 
 int64_t gox_last_launches(const gox_topo* t) { return t ? t->launches : -1; }
+
+int gox_set_pivot_tolerance(gox_topo* t, double tol) {
+  if (!t || !(tol >= 0.0) || !std::isfinite(tol)) return GOX_E_INVALID;
+  t->piv_tol = tol;
+  return GOX_OK;
+}
+
+int64_t gox_last_fallbacks(const gox_topo* t) { return t ? t->fallbacks : -1; }
 
 // ---- LinearSolver level ----------------------------------------------------
 

@@ -335,6 +335,27 @@ __device__ __forceinline__ double lds<double>(uint32_t a) {
   asm volatile("ld.shared.f64 %0, [%1];\n" : "=d"(v) : "r"(a));
   return v;
 }
+// ... with a compile-time byte offset folded into the instruction
+template <typename T, int OFF>
+__device__ __forceinline__ T lds_off(uint32_t a);
+template <>
+__device__ __forceinline__ float lds_off<float, 0>(uint32_t a) { return lds<float>(a); }
+#define GOX_LDS_OFF(TY, PT, CT, OFFV)                                                  \
+  template <>                                                                     \
+  __device__ __forceinline__ TY lds_off<TY, OFFV>(uint32_t a) {                    \
+    TY v;                                                                         \
+    asm volatile("ld.shared." PT " %0, [%1+" #OFFV "];\n" : "=" CT(v) : "r"(a));     \
+    return v;                                                                     \
+  }
+GOX_LDS_OFF(float, "f32", "f", 128)
+GOX_LDS_OFF(float, "f32", "f", 256)
+GOX_LDS_OFF(float, "f32", "f", 384)
+GOX_LDS_OFF(float, "f32", "f", 512)
+GOX_LDS_OFF(float, "f32", "f", 640)
+GOX_LDS_OFF(float, "f32", "f", 768)
+GOX_LDS_OFF(float, "f32", "f", 896)
+GOX_LDS_OFF(float, "f32", "f", 1024)
+#undef GOX_LDS_OFF
 __device__ __forceinline__ void sts(uint32_t a, float v) {
   asm volatile("st.shared.f32 [%0], %1;\n" ::"r"(a), "f"(v) : "memory");
 }
@@ -399,6 +420,9 @@ struct Rf {
     }
   }
 
+  // One step: 9 updates stage[d] -= L(d, j) * stage[j].  FP32 runs all 9
+  // (unused ones on the dummy row: no branch); FP64 skips the unused ones,
+  // since an FP64 FMA costs far more than a uniform branch on this GPU.
   static __device__ __forceinline__ void step(uint4 d, uint32_t st_lane, uint32_t ring_lane) {
     const uint32_t la = ring_lane + (d.x & 0xffffu) * RB;
     const T xj = lds<T>(st_lane + ((d.x >> 16) & 0x3ffu) * RB);
@@ -409,13 +433,39 @@ struct Rf {
       const uint32_t wd = t < 3 ? d.y : (t < 6 ? d.z : d.w);
       da[t] = st_lane + ((wd >> (10 * (t % 3))) & 0x3ffu) * RB;
     }
+    if (sizeof(T) == 4) {
+      load_l<0>(la, lv);
 #pragma unroll
-    for (int t = 0; t < kStepOps; t++) {
-      xi[t] = lds<T>(da[t]);
-      lv[t] = lds<T>(la + (uint32_t)t * RB);
+      for (int t = 0; t < kStepOps; t++) xi[t] = lds<T>(da[t]);
+#pragma unroll
+      for (int t = 0; t < kStepOps; t++) sts(da[t], xi[t] - lv[t] * xj);
+    } else {
+      const int cnt = (int)(d.x >> 26);
+#pragma unroll
+      for (int t = 0; t < kStepOps; t++)
+        if (t < cnt) {
+          xi[t] = lds<T>(da[t]);
+          lv[t] = lds<T>(la + (uint32_t)t * RB);
+        }
+#pragma unroll
+      for (int t = 0; t < kStepOps; t++)
+        if (t < cnt) sts(da[t], xi[t] - lv[t] * xj);
     }
-#pragma unroll
-    for (int t = 0; t < kStepOps; t++) sts(da[t], xi[t] - lv[t] * xj);
+  }
+  // the 9 L values of a step (FP32: offsets folded into the loads)
+  template <int Z>
+  static __device__ __forceinline__ void load_l(uint32_t la, T* lv) {
+    if constexpr (sizeof(T) == 4) {
+      lv[0] = lds_off<float, 0>(la);
+      lv[1] = lds_off<float, 128>(la);
+      lv[2] = lds_off<float, 256>(la);
+      lv[3] = lds_off<float, 384>(la);
+      lv[4] = lds_off<float, 512>(la);
+      lv[5] = lds_off<float, 640>(la);
+      lv[6] = lds_off<float, 768>(la);
+      lv[7] = lds_off<float, 896>(la);
+      lv[8] = lds_off<float, 1024>(la);
+    }
   }
 
   // m steps (even), uint4 each; the word after the last pair is readable
@@ -431,9 +481,10 @@ struct Rf {
     }
   }
 
-  // y = (first ? b : y) - sum L(k, j) y_j over m terms (multiple of 8)
-  static __device__ __forceinline__ void fwd(const int32_t* w, int m, bool first, uint32_t yrow,
-                                             uint32_t ring_lane) {
+  // y = (first ? b : y) - sum L(k, j) y_j over m terms (multiple of 8; mr
+  // of them real, the rest read the zero row; FP64 skips those)
+  static __device__ __forceinline__ void fwd(const int32_t* w, int m, int mr, bool first,
+                                             uint32_t yrow, uint32_t ring_lane) {
     T y = lds<T>(first ? yrow + RB : yrow);
     for (int f0 = 0; f0 < m; f0 += 8) {
       T a[8], b[8];
@@ -443,8 +494,14 @@ struct Rf {
         a[t] = lds<T>(ring_lane + (fw & 0xffffu) * RB);
         b[t] = lds<T>(ring_lane + (fw >> 16) * RB);
       }
+      if (sizeof(T) == 4) {
 #pragma unroll
-      for (int t = 0; t < 8; t++) y -= a[t] * b[t];
+        for (int t = 0; t < 8; t++) y -= a[t] * b[t];
+      } else {
+#pragma unroll
+        for (int t = 0; t < 8; t++)
+          if (f0 + t < mr) y -= a[t] * b[t];
+      }
     }
     sts(yrow, y);
   }
@@ -475,6 +532,7 @@ struct Rf {
       for (int t = 0; t < 8; t++) colmax = fmax(colmax, fabs(v[t]));
 #pragma unroll
       for (int t = 0; t < 8; t++) {
+        if (sizeof(T) == 8 && p0 + t >= len) break;  // FP64: no duplicate multiplies
         const int r = min(p0 + t, len - 1);
         v[t] *= inv;
         sts(st_lane + (uint32_t)r * RB, v[t]);
@@ -574,7 +632,8 @@ __global__ void __launch_bounds__(256) k_refactor(StreamDev P, SchedDev S, Batch
       R::steps(reinterpret_cast<const uint4*>(cb + sw), nst, st_lane, ring_lane);
       const int ulen = ul & 0xffff, llen = (ul >> 16) & 0xffff;
       if (fuse)
-        R::fwd(cb + sw + 4 * nst, nfw, true, st_lane + (uint32_t)(ulen + 1 + llen) * RB, ring_lane);
+        R::fwd(cb + sw + 4 * nst, nfw, cb[pc + 7], true, st_lane + (uint32_t)(ulen + 1 + llen) * RB,
+               ring_lane);
       R::finish(k, base, ulen, llen, st_lane, LUg, Xg, lane, fuse, ptol, bad, tiny);
       pc = sw + 4 * nst + nfw;
       if ((w0 >> 8) & 1) {
@@ -606,7 +665,7 @@ __global__ void __launch_bounds__(256) k_refactor(StreamDev P, SchedDev S, Batch
         case CMD_FWD: {
           const int m = (w0 >> 4) & 0xffff;
           const uint32_t w1 = (uint32_t)cb[pc + 1];
-          R::fwd(cb + pc + 2, m, (w0 >> 20) & 1,
+          R::fwd(cb + pc + 2, m, (int)(((uint32_t)w0) >> 21), (w0 >> 20) & 1,
                  ring_lane + ((w1 & 0xffffu) + (w1 >> 16)) * RB, ring_lane);
           pc += 2 + m;
           break;

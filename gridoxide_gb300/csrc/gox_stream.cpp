@@ -127,6 +127,10 @@ struct Builder {
   }
 
   int rpi() const { return 512 / (32 * P.elem); }  // rows per 16-byte-per-lane copy
+  // estimated cycles of one warp-wide FMA and of one step: FP64 FMAs run at
+  // 1/64 of the FP32 rate on this GPU
+  double fma_cost() const { return P.elem == 8 ? 64.0 : 8.0; }
+  double step_cost() const { return P.elem == 8 ? 60.0 + 5 * 64.0 : 70.0; }
   int zero_row() const { return W * R; }
   int trash_row() const { return W * R + 1; }
 
@@ -320,9 +324,11 @@ struct Builder {
     for (; q < c.items.size() && c.items[q].kind == IT_LRUN; q++) add_steps(c, c.items[q], steps);
     if (steps.size() % 2) steps.push_back(dummy_step(c));
     std::vector<int32_t> fw;
+    size_t nf_real = 0;
     if (sc.fuse_fwd) {
       for (size_t f = q; f < c.items.size(); f += 2)
         fw.push_back(c.items[f].row | (c.items[f + 1].row << 16));
+      nf_real = fw.size();
       while (fw.size() % 8) fw.push_back(zero_row() | (zero_row() << 16));
     }
     const size_t nl = late.size(), np = pref.size(), ns = steps.size(), nf = fw.size();
@@ -355,7 +361,7 @@ struct Builder {
     e.w.push_back(stage_abs | (int32_t)(nl << 16));
     e.w.push_back((int32_t)(np | (ns << 16)));
     e.w.push_back((int32_t)nf);
-    e.w.push_back(0);
+    e.w.push_back((int32_t)nf_real);
     for (const auto& r : late) e.w.push_back((int32_t)((uint32_t)r.first | ((uint32_t)r.second << 21)));
     for (const auto& r : pref) e.w.push_back((int32_t)((uint32_t)r.first | ((uint32_t)r.second << 21)));
     while (e.w.size() % 4) e.w.push_back(0);
@@ -371,7 +377,7 @@ struct Builder {
     for (const Item& it : c.items)
       if (it.state == ST_GATHERED) release_abs(it.row, it.nrows, tf);
     release_abs(stage_abs, c.brows, tf);
-    wcost[w] += 70.0 * ns + 80 + 4.0 * c.len + 8.0 * nf;
+    wcost[w] += step_cost() * ns + 80 + (4.0 + fma_cost()) * c.len + fma_cost() * nf_real;
     return true;
   }
 
@@ -464,7 +470,7 @@ struct Builder {
         return false;
       }
       add_steps(c, it, steps);
-      wcost[w] += 70.0 * ((it.nrows + kStepOps - 1) / kStepOps);
+      wcost[w] += step_cost() * ((it.nrows + kStepOps - 1) / kStepOps);
       if (it.state == ST_GATHERED) consumed.push_back(&it);
     }
     flush_steps(w, stage_abs, steps, c);
@@ -491,7 +497,7 @@ struct Builder {
           e.need(2 + 8);
           size_t m = std::min((f1 - a0) / 2, (e.room() - 2) & ~(size_t)7);
           const size_t mp = (m + 7) & ~(size_t)7;
-          e.w.push_back(CMD_FWD | (int32_t)(mp << 4) | (first ? (1 << 20) : 0));
+          e.w.push_back(CMD_FWD | (int32_t)(mp << 4) | (first ? (1 << 20) : 0) | (int32_t)(m << 21));
           e.w.push_back(stage_abs | (c.len << 16));
           for (size_t t = 0; t < m; t++) {
             const Item& la = c.items[a0 + 2 * t];
@@ -519,7 +525,7 @@ struct Builder {
     const int nfw = (int)(c.items.size() - q) / 2;
     const int64_t tf = now(w, L);
     release_abs(stage_abs, c.brows, tf);
-    wcost[w] += 80 + 4.0 * c.len + 8.0 * nfw;
+    wcost[w] += 80 + (4.0 + fma_cost()) * c.len + fma_cost() * nfw;
     return true;
   }
 
@@ -595,7 +601,8 @@ struct Builder {
           c.items.push_back(b);
         }
       }
-      c.cost = 40 + 70.0 * c.nsteps + 4.0 * c.len + 8.0 * (sc.fuse_fwd ? sc.fw_ptr[k + 1] - sc.fw_ptr[k] : 0);
+      c.cost = 40 + step_cost() * c.nsteps + 4.0 * c.len +
+               fma_cost() * (sc.fuse_fwd ? sc.fw_ptr[k + 1] - sc.fw_ptr[k] : 0);
     }
     // ---- columns to warps: per level, longest first to the least loaded
     //      warp (ties: least total so far, which rotates single columns)

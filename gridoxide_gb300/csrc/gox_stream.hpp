@@ -72,14 +72,14 @@ constexpr int kMaxRows = 2048;  // ring rows of all warps (11-bit row fields)
 //                                                     U(j, k) in stage row j_pos)
 //             y, z, w = 3 destination stage rows each (10 bits); a step
 //             always runs 9 updates, the unused ones on the block's dummy row
-//   FWD     w0 = op | m << 4 | first << 20, stage_row | len << 16, then m words
-//           l_row | y_row << 16 (L(k, j) and y_j): y = (first ? b : y) - sum;
-//           m is a multiple of 8, padded with terms on the zero row
+//   FWD     w0 = op | m << 4 | first << 20 | real_m << 21, stage_row | len << 16,
+//           then m words l_row | y_row << 16 (L(k, j) and y_j): y = (first ? b :
+//           y) - sum; m is a multiple of 8, padded with terms on the zero row
 //   FINISH  w0 = op, k, base, ulen | llen << 16, stage_row; the stage block
 //           is [column rows | y | b | dummy]
 //   COLUMN  w0 = op | wait_n << 4 | do_wait << 7 | bar_after << 8, k, base,
 //           ulen | llen << 16, stage_row | nlate << 16, npref | nsteps << 16,
-//           nfw, 0; then nlate gather words (this column, one commit group),
+//           nfw, real nfw; then nlate gather words (this column, one commit group),
 //           npref gather words (the warp's next column, one group), from the
 //           next 16-byte boundary nsteps steps, then nfw forward terms: the
 //           whole of one column in one command

@@ -299,6 +299,15 @@ class Topology:
     def last_launches(self) -> int:
         return int(_lib.load().gox_last_launches(self._h))
 
+    def set_pivot_tolerance(self, tol: float) -> None:
+        """Mixed path: scenarios whose FP32 refactor meets |u_kk| < tol *
+        max|L(:, k)| are solved again in FP64 (default 1e-6; 0 disables)."""
+        check(_lib.load().gox_set_pivot_tolerance(self._h, float(tol)), "gox_set_pivot_tolerance")
+
+    def last_fallbacks(self) -> int:
+        """Scenarios of the last solve that were solved again in FP64."""
+        return int(_lib.load().gox_last_fallbacks(self._h))
+
     def __del__(self):
         try:
             if self._h:

@@ -233,6 +233,19 @@ int gox_last_timing(const gox_topo *t, double *out);
 /* Kernel launches issued by the last gox_batch_solve* call. */
 int64_t gox_last_launches(const gox_topo *t);
 
+/* Mixed path: the pivot-ratio threshold.  A scenario whose FP32 refactor
+ * meets a pivot with |u_kk| < tol * max |L(:, k)| (before scaling) is solved
+ * again from its start point on the FP64 path, with the same pivot order,
+ * and that report replaces its mixed one.  Default 1e-6; 0 disables.
+ * No counterpart in the reference (its refactor is FP64 only); the FP64
+ * path it falls back to is the reference's static-pivot refactor,
+ * KLU_refactor (KLU/Source/klu_refactor.c:24). */
+int gox_set_pivot_tolerance(gox_topo *t, double tol);
+
+/* Scenarios of the last gox_batch_solve / gox_batch_solve_device call that
+ * were solved again in FP64 (see gox_set_pivot_tolerance). */
+int64_t gox_last_fallbacks(const gox_topo *t);
+
 /* Library version string. */
 const char *gox_version(void);
 
