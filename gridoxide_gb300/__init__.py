@@ -8,7 +8,7 @@ The GPU engine lives in ``libgridoxide_gb300.so`` (C ABI:
 * :mod:`gridoxide_gb300.grids` -- seeded synthetic grids and the Y-bus;
 * :mod:`gridoxide_gb300.build` -- in-tree build of the library (sm_103a).
 """
-from . import build, grids  # noqa: F401
+from . import build, grids, replicas  # noqa: F401
 from ._lib import (GOX_CONVERGED, GOX_MAX_ITERATIONS, GOX_PRECISION_FP64,  # noqa: F401
                    GOX_PRECISION_MIXED, GOX_SINGULAR_SCENARIO, GoxError)
 from .solver import (BatchError, BatchResult, BatchSolver, Buses, BusOverride,  # noqa: F401
