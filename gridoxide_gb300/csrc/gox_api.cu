@@ -203,6 +203,7 @@ struct DevSchedule {
   StreamDev st[2]{};
   int st_nw[2] = {0, 0};
   size_t st_smem[2] = {0, 0};
+  bool st_bwd[2] = {false, false};  // the stream runs the backward substitution too
 
   void load_streams(const Stream& s32, const Stream& s64) {
     const Stream* ss[2] = {&s32, &s64};
@@ -218,6 +219,7 @@ struct DevSchedule {
       st[i].n_bars = ss[i]->n_bars;
       st_nw[i] = ss[i]->plan.nw;
       st_smem[i] = stream_smem_bytes(ss[i]->plan);
+      st_bwd[i] = ss[i]->has_bwd;
     }
   }
 
@@ -383,6 +385,13 @@ struct Iter {
   static void solve(const SchedDev& S, const BatchDev& D, cudaStream_t st) {
     k_solve<T><<<D.G, 32 * kWarps, 0, st>>>(S, D);
   }
+  // the substitutions the refactor's stream did not run (none when it ran
+  // the backward substitution too); returns the launches
+  static int solve_rest(const DevSchedule& ds, const BatchDev& D, cudaStream_t st) {
+    if (ds.st_bwd[sizeof(T) == 4 ? 0 : 1]) return 0;
+    solve(ds.d, D, st);
+    return 1;
+  }
 };
 
 }  // namespace gox
@@ -531,9 +540,9 @@ static void run_iterations(gox_topo* t, BatchDev D, int max_iter, bool outage, c
     rec();
     Iter<T>::refactor(t->dsched, D, st);
     rec();
-    Iter<T>::solve(S, D, st);
+    const int ns = Iter<T>::solve_rest(t->dsched, D, st);
     rec();
-    t->launches += 3;
+    t->launches += 2 + ns;
     GOX_CK(cudaGetLastError());
   }
   if (it == max_iter) t->launches += Iter<T>::mismatch(S, D, max_iter, 1, outage, st);
@@ -1064,7 +1073,11 @@ int gox_topo_emulate_step(const gox_topo* t, const double* jac_vals, const doubl
       if (!(lu[x] == lu64[x]) && !(std::isnan(lu[x]) && std::isnan(lu64[x])))
         throw std::runtime_error("the two refactor streams disagree");
     bad = sing32;
-    for (int ph = 0; ph < sc.n_phases; ph++) {
+    if (t->s32.has_bwd != t->s64.has_bwd) throw std::runtime_error("stream plans disagree");
+    for (int x = 0; x < n && t->s32.has_bwd; x++)
+      if (!(X[x] == X64[x]) && !(std::isnan(X[x]) && std::isnan(X64[x])))
+        throw std::runtime_error("the two streams' substitutions disagree");
+    for (int ph = 0; ph < sc.n_phases && !t->s32.has_bwd; ph++) {
       for (int q = sc.ph_ptr[ph]; q < sc.ph_ptr[ph + 1]; q++) {
         const int k = sc.ph_rows[q];
         if (sc.ph_kind[ph] == 0) {
@@ -1110,6 +1123,8 @@ int gox_topo_info(const gox_topo* t, int64_t* info) {
   info[23] = b.rows_resident;
   info[24] = a.n_column_cmds;
   info[25] = (int64_t)a.words.size();
+  info[26] = a.has_bwd ? 1 : 0;
+  info[27] = b.has_bwd ? 1 : 0;
   return GOX_OK;
 }
 
@@ -1231,7 +1246,7 @@ static int ls_run(gox_ls* h, const double* vals, const double* rhs, double* x) {
   D.err = h->status.as<int32_t>() + 8;
   GOX_CK(cudaMemset(h->status.p, 0, 128));
   Iter<double>::refactor(h->dsched, D, nullptr);
-  Iter<double>::solve(S, D, nullptr);
+  Iter<double>::solve_rest(h->dsched, D, nullptr);
   GOX_CK(cudaGetLastError());
   int32_t werr = 0;
   GOX_CK(cudaMemcpy(&werr, h->status.as<int32_t>() + 8, 4, cudaMemcpyDeviceToHost));
@@ -1382,7 +1397,7 @@ extern "C" int gox_ls_factor_solve_values_static(gox_ls* h, const double* vals,
     D.sing = flags; D.piv_flag = flags + 32; D.gact = flags + 64; D.err = flags + 100;
     D.piv_tol = 0.0f;
     Iter<double>::refactor(h->dsched, D, nullptr);
-    Iter<double>::solve(S, D, nullptr);
+    Iter<double>::solve_rest(h->dsched, D, nullptr);
     k_static_finish<<<grid1d((size_t)n), 256>>>(reinterpret_cast<double*>(B + o_sol),
                                                 reinterpret_cast<int32_t*>(B + o_q), n,
                                                 reinterpret_cast<double*>(B + o_x), flags);

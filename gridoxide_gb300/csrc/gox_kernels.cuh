@@ -506,6 +506,35 @@ struct Rf {
     sts(yrow, y);
   }
 
+  // x_k = (y_k - sum U(k, j) x_j) / U(k, k) over m terms (multiple of 8,
+  // mr real; FP64 skips the padding); x_k to its row and to X
+  static __device__ __forceinline__ void bwd(const int32_t* w, int m, int mr, uint32_t xrow,
+                                             uint32_t yrow, uint32_t drow, uint32_t ring_lane,
+                                             T* xg, bool& bad) {
+    T v = lds<T>(yrow);
+    for (int f0 = 0; f0 < m; f0 += 8) {
+      T a[8], b[8];
+#pragma unroll
+      for (int t = 0; t < 8; t++) {
+        const uint32_t fw = (uint32_t)w[f0 + t];
+        a[t] = lds<T>(ring_lane + (fw & 0xffffu) * RB);
+        b[t] = lds<T>(ring_lane + (fw >> 16) * RB);
+      }
+      if (sizeof(T) == 4) {
+#pragma unroll
+        for (int t = 0; t < 8; t++) v -= a[t] * b[t];
+      } else {
+#pragma unroll
+        for (int t = 0; t < 8; t++)
+          if (f0 + t < mr) v -= a[t] * b[t];
+      }
+    }
+    const T x = v / lds<T>(drow);
+    bad |= !isfinite(x);
+    sts(xrow, x);
+    *xg = x;
+  }
+
   // pivot, scale L in place, write the column (and y_k) back; rows in
   // blocks of 8, the last block clamped to the column's end
   static __device__ __forceinline__ void finish(int k, int base, int ulen, int llen, uint32_t st_lane,
@@ -636,6 +665,31 @@ __global__ void __launch_bounds__(256) k_refactor(StreamDev P, SchedDev S, Batch
                ring_lane);
       R::finish(k, base, ulen, llen, st_lane, LUg, Xg, lane, fuse, ptol, bad, tiny);
       pc = sw + 4 * nst + nfw;
+      if ((w0 >> 8) & 1) {
+        __syncthreads();
+        bars++;
+      }
+    } else if (op == CMD_BWD) {
+      const uint32_t w2 = (uint32_t)cb[pc + 2], w3 = (uint32_t)cb[pc + 3], w4 = (uint32_t)cb[pc + 4];
+      const int k = cb[pc + 1];
+      const int m = (int)(w3 >> 16), nlate = (int)(w4 & 0xffffu), npref = (int)(w4 >> 16);
+      const int32_t* wl = cb + pc + 5;
+      if (nlate) {
+        R::gather(wl, nlate, ring_s, lane, LUg, Xg, RHSg, S.n_slots, S.n_u);
+        asm volatile("cp.async.commit_group;\n" ::: "memory");
+      }
+      if (npref) {
+        R::gather(wl + nlate, npref, ring_s, lane, LUg, Xg, RHSg, S.n_slots, S.n_u);
+        asm volatile("cp.async.commit_group;\n" ::: "memory");
+      }
+      if ((w0 >> 7) & 1) {
+        cp_async_wait_n((w0 >> 4) & 7);
+        __syncwarp();
+      }
+      R::bwd(wl + nlate + npref, m, (int)(((uint32_t)w0) >> 20), ring_lane + (w2 & 0xffffu) * RB,
+             ring_lane + (w2 >> 16) * RB, ring_lane + (w3 & 0xffffu) * RB, ring_lane,
+             Xg + (size_t)k * 32u + lane, bad);
+      pc += 5 + nlate + npref + m;
       if ((w0 >> 8) & 1) {
         __syncthreads();
         bars++;

@@ -22,14 +22,17 @@ inline int64_t tmake(int level, int64_t pos) { return ((int64_t)level << 32) | p
 inline int64_t tend(int level) { return ((int64_t)level << 32) | 0xffffffffLL; }
 inline int64_t tagof(int col, int rel) { return ((int64_t)col << 20) | rel; }
 
-enum { IT_LRUN = 0, IT_FWL = 1, IT_FWY = 2 };
+// value sources: L runs of an update, forward terms L(k, j) and y_j; for a
+// backward-substitution row: y_k, U(k, k), U(k, j) and x_j
+enum { IT_LRUN = 0, IT_FWL = 1, IT_FWY = 2, IT_Y = 3, IT_D = 4, IT_U = 5, IT_X = 6 };
+enum { TK_COL = 0, TK_BWD = 1 };  // task kinds: a refactor column, a backward row
 enum { ST_NONE = 0, ST_GATHERED = 1, ST_RESIDENT = 2 };
 constexpr int kPieceRows = 27;  // longest L run piece placed as one block
 
 // One value source of a column: a run of rows of another column's result.
 struct Item {
   int kind = 0, j = 0;   // producer column
-  int src = 0;           // first source row (factor slot, or X row for y_j)
+  int src = 0;           // first source row in the row space [factor | X | rhs]
   int rel = 0;           // first row within the producer's stage block
   int nrows = 0;
   int upos = -1;         // L runs: U entry p of the consuming column
@@ -40,7 +43,10 @@ struct Item {
   bool committed = false;
 };
 
+// A task: refactor column k (task k) or backward-substitution row k (task
+// n + k, whose block is one row holding x_k).
 struct ColInfo {
+  int kind = TK_COL;
   int k = 0, level = 0, warp = -1, len = 0, brows = 0, nsteps = 0;
   int block = -1;   // ring row (within its warp's ring) of the stage block
   int group = -1;   // commit group of the stage copy
@@ -89,6 +95,8 @@ struct Builder {
   std::vector<int> pinned;    // per warp, rows pinned in the current level
   Stream* out;
   std::string err;
+
+  bool with_bwd = false;  // the backward substitution runs in the stream too
 
   Builder(const Schedule& s, const StreamPlan& p) : sc(s), P(p) {
     W = p.nw;
@@ -212,9 +220,7 @@ struct Builder {
     take(w, r, it.nrows, -1);
     it.row = w * R + r;
     it.state = ST_GATHERED;
-    std::vector<std::pair<int, int>> rows;
-    for (int i = 0; i < it.nrows; i++) rows.push_back({it.src + i, it.row + i});
-    emit_gather(w, it.kind == IT_FWY ? ARR_X : ARR_LU, rows);
+    for (int i = 0; i < it.nrows; i++) pend_rows[w].push_back({it.src + i, it.row + i});
     uncommitted[w].push_back(&it);
     out->rows_gathered += it.nrows;
     return true;
@@ -224,9 +230,10 @@ struct Builder {
     ColInfo& c = C[ci];
     const int r = alloc(w, c.brows, t);
     if (r < 0) return false;
-    take(w, r, c.brows, c.k);
+    take(w, r, c.brows, ci);
     c.block = r;
     c.staged = true;
+    if (c.kind == TK_BWD) return true;  // x_k is written by the task itself
     std::vector<std::pair<int, int>> rows;
     const int base = sc.c_base[c.k];
     for (int i = 0; i < c.len; i++) rows.push_back({base + i, w * R + r + i});
@@ -381,9 +388,120 @@ struct Builder {
     return true;
   }
 
+  // Issues the warp's next task's block and every value finished before
+  // level L ahead of time (one commit group); the copies go to pref_rows.
+  void prefetch_next(int w, int ci, int L, int64_t t, std::vector<std::pair<int, int>>& pref_rows) {
+    const int sp = seqpos[ci];
+    if (sp + 1 >= (int)seq[w].size()) return;
+    const int ni = seq[w][sp + 1];
+    ColInfo& nc = C[ni];
+    if (nc.staged || !stage_col(w, ni, t)) return;
+    for (Item& it : nc.items) {
+      if (it.state != ST_NONE || C[it.j].level >= L) continue;
+      if (!gather_item(w, it, t)) break;
+      out->rows_prefetched += it.nrows;
+    }
+    pref_rows.swap(pend_rows[w]);
+    new_group(w);
+  }
+
+  // x_k = (y_k - sum U(k, j) x_j) / U(k, k) as one BWD command.
+  bool run_bwd(int w, int ci, int L) {
+    ColInfo& c = C[ci];
+    int64_t t = now(w, L);
+    bool waited_late = false;
+    if (!c.staged && !stage_col(w, ci, t)) {
+      err = "no ring room for the row of backward task " + std::to_string(c.k);
+      return false;
+    }
+    for (Item& it : c.items)
+      if (it.state == ST_NONE && gather_item(w, it, t)) {
+        out->rows_late += it.nrows;
+        waited_late = true;
+      }
+    std::vector<std::pair<int, int>> late_rows, pref_rows;
+    late_rows.swap(pend_rows[w]);
+    new_group(w);
+    bool placed = true;
+    for (const Item& it : c.items) placed = placed && it.state != ST_NONE;
+    if (placed) prefetch_next(w, ci, L, t, pref_rows);
+    int g = c.group;
+    for (const Item& it : c.items)
+      if (it.state == ST_GATHERED) g = std::max(g, it.group);
+    pad_rows(late_rows);
+    pad_rows(pref_rows);
+    const size_t nterm = (c.items.size() - 2) / 2;
+    const size_t mpad = (nterm + 7) & ~(size_t)7;
+    Emit& e = em[w];
+    if (!placed || 5 + late_rows.size() + pref_rows.size() + mpad > (size_t)e.cw - 1) {
+      // general form: copies as single commands, the rest just in time
+      for (auto* rows : {&late_rows, &pref_rows}) {
+        if (rows->empty()) continue;
+        pend_rows[w].swap(*rows);
+        flush_gather(w);
+        e.w[e.last_gather] |= (1 << 23);
+      }
+      wait_for(w, g, L, waited_late);
+      if (!placed) {
+        const int64_t tj = now(w, L);
+        for (Item& it : c.items)
+          if (it.state == ST_NONE) {
+            if (!gather_item(w, it, tj)) {
+              err = "no ring room for backward task " + std::to_string(c.k);
+              return false;
+            }
+            out->rows_jit += it.nrows;
+          }
+        commit(w);
+        int gg = -1;
+        for (const Item& it : c.items)
+          if (it.state == ST_GATHERED) gg = std::max(gg, it.group);
+        wait_for(w, gg, L, true);
+      }
+      late_rows.clear();
+      pref_rows.clear();
+      g = -1;
+      if (5 + mpad > (size_t)e.cw - 1) {
+        err = "backward row too long for a stream chunk";
+        return false;
+      }
+    }
+    const size_t need = 5 + late_rows.size() + pref_rows.size() + mpad;
+    e.need(need);
+    int32_t w0 = CMD_BWD | (int32_t)(nterm << 20);
+    if (g >= 0 && waited[w] < g) {
+      const int m = std::min(ngroups[w] - 1 - g, 7);
+      w0 |= (m << 4) | (1 << 7);
+      waited[w] = ngroups[w] - 1 - m;
+      out->n_waits++;
+      if (waited_late) wcost[w] += 1200;
+    }
+    const int xrow = w * R + c.block;
+    last_colhdr[w] = (int64_t)e.w.size();
+    e.w.push_back(w0);
+    e.w.push_back(c.k);
+    e.w.push_back(xrow | (c.items[0].row << 16));
+    e.w.push_back(c.items[1].row | (int32_t)(mpad << 16));
+    e.w.push_back((int32_t)(late_rows.size() | (pref_rows.size() << 16)));
+    for (const auto& r : late_rows) e.w.push_back((int32_t)((uint32_t)r.first | ((uint32_t)r.second << 21)));
+    for (const auto& r : pref_rows) e.w.push_back((int32_t)((uint32_t)r.first | ((uint32_t)r.second << 21)));
+    for (size_t q = 0; q < nterm; q++)
+      e.w.push_back(c.items[2 + 2 * q].row | (c.items[3 + 2 * q].row << 16));
+    for (size_t q = nterm; q < mpad; q++) e.w.push_back(zero_row() | (zero_row() << 16));
+    last_colend[w] = (int64_t)e.w.size();
+    pos[w]++;
+    const int64_t tf = now(w, L);
+    for (const Item& it : c.items)
+      if (it.state == ST_GATHERED) release_abs(it.row, it.nrows, tf);
+    release_abs(xrow, c.brows, tf);
+    wcost[w] += 100 + fma_cost() * (double)nterm;
+    return true;
+  }
+
   // Emits everything of column ci (warp w, level L).
   bool run_col(int w, int ci, int L) {
     ColInfo& c = C[ci];
+    if (c.kind == TK_BWD) return run_bwd(w, ci, L);
     int64_t t = now(w, L);
     bool waited_late = false;
     if (!c.staged) {
@@ -407,20 +525,7 @@ struct Builder {
     // take the room this column still needs)
     bool placed = true;
     for (const Item& it : c.items) placed = placed && it.state != ST_NONE;
-    const int sp = seqpos[ci];
-    if (placed && sp + 1 < (int)seq[w].size()) {
-      const int ni = seq[w][sp + 1];
-      ColInfo& nc = C[ni];
-      if (!nc.staged && stage_col(w, ni, t)) {
-        for (Item& it : nc.items) {
-          if (it.state != ST_NONE || C[it.j].level >= L) continue;
-          if (!gather_item(w, it, t)) break;
-          out->rows_prefetched += it.nrows;
-        }
-        pref_rows.swap(pend_rows[w]);
-        new_group(w);
-      }
-    }
+    if (placed) prefetch_next(w, ci, L, t, pref_rows);
     int g = c.group;
     for (const Item& it : c.items)
       if (it.state == ST_GATHERED) g = std::max(g, it.group);
@@ -594,7 +699,7 @@ struct Builder {
           Item b;
           b.kind = IT_FWY;
           b.j = j;
-          b.src = j;
+          b.src = sc.n_slots + j;
           b.rel = sc.c_ulen[j] + 1 + sc.c_llen[j];
           b.nrows = 1;
           c.items.push_back(a);
@@ -604,13 +709,61 @@ struct Builder {
       c.cost = 40 + step_cost() * c.nsteps + 4.0 * c.len +
                fma_cost() * (sc.fuse_fwd ? sc.fw_ptr[k + 1] - sc.fw_ptr[k] : 0);
     }
+    // ---- backward-substitution rows (tasks n + k), after the refactor's
+    //      levels: x_k = (y_k - sum U(k, j) x_j) / U(k, k)
+    int n_blev = 0;
+    std::vector<int32_t> blev_ptr(1, 0), blev_rows;
+    if (with_bwd) {
+      C.resize(2 * (size_t)n);
+      for (int ph = 0; ph < sc.n_phases; ph++) {
+        if (sc.ph_kind[ph] != 1) {
+          err = "backward tasks need a schedule without forward phases";
+          return false;
+        }
+        for (int q = sc.ph_ptr[ph]; q < sc.ph_ptr[ph + 1]; q++) {
+          const int k = sc.ph_rows[q];
+          ColInfo& c = C[n + k];
+          c.kind = TK_BWD;
+          c.k = k;
+          c.level = sc.n_levels + ph;
+          c.brows = 1;
+          const int ulen = sc.c_ulen[k], len = ulen + 1 + sc.c_llen[k];
+          Item y;
+          y.kind = IT_Y; y.j = k; y.src = sc.n_slots + k; y.rel = len; y.nrows = 1;
+          Item d;
+          d.kind = IT_D; d.j = k; d.src = sc.c_base[k] + ulen; d.rel = ulen; d.nrows = 1;
+          c.items.push_back(y);
+          c.items.push_back(d);
+          for (int tt = sc.bw_ptr[k]; tt < sc.bw_ptr[k + 1]; tt++) {
+            const int slot = sc.bw_slot[tt], j = sc.bw_col[tt];
+            Item u;
+            u.kind = IT_U; u.j = j; u.src = slot; u.rel = slot - sc.c_base[j]; u.nrows = 1;
+            Item xj;
+            xj.kind = IT_X; xj.j = n + j; xj.src = sc.n_slots + j; xj.rel = 0; xj.nrows = 1;
+            c.items.push_back(u);
+            c.items.push_back(xj);
+          }
+          c.cost = 100 + fma_cost() * (sc.bw_ptr[k + 1] - sc.bw_ptr[k]);
+          blev_rows.push_back(n + k);
+        }
+        blev_ptr.push_back((int32_t)blev_rows.size());
+      }
+      n_blev = sc.n_phases;
+    }
+    const int NL = sc.n_levels + n_blev;
+    auto level_tasks = [&](int L) {
+      if (L < sc.n_levels)
+        return std::vector<int>(sc.lev_cols.begin() + sc.lev_ptr[L], sc.lev_cols.begin() + sc.lev_ptr[L + 1]);
+      const int b = L - sc.n_levels;
+      return std::vector<int>(blev_rows.begin() + blev_ptr[b], blev_rows.begin() + blev_ptr[b + 1]);
+    };
     // ---- columns to warps: per level, longest first to the least loaded
     //      warp (ties: least total so far, which rotates single columns)
     seq.assign(W, {});
-    seqpos.assign(n, 0);
+    seqpos.assign(C.size(), 0);
     std::vector<double> tot(W, 0.0);
-    for (int L = 0; L < sc.n_levels; L++) {
-      std::vector<int> cols(sc.lev_cols.begin() + sc.lev_ptr[L], sc.lev_cols.begin() + sc.lev_ptr[L + 1]);
+    for (int L = 0; L < NL; L++) {
+      std::vector<int> cols = level_tasks(L);
       std::stable_sort(cols.begin(), cols.end(), [&](int a, int b) { return C[a].cost > C[b].cost; });
       std::vector<double> load(W, 0.0);
       std::vector<std::vector<int>> mine(W);
@@ -645,7 +798,7 @@ struct Builder {
     wcost.assign(W, 0.0);
     pinned.assign(W, 0);
     std::vector<int> wnext(W, 0);
-    for (int L = 0; L < sc.n_levels; L++) {
+    for (int L = 0; L < NL; L++) {
       for (int w = 0; w < W; w++) { pos[w] = 0; pinned[w] = 0; }
       // stage blocks the warps' previous columns could not issue ahead are
       // placed first, before any value is pinned for reading in place
@@ -655,8 +808,8 @@ struct Builder {
           stage_col(w, seq[w][q], now(w, L));
       }
       // values finished at earlier levels that are still in some ring
-      for (int q = sc.lev_ptr[L]; q < sc.lev_ptr[L + 1]; q++) {
-        ColInfo& c = C[sc.lev_cols[q]];
+      for (int id : level_tasks(L)) {
+        ColInfo& c = C[id];
         for (Item& it : c.items)
           if (it.state == ST_NONE) try_resident(it, L);
       }
@@ -677,7 +830,8 @@ struct Builder {
       }
       st.est_cycles += *std::max_element(wcost.begin(), wcost.end()) + 120;
     }
-    st.n_bars = sc.n_levels;
+    st.n_bars = NL;
+    st.has_bwd = with_bwd;
     // ---- assemble
     st.chunk0.assign(W, 0);
     st.nchunks.assign(W, 0);
@@ -695,8 +849,13 @@ struct Builder {
 
 }  // namespace
 
-bool build_stream(const Schedule& sc, const StreamPlan& plan, Stream& out, std::string& why) {
+static bool choose_stream_1(const Schedule& sc, int elem, size_t smem_budget, Stream& out,
+                            std::string& why, bool with_bwd);
+
+bool build_stream(const Schedule& sc, const StreamPlan& plan, Stream& out, std::string& why,
+                  bool with_bwd) {
   Builder b(sc, plan);
+  b.with_bwd = with_bwd;
   bool ok = false;
   try {
     ok = b.build(out);
@@ -710,6 +869,17 @@ bool build_stream(const Schedule& sc, const StreamPlan& plan, Stream& out, std::
 
 bool choose_stream(const Schedule& sc, int elem, size_t smem_budget, Stream& out,
                    std::string& why) {
+  // with the backward substitution in the stream when the schedule allows
+  // it (no off-diagonal BTF entries), else (or when no plan holds it) without
+  for (bool bwd : {sc.fuse_fwd, false}) {
+    if (choose_stream_1(sc, elem, smem_budget, out, why, bwd)) return true;
+    if (!bwd) break;
+  }
+  return false;
+}
+
+static bool choose_stream_1(const Schedule& sc, int elem, size_t smem_budget, Stream& out,
+                            std::string& why, bool with_bwd) {
   bool found = false;
   std::string last;
   for (int nw : {8, 6, 4, 3, 2, 1}) {
@@ -725,7 +895,7 @@ bool choose_stream(const Schedule& sc, int elem, size_t smem_budget, Stream& out
     p.ring_rows = r;
     Stream s;
     std::string w;
-    if (!build_stream(sc, p, s, w)) {
+    if (!build_stream(sc, p, s, w, with_bwd)) {
       last = w;
       continue;
     }
@@ -754,7 +924,7 @@ std::string run_stream_host(const Schedule& sc, const Stream& st, std::vector<do
   std::vector<int> col_of_slot(sc.n_slots, -1);
   for (int k = 0; k < n; k++)
     for (int p = 0; p < sc.c_ulen[k] + 1 + sc.c_llen[k]; p++) col_of_slot[sc.c_base[k] + p] = k;
-  std::vector<int> colfin(n, -1), xfin(n, -1);
+  std::vector<int> colfin(n, -1), xfin(n, -1), bfin(n, -1);  // level of FINISH / BWD
   singular = false;
   if ((int)lu.size() != sc.n_slots || (int)rhs.size() != n) return "buffer sizes";
   X.assign(n, 0.0);
@@ -807,7 +977,10 @@ std::string run_stream_host(const Schedule& sc, const Stream& st, std::vector<do
             v = lu[src];
           } else if (src < sc.n_slots + n) {
             const int r = src - sc.n_slots;
-            if (xfin[r] < 0 || xfin[r] >= L) { e = "copies y before it is final"; return false; }
+            if (bfin[r] >= 0 ? bfin[r] >= L : (xfin[r] < 0 || xfin[r] >= L)) {
+              e = "copies X before its value is final";
+              return false;
+            }
             v = X[r];
           } else if (src < sc.n_slots + 2 * n) {
             v = rhs[src - sc.n_slots - n];
@@ -957,6 +1130,46 @@ std::string run_stream_host(const Schedule& sc, const Stream& st, std::vector<do
           s.pc += 5;
           continue;
         }
+        if (op == CMD_BWD) {
+          if (s.pc + 5 > cend) return fail("BWD header past its chunk");
+          const int k = st.words[s.pc + 1];
+          const uint32_t w2 = (uint32_t)st.words[s.pc + 2], w3 = (uint32_t)st.words[s.pc + 3];
+          const uint32_t w4 = (uint32_t)st.words[s.pc + 4];
+          const int xr = (int)(w2 & 0xffff), yr = (int)(w2 >> 16), dr = (int)(w3 & 0xffff);
+          const int m = (int)(w3 >> 16), nl = (int)(w4 & 0xffff), np = (int)(w4 >> 16);
+          const int mr = (int)(((uint32_t)w0) >> 20);
+          if (!st.has_bwd || k < 0 || k >= n) return fail("bad BWD command");
+          if (s.pc + 5 + nl + np + m > cend) return fail("BWD past its chunk");
+          if (m % 8 || mr > m) return fail("BWD terms not padded");
+          if (nl && !gather(s.pc + 5, nl, true)) return fail(e);
+          if (np && !gather(s.pc + 5 + nl, np, true)) return fail(e);
+          if ((w0 >> 7) & 1) wait((w0 >> 4) & 7);
+          if (!in_ring(xr) || xr / R != w || !in_ring(yr) || !in_ring(dr)) return fail("BWD rows out of range");
+          if (!note_r(yr) || !note_r(dr)) return fail(e);
+          double v = ring[yr];
+          const int tb = s.pc + 5 + nl + np;
+          for (int f = 0; f < m; f++) {
+            const uint32_t fw = (uint32_t)st.words[tb + f];
+            const int ur = (int)(fw & 0xffff), xj = (int)(fw >> 16);
+            if (ur == zero_row && xj == zero_row) {
+              if (f < mr) return fail("padding inside the real BWD terms");
+              continue;
+            }
+            if (f >= mr) return fail("BWD term after the real count");
+            if (!in_ring(ur) || !in_ring(xj)) return fail("BWD term row out of range");
+            if (!note_r(ur) || !note_r(xj)) return fail(e);
+            v -= ring[ur] * ring[xj];
+          }
+          const double x = v / ring[dr];
+          if (!std::isfinite(x)) singular = true;
+          if (!note_w(xr)) return fail(e);
+          ring[xr] = x;
+          X[k] = x;
+          bfin[k] = L;
+          s.pc = tb + m;
+          if ((w0 >> 8) & 1) { s.bars++; break; }
+          continue;
+        }
         if (op == CMD_COLUMN) {
           if (s.pc + 8 > cend) return fail("COLUMN header past its chunk");
           const int k = st.words[s.pc + 1], base = st.words[s.pc + 2], ul = st.words[s.pc + 3];
@@ -990,6 +1203,9 @@ std::string run_stream_host(const Schedule& sc, const Stream& st, std::vector<do
     if (!ws[w].done) return "warp " + std::to_string(w) + " did not reach END";
   for (int k = 0; k < n; k++)
     if (colfin[k] < 0) return "column " + std::to_string(k) + " never finished";
+  if (st.has_bwd)
+    for (int k = 0; k < n; k++)
+      if (bfin[k] < 0) return "row " + std::to_string(k) + " of the backward substitution never solved";
   return "";
 }
 

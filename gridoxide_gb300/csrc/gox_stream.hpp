@@ -12,6 +12,8 @@
 //   COLUMN              all of one column (copies for it and for the
 //                       warp's next column, wait, steps, FWD, FINISH,
 //                       optionally BAR) in one command
+//   BWD                 one row of the backward substitution x_k = (y_k -
+//                       sum U(k, j) x_j) / U(k, k), with its copies
 //   BAR                 __syncthreads (end of a dependency level)
 //   GATHER arr m rows   cp.async copies of m rows (one row = one value for
 //                       the 32 scenarios of a group) from the factor image,
@@ -48,7 +50,8 @@ enum : int32_t {
   CMD_NEXT = 6,
   CMD_END = 7,
   CMD_FWD = 8,
-  CMD_COLUMN = 9
+  CMD_COLUMN = 9,
+  CMD_BWD = 10
 };
 enum : int32_t { ARR_LU = 0, ARR_X = 1, ARR_RHS = 2 };
 
@@ -83,6 +86,10 @@ constexpr int kMaxRows = 2048;  // ring rows of all warps (11-bit row fields)
 //           npref gather words (the warp's next column, one group), from the
 //           next 16-byte boundary nsteps steps, then nfw forward terms: the
 //           whole of one column in one command
+//   BWD     w0 = op | wait_n << 4 | do_wait << 7 | bar_after << 8 | real_m << 20,
+//           k, x_row | y_row << 16, d_row | m << 16, nlate | npref << 16; then
+//           the nlate and npref gather words, then m terms u_row | x_row << 16
+//           (U(k, j) and x_j; a multiple of 8, padded on the zero row)
 // Gather word counts are multiples of 2 copies (8 rows FP32, 4 FP64), step
 // counts are even, forward term counts multiples of 8 (padding as above);
 // 8 words after a command's last step stay inside its chunk (the step loop
@@ -99,6 +106,7 @@ struct Stream {
   std::vector<int32_t> words;            // all chunks; warp w owns chunks chunk0[w] ..
   std::vector<int32_t> chunk0, nchunks;  // per warp
   int n_bars = 0;
+  bool has_bwd = false;  // the stream also runs the backward substitution
   // statistics of the schedule
   int64_t rows_gathered = 0, rows_prefetched = 0, rows_resident = 0, rows_late = 0;
   int64_t rows_jit = 0, n_steps = 0, n_waits = 0, n_groups = 0, n_column_cmds = 0;
@@ -108,9 +116,11 @@ struct Stream {
 // Shared memory (bytes) the refactor kernel needs for a plan.
 size_t stream_smem_bytes(const StreamPlan& plan);
 
-// Compiles the refactor of a schedule for a plan.  Returns false, with the
-// reason, when the plan cannot hold it (a column longer than the ring).
-bool build_stream(const Schedule& sc, const StreamPlan& plan, Stream& out, std::string& why);
+// Compiles the refactor of a schedule for a plan (and, with with_bwd, the
+// backward substitution after it; the schedule must fuse the forward one).
+// Returns false, with the reason, when the plan cannot hold it.
+bool build_stream(const Schedule& sc, const StreamPlan& plan, Stream& out, std::string& why,
+                  bool with_bwd = false);
 
 // Chooses the plan (warps, ring) within `smem_budget` bytes with the
 // lowest estimated critical path, and builds its stream.
