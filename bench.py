@@ -310,9 +310,14 @@ def main():
     h2d = 2 * B * N * 8 + 2 * N * 8
     d2h = 2 * B * N * 8 + B * (4 + 4 + 8)
 
-    # roofline of the dominant kernel (mixed path)
+    # roofline of the dominant kernel (mixed path).  When the refactor's
+    # command streams also run the backward substitution there is no solve
+    # launch: the refactor kernel does both, and its bytes are both kernels'.
     info = topo.info()
     abytes = algorithmic_bytes(info, N, 4)
+    if info.get("rf32_with_bwd"):
+        abytes["refactor"] += abytes.pop("solve")
+        kern_mx["refactor"] += kern_mx.pop("solve")
     dom = max(kern_mx, key=lambda k: kern_mx[k])
     n_launch = sum(iters_mx) if dom != "mismatch" else sum(iters_mx) + args.steps
     per_launch_bytes = abytes[dom] * B

@@ -104,7 +104,9 @@ __global__ void __launch_bounds__(256) k_update(SchedDev S, BatchDev D, int it, 
   D.f[x] = f;
   ((T*)D.eT)[x] = (T)e;
   ((T*)D.fT)[x] = (T)f;
-  ((T*)D.ivT)[x] = (T)(1.0 / vm);
+  // 1/|V| for the Jacobian fill, in the fill's precision (an FP64 division
+  // costs far more than an FP32 one on this GPU)
+  ((T*)D.ivT)[x] = (T)1 / (T)vm;
 }
 
 // ---------------------------------------------------------------------------
