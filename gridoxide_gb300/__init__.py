@@ -12,7 +12,7 @@ from . import build, grids, replicas  # noqa: F401
 from ._lib import (GOX_CONVERGED, GOX_MAX_ITERATIONS, GOX_PRECISION_FP64,  # noqa: F401
                    GOX_PRECISION_MIXED, GOX_SINGULAR_SCENARIO, GoxError)
 from .solver import (BatchError, BatchResult, BatchSolver, Buses, BusOverride,  # noqa: F401
-                     Gb300LinearSolver, JacobianBackend, PowerFlowReport, Scenario, SolveStatus,
-                     Topology, analyze, factor_host, uniform_load_scaling)
+                     Gb300LinearSolver, JacobianBackend, PowerFlowReport, Scenario, Server,
+                     SolveStatus, Topology, analyze, factor_host, uniform_load_scaling)
 
 __version__ = "0.1.0"

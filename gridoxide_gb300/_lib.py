@@ -13,6 +13,7 @@ LIB_PATH = os.path.join(HERE, "libgridoxide_gb300.so")
 
 GOX_OK = 0
 GOX_SINGULAR = 1
+GOX_PENDING = 2
 GOX_E_OUT_OF_MEMORY = -2
 GOX_E_INVALID = -3
 GOX_E_BUS_RANGE = -4
@@ -83,6 +84,12 @@ SIGNATURES = {
     "gox_set_pivot_tolerance": (C.c_int, [vp, C.c_double]),
     "gox_last_fallbacks": (C.c_int64, [vp]),
     "gox_version": (C.c_char_p, []),
+    "gox_server_create": (C.c_int, [C.c_int32, C.c_int32, C.c_double, C.c_int32, C.POINTER(vp)]),
+    "gox_server_add_topology": (C.c_int, [vp, vp, i32p]),
+    "gox_server_submit": (C.c_int, [vp, C.c_int32, f64p, f64p, f64p, f64p, i32p, f64p, f64p, i64p]),
+    "gox_server_poll": (C.c_int, [vp, C.c_int64, f64p, f64p, i32p, i32p, f64p, f64p]),
+    "gox_server_stats": (C.c_int, [vp, i64p]),
+    "gox_server_destroy": (None, [vp]),
 }
 
 _lib = None

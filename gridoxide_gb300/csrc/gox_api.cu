@@ -1409,3 +1409,235 @@ extern "C" int gox_ls_factor_solve_values_static(gox_ls* h, const double* vals,
     return (hf[0] || hf[96]) ? GOX_SINGULAR : GOX_OK;
   });
 }
+
+// ---- serving -----------------------------------------------------------------
+// A worker thread batches queued single-scenario requests per topology
+// (continuous batching: while a batch runs, new requests queue; the next
+// batch takes the topology with the oldest request and up to max_batch of
+// its requests in arrival order) and solves each batch with
+// gox_batch_solve on the GPU.
+
+#include <chrono>
+#include <condition_variable>
+#include <deque>
+#include <thread>
+#include <unordered_map>
+
+namespace gox {
+struct ServerReq {
+  int64_t ticket = 0;
+  int topo = 0;
+  std::vector<double> p, q, vm0, va0;
+  int32_t slot[4] = {-1, -1, -1, -1};
+  double dre[4] = {0, 0, 0, 0}, dim[4] = {0, 0, 0, 0};
+  bool outage = false;
+  std::chrono::steady_clock::time_point t_submit;
+  // results
+  int rc = 1;  // 1 pending, 0 done, < 0 error
+  std::vector<double> vm, va;
+  int32_t iters = 0, status = 0;
+  double max_mis = 0, latency = 0;
+};
+}  // namespace gox
+
+struct gox_server {
+  int32_t max_batch = 1024, precision = GOX_PRECISION_MIXED, max_iter = 20;
+  double tol = 1e-8;
+  int device = 0;
+  std::vector<gox_topo*> topos;
+  std::mutex mu;
+  std::condition_variable cv;
+  std::deque<std::shared_ptr<gox::ServerReq>> queue;
+  std::unordered_map<int64_t, std::shared_ptr<gox::ServerReq>> all;
+  int64_t next_ticket = 1;
+  bool stop = false;
+  int64_t batches = 0, solved = 0;
+  std::thread worker;
+
+  void run() {
+    cudaSetDevice(device);
+    for (;;) {
+      std::vector<std::shared_ptr<gox::ServerReq>> batch;
+      {
+        std::unique_lock<std::mutex> lk(mu);
+        cv.wait(lk, [&] { return stop || !queue.empty(); });
+        if (stop && queue.empty()) return;
+        const int tp = queue.front()->topo;
+        for (auto it = queue.begin(); it != queue.end() && (int)batch.size() < max_batch;) {
+          if ((*it)->topo == tp) {
+            batch.push_back(*it);
+            it = queue.erase(it);
+          } else {
+            ++it;
+          }
+        }
+      }
+      solve(batch);
+      {
+        std::lock_guard<std::mutex> lk(mu);
+        batches++;
+        solved += (int64_t)batch.size();
+      }
+      cv.notify_all();
+    }
+  }
+
+  void solve(std::vector<std::shared_ptr<gox::ServerReq>>& batch) {
+    gox_topo* t = topos[batch[0]->topo];
+    const int n = t->n_bus, B = (int)batch.size();
+    std::vector<double> p((size_t)B * n), q((size_t)B * n), vm0((size_t)B * n), va0((size_t)B * n);
+    std::vector<double> vm((size_t)B * n), va((size_t)B * n), mm(B), dre((size_t)B * 4), dim((size_t)B * 4);
+    std::vector<int32_t> it(B), st(B), sl((size_t)B * 4, -1);
+    bool any_out = false;
+    for (int s = 0; s < B; s++) {
+      const gox::ServerReq& r = *batch[s];
+      std::copy(r.p.begin(), r.p.end(), p.begin() + (size_t)s * n);
+      std::copy(r.q.begin(), r.q.end(), q.begin() + (size_t)s * n);
+      std::copy(r.vm0.begin(), r.vm0.end(), vm0.begin() + (size_t)s * n);
+      std::copy(r.va0.begin(), r.va0.end(), va0.begin() + (size_t)s * n);
+      if (r.outage) {
+        any_out = true;
+        for (int c = 0; c < 4; c++) {
+          sl[(size_t)s * 4 + c] = r.slot[c];
+          dre[(size_t)s * 4 + c] = r.dre[c];
+          dim[(size_t)s * 4 + c] = r.dim[c];
+        }
+      }
+    }
+    const int rc = gox_batch_solve(t, B, p.data(), q.data(), vm0.data(), va0.data(), n,
+                                   any_out ? sl.data() : nullptr, any_out ? dre.data() : nullptr,
+                                   any_out ? dim.data() : nullptr, tol, max_iter, precision,
+                                   vm.data(), va.data(), it.data(), st.data(), mm.data(), nullptr);
+    const auto now = std::chrono::steady_clock::now();
+    std::lock_guard<std::mutex> lk(mu);
+    for (int s = 0; s < B; s++) {
+      gox::ServerReq& r = *batch[s];
+      if (rc < 0) {
+        r.rc = rc;
+      } else {
+        r.vm.assign(vm.begin() + (size_t)s * n, vm.begin() + (size_t)(s + 1) * n);
+        r.va.assign(va.begin() + (size_t)s * n, va.begin() + (size_t)(s + 1) * n);
+        r.iters = it[s];
+        r.status = st[s];
+        r.max_mis = mm[s];
+        r.rc = GOX_OK;
+      }
+      r.latency = std::chrono::duration<double>(now - r.t_submit).count();
+    }
+  }
+};
+
+extern "C" {
+
+int gox_server_create(int32_t max_batch, int32_t precision, double tol, int32_t max_iter,
+                      gox_server** out) {
+  if (!out || max_batch <= 0 || max_iter < 0 || !(tol > 0.0) ||
+      (precision != GOX_PRECISION_FP64 && precision != GOX_PRECISION_MIXED))
+    return GOX_E_INVALID;
+  *out = nullptr;
+  if (int r = require_device()) return r;
+  return guard_impl([&]() -> int {
+    std::unique_ptr<gox_server> s(new gox_server());
+    s->max_batch = max_batch;
+    s->precision = precision;
+    s->tol = tol;
+    s->max_iter = max_iter;
+    GOX_CK(cudaGetDevice(&s->device));
+    gox_server* raw = s.get();
+    s->worker = std::thread([raw] { raw->run(); });
+    *out = s.release();
+    return GOX_OK;
+  });
+}
+
+int gox_server_add_topology(gox_server* s, gox_topo* t, int32_t* topo_id) {
+  if (!s || !t || !topo_id) return GOX_E_INVALID;
+  std::lock_guard<std::mutex> lk(s->mu);
+  s->topos.push_back(t);
+  *topo_id = (int32_t)s->topos.size() - 1;
+  return GOX_OK;
+}
+
+int gox_server_submit(gox_server* s, int32_t topo_id, const double* p_spec, const double* q_spec,
+                      const double* vm0, const double* va0, const int32_t* out_slot,
+                      const double* out_dre, const double* out_dim, int64_t* ticket) {
+  if (!s || !p_spec || !q_spec || !vm0 || !va0 || !ticket) return GOX_E_INVALID;
+  if ((out_slot != nullptr) != (out_dre != nullptr) || (out_slot != nullptr) != (out_dim != nullptr))
+    return GOX_E_INVALID;
+  return guard_impl([&]() -> int {
+    auto r = std::make_shared<gox::ServerReq>();
+    {
+      std::lock_guard<std::mutex> lk(s->mu);
+      if (topo_id < 0 || topo_id >= (int32_t)s->topos.size()) return GOX_E_INVALID;
+      r->topo = topo_id;
+    }
+    const int n = s->topos[topo_id]->n_bus;
+    r->p.assign(p_spec, p_spec + n);
+    r->q.assign(q_spec, q_spec + n);
+    r->vm0.assign(vm0, vm0 + n);
+    r->va0.assign(va0, va0 + n);
+    if (out_slot) {
+      r->outage = true;
+      for (int c = 0; c < 4; c++) {
+        r->slot[c] = out_slot[c];
+        r->dre[c] = out_dre[c];
+        r->dim[c] = out_dim[c];
+      }
+    }
+    r->t_submit = std::chrono::steady_clock::now();
+    {
+      std::lock_guard<std::mutex> lk(s->mu);
+      if (s->stop) return GOX_E_INVALID;
+      r->ticket = s->next_ticket++;
+      s->all[r->ticket] = r;
+      s->queue.push_back(r);
+      *ticket = r->ticket;
+    }
+    s->cv.notify_all();
+    return GOX_OK;
+  });
+}
+
+int gox_server_poll(gox_server* s, int64_t ticket, double* vm, double* va, int32_t* iterations,
+                    int32_t* status, double* max_mismatch, double* latency_s) {
+  if (!s) return GOX_E_INVALID;
+  std::shared_ptr<gox::ServerReq> r;
+  {
+    std::lock_guard<std::mutex> lk(s->mu);
+    auto it = s->all.find(ticket);
+    if (it == s->all.end()) return GOX_E_INVALID;
+    r = it->second;
+    if (r->rc == 1) return GOX_PENDING;
+    s->all.erase(it);
+  }
+  if (r->rc < 0) return r->rc;
+  if (vm) std::copy(r->vm.begin(), r->vm.end(), vm);
+  if (va) std::copy(r->va.begin(), r->va.end(), va);
+  if (iterations) *iterations = r->iters;
+  if (status) *status = r->status;
+  if (max_mismatch) *max_mismatch = r->max_mis;
+  if (latency_s) *latency_s = r->latency;
+  return GOX_OK;
+}
+
+int gox_server_stats(gox_server* s, int64_t* out) {
+  if (!s || !out) return GOX_E_INVALID;
+  std::lock_guard<std::mutex> lk(s->mu);
+  out[0] = s->batches;
+  out[1] = s->solved;
+  out[2] = (int64_t)s->queue.size();
+  return GOX_OK;
+}
+
+void gox_server_destroy(gox_server* s) {
+  if (!s) return;
+  {
+    std::lock_guard<std::mutex> lk(s->mu);
+    s->stop = true;
+  }
+  s->cv.notify_all();
+  if (s->worker.joinable()) s->worker.join();
+  delete s;
+}
+
+}  // extern "C"

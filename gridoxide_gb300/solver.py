@@ -469,3 +469,83 @@ def factor_host(n: int, rows, cols, vals) -> Optional[dict]:
     out["Fi"] = out["Fi"][:nzoff]
     out["Fx"] = out["Fx"][:nzoff]
     return out
+
+
+class Server:
+    """Continuous batching of single-scenario requests over registered
+    topologies (gox_server_*): a worker thread in the library batches the
+    queued requests of one topology at a time and solves them on the GPU;
+    ``poll`` returns a request's report (with its latency) once solved.
+    A registered Topology is used by the server's thread only."""
+
+    def __init__(self, max_batch: int = 1024, precision: int = GOX_PRECISION_MIXED,
+                 tol: float = 1e-8, max_iter: int = 20):
+        L = _lib.load()
+        h = C.c_void_p()
+        check(L.gox_server_create(int(max_batch), int(precision), float(tol), int(max_iter),
+                                  C.byref(h)), "gox_server_create")
+        self._h = h
+        self._topos = []
+        self._n = []
+
+    def add_topology(self, topo: "Topology") -> int:
+        tid = C.c_int32()
+        check(_lib.load().gox_server_add_topology(self._h, topo._h, C.byref(tid)),
+              "gox_server_add_topology")
+        self._topos.append(topo)
+        self._n.append(topo.n_bus)
+        return int(tid.value)
+
+    def submit(self, topo_id: int, p_spec, q_spec, vm0, va0, outage=None) -> int:
+        n = self._n[topo_id]
+        arrs = [_f64(a) for a in (p_spec, q_spec, vm0, va0)]
+        if any(a.shape != (n,) for a in arrs):
+            raise ValueError("p_spec, q_spec, vm0, va0 must be [n_bus]")
+        if outage is not None:
+            sl, dr, di = _i32(outage[0]), _f64(outage[1]), _f64(outage[2])
+            op = (_p(sl, _lib.i32p), _p(dr, _lib.f64p), _p(di, _lib.f64p))
+        else:
+            op = (None, None, None)
+        t = C.c_int64()
+        check(_lib.load().gox_server_submit(self._h, int(topo_id), *[_p(a, _lib.f64p) for a in arrs],
+                                            *op, C.byref(t)), "gox_server_submit")
+        return int(t.value)
+
+    def poll(self, ticket: int, n_bus: int) -> Optional[dict]:
+        vm, va = np.zeros(n_bus), np.zeros(n_bus)
+        it, st = C.c_int32(), C.c_int32()
+        mm, lat = C.c_double(), C.c_double()
+        rc = _lib.load().gox_server_poll(self._h, int(ticket), _p(vm, _lib.f64p), _p(va, _lib.f64p),
+                                         C.byref(it), C.byref(st), C.byref(mm), C.byref(lat))
+        if rc == _lib.GOX_PENDING:
+            return None
+        check(rc, "gox_server_poll")
+        return dict(vm=vm, va=va, iterations=int(it.value), status=int(st.value),
+                    max_mismatch=float(mm.value), latency_s=float(lat.value))
+
+    def wait(self, ticket: int, n_bus: int, timeout: float = 120.0) -> dict:
+        import time
+        t0 = time.perf_counter()
+        while True:
+            r = self.poll(ticket, n_bus)
+            if r is not None:
+                return r
+            if time.perf_counter() - t0 > timeout:
+                raise TimeoutError(f"request {ticket} not solved in {timeout} s")
+            time.sleep(1e-4)
+
+    def stats(self) -> dict:
+        a = np.zeros(3, np.int64)
+        check(_lib.load().gox_server_stats(self._h, _p(a, _lib.i64p)), "gox_server_stats")
+        return dict(batches=int(a[0]), solved=int(a[1]), queued=int(a[2]))
+
+    def close(self) -> None:
+        if getattr(self, "_h", None):
+            _lib.load().gox_server_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

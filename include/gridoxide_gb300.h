@@ -34,6 +34,7 @@ extern "C" {
 /* ---- status codes ------------------------------------------------------ */
 #define GOX_OK 0
 #define GOX_SINGULAR 1          /* LinearSolver returned None (KLU_SINGULAR) */
+#define GOX_PENDING 2           /* gox_server_poll: the request is not solved yet */
 #define GOX_E_OUT_OF_MEMORY (-2) /* KLU_OUT_OF_MEMORY */
 #define GOX_E_INVALID (-3)      /* KLU_INVALID: bad sizes / pointers / pattern */
 #define GOX_E_BUS_RANGE (-4)    /* BatchError::BusOutOfRange (src/batch.rs:108-135) */
@@ -249,6 +250,39 @@ int64_t gox_last_fallbacks(const gox_topo *t);
 
 /* Library version string. */
 const char *gox_version(void);
+
+/* ---- serving --------------------------------------------------------------
+ * Continuous batching of single-scenario requests over registered
+ * topologies: a worker thread takes the topology with the oldest queued
+ * request and up to max_batch of its requests (arrival order), solves them
+ * with gox_batch_solve, and publishes each result with its latency (submit
+ * to completion).  Lanes are independent, so a request's result does not
+ * depend on the batch it ran in.  A topology added to a server is used by
+ * the server's thread only: do not call it directly while the server runs.
+ * The reference's serving counterpart is the Python `PowerFlowModel.solve_batch`
+ * / rayon `BatchSolver` call per batch (src/python.rs:306-341,
+ * src/batch.rs:198-289); the queue in front of it is new here. */
+typedef struct gox_server gox_server;
+
+int gox_server_create(int32_t max_batch, int32_t precision, double tol, int32_t max_iter,
+                      gox_server **out);
+/* Registers a topology (not owned by the server); its id in *topo_id. */
+int gox_server_add_topology(gox_server *s, gox_topo *t, int32_t *topo_id);
+/* Queues one scenario: p_spec, q_spec, vm0, va0 [n_bus]; optional outage
+ * (4 Y slots and the values added to them, as gox_batch_solve's out_*;
+ * all three or none).  Returns a ticket. */
+int gox_server_submit(gox_server *s, int32_t topo_id, const double *p_spec, const double *q_spec,
+                      const double *vm0, const double *va0, const int32_t *out_slot,
+                      const double *out_dre, const double *out_dim, int64_t *ticket);
+/* GOX_PENDING until the request is solved; then GOX_OK (the outputs are
+ * written and the ticket is retired) or the batch's error code.  Output
+ * pointers may be NULL. */
+int gox_server_poll(gox_server *s, int64_t ticket, double *vm, double *va, int32_t *iterations,
+                    int32_t *status, double *max_mismatch, double *latency_s);
+/* [0] batches run, [1] requests solved, [2] requests queued. */
+int gox_server_stats(gox_server *s, int64_t *out);
+/* Finishes the queued requests, stops the worker, frees the server. */
+void gox_server_destroy(gox_server *s);
 
 #ifdef __cplusplus
 }

@@ -1,0 +1,99 @@
+"""GPU: the serving loop (gox_server_*).  Requests arrive one scenario at a
+time (Poisson arrivals from a client thread) over three topologies, some
+with an N-1 outage; the worker batches them per topology.  Every report
+must equal, bit for bit, a direct batched solve of the same scenario on the
+same topology (lanes are independent, so the batch a request ran in does
+not change its result), and carry a positive latency."""
+import threading
+import time
+
+import numpy as np
+import pytest
+
+from gridoxide_gb300 import grids as G
+from helpers import grid_from_fixture, load_fixture, ybus_from_fixture
+
+pytestmark = pytest.mark.gpu
+
+
+def _grids():
+    fx = load_fixture("case118")
+    g1, y1 = grid_from_fixture(fx), ybus_from_fixture(fx)
+    g2 = G.make_grid(300, 45, 420, seed=31)
+    g3 = G.make_grid(600, 90, 840, seed=32, load_scale=0.5)
+    return [(g1, y1), (g2, G.build_ybus(g2)), (g3, G.build_ybus(g3))]
+
+
+@pytest.mark.parametrize("precision", [0, 1])
+def test_server_reports_equal_direct_solves(gox, precision):
+    grids = _grids()
+    topos = [gox.Topology(yb, g.bus_type) for g, yb in grids]
+    rng = np.random.default_rng(40)
+    reqs = []  # (topo id, p, q, outage or None)
+    for i in range(150):
+        t = int(rng.integers(0, 3))
+        g, yb = grids[t]
+        p, q = G.load_scenarios(g, 1, 0.1, 1000 + i)
+        out = None
+        if rng.random() < 0.1:
+            br = rng.choice(np.flatnonzero(~G.bridges(g)), size=1)
+            out = tuple(a[0] for a in G.outage_deltas(g, yb, br))
+        reqs.append((t, p[0], q[0], out))
+    srv = gox.Server(max_batch=64, precision=precision)
+    ids = [srv.add_topology(tp) for tp in topos]
+    tickets = [None] * len(reqs)
+
+    def client():
+        for i, (t, p, q, out) in enumerate(reqs):
+            g = grids[t][0]
+            tickets[i] = srv.submit(ids[t], p, q, g.vm, g.va, outage=out)
+            time.sleep(rng.exponential(2e-4))
+
+    th = threading.Thread(target=client)
+    th.start()
+    th.join()
+    reports = [srv.wait(tickets[i], grids[reqs[i][0]][0].n_bus) for i in range(len(reqs))]
+    st = srv.stats()
+    srv.close()
+    assert st["solved"] == len(reqs) and st["queued"] == 0 and st["batches"] >= 3
+    lat = np.array([r["latency_s"] for r in reports])
+    assert np.all(lat > 0)
+    # the same scenarios solved directly on the same topologies
+    for t in range(3):
+        idx = [i for i, r in enumerate(reqs) if r[0] == t]
+        g = grids[t][0]
+        p = np.stack([reqs[i][1] for i in idx])
+        q = np.stack([reqs[i][2] for i in idx])
+        has = [reqs[i][3] is not None for i in idx]
+        out = None
+        if any(has):
+            sl = np.full((len(idx), 4), -1, np.int32)
+            dr = np.zeros((len(idx), 4))
+            di = np.zeros((len(idx), 4))
+            for r, i in enumerate(idx):
+                if reqs[i][3] is not None:
+                    sl[r], dr[r], di[r] = reqs[i][3]
+            out = (sl, dr, di)
+        res = topos[t].solve(p, q, g.vm, g.va, precision=precision, outage=out)
+        for r, i in enumerate(idx):
+            np.testing.assert_array_equal(reports[i]["vm"], res.voltage_mag[r])
+            np.testing.assert_array_equal(reports[i]["va"], res.voltage_ang[r])
+            np.testing.assert_array_equal(
+                [reports[i]["iterations"], reports[i]["status"], reports[i]["max_mismatch"]],
+                [res.iterations[r], res.status[r], res.max_mismatch[r]])
+
+
+def test_server_rejects_bad_requests(gox):
+    g, yb = _grids()[0]
+    srv = gox.Server(max_batch=8)
+    tid = srv.add_topology(gox.Topology(yb, g.bus_type))
+    with pytest.raises(ValueError):
+        srv.submit(tid, g.p_spec[:-1], g.q_spec, g.vm, g.va)
+    with pytest.raises(Exception):
+        srv.submit(tid + 5, g.p_spec, g.q_spec, g.vm, g.va)
+    t = srv.submit(tid, g.p_spec, g.q_spec, g.vm, g.va)
+    r = srv.wait(t, g.n_bus)
+    assert r["status"] == gox.GOX_CONVERGED
+    with pytest.raises(Exception):
+        srv.poll(t, g.n_bus)  # a retired ticket
+    srv.close()
