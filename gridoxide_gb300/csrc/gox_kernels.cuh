@@ -592,12 +592,12 @@ struct Rf {
 // malformed command, sets the error flag; the warp then drains its copies
 // and still takes every remaining barrier.
 template <typename T>
-__global__ void __launch_bounds__(256) k_refactor(StreamDev P, SchedDev S, BatchDev D) {
+__global__ void __launch_bounds__(256, 1) k_refactor(StreamDev P, SchedDev S, BatchDev D) {
   using R = Rf<T>;
   const int g = blockIdx.x;
   if (!D.gact[g]) return;
   extern __shared__ __align__(128) unsigned char smem_raw[];
-  __shared__ __align__(8) uint64_t mbar[8][2];
+  __shared__ __align__(8) uint64_t mbar[kMaxRefactorWarps][2];
   __shared__ int flags[2][32];
   __shared__ int timed_out;
   constexpr uint32_t RB = R::RB;

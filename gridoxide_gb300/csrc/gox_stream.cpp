@@ -244,8 +244,8 @@ struct Builder {
   }
 
   // Reads `it` in place from the producer's block when it is still there,
-  // pinning those rows through level L; at most half of a ring is pinned,
-  // so the warps keep room for their own copies.
+  // pinning those rows through level L; at most a quarter of a ring is
+  // pinned, so the warps keep room for their own copies.
   bool try_resident(Item& it, int L) {
     const ColInfo& pc = C[it.j];
     if (pc.warp < 0 || pc.block < 0 || pc.level >= L) return false;
@@ -255,7 +255,7 @@ struct Builder {
       if (tag[b + i] != tagof(it.j, it.rel + i)) return false;
       if (busy[b + i] < tend(L)) fresh++;
     }
-    if (pinned[pc.warp] + fresh > R / 2) return false;
+    if (pinned[pc.warp] + fresh > R / 4) return false;
     pinned[pc.warp] += fresh;
     it.row = (int)b;
     it.state = ST_RESIDENT;
@@ -388,18 +388,32 @@ struct Builder {
     return true;
   }
 
-  // Issues the warp's next task's block and every value finished before
-  // level L ahead of time (one commit group); the copies go to pref_rows.
+  // Issues the blocks of the warp's next tasks and every value of theirs
+  // finished before level L ahead of time, all in one commit group (the
+  // command commits its prefetch list once): the next task always, further
+  // ones while the tasks in between are short (under kAheadCycles of
+  // estimated work, so a copy's latency would not be hidden otherwise) and
+  // the ring has room.  The copies go to pref_rows.
+  static constexpr double kAheadCycles = 2500.0;
+  static constexpr int kAheadTasks = 1;
   void prefetch_next(int w, int ci, int L, int64_t t, std::vector<std::pair<int, int>>& pref_rows) {
     const int sp = seqpos[ci];
-    if (sp + 1 >= (int)seq[w].size()) return;
-    const int ni = seq[w][sp + 1];
-    ColInfo& nc = C[ni];
-    if (nc.staged || !stage_col(w, ni, t)) return;
-    for (Item& it : nc.items) {
-      if (it.state != ST_NONE || C[it.j].level >= L) continue;
-      if (!gather_item(w, it, t)) break;
-      out->rows_prefetched += it.nrows;
+    double ahead = C[ci].cost;
+    for (int d = 1; d <= kAheadTasks && sp + d < (int)seq[w].size(); d++) {
+      const int ni = seq[w][sp + d];
+      ColInfo& nc = C[ni];
+      if (d > 1 && ahead >= kAheadCycles) break;
+      if (!nc.staged) {
+        if (!stage_col(w, ni, t)) break;
+        bool all = true;
+        for (Item& it : nc.items) {
+          if (it.state != ST_NONE || C[it.j].level >= L) continue;
+          if (!gather_item(w, it, t)) { all = false; break; }
+          out->rows_prefetched += it.nrows;
+        }
+        if (!all) break;
+      }
+      ahead += nc.cost;
     }
     pref_rows.swap(pend_rows[w]);
     new_group(w);
@@ -883,6 +897,7 @@ static bool choose_stream_1(const Schedule& sc, int elem, size_t smem_budget, St
   bool found = false;
   std::string last;
   for (int nw : {8, 6, 4, 3, 2, 1}) {
+    if (nw > kMaxRefactorWarps) continue;
     StreamPlan p;
     p.elem = elem;
     p.nw = nw;
@@ -899,10 +914,9 @@ static bool choose_stream_1(const Schedule& sc, int elem, size_t smem_budget, St
       last = w;
       continue;
     }
-    if (!found || s.est_cycles < out.est_cycles) {
-      out = std::move(s);
-      found = true;
-    }
+    out = std::move(s);
+    found = true;
+    break;  // the most warps that fit
   }
   if (!found) why = last.empty() ? "no plan fits the shared-memory budget" : last;
   return found;

@@ -61,6 +61,7 @@ constexpr int kStepOps = 9;     // update ops per step (one L(:, j) run piece)
 // and rows the unused slots of a step may read.
 constexpr int kSpareRows = 12;
 constexpr int kMaxRows = 2048;  // ring rows of all warps (11-bit row fields)
+constexpr int kMaxRefactorWarps = 8;
 
 // Encodings (all little fields of 32-bit words):
 //   GATHER  w0 = op | m << 4 | commit << 23, then m words src_row | dst_row << 21;
@@ -122,8 +123,11 @@ size_t stream_smem_bytes(const StreamPlan& plan);
 bool build_stream(const Schedule& sc, const StreamPlan& plan, Stream& out, std::string& why,
                   bool with_bwd = false);
 
-// Chooses the plan (warps, ring) within `smem_budget` bytes with the
-// lowest estimated critical path, and builds its stream.
+// Chooses the plan within `smem_budget` bytes: the most warps (up to 8)
+// whose rings hold the schedule, and builds its stream.  (Measured on
+// GB300, case2000 FP32: 3 / 4 / 6 / 8 / 12 warps took 4.90 / 4.26 / 3.72 /
+// 3.52 / 3.69 ms per refactor, while the estimate favoured 4: more warps
+// hide the latencies of the wide levels, and beyond 8 the rings shrink.)
 bool choose_stream(const Schedule& sc, int elem, size_t smem_budget, Stream& out,
                    std::string& why);
 
