@@ -401,6 +401,10 @@ using namespace gox;
 // ---------------------------------------------------------------------------
 // opaque handles
 
+struct IoStage {
+  DevMem p, q, vm, va, ovm, ova, it, st, mm, h, sl, dre, dim;
+};
+
 struct gox_topo {
   int n_bus = 0;
   std::vector<int32_t> yp, yi, bus_type;
@@ -417,6 +421,8 @@ struct gox_topo {
   Timing timing;
   int64_t launches = 0;
   int device = 0;
+  // device staging of gox_batch_solve's host arrays (grow-only)
+  IoStage io;
   // mixed path: pivot-ratio threshold |u_kk| < piv_tol * max|L(:, k)| that
   // sends a scenario to FP64, and how many the last batch sent
   double piv_tol = 1e-6;
@@ -985,7 +991,11 @@ int gox_batch_solve(gox_topo* t, int32_t B, const double* p_spec, const double* 
       ~StreamGuard() { cudaStreamDestroy(s); }
     } sg{st};
     const size_t bn = (size_t)B * n, nv = (size_t)(v_stride ? B : 1) * n;
-    DevMem dp, dq, dvm, dva, dovm, dova, dit, dst, dmm, dh, dsl, dre, dim;
+    // device copies of the host arrays, kept by the topology between calls
+    IoStage& io = t->io;
+    DevMem &dp = io.p, &dq = io.q, &dvm = io.vm, &dva = io.va, &dovm = io.ovm, &dova = io.ova,
+           &dit = io.it, &dst = io.st, &dmm = io.mm, &dh = io.h, &dsl = io.sl, &dre = io.dre,
+           &dim = io.dim;
     dp.ensure(bn * 8); dq.ensure(bn * 8); dvm.ensure(nv * 8); dva.ensure(nv * 8);
     dovm.ensure(bn * 8); dova.ensure(bn * 8); dit.ensure((size_t)B * 4); dst.ensure((size_t)B * 4);
     dmm.ensure((size_t)B * 8);

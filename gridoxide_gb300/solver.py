@@ -176,11 +176,14 @@ class Topology:
         check(_lib.load().gox_topo_reset(self._h), "gox_topo_reset")
 
     def solve(self, p_spec, q_spec, vm0, va0, tol=1e-8, max_iter=20,
-              precision=GOX_PRECISION_MIXED, outage=None, history=False) -> BatchResult:
+              precision=GOX_PRECISION_MIXED, outage=None, history=False,
+              out: Optional[BatchResult] = None) -> BatchResult:
         """Batched NR on host arrays (inputs/outputs copied to/from the GPU).
 
         p_spec/q_spec [B, N]; vm0/va0 [N] (shared) or [B, N];
-        outage = (slots [B,4], dre [B,4], dim [B,4]) or None."""
+        outage = (slots [B,4], dre [B,4], dim [B,4]) or None.
+        out: a BatchResult of the right shapes to write into (e.g. over
+        pinned memory, reused across calls) instead of fresh arrays."""
         L = _lib.load()
         p_spec = _f64(np.atleast_2d(p_spec))
         q_spec = _f64(np.atleast_2d(q_spec))
@@ -190,12 +193,25 @@ class Topology:
         vm0 = _f64(vm0)
         va0 = _f64(va0)
         stride = n if vm0.ndim == 2 else 0
-        vm = np.zeros((B, n))
-        va = np.zeros((B, n))
-        iters = np.zeros(B, np.int32)
-        status = np.zeros(B, np.int32)
-        mis = np.zeros(B)
-        hist = np.zeros((B, max_iter)) if history else None
+        if out is not None:
+            vm, va, iters, status, mis = (out.voltage_mag, out.voltage_ang, out.iterations,
+                                          out.status, out.max_mismatch)
+            hist = out.history if history else None
+            ok = (vm.shape == (B, n) and va.shape == (B, n) and iters.shape == (B,) and
+                  status.shape == (B,) and mis.shape == (B,) and vm.dtype == np.float64 and
+                  va.dtype == np.float64 and iters.dtype == np.int32 and status.dtype == np.int32 and
+                  mis.dtype == np.float64 and all(a.flags.c_contiguous for a in (vm, va, iters, status, mis)) and
+                  (not history or (hist is not None and hist.shape == (B, max_iter) and
+                                   hist.dtype == np.float64 and hist.flags.c_contiguous)))
+            if not ok:
+                raise ValueError("out arrays do not match the batch")
+        else:
+            vm = np.empty((B, n))
+            va = np.empty((B, n))
+            iters = np.zeros(B, np.int32)
+            status = np.zeros(B, np.int32)
+            mis = np.zeros(B)
+            hist = np.zeros((B, max_iter)) if history else None
         if outage is not None:
             sl, dr, di = _i32(outage[0]), _f64(outage[1]), _f64(outage[2])
         else:
