@@ -195,7 +195,7 @@ struct DevSchedule {
   DevMem yp, yi, yre, yim, bus_rowP, bus_rowQ, bus_colA, bus_colV, a_kind, a_bi, a_bk, a_yslot,
       a_dst, lev_ptr, lev_cols, c_base, c_ulen, c_llen, c_abeg, c_aend, op_ptr, op_slot, op_pos, ph_ptr,
       ph_rows, ph_kind, fw_ptr, fw_slot, fw_col, bw_ptr, bw_slot, bw_col, diag_slot, bt_ptr, bt_cnt,
-      pk_off, pk, slot_a, off_a;
+      pk_off, pk, slot_a, off_a, fill_rec, fill_y;
   SchedDev d{};
   int max_collen = 0, max_ops = 0, max_pk = 0, max_head = 0, max_fw = 0;
   // refactor command streams, FP32 and FP64 plans
@@ -241,6 +241,31 @@ struct DevSchedule {
     upload(bt_ptr, sc.bt_ptr); upload(bt_cnt, sc.bt_cnt);
     upload(pk_off, sc.pk_off); upload(pk, sc.pk);
     upload(slot_a, sc.slot_a); upload(off_a, sc.off_a);
+    {
+      // fill recipe: per LU slot, then per off-diagonal entry
+      const int nx = sc.n_slots + sc.n_off;
+      std::vector<int32_t> rec((size_t)nx * 4, 0);
+      std::vector<double> yv((size_t)nx * 2, 0.0);
+      for (int x = 0; x < nx; x++) {
+        const int a = x < sc.n_slots ? sc.slot_a[x] : sc.off_a[x - sc.n_slots];
+        int32_t* r = &rec[(size_t)x * 4];
+        if (a < 0) {
+          r[0] = -1; r[1] = 0; r[2] = 0; r[3] = -2;  // matches no outage slot (-1 = none)
+          continue;
+        }
+        const int kind = sc.a_kind[a];
+        const bool diag = kind == 0 || kind == 1 || kind == 4 || kind == 5;
+        r[0] = kind; r[1] = sc.a_bi[a]; r[2] = diag ? sc.a_bi[a] : sc.a_bk[a]; r[3] = sc.a_yslot[a];
+        if (!yre_h.empty()) {
+          yv[(size_t)x * 2] = yre_h[sc.a_yslot[a]];
+          yv[(size_t)x * 2 + 1] = yim_h[sc.a_yslot[a]];
+        }
+      }
+      upload(fill_rec, rec);
+      upload(fill_y, yv);
+      d.fill_rec = reinterpret_cast<const int4*>(fill_rec.p);
+      d.fill_y = reinterpret_cast<const double2*>(fill_y.p);
+    }
     d.slot_a = slot_a.as<int32_t>(); d.off_a = off_a.as<int32_t>();
     d.n_off_real = sc.n_off;
     d.bt_ptr = bt_ptr.as<int32_t>(); d.bt_cnt = bt_cnt.as<uint8_t>();

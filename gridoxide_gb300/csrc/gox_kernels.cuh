@@ -40,6 +40,10 @@ struct SchedDev {
   const uint8_t* bt_cnt;
   const int32_t *pk_off, *pk;
   const int32_t *slot_a, *off_a;
+  // fill recipe per LU slot, then per off-diagonal entry: {kind (-1: zero
+  // fill-in), bus i, bus k (= i on the diagonal), Y slot} and Y's value
+  const int4* fill_rec;
+  const double2* fill_y;
   const int32_t *ph_ptr, *ph_rows, *ph_kind, *fw_ptr, *fw_slot, *fw_col, *bw_ptr, *bw_slot,
       *bw_col, *diag_slot;
 };
@@ -231,6 +235,46 @@ __global__ void k_decide(BatchDev D, int it, int mode) {
 // copy.  Index space: the LU slots, then the off-diagonal (BTF) entries.
 // grid (chunks, G); each warp fills a contiguous run of slots.
 template <typename T, bool OUTAGE>
+__device__ __forceinline__ T fill_value(const SchedDev& S, const BatchDev& D, int x, int g,
+                                        int lane, int s, int os0, int os1, int os2, int os3) {
+  const int N = S.n_bus;
+  const int4 r = __ldg(S.fill_rec + x);
+  const double2 y = __ldg(S.fill_y + x);
+  double gd = y.x, bd = y.y;
+  if (OUTAGE) {
+    const int c = (r.w == os0) ? 0 : (r.w == os1) ? 1 : (r.w == os2) ? 2 : (r.w == os3) ? 3 : -1;
+    if (c >= 0) { gd += D.o_dre[4 * s + c]; bd += D.o_dim[4 * s + c]; }
+  }
+  const T G = (T)gd, B = (T)bd;
+  const T* eT = (const T*)D.eT; const T* fT = (const T*)D.fT; const T* ivT = (const T*)D.ivT;
+  const T* pT = (const T*)D.pT; const T* qT = (const T*)D.qT;
+  const int kind = r.x;
+  if (kind < 0) return (T)0;  // fill-in: starts at zero
+  const size_t xi = gidx(g, N, r.y, lane);
+  if (kind == 0 || kind == 1 || kind == 4 || kind == 5) {
+    const T ei = eT[xi], fi = fT[xi], iv = ivT[xi], P = pT[xi], Q = qT[xi];
+    const T vi2 = ei * ei + fi * fi;
+    const T vi = vi2 * iv;  // |V_i|^2 / |V_i|
+    switch (kind) {
+      case 0: return -Q - vi2 * B;      // H_ii
+      case 1: return P * iv + vi * G;   // N_ii
+      case 4: return P - vi2 * G;       // M_ii
+      default: return Q * iv - vi * B;  // L_ii
+    }
+  }
+  const size_t xk = gidx(g, N, r.z, lane);
+  const T ei = eT[xi], fi = fT[xi], ek = eT[xk], fk = fT[xk];
+  const T c = ei * ek + fi * fk;   // V_i V_k cos
+  const T sn = fi * ek - ei * fk;  // V_i V_k sin
+  switch (kind) {
+    case 2: return G * sn - B * c;                 // H_ik
+    case 3: return (G * c + B * sn) * ivT[xk];     // N_ik
+    case 6: return -(G * c + B * sn);              // M_ik
+    default: return (G * sn - B * c) * ivT[xk];    // L_ik
+  }
+}
+
+template <typename T, bool OUTAGE>
 __global__ void __launch_bounds__(256) k_fill(SchedDev S, BatchDev D, int per_warp) {
   const int g = blockIdx.y;
   if (!D.gact[g]) return;
@@ -240,55 +284,29 @@ __global__ void __launch_bounds__(256) k_fill(SchedDev S, BatchDev D, int per_wa
   const int a0 = wglob * per_warp;
   if (a0 >= total) return;
   const int a1 = min(total, a0 + per_warp);
-  const int N = S.n_bus;
   const int s = g * 32 + lane;
-  const T* eT = (const T*)D.eT; const T* fT = (const T*)D.fT; const T* ivT = (const T*)D.ivT;
-  const T* pT = (const T*)D.pT; const T* qT = (const T*)D.qT;
   T* LU = (T*)D.lu;
   T* OFF = (T*)D.off;
   int os0 = -1, os1 = -1, os2 = -1, os3 = -1;
   if (OUTAGE && D.o_bf[s] >= 0) {
     os0 = D.o_slot[4 * s]; os1 = D.o_slot[4 * s + 1]; os2 = D.o_slot[4 * s + 2]; os3 = D.o_slot[4 * s + 3];
   }
-  for (int x = a0; x < a1; x++) {
-    const int a = (x < S.n_slots) ? __ldg(S.slot_a + x) : __ldg(S.off_a + (x - S.n_slots));
-    T v = (T)0;
-    if (a >= 0) {
-      const int kind = __ldg(S.a_kind + a), i = __ldg(S.a_bi + a), k = __ldg(S.a_bk + a);
-      const int ys = __ldg(S.a_yslot + a);
-      double gd = __ldg(S.yre + ys), bd = __ldg(S.yim + ys);
-      if (OUTAGE) {
-        const int c = (ys == os0) ? 0 : (ys == os1) ? 1 : (ys == os2) ? 2 : (ys == os3) ? 3 : -1;
-        if (c >= 0) { gd += D.o_dre[4 * s + c]; bd += D.o_dim[4 * s + c]; }
-      }
-      const T G = (T)gd, B = (T)bd;
-      const size_t xi = gidx(g, N, i, lane);
-      if (kind == 0 || kind == 1 || kind == 4 || kind == 5) {
-        const T ei = eT[xi], fi = fT[xi], iv = ivT[xi];
-        const T vi2 = ei * ei + fi * fi;
-        const T vi = vi2 * iv;  // |V_i|^2 / |V_i|
-        const T P = pT[xi], Q = qT[xi];
-        switch (kind) {
-          case 0: v = -Q - vi2 * B; break;            // H_ii
-          case 1: v = P * iv + vi * G; break;         // N_ii
-          case 4: v = P - vi2 * G; break;             // M_ii
-          default: v = Q * iv - vi * B; break;        // L_ii
-        }
-      } else {
-        const size_t xk = gidx(g, N, k, lane);
-        const T ei = eT[xi], fi = fT[xi], ek = eT[xk], fk = fT[xk];
-        const T c = ei * ek + fi * fk;   // V_i V_k cos
-        const T sn = fi * ek - ei * fk;  // V_i V_k sin
-        switch (kind) {
-          case 2: v = G * sn - B * c; break;                 // H_ik
-          case 3: v = (G * c + B * sn) * ivT[xk]; break;     // N_ik
-          case 6: v = -(G * c + B * sn); break;              // M_ik
-          default: v = (G * sn - B * c) * ivT[xk]; break;    // L_ik
-        }
+  constexpr int U = 4;  // slots in flight per warp
+  for (int x0 = a0; x0 < a1; x0 += U) {
+    T v[U];
+#pragma unroll
+    for (int u = 0; u < U; u++) {
+      const int x = min(x0 + u, a1 - 1);
+      v[u] = fill_value<T, OUTAGE>(S, D, x, g, lane, s, os0, os1, os2, os3);
+    }
+#pragma unroll
+    for (int u = 0; u < U; u++) {
+      const int x = x0 + u;
+      if (x < a1) {
+        if (x < S.n_slots) LU[gidx(g, S.n_slots, x, lane)] = v[u];
+        else OFF[gidx(g, S.n_off, x - S.n_slots, lane)] = v[u];
       }
     }
-    if (x < S.n_slots) LU[gidx(g, S.n_slots, x, lane)] = v;
-    else OFF[gidx(g, S.n_off, x - S.n_slots, lane)] = v;
   }
 }
 
