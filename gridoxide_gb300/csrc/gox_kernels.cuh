@@ -681,9 +681,9 @@ __global__ void __launch_bounds__(256, 1) k_refactor(StreamDev P, SchedDev S, Ba
       R::steps(reinterpret_cast<const uint4*>(cb + sw), nst, st_lane, ring_lane);
       const int ulen = ul & 0xffff, llen = (ul >> 16) & 0xffff;
       if (fuse)
-        R::fwd(cb + sw + 4 * nst, nfw, cb[pc + 7], true, st_lane + (uint32_t)(ulen + 1 + llen) * RB,
-               ring_lane);
-      R::finish(k, base, ulen, llen, st_lane, LUg, Xg, lane, fuse, ptol, bad, tiny);
+        R::fwd(cb + sw + 4 * nst, nfw, cb[pc + 7], !((w0 >> 9) & 1),
+               st_lane + (uint32_t)(ulen + 1 + llen) * RB, ring_lane);
+      if (!((w0 >> 10) & 1)) R::finish(k, base, ulen, llen, st_lane, LUg, Xg, lane, fuse, ptol, bad, tiny);
       pc = sw + 4 * nst + nfw;
       if ((w0 >> 8) & 1) {
         __syncthreads();

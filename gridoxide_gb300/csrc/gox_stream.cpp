@@ -52,6 +52,12 @@ struct ColInfo {
   int group = -1;   // commit group of the stage copy
   bool staged = false, committed = false;
   double cost = 0;
+  // a column of a narrow level runs in two parts: PRE, one level early (its
+  // stage, the prefix of its updates and forward terms whose sources finished
+  // two levels before), and the rest; prefixes keep the operation order
+  int nlr = 0;                   // L-run items (they come first in items)
+  int pre_runs = 0, pre_fw = 0;  // prefix lengths (items, forward pairs)
+  bool split = false, pre_done = false;
   std::vector<Item> items;  // consumption order: L-run pieces (U order), fw pairs
 };
 
@@ -97,6 +103,7 @@ struct Builder {
   std::string err;
 
   bool with_bwd = false;  // the backward substitution runs in the stream too
+  bool with_pre = true;   // narrow levels' columns run their prefix one level early
 
   Builder(const Schedule& s, const StreamPlan& p) : sc(s), P(p) {
     W = p.nw;
@@ -322,18 +329,37 @@ struct Builder {
   // The whole of column c as one COLUMN command, when every value is placed
   // and the command fits in a stream chunk.  g: the last commit group the
   // column's values arrive in.
+  // Which part of a column a command runs: L-run items [r0, r1), forward
+  // pairs from item f0 to f1, whether the forward sum starts from b, and
+  // whether the command finishes the column.
+  struct Part {
+    size_t r0, r1, f0, f1;
+    bool first, finish;
+  };
+  Part whole(const ColInfo& c) const {
+    return {0, (size_t)c.nlr, (size_t)c.nlr, c.items.size(), true, true};
+  }
+  Part pre_part(const ColInfo& c) const {
+    return {0, (size_t)c.pre_runs, (size_t)c.nlr, (size_t)c.nlr + 2 * (size_t)c.pre_fw, true, false};
+  }
+  Part main_part(const ColInfo& c) const {
+    if (!c.pre_done) return whole(c);
+    return {(size_t)c.pre_runs, (size_t)c.nlr, (size_t)c.nlr + 2 * (size_t)c.pre_fw, c.items.size(),
+            false, true};
+  }
+
   bool column_cmd(int w, ColInfo& c, int L, std::vector<std::pair<int, int>>& late,
-                  std::vector<std::pair<int, int>>& pref, int g, bool on_path) {
+                  std::vector<std::pair<int, int>>& pref, int g, bool on_path, const Part& pt) {
     pad_rows(late);
     pad_rows(pref);
     std::vector<Step> steps;
-    size_t q = 0;
-    for (; q < c.items.size() && c.items[q].kind == IT_LRUN; q++) add_steps(c, c.items[q], steps);
+    const size_t q = pt.r1;
+    for (size_t r = pt.r0; r < pt.r1; r++) add_steps(c, c.items[r], steps);
     if (steps.size() % 2) steps.push_back(dummy_step(c));
     std::vector<int32_t> fw;
     size_t nf_real = 0;
     if (sc.fuse_fwd) {
-      for (size_t f = q; f < c.items.size(); f += 2)
+      for (size_t f = pt.f0; f < pt.f1; f += 2)
         fw.push_back(c.items[f].row | (c.items[f + 1].row << 16));
       nf_real = fw.size();
       while (fw.size() % 8) fw.push_back(zero_row() | (zero_row() << 16));
@@ -346,12 +372,12 @@ struct Builder {
     Emit& e = em[w];
     if (!fits(0, (size_t)e.cw) || nl > 0xffff || np > 0xffff || ns > 0xffff) {
       // the general form counts the steps again
-      for (size_t f = 0; f < q; f++)
+      for (size_t f = pt.r0; f < q; f++)
         out->n_steps -= (c.items[f].nrows + kStepOps - 1) / kStepOps;
       return false;
     }
     if (!fits(e.w.size(), e.cstart + e.cw)) e.next_chunk();
-    int32_t w0 = CMD_COLUMN;
+    int32_t w0 = CMD_COLUMN | (pt.first ? 0 : (1 << 9)) | (pt.finish ? 0 : (1 << 10));
     if (g >= 0 && waited[w] < g) {
       const int m = std::min(ngroups[w] - 1 - g, 7);
       w0 |= (m << 4) | (1 << 7);
@@ -381,11 +407,70 @@ struct Builder {
     out->n_column_cmds++;
     pos[w]++;
     const int64_t tf = now(w, L);
-    for (const Item& it : c.items)
-      if (it.state == ST_GATHERED) release_abs(it.row, it.nrows, tf);
-    release_abs(stage_abs, c.brows, tf);
-    wcost[w] += step_cost() * ns + 80 + (4.0 + fma_cost()) * c.len + fma_cost() * nf_real;
+    for (size_t r = pt.r0; r < pt.r1; r++)
+      if (c.items[r].state == ST_GATHERED) release_abs(c.items[r].row, c.items[r].nrows, tf);
+    for (size_t f = pt.f0; f < pt.f1; f++)
+      if (c.items[f].state == ST_GATHERED) release_abs(c.items[f].row, c.items[f].nrows, tf);
+    if (pt.finish) release_abs(stage_abs, c.brows, tf);
+    wcost[w] += step_cost() * ns + 80 + (pt.finish ? (4.0 + fma_cost()) * c.len : 0.0) +
+                fma_cost() * nf_real;
     return true;
+  }
+
+  // PRE of a split column (level L + 1) on its warp w during level L: its
+  // stage, the copies of its prefix values, the prefix steps and forward
+  // terms, as one COLUMN command without finish.  When something does not
+  // fit, the copies placed so far stay for the column and it runs whole.
+  void run_pre(int w, int ci, int L) {
+    ColInfo& c = C[ci];
+    const int64_t t = now(w, L);
+    bool waited_late = false;
+    const Part pt = pre_part(c);
+    if (!c.staged) {
+      if (!stage_col(w, ci, t)) {
+        c.split = false;
+        for (size_t r = pt.r0; r < pt.r1; r++)
+          if (c.items[r].state == ST_RESIDENT) { c.items[r].state = ST_NONE; c.items[r].row = -1; }
+        for (size_t f = pt.f0; f < pt.f1; f++)
+          if (c.items[f].state == ST_RESIDENT) { c.items[f].state = ST_NONE; c.items[f].row = -1; }
+        return;
+      }
+      waited_late = true;
+    }
+    bool ok = true;
+    auto place = [&](Item& it) {
+      if (it.state == ST_NONE) {
+        if (gather_item(w, it, t)) { out->rows_late += it.nrows; waited_late = true; }
+        else ok = false;
+      }
+    };
+    for (size_t r = pt.r0; r < pt.r1 && ok; r++) place(c.items[r]);
+    for (size_t f = pt.f0; f < pt.f1 && ok; f++) place(c.items[f]);
+    std::vector<std::pair<int, int>> late_rows, none;
+    late_rows.swap(pend_rows[w]);
+    new_group(w);
+    int g = c.group;
+    for (size_t r = pt.r0; r < pt.r1; r++)
+      if (c.items[r].state == ST_GATHERED) g = std::max(g, c.items[r].group);
+    for (size_t f = pt.f0; f < pt.f1; f++)
+      if (c.items[f].state == ST_GATHERED) g = std::max(g, c.items[f].group);
+    if (ok && column_cmd(w, c, L, late_rows, none, g, waited_late, pt)) {
+      c.pre_done = true;
+      out->n_pre++;
+      return;
+    }
+    c.split = false;  // the whole column runs at its own level
+    // values read in place were pinned for this level only: decide them
+    // again at the column's level
+    for (size_t r = pt.r0; r < pt.r1; r++)
+      if (c.items[r].state == ST_RESIDENT) { c.items[r].state = ST_NONE; c.items[r].row = -1; }
+    for (size_t f = pt.f0; f < pt.f1; f++)
+      if (c.items[f].state == ST_RESIDENT) { c.items[f].state = ST_NONE; c.items[f].row = -1; }
+    if (!late_rows.empty()) {
+      pend_rows[w].swap(late_rows);
+      flush_gather(w);
+      em[w].w[em[w].last_gather] |= (1 << 23);
+    }
   }
 
   // Issues the blocks of the warp's next tasks and every value of theirs
@@ -543,7 +628,8 @@ struct Builder {
     int g = c.group;
     for (const Item& it : c.items)
       if (it.state == ST_GATHERED) g = std::max(g, it.group);
-    if (placed && column_cmd(w, c, L, late_rows, pref_rows, g, waited_late)) return true;
+    const Part mp = main_part(c);
+    if (placed && column_cmd(w, c, L, late_rows, pref_rows, g, waited_late, mp)) return true;
     // the general form: single commands, values fetched in pieces as room allows
     for (auto* rows : {&late_rows, &pref_rows}) {
       if (rows->empty()) continue;
@@ -581,8 +667,8 @@ struct Builder {
       wait_for(w, gg, L, true);
       return true;
     };
-    size_t q = 0;
-    for (; q < c.items.size() && c.items[q].kind == IT_LRUN; q++) {
+    size_t q = mp.r0;
+    for (; q < mp.r1; q++) {
       Item& it = c.items[q];
       if (it.state == ST_NONE && !jit(q)) {
         err = "no ring room for an update run of column " + std::to_string(c.k);
@@ -597,9 +683,10 @@ struct Builder {
     // forward substitution y_k = b_k - sum L(k, j) y_j, in order, in pieces
     // whose values fit in the ring
     Emit& e = em[w];
+    q = mp.f0;
     if (sc.fuse_fwd) {
       size_t f = q;
-      bool first = true;
+      bool first = mp.first;
       do {
         if (f < c.items.size()) {
           const size_t h = c.items[f].state == ST_NONE ? f : f + 1;
@@ -697,6 +784,7 @@ struct Builder {
           c.nsteps += (it.nrows + kStepOps - 1) / kStepOps;
         }
       }
+      c.nlr = (int)c.items.size();
       if (sc.fuse_fwd) {
         for (int tt = sc.fw_ptr[k]; tt < sc.fw_ptr[k + 1]; tt++) {
           const int slot = sc.fw_slot[tt], j = sc.fw_col[tt];
@@ -796,6 +884,24 @@ struct Builder {
           seq[w].push_back(k);
         }
     }
+    // ---- columns of narrow levels run their prefix one level early
+    for (int L = 2; L < sc.n_levels; L++) {
+      const int width = sc.lev_ptr[L + 1] - sc.lev_ptr[L];
+      if (width > std::max(1, W / 4)) continue;
+      for (int q = sc.lev_ptr[L]; q < sc.lev_ptr[L + 1]; q++) {
+        ColInfo& c = C[sc.lev_cols[q]];
+        int r = 0;
+        while (r < c.nlr && C[c.items[r].j].level <= L - 2) r++;
+        int f = 0;
+        while (c.nlr + 2 * f < (int)c.items.size() &&
+               C[c.items[c.nlr + 2 * f].j].level <= L - 2 &&
+               C[c.items[c.nlr + 2 * f + 1].j].level <= L - 2)
+          f++;
+        c.pre_runs = r;
+        c.pre_fw = f;
+        c.split = with_pre && (r > 0 || f > 0);
+      }
+    }
     // ---- simulate the warps level by level and emit
     busy.assign((size_t)W * R, -1);
     tag.assign((size_t)W * R, -1);
@@ -827,12 +933,24 @@ struct Builder {
         for (Item& it : c.items)
           if (it.state == ST_NONE) try_resident(it, L);
       }
+      if (L + 1 < sc.n_levels)
+        for (int id : level_tasks(L + 1)) {
+          ColInfo& c = C[id];
+          if (!c.split) continue;
+          const Part pt = pre_part(c);
+          for (size_t r = pt.r0; r < pt.r1; r++)
+            if (c.items[r].state == ST_NONE) try_resident(c.items[r], L);
+          for (size_t f = pt.f0; f < pt.f1; f++)
+            if (c.items[f].state == ST_NONE) try_resident(c.items[f], L);
+        }
       std::fill(wcost.begin(), wcost.end(), 0.0);
       for (int w = 0; w < W; w++) {
         while (wnext[w] < (int)seq[w].size() && C[seq[w][wnext[w]]].level == L) {
           if (!run_col(w, seq[w][wnext[w]], L)) return false;
           wnext[w]++;
         }
+        for (int q = wnext[w]; q < (int)seq[w].size() && C[seq[w][q]].level == L + 1; q++)
+          if (C[seq[w][q]].kind == TK_COL && C[seq[w][q]].split) run_pre(w, seq[w][q], L);
         Emit& e = em[w];
         if (last_colhdr[w] >= 0 && last_colend[w] == (int64_t)e.w.size()) {
           e.w[last_colhdr[w]] |= (1 << 8);  // the level's barrier rides on the last column
@@ -957,20 +1075,29 @@ std::string run_stream_host(const Schedule& sc, const Stream& st, std::vector<do
       if (s.done || s.bars > L) continue;  // finished, or already past this level's barrier
       std::string e;
       auto fail = [&](const std::string& m) {
-        return "warp " + std::to_string(w) + " word " + std::to_string(s.pc) + ": " + m;
+        return "warp " + std::to_string(w) + " word " + std::to_string(s.pc) + " (op " +
+               std::to_string(st.words[s.pc] & 15) + "): " + m;
       };
       auto in_ring = [&](int r) { return r >= 0 && r < W * R; };
       auto note_w = [&](int r) -> bool {
         if (r == zero_row) { e = "writes the zero row"; return false; }
         if (stamp_w[r] == L && wr_by[r] != w) { e = "two warps write row " + std::to_string(r); return false; }
-        if (stamp_r[r] == L && rd_by[r] != w) { e = "row " + std::to_string(r) + " written while another warp reads it"; return false; }
+        if (stamp_r[r] == L && rd_by[r] != w) {
+          e = "row " + std::to_string(r) + " written while warp " + std::to_string(rd_by[r]) +
+              " reads it (level " + std::to_string(L) + ")";
+          return false;
+        }
         stamp_w[r] = L;
         wr_by[r] = w;
         return true;
       };
       auto note_r = [&](int r) -> bool {
         if (pend[r] >= 0) { e = "row " + std::to_string(r) + " read before its copy is waited for"; return false; }
-        if (stamp_w[r] == L && wr_by[r] != w) { e = "row " + std::to_string(r) + " read while another warp writes it"; return false; }
+        if (stamp_w[r] == L && wr_by[r] != w) {
+          e = "row " + std::to_string(r) + " read while warp " + std::to_string(wr_by[r]) +
+              " writes it (level " + std::to_string(L) + ")";
+          return false;
+        }
         if (stamp_r[r] == L && rd_by[r] != w) rd_by[r] = -2;
         else if (stamp_r[r] != L) { stamp_r[r] = L; rd_by[r] = w; }
         return true;
@@ -1197,9 +1324,9 @@ std::string run_stream_host(const Schedule& sc, const Stream& st, std::vector<do
           if (np && !gather(s.pc + 8 + nl, np, true)) return fail(e);
           if ((w0 >> 7) & 1) wait((w0 >> 4) & 7);
           if (!steps(sw, ns, S0)) return fail(e);
-          if (sc.fuse_fwd && !fwd(sw + 4 * ns, nf, true, S0, ulen + 1 + llen)) return fail(e);
+          if (sc.fuse_fwd && !fwd(sw + 4 * ns, nf, !((w0 >> 9) & 1), S0, ulen + 1 + llen)) return fail(e);
           if (!sc.fuse_fwd && nf) return fail("forward terms without fusion");
-          if (!finish(k, base, ulen, llen, S0)) return fail(e);
+          if (!((w0 >> 10) & 1) && !finish(k, base, ulen, llen, S0)) return fail(e);
           s.pc = sw + 4 * ns + nf;
           if ((w0 >> 8) & 1) { s.bars++; break; }
           continue;

@@ -81,7 +81,8 @@ constexpr int kMaxRefactorWarps = 8;
 //           y) - sum; m is a multiple of 8, padded with terms on the zero row
 //   FINISH  w0 = op, k, base, ulen | llen << 16, stage_row; the stage block
 //           is [column rows | y | b | dummy]
-//   COLUMN  w0 = op | wait_n << 4 | do_wait << 7 | bar_after << 8, k, base,
+//   COLUMN  w0 = op | wait_n << 4 | do_wait << 7 | bar_after << 8 | fwd_continues << 9 |
+//           no_finish << 10 (a column's prefix part, or the rest after it), k, base,
 //           ulen | llen << 16, stage_row | nlate << 16, npref | nsteps << 16,
 //           nfw, real nfw; then nlate gather words (this column, one commit group),
 //           npref gather words (the warp's next column, one group), from the
@@ -110,7 +111,7 @@ struct Stream {
   bool has_bwd = false;  // the stream also runs the backward substitution
   // statistics of the schedule
   int64_t rows_gathered = 0, rows_prefetched = 0, rows_resident = 0, rows_late = 0;
-  int64_t rows_jit = 0, n_steps = 0, n_waits = 0, n_groups = 0, n_column_cmds = 0;
+  int64_t rows_jit = 0, n_steps = 0, n_waits = 0, n_groups = 0, n_column_cmds = 0, n_pre = 0;
   double est_cycles = 0;  // rough critical-path estimate, used to choose a plan
 };
 

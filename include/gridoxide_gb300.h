@@ -211,7 +211,8 @@ int gox_factor_host(int32_t n, int32_t nnz, const int32_t *rows, const int32_t *
  * plan: [20] warps, [21] ring rows, [22] estimated cycles, [23] rows read
  * in place; [24] columns of the FP32 plan run as one command, [25] its
  * stream words; [26] / [27] 1 when the FP32 / FP64 refactor also runs the
- * backward substitution (no separate solve launch).  info must hold 28
+ * backward substitution (no separate solve launch); [28] columns of the FP32
+ * plan whose update prefix runs one level early.  info must hold 29
  * entries.  Returns GOX_E_INVALID before the first solve. */
 int gox_topo_info(const gox_topo *t, int64_t *info);
 
