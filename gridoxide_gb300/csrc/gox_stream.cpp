@@ -52,12 +52,15 @@ struct ColInfo {
   int group = -1;   // commit group of the stage copy
   bool staged = false, committed = false;
   double cost = 0;
-  // a column of a narrow level runs in two parts: PRE, one level early (its
-  // stage, the prefix of its updates and forward terms whose sources finished
-  // two levels before), and the rest; prefixes keep the operation order
+  // A column of a narrow level runs in slices: at each earlier level its
+  // warp runs the next updates and forward terms whose sources are finished
+  // (in order: a prefix), and the column's own level runs the rest and the
+  // finish.  run_early[i] / fw_early[f]: the first level at which run item i
+  // / forward pair f (and everything before it) may run.
   int nlr = 0;                   // L-run items (they come first in items)
-  int pre_runs = 0, pre_fw = 0;  // prefix lengths (items, forward pairs)
-  bool split = false, pre_done = false;
+  std::vector<int> run_early, fw_early;
+  int done_runs = 0, done_fw = 0;  // items / forward pairs already run
+  bool split = false, fwd_started = false;
   std::vector<Item> items;  // consumption order: L-run pieces (U order), fw pairs
 };
 
@@ -339,14 +342,29 @@ struct Builder {
   Part whole(const ColInfo& c) const {
     return {0, (size_t)c.nlr, (size_t)c.nlr, c.items.size(), true, true};
   }
-  Part pre_part(const ColInfo& c) const {
-    return {0, (size_t)c.pre_runs, (size_t)c.nlr, (size_t)c.nlr + 2 * (size_t)c.pre_fw, true, false};
+  // the slice of a split column that may run at level L: the next run
+  // items and forward pairs whose sources are finished, at most
+  // kSliceSteps steps and kSliceTerms terms (a slice runs beside another
+  // warp's column; spreading the prefix over the idle levels keeps each
+  // level short)
+  static constexpr int kSliceSteps = 4, kSliceTerms = 8;
+  Part slice_part(const ColInfo& c, int L) const {
+    int r1 = c.done_runs, f1 = c.done_fw, steps = 0;
+    while (r1 < c.nlr && c.run_early[r1] <= L) {
+      const int st = (c.items[r1].nrows + kStepOps - 1) / kStepOps;
+      if (steps > 0 && steps + st > kSliceSteps) break;
+      steps += st;
+      r1++;
+    }
+    while (f1 < (int)c.fw_early.size() && c.fw_early[f1] <= L && f1 - c.done_fw < kSliceTerms) f1++;
+    return {(size_t)c.done_runs, (size_t)r1, (size_t)c.nlr + 2 * (size_t)c.done_fw,
+            (size_t)c.nlr + 2 * (size_t)f1, !c.fwd_started, false};
   }
   Part main_part(const ColInfo& c) const {
-    if (!c.pre_done) return whole(c);
-    return {(size_t)c.pre_runs, (size_t)c.nlr, (size_t)c.nlr + 2 * (size_t)c.pre_fw, c.items.size(),
-            false, true};
+    return {(size_t)c.done_runs, (size_t)c.nlr, (size_t)c.nlr + 2 * (size_t)c.done_fw, c.items.size(),
+            !c.fwd_started, true};
   }
+  static bool part_empty(const Part& p) { return p.r0 == p.r1 && p.f0 == p.f1; }
 
   bool column_cmd(int w, ColInfo& c, int L, std::vector<std::pair<int, int>>& late,
                   std::vector<std::pair<int, int>>& pref, int g, bool on_path, const Part& pt) {
@@ -417,22 +435,28 @@ struct Builder {
     return true;
   }
 
-  // PRE of a split column (level L + 1) on its warp w during level L: its
-  // stage, the copies of its prefix values, the prefix steps and forward
-  // terms, as one COLUMN command without finish.  When something does not
-  // fit, the copies placed so far stay for the column and it runs whole.
-  void run_pre(int w, int ci, int L) {
+  // A slice of split column ci on its warp w during level L (before the
+  // column's own level): its stage (first slice), the copies of the slice's
+  // values, its steps and forward terms, as one COLUMN command without
+  // finish.  When something does not fit, the copies placed so far stay for
+  // the column, values read in place are decided again, and the rest of the
+  // column runs at its own level.
+  void run_slice(int w, int ci, int L) {
     ColInfo& c = C[ci];
+    const Part pt = slice_part(c, L);
+    if (part_empty(pt)) return;
+    auto undo_in_place = [&]() {
+      for (size_t r = pt.r0; r < pt.r1; r++)
+        if (c.items[r].state == ST_RESIDENT) { c.items[r].state = ST_NONE; c.items[r].row = -1; }
+      for (size_t f = pt.f0; f < pt.f1; f++)
+        if (c.items[f].state == ST_RESIDENT) { c.items[f].state = ST_NONE; c.items[f].row = -1; }
+    };
     const int64_t t = now(w, L);
     bool waited_late = false;
-    const Part pt = pre_part(c);
     if (!c.staged) {
       if (!stage_col(w, ci, t)) {
         c.split = false;
-        for (size_t r = pt.r0; r < pt.r1; r++)
-          if (c.items[r].state == ST_RESIDENT) { c.items[r].state = ST_NONE; c.items[r].row = -1; }
-        for (size_t f = pt.f0; f < pt.f1; f++)
-          if (c.items[f].state == ST_RESIDENT) { c.items[f].state = ST_NONE; c.items[f].row = -1; }
+        undo_in_place();
         return;
       }
       waited_late = true;
@@ -455,17 +479,14 @@ struct Builder {
     for (size_t f = pt.f0; f < pt.f1; f++)
       if (c.items[f].state == ST_GATHERED) g = std::max(g, c.items[f].group);
     if (ok && column_cmd(w, c, L, late_rows, none, g, waited_late, pt)) {
-      c.pre_done = true;
+      c.done_runs = (int)pt.r1;
+      c.done_fw = (int)(pt.f1 - (size_t)c.nlr) / 2;
+      c.fwd_started = true;
       out->n_pre++;
       return;
     }
-    c.split = false;  // the whole column runs at its own level
-    // values read in place were pinned for this level only: decide them
-    // again at the column's level
-    for (size_t r = pt.r0; r < pt.r1; r++)
-      if (c.items[r].state == ST_RESIDENT) { c.items[r].state = ST_NONE; c.items[r].row = -1; }
-    for (size_t f = pt.f0; f < pt.f1; f++)
-      if (c.items[f].state == ST_RESIDENT) { c.items[f].state = ST_NONE; c.items[f].row = -1; }
+    c.split = false;
+    undo_in_place();
     if (!late_rows.empty()) {
       pend_rows[w].swap(late_rows);
       flush_gather(w);
@@ -502,6 +523,16 @@ struct Builder {
     }
     pref_rows.swap(pend_rows[w]);
     new_group(w);
+  }
+
+  // The index in seq[w] of the warp's next task after its level-L tasks
+  // (from q0), when that is a split column of a later level; else -1.
+  int next_own(int w, int q0, int L) const {
+    int q = q0;
+    while (q < (int)seq[w].size() && C[seq[w][q]].level <= L) q++;
+    if (q >= (int)seq[w].size()) return -1;
+    const ColInfo& c = C[seq[w][q]];
+    return (c.kind == TK_COL && c.split && c.level > L) ? q : -1;
   }
 
   // x_k = (y_k - sum U(k, j) x_j) / U(k, k) as one BWD command.
@@ -884,22 +915,27 @@ struct Builder {
           seq[w].push_back(k);
         }
     }
-    // ---- columns of narrow levels run their prefix one level early
+    // ---- columns of narrow levels run in slices at earlier levels
     for (int L = 2; L < sc.n_levels; L++) {
       const int width = sc.lev_ptr[L + 1] - sc.lev_ptr[L];
       if (width > std::max(1, W / 4)) continue;
       for (int q = sc.lev_ptr[L]; q < sc.lev_ptr[L + 1]; q++) {
         ColInfo& c = C[sc.lev_cols[q]];
-        int r = 0;
-        while (r < c.nlr && C[c.items[r].j].level <= L - 2) r++;
-        int f = 0;
-        while (c.nlr + 2 * f < (int)c.items.size() &&
-               C[c.items[c.nlr + 2 * f].j].level <= L - 2 &&
-               C[c.items[c.nlr + 2 * f + 1].j].level <= L - 2)
-          f++;
-        c.pre_runs = r;
-        c.pre_fw = f;
-        c.split = with_pre && (r > 0 || f > 0);
+        c.run_early.assign(c.nlr, 0);
+        int e = 0;
+        for (int r = 0; r < c.nlr; r++) {
+          e = std::max(e, C[c.items[r].j].level + 1);
+          c.run_early[r] = e;
+        }
+        const int nfw = ((int)c.items.size() - c.nlr) / 2;
+        c.fw_early.assign(nfw, 0);
+        e = 0;
+        for (int f = 0; f < nfw; f++) {
+          e = std::max(e, std::max(C[c.items[c.nlr + 2 * f].j].level,
+                                   C[c.items[c.nlr + 2 * f + 1].j].level) + 1);
+          c.fw_early[f] = e;
+        }
+        c.split = with_pre && ((c.nlr > 0 && c.run_early[0] < L) || (nfw > 0 && c.fw_early[0] < L));
       }
     }
     // ---- simulate the warps level by level and emit
@@ -933,24 +969,29 @@ struct Builder {
         for (Item& it : c.items)
           if (it.state == ST_NONE) try_resident(it, L);
       }
-      if (L + 1 < sc.n_levels)
-        for (int id : level_tasks(L + 1)) {
-          ColInfo& c = C[id];
-          if (!c.split) continue;
-          const Part pt = pre_part(c);
-          for (size_t r = pt.r0; r < pt.r1; r++)
-            if (c.items[r].state == ST_NONE) try_resident(c.items[r], L);
-          for (size_t f = pt.f0; f < pt.f1; f++)
-            if (c.items[f].state == ST_NONE) try_resident(c.items[f], L);
-        }
+      // ... and of the slices the idle warps will run for their next columns
+      for (int w = 0; w < W; w++) {
+        if (wnext[w] < (int)seq[w].size() && C[seq[w][wnext[w]]].level == L) continue;  // busy
+        const int nq = next_own(w, wnext[w], L);
+        if (nq < 0) continue;
+        ColInfo& c = C[seq[w][nq]];
+        const Part pt = slice_part(c, L);
+        for (size_t r = pt.r0; r < pt.r1; r++)
+          if (c.items[r].state == ST_NONE) try_resident(c.items[r], L);
+        for (size_t f = pt.f0; f < pt.f1; f++)
+          if (c.items[f].state == ST_NONE) try_resident(c.items[f], L);
+      }
       std::fill(wcost.begin(), wcost.end(), 0.0);
       for (int w = 0; w < W; w++) {
+        const bool idle = !(wnext[w] < (int)seq[w].size() && C[seq[w][wnext[w]]].level == L);
         while (wnext[w] < (int)seq[w].size() && C[seq[w][wnext[w]]].level == L) {
           if (!run_col(w, seq[w][wnext[w]], L)) return false;
           wnext[w]++;
         }
-        for (int q = wnext[w]; q < (int)seq[w].size() && C[seq[w][q]].level == L + 1; q++)
-          if (C[seq[w][q]].kind == TK_COL && C[seq[w][q]].split) run_pre(w, seq[w][q], L);
+        if (idle) {  // a warp with no column of its own here runs a slice of its next one
+          const int nq = next_own(w, wnext[w], L);
+          if (nq >= 0) run_slice(w, seq[w][nq], L);
+        }
         Emit& e = em[w];
         if (last_colhdr[w] >= 0 && last_colend[w] == (int64_t)e.w.size()) {
           e.w[last_colhdr[w]] |= (1 << 8);  // the level's barrier rides on the last column
