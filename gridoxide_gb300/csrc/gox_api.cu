@@ -295,7 +295,7 @@ struct DevSchedule {
 // Device buffers of one batch (capacity in groups of 32 scenarios).
 struct DevBatch {
   int G = 0, prec = -1, max_iter = 0;
-  DevMem vm, va, e, f, psp, qsp, eT, fT, ivT, pT, qT, jbuf, lu, off, rhs, sol;
+  DevMem vm, va, e, f, psp, qsp, cth, sth, eT, fT, ivT, pT, qT, jbuf, lu, off, rhs, sol;
   DevMem status, iters, sing, piv, maxmis, maxacc, hist, gact, nactive, err;
   DevMem o_slot, o_bf, o_bt, o_dre, o_dim;
   DevMem in_stage, out_stage;  // host I/O staging (row-major)
@@ -303,7 +303,7 @@ struct DevBatch {
   void ensure(const SchedDev& S, int G_, int prec_, int max_iter_, bool want_hist) {
     const size_t nb = (size_t)G_ * S.n_bus * 32, w = prec_ == GOX_PRECISION_FP64 ? 8 : 4;
     vm.ensure(nb * 8); va.ensure(nb * 8); e.ensure(nb * 8); f.ensure(nb * 8);
-    psp.ensure(nb * 8); qsp.ensure(nb * 8);
+    psp.ensure(nb * 8); qsp.ensure(nb * 8); cth.ensure(nb * 8); sth.ensure(nb * 8);
     eT.ensure(nb * w); fT.ensure(nb * w); ivT.ensure(nb * w); pT.ensure(nb * w); qT.ensure(nb * w);
     jbuf.ensure((size_t)G_ * S.n_a * 32 * w);
     lu.ensure((size_t)G_ * S.n_slots * 32 * w);
@@ -326,6 +326,7 @@ struct DevBatch {
     D.G = G; D.max_iter = max_iter; D.tol = tol;
     D.vm = vm.as<double>(); D.va = va.as<double>(); D.e = e.as<double>(); D.f = f.as<double>();
     D.psp = psp.as<double>(); D.qsp = qsp.as<double>();
+    D.cth = cth.as<double>(); D.sth = sth.as<double>();
     D.eT = eT.p; D.fT = fT.p; D.ivT = ivT.p; D.pT = pT.p; D.qT = qT.p;
     D.jbuf = jbuf.p; D.lu = lu.p; D.off = off.p; D.rhs = rhs.p; D.sol = sol.p;
     D.status = status.as<int32_t>(); D.iters = iters.as<int32_t>(); D.sing = sing.as<int32_t>();

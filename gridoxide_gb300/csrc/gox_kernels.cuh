@@ -52,8 +52,8 @@ struct BatchDev {
   int G;          // groups of 32 scenarios
   int max_iter;
   double tol;
-  // FP64 state [G][n_bus][32]
-  double *vm, *va, *e, *f, *psp, *qsp;
+  // FP64 state [G][n_bus][32]; cth, sth: cos / sin of va
+  double *vm, *va, *e, *f, *psp, *qsp, *cth, *sth;
   // typed working arrays (T = float or double)
   void *eT, *fT, *ivT, *pT, *qT;  // [G][n_bus][32]
   void *jbuf;                      // [G][n_a][32]
@@ -92,17 +92,38 @@ __global__ void __launch_bounds__(256) k_update(SchedDev S, BatchDev D, int it, 
   const bool upd = D.status[s] == ST_RUNNING && (it > 0 || mode == 1) && D.sing[s] == 0;
   const size_t x = gidx(g, N, i, lane);
   double vm = D.vm[x], va = D.va[x];
+  double dth = 0.0;
   if (upd) {
     const T* sol = (const T*)D.sol;
     const int ca = __ldg(S.bus_colA + i), cv = __ldg(S.bus_colV + i);
-    if (ca >= 0) va += (double)sol[gidx(g, S.n_u, ca, lane)];
+    if (ca >= 0) {
+      const double va1 = va + (double)sol[gidx(g, S.n_u, ca, lane)];
+      dth = va1 - va;
+      va = va1;
+    }
     if (cv >= 0) vm += (double)sol[gidx(g, S.n_u, cv, lane)];
     D.vm[x] = vm;
     D.va[x] = va;
   }
   if (mode != 0) return;
+  // cos / sin of the angle: at the first iteration and after a large step
+  // from sincos; after a small step (|d| < 1/32) by rotating the previous
+  // pair by d, with cos d and sin d from their Taylor series (the first
+  // omitted terms are below 1e-19 there; the rotation adds about one
+  // rounding per iteration)
   double sn, cs;
-  sincos(va, &sn, &cs);
+  if (it > 0 && fabs(dth) < 0.03125) {
+    const double d2 = dth * dth;
+    const double cd = 1.0 + d2 * (-1.0 / 2 + d2 * (1.0 / 24 + d2 * (-1.0 / 720 + d2 * (1.0 / 40320))));
+    const double sd = dth * (1.0 + d2 * (-1.0 / 6 + d2 * (1.0 / 120 + d2 * (-1.0 / 5040))));
+    const double c0 = D.cth[x], s0 = D.sth[x];
+    cs = c0 * cd - s0 * sd;
+    sn = s0 * cd + c0 * sd;
+  } else {
+    sincos(va, &sn, &cs);
+  }
+  D.cth[x] = cs;
+  D.sth[x] = sn;
   const double e = vm * cs, f = vm * sn;
   D.e[x] = e;
   D.f[x] = f;
@@ -145,11 +166,14 @@ __global__ void __launch_bounds__(256) k_inject(SchedDev S, BatchDev D, int it) 
           fk[t] = D.f[xk];
         }
       }
+      // I += Y V as four FMAs per entry (FP64 operations are the cost here)
 #pragma unroll
       for (int t = 0; t < 8; t++) {
         if (p + t < pe) {
-          ir += gr[t] * ek[t] - gi[t] * fk[t];
-          ii += gr[t] * fk[t] + gi[t] * ek[t];
+          ir = fma(gr[t], ek[t], ir);
+          ir = fma(-gi[t], fk[t], ir);
+          ii = fma(gr[t], fk[t], ii);
+          ii = fma(gi[t], ek[t], ii);
         }
       }
     }

@@ -347,7 +347,7 @@ struct Builder {
   // kSliceSteps steps and kSliceTerms terms (a slice runs beside another
   // warp's column; spreading the prefix over the idle levels keeps each
   // level short)
-  static constexpr int kSliceSteps = 4, kSliceTerms = 8;
+  static constexpr int kSliceSteps = 6, kSliceTerms = 8;
   Part slice_part(const ColInfo& c, int L) const {
     int r1 = c.done_runs, f1 = c.done_fw, steps = 0;
     while (r1 < c.nlr && c.run_early[r1] <= L) {
