@@ -195,7 +195,7 @@ struct DevSchedule {
   DevMem yp, yi, yre, yim, bus_rowP, bus_rowQ, bus_colA, bus_colV, a_kind, a_bi, a_bk, a_yslot,
       a_dst, lev_ptr, lev_cols, c_base, c_ulen, c_llen, c_abeg, c_aend, op_ptr, op_slot, op_pos, ph_ptr,
       ph_rows, ph_kind, fw_ptr, fw_slot, fw_col, bw_ptr, bw_slot, bw_col, diag_slot, bt_ptr, bt_cnt,
-      pk_off, pk, slot_a, off_a, fill_rec, fill_y;
+      pk_off, pk, slot_a, off_a, fill_rec, fill_y, fill_yf;
   SchedDev d{};
   int max_collen = 0, max_ops = 0, max_pk = 0, max_head = 0, max_fw = 0;
   // refactor command streams, FP32 and FP64 plans
@@ -246,6 +246,7 @@ struct DevSchedule {
       const int nx = sc.n_slots + sc.n_off;
       std::vector<int32_t> rec((size_t)nx * 4, 0);
       std::vector<double> yv((size_t)nx * 2, 0.0);
+      std::vector<float> yvf((size_t)nx * 2, 0.0f);  // the FP32 fill's copy (no conversions)
       for (int x = 0; x < nx; x++) {
         const int a = x < sc.n_slots ? sc.slot_a[x] : sc.off_a[x - sc.n_slots];
         int32_t* r = &rec[(size_t)x * 4];
@@ -259,12 +260,16 @@ struct DevSchedule {
         if (!yre_h.empty()) {
           yv[(size_t)x * 2] = yre_h[sc.a_yslot[a]];
           yv[(size_t)x * 2 + 1] = yim_h[sc.a_yslot[a]];
+          yvf[(size_t)x * 2] = (float)yv[(size_t)x * 2];
+          yvf[(size_t)x * 2 + 1] = (float)yv[(size_t)x * 2 + 1];
         }
       }
       upload(fill_rec, rec);
       upload(fill_y, yv);
+      upload(fill_yf, yvf);
       d.fill_rec = reinterpret_cast<const int4*>(fill_rec.p);
       d.fill_y = reinterpret_cast<const double2*>(fill_y.p);
+      d.fill_yf = reinterpret_cast<const float2*>(fill_yf.p);
     }
     d.slot_a = slot_a.as<int32_t>(); d.off_a = off_a.as<int32_t>();
     d.n_off_real = sc.n_off;

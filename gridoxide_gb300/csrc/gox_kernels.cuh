@@ -42,8 +42,10 @@ struct SchedDev {
   const int32_t *slot_a, *off_a;
   // fill recipe per LU slot, then per off-diagonal entry: {kind (-1: zero
   // fill-in), bus i, bus k (= i on the diagonal), Y slot} and Y's value
+  // (FP64, and rounded to FP32 for the FP32 fill)
   const int4* fill_rec;
   const double2* fill_y;
+  const float2* fill_yf;
   const int32_t *ph_ptr, *ph_rows, *ph_kind, *fw_ptr, *fw_slot, *fw_col, *bw_ptr, *bw_slot,
       *bw_col, *diag_slot;
 };
@@ -110,9 +112,19 @@ __global__ void __launch_bounds__(256) k_update(SchedDev S, BatchDev D, int it, 
   // from sincos; after a small step (|d| < 1/32) by rotating the previous
   // pair by d, with cos d and sin d from their Taylor series (the first
   // omitted terms are below 1e-19 there; the rotation adds about one
-  // rounding per iteration)
+  // rounding per iteration).  When every step of the warp is below 2^-10
+  // (the later iterations) two terms of each series suffice (the first
+  // omitted ones are below 2e-21).
   double sn, cs;
-  if (it > 0 && fabs(dth) < 0.03125) {
+  const bool small = it > 0 && fabs(dth) < 0.03125;
+  if (__all_sync(0xffffffffu, it > 0 && fabs(dth) < 0.0009765625)) {
+    const double d2 = dth * dth;
+    const double cd = 1.0 + d2 * (-1.0 / 2 + d2 * (1.0 / 24));
+    const double sd = dth * (1.0 + d2 * (-1.0 / 6 + d2 * (1.0 / 120)));
+    const double c0 = D.cth[x], s0 = D.sth[x];
+    cs = c0 * cd - s0 * sd;
+    sn = s0 * cd + c0 * sd;
+  } else if (small) {
     const double d2 = dth * dth;
     const double cd = 1.0 + d2 * (-1.0 / 2 + d2 * (1.0 / 24 + d2 * (-1.0 / 720 + d2 * (1.0 / 40320))));
     const double sd = dth * (1.0 + d2 * (-1.0 / 6 + d2 * (1.0 / 120 + d2 * (-1.0 / 5040))));
@@ -136,52 +148,81 @@ __global__ void __launch_bounds__(256) k_update(SchedDev S, BatchDev D, int it, 
 
 // ---------------------------------------------------------------------------
 // K1b: S = V conj(Y V), F, max|F|.  grid (ceil(N / (8*BPW)), G), 8 warps,
-// each warp BPW consecutive buses; neighbour loads issued 8 at a time.
+// each warp BPW consecutive buses.  FP64 instructions are the cost of this
+// kernel (the GPU runs them at 1/64 of the FP32 rate, and an instruction
+// whose predicate is false for every lane still takes its issue slot), so a
+// row of Y runs exactly its entries: a warp-uniform switch on the row's
+// length into a fully unrolled body that issues its L neighbour loads
+// before its 4 L FMAs.  max|F| is kept as the bit pattern of |F| (ordered
+// like the value for non-negative doubles) by integer max, NaN skipped as
+// fmax does.
+template <int L>
+__device__ __forceinline__ void y_row(const SchedDev& S, const double* __restrict__ e,
+                                      const double* __restrict__ f, int g, int N, int lane,
+                                      int p, double& ir, double& ii) {
+  double ek[L], fk[L], gr[L], gi[L];
+#pragma unroll
+  for (int t = 0; t < L; t++) {
+    const int k = __ldg(S.yi + p + t);
+    gr[t] = __ldg(S.yre + p + t);
+    gi[t] = __ldg(S.yim + p + t);
+    const size_t xk = gidx(g, N, k, lane);
+    ek[t] = e[xk];
+    fk[t] = f[xk];
+  }
+#pragma unroll
+  for (int t = 0; t < L; t++) {
+    ir = fma(gr[t], ek[t], ir);
+    ir = fma(-gi[t], fk[t], ir);
+    ii = fma(gr[t], fk[t], ii);
+    ii = fma(gi[t], ek[t], ii);
+  }
+}
+
+__device__ __forceinline__ unsigned long long abs_bits(double v) {
+  const unsigned long long b = (unsigned long long)__double_as_longlong(v) & 0x7fffffffffffffffull;
+  return b > 0x7ff0000000000000ull ? 0ull : b;  // NaN: skipped
+}
+
 template <typename T, bool OUTAGE, int BPW>
 __global__ void __launch_bounds__(256) k_inject(SchedDev S, BatchDev D, int it) {
   const int g = blockIdx.y;
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   const int s = g * 32 + lane;
   const int N = S.n_bus;
-  __shared__ double red[8][32];
+  __shared__ unsigned long long red[8][32];
   const bool active = D.status[s] == ST_RUNNING && !(it > 0 && D.sing[s] != 0);
   T* rhs = (T*)D.rhs;
+  const double* __restrict__ e = D.e;
+  const double* __restrict__ f = D.f;
   int obf = -1, obt = -1;
   if (OUTAGE) { obf = D.o_bf[s]; obt = D.o_bt[s]; }
-  double mx = 0.0;
+  unsigned long long mx = 0ull;
   const int i0 = (blockIdx.x * 8 + warp) * BPW;
   for (int i = i0; i < min(N, i0 + BPW); i++) {
     double ir = 0.0, ii = 0.0;
-    const int pb = __ldg(S.yp + i), pe = __ldg(S.yp + i + 1);
-    for (int p = pb; p < pe; p += 8) {
-      double ek[8], fk[8], gr[8], gi[8];
-#pragma unroll
-      for (int t = 0; t < 8; t++) {
-        if (p + t < pe) {
-          const int k = __ldg(S.yi + p + t);
-          gr[t] = __ldg(S.yre + p + t);
-          gi[t] = __ldg(S.yim + p + t);
-          const size_t xk = gidx(g, N, k, lane);
-          ek[t] = D.e[xk];
-          fk[t] = D.f[xk];
-        }
-      }
-      // I += Y V as four FMAs per entry (FP64 operations are the cost here)
-#pragma unroll
-      for (int t = 0; t < 8; t++) {
-        if (p + t < pe) {
-          ir = fma(gr[t], ek[t], ir);
-          ir = fma(-gi[t], fk[t], ir);
-          ii = fma(gr[t], fk[t], ii);
-          ii = fma(gi[t], ek[t], ii);
-        }
-      }
+    int p = __ldg(S.yp + i);
+    const int pe = __ldg(S.yp + i + 1);
+    while (pe - p > 8) {
+      y_row<8>(S, e, f, g, N, lane, p, ir, ii);
+      p += 8;
+    }
+    switch (pe - p) {
+      case 1: y_row<1>(S, e, f, g, N, lane, p, ir, ii); break;
+      case 2: y_row<2>(S, e, f, g, N, lane, p, ir, ii); break;
+      case 3: y_row<3>(S, e, f, g, N, lane, p, ir, ii); break;
+      case 4: y_row<4>(S, e, f, g, N, lane, p, ir, ii); break;
+      case 5: y_row<5>(S, e, f, g, N, lane, p, ir, ii); break;
+      case 6: y_row<6>(S, e, f, g, N, lane, p, ir, ii); break;
+      case 7: y_row<7>(S, e, f, g, N, lane, p, ir, ii); break;
+      case 8: y_row<8>(S, e, f, g, N, lane, p, ir, ii); break;
+      default: break;
     }
     const size_t x = gidx(g, N, i, lane);
-    const double ei = D.e[x], fi = D.f[x];
+    const double ei = e[x], fi = f[x];
     if (OUTAGE && (i == obf || i == obt)) {
       const size_t xf = gidx(g, N, obf, lane), xt = gidx(g, N, obt, lane);
-      const double ef = D.e[xf], ff = D.f[xf], et = D.e[xt], ft = D.f[xt];
+      const double ef = e[xf], ff = f[xf], et = e[xt], ft = f[xt];
       const int c0 = (i == obf) ? 0 : 2;
       const double ar = D.o_dre[4 * s + c0], ai = D.o_dim[4 * s + c0];
       const double br = D.o_dre[4 * s + c0 + 1], bi = D.o_dim[4 * s + c0 + 1];
@@ -194,12 +235,12 @@ __global__ void __launch_bounds__(256) k_inject(SchedDev S, BatchDev D, int it) 
     if (active) {
       if (rp >= 0) {
         const double F = D.psp[x] - pc;
-        mx = fmax(mx, fabs(F));
+        mx = max(mx, abs_bits(F));
         rhs[gidx(g, S.n_u, rp, lane)] = (T)F;
       }
       if (rq >= 0) {
         const double F = D.qsp[x] - qc;
-        mx = fmax(mx, fabs(F));
+        mx = max(mx, abs_bits(F));
         rhs[gidx(g, S.n_u, rq, lane)] = (T)F;
       }
     }
@@ -209,16 +250,13 @@ __global__ void __launch_bounds__(256) k_inject(SchedDev S, BatchDev D, int it) 
   red[warp][lane] = mx;
   __syncthreads();
   if (warp == 0) {
-    double m = 0.0;
+    unsigned long long m = 0ull;
 #pragma unroll
-    for (int w = 0; w < 8; w++) m = fmax(m, red[w][lane]);
-    if (active && m > 0.0) atomicMax(D.maxacc + s, (unsigned long long)__double_as_longlong(m));
+    for (int w = 0; w < 8; w++) m = max(m, red[w][lane]);
+    if (active && m > 0ull) atomicMax(D.maxacc + s, m);
   }
 }
 
-// ---------------------------------------------------------------------------
-// K1c: convergence decision (newton_raphson_cached's strict max|F| < tol,
-// src/solver.rs:699-703).  grid G, one warp.
 __global__ void k_decide(BatchDev D, int it, int mode) {
   const int g = blockIdx.x, lane = threadIdx.x;
   const int s = g * 32 + lane;
@@ -263,13 +301,30 @@ __device__ __forceinline__ T fill_value(const SchedDev& S, const BatchDev& D, in
                                         int lane, int s, int os0, int os1, int os2, int os3) {
   const int N = S.n_bus;
   const int4 r = __ldg(S.fill_rec + x);
-  const double2 y = __ldg(S.fill_y + x);
-  double gd = y.x, bd = y.y;
-  if (OUTAGE) {
-    const int c = (r.w == os0) ? 0 : (r.w == os1) ? 1 : (r.w == os2) ? 2 : (r.w == os3) ? 3 : -1;
-    if (c >= 0) { gd += D.o_dre[4 * s + c]; bd += D.o_dim[4 * s + c]; }
+  T G, B;
+  if constexpr (sizeof(T) == 4) {
+    // FP32 fill: Y rounded once on the host (a conversion per value here
+    // would run on the FP64 pipe, the bound of this kernel otherwise)
+    const float2 y = __ldg(S.fill_yf + x);
+    G = y.x;
+    B = y.y;
+  } else {
+    const double2 y = __ldg(S.fill_y + x);
+    G = y.x;
+    B = y.y;
   }
-  const T G = (T)gd, B = (T)bd;
+  if (OUTAGE) {
+    // the outaged branch's slots: Y + delta in FP64, then rounded (the
+    // warp takes this branch only when one of its lanes needs it)
+    const int c = (r.w == os0) ? 0 : (r.w == os1) ? 1 : (r.w == os2) ? 2 : (r.w == os3) ? 3 : -1;
+    if (__any_sync(0xffffffffu, c >= 0)) {
+      if (c >= 0) {
+        const double2 y = __ldg(S.fill_y + x);
+        G = (T)(y.x + D.o_dre[4 * s + c]);
+        B = (T)(y.y + D.o_dim[4 * s + c]);
+      }
+    }
+  }
   const T* eT = (const T*)D.eT; const T* fT = (const T*)D.fT; const T* ivT = (const T*)D.ivT;
   const T* pT = (const T*)D.pT; const T* qT = (const T*)D.qT;
   const int kind = r.x;
