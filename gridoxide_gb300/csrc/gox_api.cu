@@ -1165,6 +1165,7 @@ int gox_topo_info(const gox_topo* t, int64_t* info) {
   info[24] = a.n_column_cmds;
   info[25] = (int64_t)a.words.size();
   info[28] = a.n_pre;
+  info[29] = a.rows_helper;
   info[26] = a.has_bwd ? 1 : 0;
   info[27] = b.has_bwd ? 1 : 0;
   return GOX_OK;

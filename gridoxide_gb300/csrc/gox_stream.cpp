@@ -102,11 +102,28 @@ struct Builder {
   std::vector<int64_t> last_colhdr, last_colend;           // the warp's last COLUMN command
   std::vector<double> wcost;  // per warp, cycles in the current level (estimate)
   std::vector<int> pinned;    // per warp, rows pinned in the current level
+  // Copies for the busy warps' next tasks that the level's idle warps issue
+  // (one warp issues cp.async copies far slower than the SM takes them from
+  // several warps, so the copies of a narrow level's next column go to the
+  // warps that would wait at its barrier).  A bundle is one task's copies
+  // and the last level whose barrier they must complete before (its
+  // deadline): the level before the task's own, or this level when the
+  // task is a split column whose slices may start at the next one.  Each
+  // helper waits for its share before the deadline's barrier.
+  struct Bundle {
+    std::vector<std::pair<int, int>> rows;
+    int deadline;
+  };
+  std::vector<Bundle> bundles;
+  std::vector<int> idle_warps;
+  std::vector<std::vector<std::pair<int, int>>> hpend;  // per warp: helper groups (group, deadline)
+  static constexpr int kHelperMinRows = 32;  // same-level helper copies only for prefetches this large
   Stream* out;
   std::string err;
 
   bool with_bwd = false;  // the backward substitution runs in the stream too
   bool with_pre = true;   // narrow levels' columns run their prefix one level early
+  bool with_helpers = true;  // idle warps issue the copies of busy warps' next tasks
 
   Builder(const Schedule& s, const StreamPlan& p) : sc(s), P(p) {
     W = p.nw;
@@ -504,6 +521,20 @@ struct Builder {
   static constexpr int kAheadTasks = 1;
   void prefetch_next(int w, int ci, int L, int64_t t, std::vector<std::pair<int, int>>& pref_rows) {
     const int sp = seqpos[ci];
+    // by the idle warps when the next task runs at a later level: its rows
+    // must then be free during the whole level, since the copies run
+    // concurrently with this warp's tasks
+    bool helpers = false;
+    int deadline = L;
+    if (!idle_warps.empty() && sp + 1 < (int)seq[w].size() && C[seq[w][sp + 1]].level > L) {
+      const ColInfo& nc = C[seq[w][sp + 1]];
+      deadline = (nc.kind == TK_COL && nc.split) ? L : nc.level - 1;
+      int rows = nc.staged ? 0 : (nc.kind == TK_BWD ? 0 : nc.len + (sc.fuse_fwd ? 1 : 0));
+      for (const Item& it : nc.items)
+        if (it.state == ST_NONE && C[it.j].level < L) rows += it.nrows;
+      helpers = rows > 0 && (deadline > L || rows >= kHelperMinRows);
+    }
+    if (helpers) t = tmake(L, 0);
     double ahead = C[ci].cost;
     for (int d = 1; d <= kAheadTasks && sp + d < (int)seq[w].size(); d++) {
       const int ni = seq[w][sp + d];
@@ -520,9 +551,50 @@ struct Builder {
         if (!all) break;
       }
       ahead += nc.cost;
+      if (helpers) break;
+    }
+    if (helpers) {
+      // complete at the level's barrier: nothing for this warp to wait for
+      for (Item* it : uncommitted[w]) { it->group = -1; it->committed = true; }
+      for (int c2 : uncommitted_cols[w]) { C[c2].group = -1; C[c2].committed = true; }
+      uncommitted[w].clear();
+      uncommitted_cols[w].clear();
+      out->rows_helper += (int64_t)pend_rows[w].size();
+      if (!pend_rows[w].empty()) bundles.push_back({std::move(pend_rows[w]), deadline});
+      pend_rows[w].clear();
+      return;
     }
     pref_rows.swap(pend_rows[w]);
     new_group(w);
+  }
+
+  // The idle warp h issues its share of the level's helper copies (one
+  // commit group) before its own slice; helper_wait then waits for them
+  // before the level's barrier.
+  void helper_gather(int h, std::vector<std::pair<int, int>>& rows, int deadline) {
+    if (rows.empty()) return;
+    if (!pend_rows[h].empty()) throw std::logic_error("helper copies with copies pending");
+    const size_t nreal = rows.size();
+    pend_rows[h].swap(rows);
+    flush_gather(h);
+    em[h].w[em[h].last_gather] |= (1 << 23);
+    const int g = ngroups[h]++;
+    out->n_groups++;
+    wcost[h] += 70.0 * (double)((nreal + rpi() - 1) / rpi());
+    hpend[h].push_back({g, deadline});
+  }
+  // Before warp h's barrier of level L: waits for its helper groups due.
+  void helper_wait(int h, int L) {
+    int g = -1;
+    for (const auto& pg : hpend[h])
+      if (pg.second <= L) g = std::max(g, pg.first);
+    if (g < 0) return;
+    wait_for(h, g, L, false);
+    std::vector<std::pair<int, int>> keep;
+    for (const auto& pg : hpend[h])
+      if (pg.first > g) keep.push_back(pg);
+    hpend[h].swap(keep);
+    wcost[h] += 1000;
   }
 
   // The index in seq[w] of the warp's next task after its level-L tasks
@@ -953,6 +1025,7 @@ struct Builder {
     last_colend.assign(W, -1);
     wcost.assign(W, 0.0);
     pinned.assign(W, 0);
+    hpend.assign(W, {});
     std::vector<int> wnext(W, 0);
     for (int L = 0; L < NL; L++) {
       for (int w = 0; w < W; w++) { pos[w] = 0; pinned[w] = 0; }
@@ -982,16 +1055,15 @@ struct Builder {
           if (c.items[f].state == ST_NONE) try_resident(c.items[f], L);
       }
       std::fill(wcost.begin(), wcost.end(), 0.0);
+      std::vector<char> idle(W, 0);
+      idle_warps.clear();
+      bundles.clear();
       for (int w = 0; w < W; w++) {
-        const bool idle = !(wnext[w] < (int)seq[w].size() && C[seq[w][wnext[w]]].level == L);
-        while (wnext[w] < (int)seq[w].size() && C[seq[w][wnext[w]]].level == L) {
-          if (!run_col(w, seq[w][wnext[w]], L)) return false;
-          wnext[w]++;
-        }
-        if (idle) {  // a warp with no column of its own here runs a slice of its next one
-          const int nq = next_own(w, wnext[w], L);
-          if (nq >= 0) run_slice(w, seq[w][nq], L);
-        }
+        idle[w] = !(wnext[w] < (int)seq[w].size() && C[seq[w][wnext[w]]].level == L);
+        if (idle[w] && with_helpers) idle_warps.push_back(w);
+      }
+      auto bar = [&](int w) {
+        helper_wait(w, L);
         Emit& e = em[w];
         if (last_colhdr[w] >= 0 && last_colend[w] == (int64_t)e.w.size()) {
           e.w[last_colhdr[w]] |= (1 << 8);  // the level's barrier rides on the last column
@@ -1000,6 +1072,53 @@ struct Builder {
           e.w.push_back(CMD_BAR);
         }
         last_colhdr[w] = -1;
+      };
+      for (int w = 0; w < W; w++) {
+        if (idle[w]) continue;
+        while (wnext[w] < (int)seq[w].size() && C[seq[w][wnext[w]]].level == L) {
+          if (!run_col(w, seq[w][wnext[w]], L)) return false;
+          wnext[w]++;
+        }
+        bar(w);
+      }
+      // the idle warps: shares of the helper copies (pairs of copies to the
+      // warp with the least estimated work: its slice and its shares so
+      // far), then a slice of their next column, then the waits due
+      std::vector<double> load(W, 0.0);
+      std::vector<int> slice_q(W, -1);
+      for (int w : idle_warps) {
+        const int nq = next_own(w, wnext[w], L);
+        slice_q[w] = nq;
+        if (nq < 0) continue;
+        const ColInfo& c = C[seq[w][nq]];
+        const Part pt = slice_part(c, L);
+        size_t st = 0;
+        for (size_t r = pt.r0; r < pt.r1; r++) st += (c.items[r].nrows + kStepOps - 1) / kStepOps;
+        load[w] = part_empty(pt) ? 0.0 : 80 + step_cost() * st + fma_cost() * ((pt.f1 - pt.f0) / 2);
+      }
+      // shares[w]: per deadline, the rows warp w copies
+      std::vector<std::vector<Bundle>> shares(W);
+      const size_t q2 = 2 * (size_t)rpi();
+      std::stable_sort(bundles.begin(), bundles.end(),
+                       [](const Bundle& a, const Bundle& b) { return a.deadline < b.deadline; });
+      for (Bundle& b : bundles) {
+        for (size_t i = 0; i < b.rows.size(); i += q2) {
+          int h = idle_warps[0];
+          for (int x : idle_warps)
+            if (load[x] < load[h]) h = x;
+          load[h] += 140;
+          std::vector<Bundle>& sh = shares[h];
+          if (sh.empty() || sh.back().deadline != b.deadline) sh.push_back({{}, b.deadline});
+          sh.back().rows.insert(sh.back().rows.end(), b.rows.begin() + i,
+                                b.rows.begin() + std::min(b.rows.size(), i + q2));
+        }
+      }
+      for (int w = 0; w < W; w++) {
+        if (!idle[w]) continue;
+        for (Bundle& sh : shares[w]) helper_gather(w, sh.rows, sh.deadline);
+        const int nq = with_helpers ? slice_q[w] : next_own(w, wnext[w], L);
+        if (nq >= 0) run_slice(w, seq[w][nq], L);
+        bar(w);
       }
       st.est_cycles += *std::max_element(wcost.begin(), wcost.end()) + 120;
     }
@@ -1150,7 +1269,9 @@ std::string run_stream_host(const Schedule& sc, const Stream& st, std::vector<do
           const uint32_t rw = (uint32_t)st.words[at + q];
           const int src = (int)(rw & 0x1fffff), dst = (int)(rw >> 21);
           if (dst == trash_row && src == 0) continue;  // padding copy
-          if (dst < 0 || dst >= W * R || dst / R != w) { e = "gather outside the warp's ring"; return false; }
+          // (into any warp's ring: an idle warp copies for another warp's
+          // next task, and the race checks below cover the sharing)
+          if (dst < 0 || dst >= W * R) { e = "gather outside the rings"; return false; }
           if (pend[dst] >= 0) { e = "gather onto a row with a copy in flight"; return false; }
           double v;
           if (src < sc.n_slots) {

@@ -112,6 +112,7 @@ struct Stream {
   // statistics of the schedule
   int64_t rows_gathered = 0, rows_prefetched = 0, rows_resident = 0, rows_late = 0;
   int64_t rows_jit = 0, n_steps = 0, n_waits = 0, n_groups = 0, n_column_cmds = 0, n_pre = 0;
+  int64_t rows_helper = 0;  // rows copied by warps idle in the level, for other warps' tasks
   double est_cycles = 0;  // rough critical-path estimate, used to choose a plan
 };
 
