@@ -689,7 +689,7 @@ struct Rf {
 // malformed command, sets the error flag; the warp then drains its copies
 // and still takes every remaining barrier.
 template <typename T>
-__global__ void __launch_bounds__(256, 1) k_refactor(StreamDev P, SchedDev S, BatchDev D) {
+__global__ void __launch_bounds__(sizeof(T) == 4 ? 32 * kMaxRefactorWarps : 256, 1) k_refactor(StreamDev P, SchedDev S, BatchDev D) {
   using R = Rf<T>;
   const int g = blockIdx.x;
   if (!D.gact[g]) return;

@@ -1174,12 +1174,12 @@ static bool choose_stream_1(const Schedule& sc, int elem, size_t smem_budget, St
                             std::string& why, bool with_bwd) {
   bool found = false;
   std::string last;
-  for (int nw : {8, 6, 4, 3, 2, 1}) {
-    if (nw > kMaxRefactorWarps) continue;
+  for (int nw : {12, 10, 8, 6, 4, 3, 2, 1}) {
+    if (nw > (elem == 4 ? kMaxRefactorWarps : 8)) continue;
     StreamPlan p;
     p.elem = elem;
     p.nw = nw;
-    p.chunk_words = 512;
+    p.chunk_words = nw >= 10 ? 320 : 512;
     const size_t fixed = (size_t)nw * 2 * p.chunk_words * 4 + (size_t)kSpareRows * 32 * elem;
     if (fixed >= smem_budget) continue;
     int r = (int)((smem_budget - fixed) / ((size_t)32 * elem) / nw);

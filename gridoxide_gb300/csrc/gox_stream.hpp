@@ -61,7 +61,7 @@ constexpr int kStepOps = 9;     // update ops per step (one L(:, j) run piece)
 // and rows the unused slots of a step may read.
 constexpr int kSpareRows = 12;
 constexpr int kMaxRows = 2048;  // ring rows of all warps (11-bit row fields)
-constexpr int kMaxRefactorWarps = 8;
+constexpr int kMaxRefactorWarps = 12;  // FP32 plans; FP64 plans up to 8 (register budget)
 
 // Encodings (all little fields of 32-bit words):
 //   GATHER  w0 = op | m << 4 | commit << 23, then m words src_row | dst_row << 21;
@@ -125,11 +125,13 @@ size_t stream_smem_bytes(const StreamPlan& plan);
 bool build_stream(const Schedule& sc, const StreamPlan& plan, Stream& out, std::string& why,
                   bool with_bwd = false);
 
-// Chooses the plan within `smem_budget` bytes: the most warps (up to 8)
-// whose rings hold the schedule, and builds its stream.  (Measured on
-// GB300, case2000 FP32: 3 / 4 / 6 / 8 / 12 warps took 4.90 / 4.26 / 3.72 /
-// 3.52 / 3.69 ms per refactor, while the estimate favoured 4: more warps
-// hide the latencies of the wide levels, and beyond 8 the rings shrink.)
+// Chooses the plan within `smem_budget` bytes: the most warps (up to 12 in
+// FP32, 8 in FP64) whose rings hold the schedule, and builds its stream.
+// (Measured on GB300, case2000 x 4096 FP32, refactor with both
+// substitutions: 8 / 10 / 11 / 12 warps took 2.31 / 2.23 / 2.20 / 2.17 ms
+// with 512-, 512-, 256- and 320-word chunks; more warps hide more of the
+// latencies of the wide levels and give the narrow ones more idle warps to
+// issue copies, and smaller chunks leave the rings room.)
 bool choose_stream(const Schedule& sc, int elem, size_t smem_budget, Stream& out,
                    std::string& why);
 
