@@ -6,6 +6,7 @@
 #include <algorithm>
 #include <cmath>
 #include <functional>
+#include <map>
 #include <cstdio>
 #include <cstring>
 #include <memory>
@@ -195,7 +196,7 @@ struct DevSchedule {
   DevMem yp, yi, yre, yim, bus_rowP, bus_rowQ, bus_colA, bus_colV, a_kind, a_bi, a_bk, a_yslot,
       a_dst, lev_ptr, lev_cols, c_base, c_ulen, c_llen, c_abeg, c_aend, op_ptr, op_slot, op_pos, ph_ptr,
       ph_rows, ph_kind, fw_ptr, fw_slot, fw_col, bw_ptr, bw_slot, bw_col, diag_slot, bt_ptr, bt_cnt,
-      pk_off, pk, slot_a, off_a, fill_rec, fill_y, fill_yf;
+      pk_off, pk, slot_a, off_a, ft_dst, ft_bus, ft_y, ft_yf, fz_slot;
   SchedDev d{};
   int max_collen = 0, max_ops = 0, max_pk = 0, max_head = 0, max_fw = 0;
   // refactor command streams, FP32 and FP64 plans
@@ -242,34 +243,62 @@ struct DevSchedule {
     upload(pk_off, sc.pk_off); upload(pk, sc.pk);
     upload(slot_a, sc.slot_a); upload(off_a, sc.off_a);
     {
-      // fill recipe: per LU slot, then per off-diagonal entry
-      const int nx = sc.n_slots + sc.n_off;
-      std::vector<int32_t> rec((size_t)nx * 4, 0);
-      std::vector<double> yv((size_t)nx * 2, 0.0);
-      std::vector<float> yvf((size_t)nx * 2, 0.0f);  // the FP32 fill's copy (no conversions)
-      for (int x = 0; x < nx; x++) {
-        const int a = x < sc.n_slots ? sc.slot_a[x] : sc.off_a[x - sc.n_slots];
-        int32_t* r = &rec[(size_t)x * 4];
-        if (a < 0) {
-          r[0] = -1; r[1] = 0; r[2] = 0; r[3] = -2;  // matches no outage slot (-1 = none)
-          continue;
-        }
-        const int kind = sc.a_kind[a];
-        const bool diag = kind == 0 || kind == 1 || kind == 4 || kind == 5;
-        r[0] = kind; r[1] = sc.a_bi[a]; r[2] = diag ? sc.a_bi[a] : sc.a_bk[a]; r[3] = sc.a_yslot[a];
-        if (!yre_h.empty()) {
-          yv[(size_t)x * 2] = yre_h[sc.a_yslot[a]];
-          yv[(size_t)x * 2 + 1] = yim_h[sc.a_yslot[a]];
-          yvf[(size_t)x * 2] = (float)yv[(size_t)x * 2];
-          yvf[(size_t)x * 2 + 1] = (float)yv[(size_t)x * 2 + 1];
+      // fill tasks: one per Y entry (i, k) with Jacobian entries, holding the
+      // destinations of its H, N, M, L entries (diagonal tasks first), then
+      // the zero fill-in slots of the factor (power-flow topologies only: a
+      // linear-solver handle has no Y and no Jacobian kinds)
+      const bool pf = !yre_h.empty();
+      std::vector<int32_t> dst_of_a(sc.n_a, -1);
+      std::vector<int32_t> zeros;
+      for (int x = 0; pf && x < sc.n_slots; x++) {
+        if (sc.slot_a[x] >= 0) dst_of_a[sc.slot_a[x]] = x;
+        else zeros.push_back(x);
+      }
+      for (int j = 0; pf && j < sc.n_off; j++) dst_of_a[sc.off_a[j]] = sc.n_slots + j;
+      std::map<std::pair<int, int>, int> task_of;
+      std::vector<int32_t> tdst, tbus;
+      std::vector<double> ty;
+      std::vector<float> tyf;
+      auto quad = [](int kind) { return kind == 0 || kind == 2 ? 0 : kind == 1 || kind == 3 ? 1
+                                        : kind == 4 || kind == 6 ? 2 : 3; };
+      for (int pass = 0; pf && pass < 2; pass++) {  // diagonal tasks, then off-diagonal ones
+        for (int a = 0; a < sc.n_a; a++) {
+          const int kind = sc.a_kind[a];
+          const bool diag = kind == 0 || kind == 1 || kind == 4 || kind == 5;
+          if (diag != (pass == 0)) continue;
+          const int bi = sc.a_bi[a], bk = diag ? sc.a_bi[a] : sc.a_bk[a];
+          auto it = task_of.find({bi, bk});
+          int t;
+          if (it == task_of.end()) {
+            t = (int)(tbus.size() / 4);
+            task_of[{bi, bk}] = t;
+            tdst.insert(tdst.end(), {-1, -1, -1, -1});
+            tbus.insert(tbus.end(), {bi, bk, sc.a_yslot[a], diag ? 1 : 0});
+            const double yr = yre_h[sc.a_yslot[a]], yi = yim_h[sc.a_yslot[a]];
+            ty.insert(ty.end(), {yr, yi});
+            tyf.insert(tyf.end(), {(float)yr, (float)yi});
+          } else {
+            t = it->second;
+            if (tbus[(size_t)t * 4 + 2] != sc.a_yslot[a])
+              throw std::logic_error("Jacobian entries of one bus pair on two Y slots");
+          }
+          int32_t& d = tdst[(size_t)t * 4 + quad(kind)];
+          if (d != -1) throw std::logic_error("two Jacobian entries of one kind and bus pair");
+          d = dst_of_a[a];
         }
       }
-      upload(fill_rec, rec);
-      upload(fill_y, yv);
-      upload(fill_yf, yvf);
-      d.fill_rec = reinterpret_cast<const int4*>(fill_rec.p);
-      d.fill_y = reinterpret_cast<const double2*>(fill_y.p);
-      d.fill_yf = reinterpret_cast<const float2*>(fill_yf.p);
+      upload(ft_dst, tdst);
+      upload(ft_bus, tbus);
+      upload(ft_y, ty);
+      upload(ft_yf, tyf);
+      upload(fz_slot, zeros);
+      d.n_ftask = (int)(tbus.size() / 4);
+      d.n_fzero = (int)zeros.size();
+      d.ft_dst = reinterpret_cast<const int4*>(ft_dst.p);
+      d.ft_bus = reinterpret_cast<const int4*>(ft_bus.p);
+      d.ft_y = reinterpret_cast<const double2*>(ft_y.p);
+      d.ft_yf = reinterpret_cast<const float2*>(ft_yf.p);
+      d.fz_slot = fz_slot.as<int32_t>();
     }
     d.slot_a = slot_a.as<int32_t>(); d.off_a = off_a.as<int32_t>();
     d.n_off_real = sc.n_off;
@@ -401,11 +430,12 @@ struct Iter {
     return mode == 0 ? 3 : 2;
   }
   static void fill(const SchedDev& S, const BatchDev& D, bool outage, cudaStream_t st) {
-    const int per_warp = 32;
-    int warps = (S.n_slots + S.n_off_real + per_warp - 1) / per_warp;
+    const int per_warp = 8;  // tasks per warp
+    const int tw = (S.n_ftask + per_warp - 1) / per_warp;
+    const int warps = tw + (S.n_fzero + 31) / 32;
     dim3 grid((warps + kWarps - 1) / kWarps, D.G), block(32 * kWarps);
-    if (outage) k_fill<T, true><<<grid, block, 0, st>>>(S, D, per_warp);
-    else k_fill<T, false><<<grid, block, 0, st>>>(S, D, per_warp);
+    if (outage) k_fill<T, true><<<grid, block, 0, st>>>(S, D, tw, per_warp);
+    else k_fill<T, false><<<grid, block, 0, st>>>(S, D, tw, per_warp);
   }
   static void refactor(const DevSchedule& ds, const BatchDev& D, cudaStream_t st) {
     const int i = sizeof(T) == 4 ? 0 : 1;

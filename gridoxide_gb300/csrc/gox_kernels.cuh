@@ -40,12 +40,14 @@ struct SchedDev {
   const uint8_t* bt_cnt;
   const int32_t *pk_off, *pk;
   const int32_t *slot_a, *off_a;
-  // fill recipe per LU slot, then per off-diagonal entry: {kind (-1: zero
-  // fill-in), bus i, bus k (= i on the diagonal), Y slot} and Y's value
-  // (FP64, and rounded to FP32 for the FP32 fill)
-  const int4* fill_rec;
-  const double2* fill_y;
-  const float2* fill_yf;
+  // fill tasks (one per Y entry with Jacobian entries): destinations of
+  // H, N, M, L; {bus i, bus k, Y slot, diagonal}; Y's value (FP64, and
+  // rounded to FP32 for the FP32 fill); then the zero fill-in slots
+  int n_ftask, n_fzero;
+  const int4 *ft_dst, *ft_bus;
+  const double2* ft_y;
+  const float2* ft_yf;
+  const int32_t* fz_slot;
   const int32_t *ph_ptr, *ph_rows, *ph_kind, *fw_ptr, *fw_slot, *fw_col, *bw_ptr, *bw_slot,
       *bw_col, *diag_slot;
 };
@@ -292,99 +294,135 @@ __global__ void k_decide(BatchDev D, int it, int mode) {
 // ---------------------------------------------------------------------------
 // K2: Jacobian fill (src/jacobian.rs:202-250 formulas in rectangular form:
 // V_i V_k cos(th_i - th_k) = e_i e_k + f_i f_k, V_i V_k sin(..) = f_i e_k - e_i f_k),
-// written straight into the factor's layout: each LU slot receives its
-// A entry or zero (fill-in), so the refactor starts a column with one bulk
-// copy.  Index space: the LU slots, then the off-diagonal (BTF) entries.
-// grid (chunks, G); each warp fills a contiguous run of slots.
-template <typename T, bool OUTAGE>
-__device__ __forceinline__ T fill_value(const SchedDev& S, const BatchDev& D, int x, int g,
-                                        int lane, int s, int os0, int os1, int os2, int os3) {
-  const int N = S.n_bus;
-  const int4 r = __ldg(S.fill_rec + x);
-  T G, B;
-  if constexpr (sizeof(T) == 4) {
-    // FP32 fill: Y rounded once on the host (a conversion per value here
-    // would run on the FP64 pipe, the bound of this kernel otherwise)
-    const float2 y = __ldg(S.fill_yf + x);
-    G = y.x;
-    B = y.y;
-  } else {
-    const double2 y = __ldg(S.fill_y + x);
-    G = y.x;
-    B = y.y;
-  }
-  if (OUTAGE) {
-    // the outaged branch's slots: Y + delta in FP64, then rounded (the
-    // warp takes this branch only when one of its lanes needs it)
-    const int c = (r.w == os0) ? 0 : (r.w == os1) ? 1 : (r.w == os2) ? 2 : (r.w == os3) ? 3 : -1;
-    if (__any_sync(0xffffffffu, c >= 0)) {
-      if (c >= 0) {
-        const double2 y = __ldg(S.fill_y + x);
-        G = (T)(y.x + D.o_dre[4 * s + c]);
-        B = (T)(y.y + D.o_dim[4 * s + c]);
-      }
-    }
-  }
-  const T* eT = (const T*)D.eT; const T* fT = (const T*)D.fT; const T* ivT = (const T*)D.ivT;
-  const T* pT = (const T*)D.pT; const T* qT = (const T*)D.qT;
-  const int kind = r.x;
-  if (kind < 0) return (T)0;  // fill-in: starts at zero
-  const size_t xi = gidx(g, N, r.y, lane);
-  if (kind == 0 || kind == 1 || kind == 4 || kind == 5) {
-    const T ei = eT[xi], fi = fT[xi], iv = ivT[xi], P = pT[xi], Q = qT[xi];
-    const T vi2 = ei * ei + fi * fi;
-    const T vi = vi2 * iv;  // |V_i|^2 / |V_i|
-    switch (kind) {
-      case 0: return -Q - vi2 * B;      // H_ii
-      case 1: return P * iv + vi * G;   // N_ii
-      case 4: return P - vi2 * G;       // M_ii
-      default: return Q * iv - vi * B;  // L_ii
-    }
-  }
-  const size_t xk = gidx(g, N, r.z, lane);
-  const T ei = eT[xi], fi = fT[xi], ek = eT[xk], fk = fT[xk];
-  const T c = ei * ek + fi * fk;   // V_i V_k cos
-  const T sn = fi * ek - ei * fk;  // V_i V_k sin
-  switch (kind) {
-    case 2: return G * sn - B * c;                 // H_ik
-    case 3: return (G * c + B * sn) * ivT[xk];     // N_ik
-    case 6: return -(G * c + B * sn);              // M_ik
-    default: return (G * sn - B * c) * ivT[xk];    // L_ik
-  }
+// written straight into the factor's layout, so the refactor starts a
+// column with one copy of its rows.  One task per Y entry (i, k) that has
+// Jacobian entries: its four entries H, N, M, L share the bus values and
+// the products, so a task loads five rows and stores up to four (entries
+// absent from the Jacobian have destination -1).  A destination below
+// n_slots is an LU slot, else an off-diagonal (BTF) entry.  The fill-in
+// slots of the factor are zeroed by the last warps, four rows (FP32) per
+// 16-byte store.  grid (chunks, G): warps [0, tw) run `per_warp` tasks
+// each, the others zero 32 slots each.
+template <typename T>
+__device__ __forceinline__ void fill_store(T* LU, T* OFF, int n_slots, int x, int lane, T v) {
+  if (x < 0) return;
+  if (x < n_slots) LU[(size_t)x * 32u + lane] = v;
+  else OFF[(size_t)(x - n_slots) * 32u + lane] = v;
 }
 
 template <typename T, bool OUTAGE>
-__global__ void __launch_bounds__(256) k_fill(SchedDev S, BatchDev D, int per_warp) {
+__global__ void __launch_bounds__(256) k_fill(SchedDev S, BatchDev D, int tw, int per_warp) {
   const int g = blockIdx.y;
   if (!D.gact[g]) return;
   const int lane = threadIdx.x & 31;
   const int wglob = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
-  const int total = S.n_slots + S.n_off_real;
-  const int a0 = wglob * per_warp;
-  if (a0 >= total) return;
-  const int a1 = min(total, a0 + per_warp);
+  const int N = S.n_bus;
+  T* LU = (T*)D.lu + (size_t)g * S.n_slots * 32u;
+  T* OFF = (T*)D.off + (size_t)g * S.n_off * 32u;
+  if (wglob >= tw) {
+    // zero fill-in slots: lanes of a 16-byte store cover one row
+    constexpr int LPR = 32 * (int)sizeof(T) / 16;  // lanes per row
+    constexpr int RPI = 32 / LPR;                  // rows per store
+    const int z0 = (wglob - tw) * 32;
+    const int sub = lane % LPR;
+#pragma unroll
+    for (int q = 0; q < 32; q += RPI) {
+      const int z = z0 + q + lane / LPR;
+      if (z < S.n_fzero) {
+        const int x = __ldg(S.fz_slot + z);
+        *reinterpret_cast<float4*>(reinterpret_cast<char*>(LU + (size_t)x * 32u) + sub * 16) =
+            make_float4(0.f, 0.f, 0.f, 0.f);
+      }
+    }
+    return;
+  }
+  const int t0 = wglob * per_warp;
+  if (t0 >= S.n_ftask) return;
+  const int t1 = min(S.n_ftask, t0 + per_warp);
   const int s = g * 32 + lane;
-  T* LU = (T*)D.lu;
-  T* OFF = (T*)D.off;
+  const size_t gb = (size_t)g * N * 32u + lane;
+  const T* eT = (const T*)D.eT + gb;
+  const T* fT = (const T*)D.fT + gb;
+  const T* ivT = (const T*)D.ivT + gb;
+  const T* pT = (const T*)D.pT + gb;
+  const T* qT = (const T*)D.qT + gb;
   int os0 = -1, os1 = -1, os2 = -1, os3 = -1;
   if (OUTAGE && D.o_bf[s] >= 0) {
     os0 = D.o_slot[4 * s]; os1 = D.o_slot[4 * s + 1]; os2 = D.o_slot[4 * s + 2]; os3 = D.o_slot[4 * s + 3];
   }
-  constexpr int U = 4;  // slots in flight per warp
-  for (int x0 = a0; x0 < a1; x0 += U) {
-    T v[U];
+  constexpr int U = 4;  // tasks in flight per warp
+  for (int ta = t0; ta < t1; ta += U) {
+    int4 dst[U], bus[U];
+    T G[U], B[U], v[U][5];
 #pragma unroll
     for (int u = 0; u < U; u++) {
-      const int x = min(x0 + u, a1 - 1);
-      v[u] = fill_value<T, OUTAGE>(S, D, x, g, lane, s, os0, os1, os2, os3);
+      const int t = min(ta + u, t1 - 1);
+      dst[u] = __ldg(S.ft_dst + t);
+      bus[u] = __ldg(S.ft_bus + t);
+      if constexpr (sizeof(T) == 4) {
+        // FP32 fill: Y rounded once on the host (a conversion per value here
+        // would run on the FP64 pipe)
+        const float2 y = __ldg(S.ft_yf + t);
+        G[u] = y.x;
+        B[u] = y.y;
+      } else {
+        const double2 y = __ldg(S.ft_y + t);
+        G[u] = y.x;
+        B[u] = y.y;
+      }
+      // five rows: e_i, f_i and (diagonal) 1/|V_i|, P_i, Q_i or
+      // (off-diagonal) e_k, f_k, 1/|V_k|
+      const size_t xi = (size_t)bus[u].x * 32u, xk = (size_t)bus[u].y * 32u;
+      const bool dg = bus[u].w != 0;
+      v[u][0] = eT[xi];
+      v[u][1] = fT[xi];
+      v[u][2] = dg ? ivT[xi] : eT[xk];
+      v[u][3] = dg ? pT[xi] : fT[xk];
+      v[u][4] = dg ? qT[xi] : ivT[xk];
+    }
+    if (OUTAGE) {
+      // the outaged branch's Y entries: Y + delta in FP64, then rounded
+      // (the warp takes this branch only when one of its lanes needs it)
+#pragma unroll
+      for (int u = 0; u < U; u++) {
+        const int ys = bus[u].z;
+        const int c = (ys == os0) ? 0 : (ys == os1) ? 1 : (ys == os2) ? 2 : (ys == os3) ? 3 : -1;
+        if (__any_sync(0xffffffffu, c >= 0)) {
+          if (c >= 0) {
+            const double2 y = __ldg(S.ft_y + min(ta + u, t1 - 1));
+            G[u] = (T)(y.x + D.o_dre[4 * s + c]);
+            B[u] = (T)(y.y + D.o_dim[4 * s + c]);
+          }
+        }
+      }
     }
 #pragma unroll
     for (int u = 0; u < U; u++) {
-      const int x = x0 + u;
-      if (x < a1) {
-        if (x < S.n_slots) LU[gidx(g, S.n_slots, x, lane)] = v[u];
-        else OFF[gidx(g, S.n_off, x - S.n_slots, lane)] = v[u];
+      if (ta + u >= t1) break;
+      T h, nn, m, l;
+      if (bus[u].w != 0) {
+        const T ei = v[u][0], fi = v[u][1], iv = v[u][2], P = v[u][3], Q = v[u][4];
+        const T vi2 = ei * ei + fi * fi;
+        const T vi = vi2 * iv;  // |V_i|^2 / |V_i|
+        h = -Q - vi2 * B[u];       // H_ii
+        nn = P * iv + vi * G[u];   // N_ii
+        m = P - vi2 * G[u];        // M_ii
+        l = Q * iv - vi * B[u];    // L_ii
+      } else {
+        const T ei = v[u][0], fi = v[u][1], ek = v[u][2], fk = v[u][3], ivk = v[u][4];
+        const T c = ei * ek + fi * fk;   // V_i V_k cos
+        const T sn = fi * ek - ei * fk;  // V_i V_k sin
+        const T a = G[u] * sn - B[u] * c;
+        const T b = G[u] * c + B[u] * sn;
+        h = a;          // H_ik
+        nn = b * ivk;   // N_ik
+        m = -b;         // M_ik
+        l = a * ivk;    // L_ik
       }
+      fill_store(LU, OFF, S.n_slots, dst[u].x, lane, h);
+      fill_store(LU, OFF, S.n_slots, dst[u].y, lane, nn);
+      fill_store(LU, OFF, S.n_slots, dst[u].z, lane, m);
+      fill_store(LU, OFF, S.n_slots, dst[u].w, lane, l);
     }
   }
 }
