@@ -83,6 +83,47 @@ __device__ __forceinline__ size_t gidx(int g, int n, int e, int lane) {
 }
 
 // ---------------------------------------------------------------------------
+// Conversions between FP64 and FP32 by integer operations.  This GPU runs
+// a cvt between the two at the rate of an FP64 FMA, and the FP64 pipe is
+// what bounds the mismatch kernels.
+// f32_rn: round to nearest even (the value of (float)x) for results in the
+// normal FP32 range; overflow gives infinity and NaN a quiet NaN, results
+// below the smallest normal FP32 number (1.2e-38) become a zero of x's sign.
+__device__ __forceinline__ float f32_rn(double x) {
+  const unsigned long long b = (unsigned long long)__double_as_longlong(x);
+  const unsigned hi = (unsigned)(b >> 32), lo = (unsigned)b;
+  const unsigned ex = (hi >> 20) & 0x7ffu;
+  const unsigned mant = ((hi & 0xfffffu) << 3) | (lo >> 29);  // top 23 fraction bits
+  unsigned f = ((ex - 896u) << 23) + mant;
+  const unsigned rem = lo & 0x1fffffffu;  // the 29 bits rounded off
+  f += (rem > 0x10000000u || (rem == 0x10000000u && (f & 1u))) ? 1u : 0u;
+  f = ex < 897u ? 0u : f;
+  f = ex > 1150u ? 0x7f800000u : f;
+  f = (ex == 2047u && ((hi & 0xfffffu) | lo) != 0u) ? 0x7fc00000u : f;
+  return __uint_as_float(f | (hi & 0x80000000u));
+}
+// f64_of: the exact FP64 value of an FP32 number (FP32 subnormals, below
+// 1.2e-38, become a zero of the same sign)
+__device__ __forceinline__ double f64_of(float v) {
+  const unsigned u = __float_as_uint(v);
+  const unsigned ex = (u >> 23) & 0xffu;
+  unsigned hi = ((ex + 896u) << 20) | ((u & 0x7fffffu) >> 3);
+  hi = ex == 0u ? 0u : (ex == 255u ? (0x7ff00000u | ((u & 0x7fffffu) >> 3) | ((u & 0x7fffffu) ? 0x80000u : 0u)) : hi);
+  const unsigned lo = ex == 0u ? 0u : (u << 29);
+  return __longlong_as_double((long long)(((unsigned long long)(hi | (u & 0x80000000u)) << 32) | lo));
+}
+template <typename T>
+__device__ __forceinline__ T to_T(double x) {
+  if constexpr (sizeof(T) == 4) return f32_rn(x);
+  else return x;
+}
+template <typename T>
+__device__ __forceinline__ double from_T(T v) {
+  if constexpr (sizeof(T) == 4) return f64_of(v);
+  else return v;
+}
+
+// ---------------------------------------------------------------------------
 // K5 + K1a.  grid (ceil(N/8), G), 8 warps: warp -> bus, lane -> scenario.
 // mode 0: iteration `it`; mode 1: the update after the last iteration.
 template <typename T>
@@ -97,15 +138,18 @@ __global__ void __launch_bounds__(256) k_update(SchedDev S, BatchDev D, int it, 
   const size_t x = gidx(g, N, i, lane);
   double vm = D.vm[x], va = D.va[x];
   double dth = 0.0;
+  float step = 0.0f;  // the angle step as solved (FP32 path): picks the formula below
   if (upd) {
     const T* sol = (const T*)D.sol;
     const int ca = __ldg(S.bus_colA + i), cv = __ldg(S.bus_colV + i);
     if (ca >= 0) {
-      const double va1 = va + (double)sol[gidx(g, S.n_u, ca, lane)];
+      const T sa = sol[gidx(g, S.n_u, ca, lane)];
+      if constexpr (sizeof(T) == 4) step = sa;
+      const double va1 = va + from_T<T>(sa);
       dth = va1 - va;
       va = va1;
     }
-    if (cv >= 0) vm += (double)sol[gidx(g, S.n_u, cv, lane)];
+    if (cv >= 0) vm += from_T<T>(sol[gidx(g, S.n_u, cv, lane)]);
     D.vm[x] = vm;
     D.va[x] = va;
   }
@@ -117,9 +161,12 @@ __global__ void __launch_bounds__(256) k_update(SchedDev S, BatchDev D, int it, 
   // rounding per iteration).  When every step of the warp is below 2^-10
   // (the later iterations) two terms of each series suffice (the first
   // omitted ones are below 2e-21).
+  // (the FP32 path compares the step as solved: an FP32 compare)
   double sn, cs;
-  const bool small = it > 0 && fabs(dth) < 0.03125;
-  if (__all_sync(0xffffffffu, it > 0 && fabs(dth) < 0.0009765625)) {
+  const float ad = sizeof(T) == 4 ? fabsf(step) : 0.0f;
+  const bool small = it > 0 && (sizeof(T) == 4 ? ad < 0.03125f : fabs(dth) < 0.03125);
+  const bool tiny = it > 0 && (sizeof(T) == 4 ? ad < 0.0009765625f : fabs(dth) < 0.0009765625);
+  if (__all_sync(0xffffffffu, tiny)) {
     const double d2 = dth * dth;
     const double cd = 1.0 + d2 * (-1.0 / 2 + d2 * (1.0 / 24));
     const double sd = dth * (1.0 + d2 * (-1.0 / 6 + d2 * (1.0 / 120)));
@@ -141,11 +188,11 @@ __global__ void __launch_bounds__(256) k_update(SchedDev S, BatchDev D, int it, 
   const double e = vm * cs, f = vm * sn;
   D.e[x] = e;
   D.f[x] = f;
-  ((T*)D.eT)[x] = (T)e;
-  ((T*)D.fT)[x] = (T)f;
+  ((T*)D.eT)[x] = to_T<T>(e);
+  ((T*)D.fT)[x] = to_T<T>(f);
   // 1/|V| for the Jacobian fill, in the fill's precision (an FP64 division
   // costs far more than an FP32 one on this GPU)
-  ((T*)D.ivT)[x] = (T)1 / (T)vm;
+  ((T*)D.ivT)[x] = (T)1 / to_T<T>(vm);
 }
 
 // ---------------------------------------------------------------------------
@@ -231,23 +278,52 @@ __global__ void __launch_bounds__(256) k_inject(SchedDev S, BatchDev D, int it) 
       ir += ar * ef - ai * ff + br * et - bi * ft;
       ii += ar * ff + ai * ef + br * ft + bi * et;
     }
-    const double pc = ei * ir + fi * ii;
-    const double qc = fi * ir - ei * ii;
     const int rp = __ldg(S.bus_rowP + i), rq = __ldg(S.bus_rowQ + i);
-    if (active) {
+    if constexpr (sizeof(T) == 4) {
+      // F = S_spec - V conj(I) in FP64 as two FMAs per component; the FP32
+      // Jacobian's P and Q are S_spec - F in FP32 (only the buses with a P
+      // row have Jacobian entries that use them; a PV bus's Q comes from
+      // the products, it has no Q row)
       if (rp >= 0) {
-        const double F = D.psp[x] - pc;
-        mx = max(mx, abs_bits(F));
-        rhs[gidx(g, S.n_u, rp, lane)] = (T)F;
+        const double psp = D.psp[x];
+        const double FP = fma(-fi, ii, fma(-ei, ir, psp));
+        const float fp = f32_rn(FP);
+        if (active) {
+          mx = max(mx, abs_bits(FP));
+          rhs[gidx(g, S.n_u, rp, lane)] = fp;
+        }
+        ((float*)D.pT)[x] = f32_rn(psp) - fp;
+        if (rq >= 0) {
+          const double qsp = D.qsp[x];
+          const double FQ = fma(ei, ii, fma(-fi, ir, qsp));
+          const float fq = f32_rn(FQ);
+          if (active) {
+            mx = max(mx, abs_bits(FQ));
+            rhs[gidx(g, S.n_u, rq, lane)] = fq;
+          }
+          ((float*)D.qT)[x] = f32_rn(qsp) - fq;
+        } else {
+          ((float*)D.qT)[x] = f32_rn(fi * ir - ei * ii);
+        }
       }
-      if (rq >= 0) {
-        const double F = D.qsp[x] - qc;
-        mx = max(mx, abs_bits(F));
-        rhs[gidx(g, S.n_u, rq, lane)] = (T)F;
+    } else {
+      const double pc = ei * ir + fi * ii;
+      const double qc = fi * ir - ei * ii;
+      if (active) {
+        if (rp >= 0) {
+          const double F = D.psp[x] - pc;
+          mx = max(mx, abs_bits(F));
+          rhs[gidx(g, S.n_u, rp, lane)] = (T)F;
+        }
+        if (rq >= 0) {
+          const double F = D.qsp[x] - qc;
+          mx = max(mx, abs_bits(F));
+          rhs[gidx(g, S.n_u, rq, lane)] = (T)F;
+        }
       }
+      ((T*)D.pT)[x] = (T)pc;
+      ((T*)D.qT)[x] = (T)qc;
     }
-    ((T*)D.pT)[x] = (T)pc;
-    ((T*)D.qT)[x] = (T)qc;
   }
   red[warp][lane] = mx;
   __syncthreads();
