@@ -399,12 +399,29 @@ struct Builder {
       nf_real = fw.size();
       while (fw.size() % 8) fw.push_back(zero_row() | (zero_row() << 16));
     }
-    const size_t nl = late.size(), np = pref.size(), ns = steps.size(), nf = fw.size();
+    size_t nl = late.size(), np = pref.size();
+    const size_t ns = steps.size(), nf = fw.size();
     auto fits = [&](size_t at, size_t end) {
       const size_t sw = (at + 8 + nl + np + 3) & ~(size_t)3;
       return sw + 4 * ns + nf <= end - 1 && sw + 4 * ns + 8 <= end;
     };
     Emit& e = em[w];
+    if ((!fits(0, (size_t)e.cw) || nl > 0xffff || np > 0xffff) && ns <= 0xffff) {
+      // the copies as GATHER commands before the command (same commit
+      // groups), when the rest fits in a chunk
+      nl = np = 0;
+      if (fits(0, (size_t)e.cw)) {
+        for (auto* rows : {&late, &pref}) {
+          if (rows->empty()) continue;
+          pend_rows[w].swap(*rows);
+          flush_gather(w);
+          e.w[e.last_gather] |= (1 << 23);
+        }
+      } else {
+        nl = late.size();
+        np = pref.size();
+      }
+    }
     if (!fits(0, (size_t)e.cw) || nl > 0xffff || np > 0xffff || ns > 0xffff) {
       // the general form counts the steps again
       for (size_t f = pt.r0; f < q; f++)
@@ -511,50 +528,46 @@ struct Builder {
     }
   }
 
-  // Issues the blocks of the warp's next tasks and every value of theirs
-  // finished before level L ahead of time, all in one commit group (the
-  // command commits its prefetch list once): the next task always, further
-  // ones while the tasks in between are short (under kAheadCycles of
-  // estimated work, so a copy's latency would not be hidden otherwise) and
-  // the ring has room.  The copies go to pref_rows.
-  static constexpr double kAheadCycles = 2500.0;
-  static constexpr int kAheadTasks = 1;
+  // Issues the block of the warp's next task and every value of it finished
+  // before level L ahead of time: by this warp (one commit group, in the
+  // command's prefetch list, waited for when that task starts), or, when
+  // the level has idle warps and the task runs at a later level, by the
+  // idle warps (see Bundle), as are then the values of the tasks after it
+  // whose deadline is after this level (up to kHelperAhead tasks ahead).
+  // Copies by idle warps run concurrently with this warp's tasks, so their
+  // rows must be free during the whole level.
+  static constexpr int kHelperAhead = 1;
   void prefetch_next(int w, int ci, int L, int64_t t, std::vector<std::pair<int, int>>& pref_rows) {
     const int sp = seqpos[ci];
-    // by the idle warps when the next task runs at a later level: its rows
-    // must then be free during the whole level, since the copies run
-    // concurrently with this warp's tasks
-    bool helpers = false;
-    int deadline = L;
-    if (!idle_warps.empty() && sp + 1 < (int)seq[w].size() && C[seq[w][sp + 1]].level > L) {
-      const ColInfo& nc = C[seq[w][sp + 1]];
-      deadline = (nc.kind == TK_COL && nc.split) ? L : nc.level - 1;
-      int rows = nc.staged ? 0 : (nc.kind == TK_BWD ? 0 : nc.len + (sc.fuse_fwd ? 1 : 0));
+    const int nseq = (int)seq[w].size();
+    const bool can_help = !idle_warps.empty() && sp + 1 < nseq && C[seq[w][sp + 1]].level > L;
+    // the last level whose barrier the copies for task d must complete
+    // before: the one before the task's own, or, for a split column whose
+    // slices may start once the warp's previous task is done, that task's
+    auto deadline_of = [&](int d) {
+      const ColInfo& nc = C[seq[w][sp + d]];
+      const int prev = d == 1 ? L : C[seq[w][sp + d - 1]].level;
+      return (nc.kind == TK_COL && nc.split) ? prev : nc.level - 1;
+    };
+    auto rows_needed = [&](const ColInfo& nc) {
+      int rows = nc.staged || nc.kind == TK_BWD ? 0 : nc.len + (sc.fuse_fwd ? 1 : 0);
       for (const Item& it : nc.items)
         if (it.state == ST_NONE && C[it.j].level < L) rows += it.nrows;
-      helpers = rows > 0 && (deadline > L || rows >= kHelperMinRows);
-    }
-    if (helpers) t = tmake(L, 0);
-    double ahead = C[ci].cost;
-    for (int d = 1; d <= kAheadTasks && sp + d < (int)seq[w].size(); d++) {
+      return rows;
+    };
+    auto place = [&](int d, int64_t tt) -> bool {
       const int ni = seq[w][sp + d];
       ColInfo& nc = C[ni];
-      if (d > 1 && ahead >= kAheadCycles) break;
-      if (!nc.staged) {
-        if (!stage_col(w, ni, t)) break;
-        bool all = true;
-        for (Item& it : nc.items) {
-          if (it.state != ST_NONE || C[it.j].level >= L) continue;
-          if (!gather_item(w, it, t)) { all = false; break; }
-          out->rows_prefetched += it.nrows;
-        }
-        if (!all) break;
+      if (!nc.staged && !stage_col(w, ni, tt)) return false;
+      for (Item& it : nc.items) {
+        if (it.state != ST_NONE || C[it.j].level >= L) continue;
+        if (!gather_item(w, it, tt)) return false;
+        out->rows_prefetched += it.nrows;
       }
-      ahead += nc.cost;
-      if (helpers) break;
-    }
-    if (helpers) {
-      // complete at the level's barrier: nothing for this warp to wait for
+      return true;
+    };
+    auto to_helpers = [&](int deadline) {
+      // complete before the deadline's barrier: nothing for this warp to wait for
       for (Item* it : uncommitted[w]) { it->group = -1; it->committed = true; }
       for (int c2 : uncommitted_cols[w]) { C[c2].group = -1; C[c2].committed = true; }
       uncommitted[w].clear();
@@ -562,10 +575,26 @@ struct Builder {
       out->rows_helper += (int64_t)pend_rows[w].size();
       if (!pend_rows[w].empty()) bundles.push_back({std::move(pend_rows[w]), deadline});
       pend_rows[w].clear();
-      return;
+    };
+    if (sp + 1 >= nseq) return;
+    const int d1 = can_help ? deadline_of(1) : L;
+    const int need1 = rows_needed(C[seq[w][sp + 1]]);
+    const bool h1 = can_help && need1 > 0 && (d1 > L || need1 >= kHelperMinRows);
+    const bool ok = place(1, h1 ? tmake(L, 0) : t);
+    if (h1) {
+      to_helpers(d1);
+    } else {
+      pref_rows.swap(pend_rows[w]);
+      new_group(w);
     }
-    pref_rows.swap(pend_rows[w]);
-    new_group(w);
+    if (!ok || !can_help) return;
+    for (int d = 2; d <= kHelperAhead && sp + d < nseq; d++) {
+      const int dd = deadline_of(d);
+      if (dd <= L) break;
+      const bool okd = place(d, tmake(L, 0));
+      to_helpers(dd);
+      if (!okd) break;
+    }
   }
 
   // The idle warp h issues its share of the level's helper copies (one
