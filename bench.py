@@ -135,41 +135,112 @@ def read_traffic(kernel: str):
     return None
 
 
-def serve(gox, topo, g, p, q, rate: float, seconds: float) -> dict:
-    """Serving leg: single-scenario requests of the workload arrive as a
-    Poisson process at `rate` per second for `seconds`, through the
-    library's serving loop (continuous batching on a worker thread, mixed
-    precision).  Latency = submit to completion of each request."""
-    srv = gox.Server(max_batch=4096, precision=gox.GOX_PRECISION_MIXED,
+def serve(gox, rate: float, seconds: float) -> dict:
+    """Serving leg: single-scenario requests arrive as a Poisson process at
+    `rate` per second for `seconds` over 16 family grids of 100-50,000 buses
+    (log-uniform sizes, each request's grid uniform at random), loads x
+    lognormal(0, 0.1), 10 % of the requests with one non-bridge branch out,
+    flat start, through the library's serving loop (continuous batching on
+    worker threads, mixed precision, host buffers).  Latency = submit to
+    completion of each request."""
+    from gridoxide_gb300 import grids as G
+    spec = G.many_topologies(count=16, n_min=100, n_max=50000, seed=5)
+    grids, topos, cand = [], [], []
+    for (n, gs, _b, _ss) in spec:
+        g = G.family_grid(n, gs)
+        yb = G.build_ybus(g)
+        grids.append((g, yb))
+        topos.append(gox.Topology(yb, g.bus_type))
+        cand.append(np.flatnonzero(~G.bridges(g)))
+    srv = gox.Server(max_batch=1024, precision=gox.GOX_PRECISION_MIXED,
                      tol=WORKLOAD["tol"], max_iter=WORKLOAD["max_iter"])
-    tid = srv.add_topology(topo)
+    ids = [srv.add_topology(t) for t in topos]
     rng = np.random.default_rng(7)
     n_req = max(1, int(rate * seconds))
     gaps = rng.exponential(1.0 / rate, size=n_req)
-    rows = rng.integers(0, p.shape[0], size=n_req)
+    which = rng.integers(0, len(spec), size=n_req)
+    reqs = []
+    for i in range(n_req):
+        t = int(which[i])
+        g, yb = grids[t]
+        p, q = G.load_scenarios(g, 1, 0.1, 5000 + i)
+        out = None
+        if rng.random() < 0.1:
+            br = rng.choice(cand[t], size=1)
+            out = tuple(a[0] for a in G.outage_deltas(g, yb, br))
+        reqs.append((t, p[0], q[0], out))
+    # warm-up: one request per grid (first-use allocations, pivot orders)
+    for t in range(len(spec)):
+        g = grids[t][0]
+        srv.wait(srv.submit(ids[t], g.p_spec, g.q_spec, g.vm, g.va), g.n_bus)
+    st0 = srv.stats()
     tickets = []
     t0 = time.perf_counter()
     due = t0
-    for i in range(n_req):
+    for i, (t, p, q, out) in enumerate(reqs):
         due += gaps[i]
         while time.perf_counter() < due:
             pass
-        tickets.append(srv.submit(tid, p[rows[i]], q[rows[i]], g.vm, g.va))
+        g = grids[t][0]
+        tickets.append(srv.submit(ids[t], p, q, g.vm, g.va, outage=out))
     lat, conv = [], 0
-    for t in tickets:
-        r = srv.wait(t, g.n_bus)
+    for (t, _, _, _), tk in zip(reqs, tickets):
+        r = srv.wait(tk, grids[t][0].n_bus)
         lat.append(r["latency_s"])
         conv += int(r["status"] == 0 and r["max_mismatch"] < WORKLOAD["tol"])
     t1 = time.perf_counter()
     st = srv.stats()
     srv.close()
     lat = np.array(lat) * 1000.0
+    nb = st["batches"] - st0["batches"]
     return {"offered_rps": rate, "requests": n_req, "completed_rps": round(n_req / (t1 - t0), 1),
             "p50_ms": round(float(np.percentile(lat, 50)), 3),
-            "p99_ms": round(float(np.percentile(lat, 99)), 3), "batches": st["batches"],
-            "mean_batch": round(n_req / max(st["batches"], 1), 1), "converged": conv,
-            "note": "Poisson arrivals of single scenarios, gox_server_* continuous batching, "
-                    "mixed precision, host buffers"}
+            "p99_ms": round(float(np.percentile(lat, 99)), 3), "batches": nb,
+            "mean_batch": round(n_req / max(nb, 1), 1), "converged": conv,
+            "grids": len(spec), "buses": [int(min(x[0] for x in spec)), int(max(x[0] for x in spec))],
+            "note": "Poisson arrivals of single scenarios over 16 grids (100-50,000 buses), 10 % "
+                    "with an N-1 outage, gox_server_* continuous batching on 8 workers, mixed "
+                    "precision, host buffers, flat start"}
+
+
+def many_topologies(gox, rounds: int) -> dict:
+    """Many-topology leg: 48 family grids (log-uniform 30-20,000 buses), a
+    batch of 8-1,024 scenarios each (loads x lognormal(0, 0.15), flat
+    start); a round solves every grid's batch once, the 48 calls issued from
+    8 host threads (each call has its own stream, so small batches of
+    different grids overlap on the GPU); host buffers, mixed precision."""
+    from concurrent.futures import ThreadPoolExecutor
+    from gridoxide_gb300 import grids as G
+    spec = G.many_topologies()
+    jobs = []
+    for (n, gs, b, ss) in spec:
+        g = G.family_grid(n, gs)
+        topo = gox.Topology(G.build_ybus(g), g.bus_type)
+        p, q = G.load_scenarios(g, b, 0.15, ss)
+        jobs.append((topo, g, p, q))
+
+    def one(j):
+        topo, g, p, q = j
+        return topo.solve(p, q, g.vm, g.va, tol=WORKLOAD["tol"], max_iter=WORKLOAD["max_iter"],
+                          precision=gox.GOX_PRECISION_MIXED)
+
+    ex = ThreadPoolExecutor(max_workers=8)
+    res = list(ex.map(one, jobs))  # warm-up (allocations, pivot orders)
+    times = []
+    for _ in range(rounds):
+        t0 = time.perf_counter()
+        res = list(ex.map(one, jobs))
+        times.append(time.perf_counter() - t0)
+    ex.shutdown()
+    total = sum(x[2] for x in spec)
+    conv = sum(int(np.sum(r.status == 0)) for r in res)
+    t = float(np.median(times))
+    return {"value": round(total / t, 1), "unit": "solves/s", "grids": len(spec),
+            "scenarios_per_round": total, "ms_per_round": round(1000 * t, 2),
+            "buses": [int(min(x[0] for x in spec)), int(max(x[0] for x in spec))],
+            "converged": conv, "rounds": rounds,
+            "note": "48 grids solved once per round from 8 host threads, host buffers, mixed "
+                    "precision, flat start"}
 
 
 _ORACLE_TOPO = {}
@@ -254,8 +325,10 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--serve-rate", type=float, default=8000.0,
+    ap.add_argument("--serve-rate", type=float, default=2000.0,
                     help="serving leg: Poisson arrivals per second (0 = skip)")
+    ap.add_argument("--many-rounds", type=int, default=3,
+                    help="many-topology leg: timed rounds (0 = skip)")
     ap.add_argument("--serve-seconds", type=float, default=1.0)
     ap.add_argument("--grid", default=WORKLOAD["grid"], help="profiling: another grid")
     ap.add_argument("--scenarios", type=int, default=WORKLOAD["scenarios"],
@@ -440,8 +513,10 @@ def main():
         "kernels": kernels,
         "clocks": cl,
     }
-    if rank == 0 and args.serve_rate > 0:
-        line["serving"] = serve(gox, topo, g, p, q, args.serve_rate, args.serve_seconds)
+    if rank == 0 and args.serve_rate > 0 and not args.quick:
+        line["serving"] = serve(gox, args.serve_rate, args.serve_seconds)
+    if rank == 0 and args.many_rounds > 0 and not args.quick:
+        line["many_topologies"] = many_topologies(gox, args.many_rounds)
     if rank == 0 and not args.no_cpu_baseline:
         threads = os.cpu_count() or 1
         v, dt, passes = cpu_baseline(g, yb, p, q, threads)

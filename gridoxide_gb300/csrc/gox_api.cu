@@ -216,6 +216,7 @@ struct DevSchedule {
       st[i].chunk0 = sc0[i].as<int32_t>();
       st[i].nchunks = snc[i].as<int32_t>();
       st[i].ring_rows = ss[i]->plan.ring_rows;
+      st[i].rows_total = ring_total(ss[i]->plan);
       st[i].chunk_words = ss[i]->plan.chunk_words;
       st[i].n_bars = ss[i]->n_bars;
       st_nw[i] = ss[i]->plan.nw;
@@ -439,8 +440,11 @@ struct Iter {
   }
   static void refactor(const DevSchedule& ds, const BatchDev& D, cudaStream_t st) {
     const int i = sizeof(T) == 4 ? 0 : 1;
+    // the budget every plan fits in, the same value from every thread (calls
+    // on different topologies may run concurrently; a plan-sized value set
+    // by one could undercut another's launch)
     GOX_CK(cudaFuncSetAttribute(k_refactor<T>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                (int)ds.st_smem[i]));
+                                (int)kRefactorSmem));
     k_refactor<T><<<D.G, 32 * ds.st_nw[i], ds.st_smem[i], st>>>(ds.st[i], ds.d, D);
   }
   static void solve(const SchedDev& S, const BatchDev& D, cudaStream_t st) {
@@ -1484,11 +1488,11 @@ extern "C" int gox_ls_factor_solve_values_static(gox_ls* h, const double* vals,
 }
 
 // ---- serving -----------------------------------------------------------------
-// A worker thread batches queued single-scenario requests per topology
-// (continuous batching: while a batch runs, new requests queue; the next
-// batch takes the topology with the oldest request and up to max_batch of
-// its requests in arrival order) and solves each batch with
-// gox_batch_solve on the GPU.
+// Worker threads batch queued single-scenario requests per topology
+// (continuous batching: while a batch runs, new requests queue; a free
+// worker takes the oldest request whose topology is not being solved and up
+// to max_batch of that topology's requests in arrival order) and solve each
+// batch with gox_batch_solve on the GPU.
 
 #include <chrono>
 #include <condition_variable>
@@ -1525,17 +1529,34 @@ struct gox_server {
   int64_t next_ticket = 1;
   bool stop = false;
   int64_t batches = 0, solved = 0;
-  std::thread worker;
+  // Workers: each takes the oldest queued request whose topology no other
+  // worker is solving, with up to max_batch queued requests of that
+  // topology, so batches of different topologies run concurrently (each
+  // solve has its own stream) while one topology's state is used by one
+  // worker at a time.
+  static constexpr int kWorkers = 8;
+  std::vector<std::thread> workers;
+  std::vector<char> busy;  // per topology
 
   void run() {
     cudaSetDevice(device);
     for (;;) {
       std::vector<std::shared_ptr<gox::ServerReq>> batch;
+      int tp = -1;
+      gox_topo* t = nullptr;
       {
         std::unique_lock<std::mutex> lk(mu);
-        cv.wait(lk, [&] { return stop || !queue.empty(); });
+        cv.wait(lk, [&] {
+          if (stop && queue.empty()) return true;
+          for (const auto& r : queue)
+            if (!busy[r->topo]) return true;
+          return false;
+        });
         if (stop && queue.empty()) return;
-        const int tp = queue.front()->topo;
+        for (const auto& r : queue)
+          if (!busy[r->topo]) { tp = r->topo; break; }
+        busy[tp] = 1;
+        t = topos[tp];
         for (auto it = queue.begin(); it != queue.end() && (int)batch.size() < max_batch;) {
           if ((*it)->topo == tp) {
             batch.push_back(*it);
@@ -1545,9 +1566,10 @@ struct gox_server {
           }
         }
       }
-      solve(batch);
+      solve(t, batch);
       {
         std::lock_guard<std::mutex> lk(mu);
+        busy[tp] = 0;
         batches++;
         solved += (int64_t)batch.size();
       }
@@ -1555,8 +1577,7 @@ struct gox_server {
     }
   }
 
-  void solve(std::vector<std::shared_ptr<gox::ServerReq>>& batch) {
-    gox_topo* t = topos[batch[0]->topo];
+  void solve(gox_topo* t, std::vector<std::shared_ptr<gox::ServerReq>>& batch) {
     const int n = t->n_bus, B = (int)batch.size();
     std::vector<double> p((size_t)B * n), q((size_t)B * n), vm0((size_t)B * n), va0((size_t)B * n);
     std::vector<double> vm((size_t)B * n), va((size_t)B * n), mm(B), dre((size_t)B * 4), dim((size_t)B * 4);
@@ -1617,7 +1638,17 @@ int gox_server_create(int32_t max_batch, int32_t precision, double tol, int32_t 
     s->max_iter = max_iter;
     GOX_CK(cudaGetDevice(&s->device));
     gox_server* raw = s.get();
-    s->worker = std::thread([raw] { raw->run(); });
+    try {
+      for (int w = 0; w < gox_server::kWorkers; w++) s->workers.emplace_back([raw] { raw->run(); });
+    } catch (...) {
+      {
+        std::lock_guard<std::mutex> lk(raw->mu);
+        raw->stop = true;
+      }
+      raw->cv.notify_all();
+      for (std::thread& w : raw->workers) w.join();
+      throw;
+    }
     *out = s.release();
     return GOX_OK;
   });
@@ -1627,6 +1658,7 @@ int gox_server_add_topology(gox_server* s, gox_topo* t, int32_t* topo_id) {
   if (!s || !t || !topo_id) return GOX_E_INVALID;
   std::lock_guard<std::mutex> lk(s->mu);
   s->topos.push_back(t);
+  s->busy.push_back(0);
   *topo_id = (int32_t)s->topos.size() - 1;
   return GOX_OK;
 }
@@ -1709,7 +1741,8 @@ void gox_server_destroy(gox_server* s) {
     s->stop = true;
   }
   s->cv.notify_all();
-  if (s->worker.joinable()) s->worker.join();
+  for (std::thread& w : s->workers)
+    if (w.joinable()) w.join();
   delete s;
 }
 

@@ -602,6 +602,7 @@ struct StreamDev {
   const int32_t* chunk0;
   const int32_t* nchunks;
   int ring_rows, chunk_words, n_bars;
+  int rows_total;  // rows of all rings (the zero row follows them)
 };
 
 // Pieces of the refactor interpreter.  Every loop below runs over counts the
@@ -833,7 +834,7 @@ __global__ void __launch_bounds__(sizeof(T) == 4 ? 32 * kMaxRefactorWarps : 256,
   }
   asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
   // the zero row (padding terms of the forward substitution read it)
-  if (warp == 0) sts(ring_lane + (uint32_t)(nw * P.ring_rows) * RB, (T)0);
+  if (warp == 0) sts(ring_lane + (uint32_t)P.rows_total * RB, (T)0);
   __syncthreads();
 
   const int32_t* gw = P.words + (size_t)P.chunk0[warp] * CW;

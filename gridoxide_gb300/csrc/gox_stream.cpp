@@ -12,7 +12,7 @@ namespace gox {
 
 size_t stream_smem_bytes(const StreamPlan& p) {
   return (size_t)p.nw * 2 * p.chunk_words * 4 +
-         ((size_t)p.nw * p.ring_rows + kSpareRows) * 32 * p.elem;
+         ((size_t)ring_total(p) + kSpareRows) * 32 * p.elem;
 }
 
 namespace {
@@ -89,6 +89,9 @@ struct Builder {
   const Schedule& sc;
   StreamPlan P;
   int W, R, n;
+  int T = 0;  // rows of all rings
+  int base(int w) const { return ring_base(P, w); }
+  int rsize(int w) const { return ring_size(P, w); }
   std::vector<ColInfo> C;
   std::vector<std::vector<int>> seq;
   std::vector<int> seqpos;
@@ -128,21 +131,23 @@ struct Builder {
   Builder(const Schedule& s, const StreamPlan& p) : sc(s), P(p) {
     W = p.nw;
     R = p.ring_rows;
+    T = ring_total(p);
     n = s.n_u;
   }
 
   int64_t now(int w, int L) { return tmake(L, pos[w]++); }
 
   int alloc(int w, int m, int64_t t) {
-    if (m > R || m <= 0) return -1;
-    const int64_t* b = &busy[(size_t)w * R];
+    const int Rw = rsize(w);
+    if (m > Rw || m <= 0) return -1;
+    const int64_t* b = &busy[(size_t)base(w)];
     int run = 0;
-    for (int i = 0; i < 2 * R; i++) {
-      const int r = (cursor[w] + i) % R;
+    for (int i = 0; i < 2 * Rw; i++) {
+      const int r = (cursor[w] + i) % Rw;
       if (r == 0) run = 0;
       if (b[r] < t) {
         if (++run >= m) {
-          cursor[w] = (r + 1) % R;
+          cursor[w] = (r + 1) % Rw;
           return r - m + 1;
         }
       } else {
@@ -153,8 +158,8 @@ struct Builder {
   }
   void take(int w, int r0, int m, int64_t tg_col) {
     for (int i = 0; i < m; i++) {
-      busy[(size_t)w * R + r0 + i] = kInf;
-      tag[(size_t)w * R + r0 + i] = tg_col >= 0 ? tagof((int)tg_col, i) : -1;
+      busy[(size_t)base(w) + r0 + i] = kInf;
+      tag[(size_t)base(w) + r0 + i] = tg_col >= 0 ? tagof((int)tg_col, i) : -1;
     }
   }
   void release_abs(int row, int m, int64_t t) {
@@ -166,8 +171,8 @@ struct Builder {
   // 1/64 of the FP32 rate on this GPU
   double fma_cost() const { return P.elem == 8 ? 64.0 : 8.0; }
   double step_cost() const { return P.elem == 8 ? 60.0 + 5 * 64.0 : 70.0; }
-  int zero_row() const { return W * R; }
-  int trash_row() const { return W * R + 1; }
+  int zero_row() const { return T; }
+  int trash_row() const { return T + 1; }
 
   // Source rows of the three arrays as one row space: the factor image,
   // then the forward-substitution vector, then the right-hand side.
@@ -245,7 +250,7 @@ struct Builder {
     const int r = alloc(w, it.nrows, t);
     if (r < 0) return false;
     take(w, r, it.nrows, -1);
-    it.row = w * R + r;
+    it.row = base(w) + r;
     it.state = ST_GATHERED;
     for (int i = 0; i < it.nrows; i++) pend_rows[w].push_back({it.src + i, it.row + i});
     uncommitted[w].push_back(&it);
@@ -262,10 +267,10 @@ struct Builder {
     c.staged = true;
     if (c.kind == TK_BWD) return true;  // x_k is written by the task itself
     std::vector<std::pair<int, int>> rows;
-    const int base = sc.c_base[c.k];
-    for (int i = 0; i < c.len; i++) rows.push_back({base + i, w * R + r + i});
+    const int cb = sc.c_base[c.k];
+    for (int i = 0; i < c.len; i++) rows.push_back({cb + i, base(w) + r + i});
     emit_gather(w, ARR_LU, rows);
-    if (sc.fuse_fwd) emit_gather(w, ARR_RHS, {{c.k, w * R + r + c.len + 1}});
+    if (sc.fuse_fwd) emit_gather(w, ARR_RHS, {{c.k, base(w) + r + c.len + 1}});
     uncommitted_cols[w].push_back(ci);
     return true;
   }
@@ -276,13 +281,13 @@ struct Builder {
   bool try_resident(Item& it, int L) {
     const ColInfo& pc = C[it.j];
     if (pc.warp < 0 || pc.block < 0 || pc.level >= L) return false;
-    const size_t b = (size_t)pc.warp * R + pc.block + it.rel;
+    const size_t b = (size_t)base(pc.warp) + pc.block + it.rel;
     int fresh = 0;
     for (int i = 0; i < it.nrows; i++) {
       if (tag[b + i] != tagof(it.j, it.rel + i)) return false;
       if (busy[b + i] < tend(L)) fresh++;
     }
-    if (pinned[pc.warp] + fresh > R / 4) return false;
+    if (pinned[pc.warp] + fresh > rsize(pc.warp) / 4) return false;
     pinned[pc.warp] += fresh;
     it.row = (int)b;
     it.state = ST_RESIDENT;
@@ -437,7 +442,7 @@ struct Builder {
       out->n_waits++;
       if (on_path) wcost[w] += 1200;
     }
-    const int stage_abs = w * R + c.block;
+    const int stage_abs = base(w) + c.block;
     last_colhdr[w] = (int64_t)e.w.size();
     e.w.push_back(w0);
     e.w.push_back(c.k);
@@ -707,7 +712,7 @@ struct Builder {
       out->n_waits++;
       if (waited_late) wcost[w] += 1200;
     }
-    const int xrow = w * R + c.block;
+    const int xrow = base(w) + c.block;
     last_colhdr[w] = (int64_t)e.w.size();
     e.w.push_back(w0);
     e.w.push_back(c.k);
@@ -773,7 +778,7 @@ struct Builder {
     // updates, fetching values that found no room just in time
     std::vector<Step> steps;
     std::vector<Item*> consumed;
-    const int stage_abs = w * R + c.block;
+    const int stage_abs = base(w) + c.block;
     auto release_consumed = [&]() {
       const int64_t tf = now(w, L);
       for (Item* it : consumed) release_abs(it->row, it->nrows, tf);
@@ -875,7 +880,7 @@ struct Builder {
       err = "bad plan";
       return false;
     }
-    if (W * R + kSpareRows > kMaxRows) {
+    if (T + kSpareRows > kMaxRows) {
       err = "ring rows exceed the 11-bit row fields";
       return false;
     }
@@ -895,7 +900,7 @@ struct Builder {
         err = "column too long for 10-bit stage rows";
         return false;
       }
-      if (c.brows > R) {
+      if (c.brows > rsize(0)) {
         err = "column " + std::to_string(k) + " longer than the ring";
         return false;
       }
@@ -1003,8 +1008,12 @@ struct Builder {
       std::vector<std::vector<int>> mine(W);
       for (int k : cols) {
         int best = 0;
-        for (int w = 1; w < W; w++)
-          if (load[w] < load[best] || (load[w] == load[best] && tot[w] < tot[best])) best = w;
+        // a column whose block leaves less than two update pieces of room in
+        // a regular ring runs on warp 0 (whose ring is larger when the plan
+        // has such columns)
+        if (P.big_rows <= R || C[k].brows <= R - 2 * kPieceRows)
+          for (int w = 1; w < W; w++)
+            if (load[w] < load[best] || (load[w] == load[best] && tot[w] < tot[best])) best = w;
         load[best] += C[k].cost;
         tot[best] += C[k].cost;
         C[k].warp = best;
@@ -1040,8 +1049,8 @@ struct Builder {
       }
     }
     // ---- simulate the warps level by level and emit
-    busy.assign((size_t)W * R, -1);
-    tag.assign((size_t)W * R, -1);
+    busy.assign((size_t)T, -1);
+    tag.assign((size_t)T, -1);
     cursor.assign(W, 0);
     ngroups.assign(W, 0);
     waited.assign(W, -1);
@@ -1203,6 +1212,8 @@ static bool choose_stream_1(const Schedule& sc, int elem, size_t smem_budget, St
                             std::string& why, bool with_bwd) {
   bool found = false;
   std::string last;
+  int max_brows = 1;
+  for (int k = 0; k < sc.n_u; k++) max_brows = std::max(max_brows, sc.c_ulen[k] + 1 + sc.c_llen[k] + 3);
   for (int nw : {12, 10, 8, 6, 4, 3, 2, 1}) {
     if (nw > (elem == 4 ? kMaxRefactorWarps : 8)) continue;
     StreamPlan p;
@@ -1211,10 +1222,18 @@ static bool choose_stream_1(const Schedule& sc, int elem, size_t smem_budget, St
     p.chunk_words = nw >= 10 ? 320 : 512;
     const size_t fixed = (size_t)nw * 2 * p.chunk_words * 4 + (size_t)kSpareRows * 32 * elem;
     if (fixed >= smem_budget) continue;
-    int r = (int)((smem_budget - fixed) / ((size_t)32 * elem) / nw);
-    r = std::min(r, (kMaxRows - kSpareRows) / nw);
+    const int total = std::min((int)((smem_budget - fixed) / ((size_t)32 * elem)), kMaxRows - kSpareRows);
+    int r = total / nw;
+    int big = 0;
+    if (max_brows > r && nw > 1) {
+      // one large ring (warp 0) for the columns the even split cannot hold
+      big = max_brows + max_brows / 8;
+      r = (total - big) / (nw - 1);
+      if (r < 32 || big <= r) continue;
+    }
     if (r < 16) continue;
     p.ring_rows = r;
+    p.big_rows = big;
     Stream s;
     std::string w;
     if (!build_stream(sc, p, s, w, with_bwd)) {
@@ -1236,9 +1255,10 @@ std::string run_stream_host(const Schedule& sc, const Stream& st, std::vector<do
                             const std::vector<double>& rhs, std::vector<double>& X,
                             bool& singular) {
   const StreamPlan& P = st.plan;
-  const int W = P.nw, R = P.ring_rows, CW = P.chunk_words, n = sc.n_u;
-  const int rows = W * R + kSpareRows;
-  const int zero_row = W * R, trash_row = W * R + 1;
+  const int W = P.nw, CW = P.chunk_words, n = sc.n_u;
+  const int T = ring_total(P);
+  const int rows = T + kSpareRows;
+  const int zero_row = T, trash_row = T + 1;
   const int rpi2 = 2 * (512 / (32 * P.elem));
   std::vector<double> ring(rows, 0.0);
   std::vector<int> pend(rows, -1);  // commit group of a copy not yet waited for
@@ -1267,7 +1287,7 @@ std::string run_stream_host(const Schedule& sc, const Stream& st, std::vector<do
         return "warp " + std::to_string(w) + " word " + std::to_string(s.pc) + " (op " +
                std::to_string(st.words[s.pc] & 15) + "): " + m;
       };
-      auto in_ring = [&](int r) { return r >= 0 && r < W * R; };
+      auto in_ring = [&](int r) { return r >= 0 && r < T; };
       auto note_w = [&](int r) -> bool {
         if (r == zero_row) { e = "writes the zero row"; return false; }
         if (stamp_w[r] == L && wr_by[r] != w) { e = "two warps write row " + std::to_string(r); return false; }
@@ -1300,7 +1320,7 @@ std::string run_stream_host(const Schedule& sc, const Stream& st, std::vector<do
           if (dst == trash_row && src == 0) continue;  // padding copy
           // (into any warp's ring: an idle warp copies for another warp's
           // next task, and the race checks below cover the sharing)
-          if (dst < 0 || dst >= W * R) { e = "gather outside the rings"; return false; }
+          if (dst < 0 || dst >= T) { e = "gather outside the rings"; return false; }
           if (pend[dst] >= 0) { e = "gather onto a row with a copy in flight"; return false; }
           double v;
           if (src < sc.n_slots) {
@@ -1390,7 +1410,8 @@ std::string run_stream_host(const Schedule& sc, const Stream& st, std::vector<do
           e = "FINISH header does not match the column";
           return false;
         }
-        if (!in_ring(S0) || !in_ring(S0 + len + 2) || S0 / R != (S0 + len + 2) / R || S0 / R != w) {
+        if (!in_ring(S0) || !in_ring(S0 + len + 2) || ring_warp(P, S0) != w ||
+            ring_warp(P, S0 + len + 2) != w) {
           e = "stage block out of range";
           return false;
         }
@@ -1476,7 +1497,8 @@ std::string run_stream_host(const Schedule& sc, const Stream& st, std::vector<do
           if (nl && !gather(s.pc + 5, nl, true)) return fail(e);
           if (np && !gather(s.pc + 5 + nl, np, true)) return fail(e);
           if ((w0 >> 7) & 1) wait((w0 >> 4) & 7);
-          if (!in_ring(xr) || xr / R != w || !in_ring(yr) || !in_ring(dr)) return fail("BWD rows out of range");
+          if (!in_ring(xr) || ring_warp(P, xr) != w || !in_ring(yr) || !in_ring(dr))
+            return fail("BWD rows out of range");
           if (!note_r(yr) || !note_r(dr)) return fail(e);
           double v = ring[yr];
           const int tb = s.pc + 5 + nl + np;

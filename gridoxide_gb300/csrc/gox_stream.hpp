@@ -100,8 +100,20 @@ struct StreamPlan {
   int elem = 4;             // bytes per value: 4 (FP32) or 8 (FP64)
   int nw = 8;               // warps per CTA
   int ring_rows = 0;        // ring rows per warp
+  int big_rows = 0;         // ring rows of warp 0 when larger (columns too
+                            // long for the other rings run there); 0: ring_rows
   int chunk_words = 512;    // stream chunk, 32-bit words (multiple of 4)
 };
+// The rings in the row space: warp 0's first, then the others'.
+inline int ring_size(const StreamPlan& p, int w) {
+  return w == 0 && p.big_rows > p.ring_rows ? p.big_rows : p.ring_rows;
+}
+inline int ring_base(const StreamPlan& p, int w) { return w == 0 ? 0 : ring_size(p, 0) + (w - 1) * p.ring_rows; }
+inline int ring_total(const StreamPlan& p) { return ring_size(p, 0) + (p.nw - 1) * p.ring_rows; }
+inline int ring_warp(const StreamPlan& p, int row) {
+  const int r0 = ring_size(p, 0);
+  return row < r0 ? 0 : 1 + (row - r0) / p.ring_rows;
+}
 
 struct Stream {
   StreamPlan plan;

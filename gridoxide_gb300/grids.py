@@ -400,3 +400,37 @@ def config_grid(name: str) -> Grid:
     """The grids the batched workloads are quoted on (seed = 1 + index)."""
     n, npv, nbr, seed, ls, rs = CONFIGS[name]
     return make_grid(n, npv, nbr, seed=seed, load_scale=ls, r_scale=rs)
+
+
+# ---------------------------------------------------------------------------
+# Multi-topology workloads: grids of any size from the same family.  The
+# value scales follow the log-linear trend between the 2,000- and 10,000-bus
+# configs (capped for small grids) and are halved; every one of the 48
+# many-topology grids below then converges from flat start (checked against
+# the oracle when the list was fixed).
+
+def family_scales(n_bus: int) -> tuple[float, float]:
+    """(load_scale, r_scale) for a family grid of n_bus buses."""
+    lg = np.log10(max(n_bus, 2))
+    ls = min(0.3, 10.0 ** (3.72 - 1.43 * lg)) * 0.5
+    rs = min(0.5, 10.0 ** (2.143 - 0.861 * lg)) * 0.5
+    return float(ls), float(rs)
+
+
+def family_grid(n_bus: int, seed: int, pv_frac: float = 0.15) -> Grid:
+    """A family grid: pv_frac PV buses, 40 chords per 100 buses."""
+    ls, rs = family_scales(n_bus)
+    n_pv = max(1, int(round(pv_frac * n_bus)))
+    n_branch = (n_bus - 1) + int(round(0.4 * n_bus))
+    return make_grid(int(n_bus), n_pv, n_branch, seed=seed, load_scale=ls, r_scale=rs)
+
+
+def many_topologies(count: int = 48, n_min: int = 30, n_max: int = 20000, b_min: int = 8,
+                    b_max: int = 1024, seed: int = 4):
+    """The many-topology workload: `count` grids with bus counts log-uniform
+    in [n_min, n_max] and batch sizes uniform in [b_min, b_max]; returns
+    [(n_bus, grid seed, batch, scenario seed)]."""
+    rng = np.random.default_rng(seed)
+    ns = np.exp(rng.uniform(np.log(n_min), np.log(n_max), size=count)).astype(int)
+    bs = rng.integers(b_min, b_max + 1, size=count)
+    return [(int(n), 1000 + t, int(b), 40 + t) for t, (n, b) in enumerate(zip(ns, bs))]

@@ -255,12 +255,14 @@ const char *gox_version(void);
 
 /* ---- serving --------------------------------------------------------------
  * Continuous batching of single-scenario requests over registered
- * topologies: a worker thread takes the topology with the oldest queued
- * request and up to max_batch of its requests (arrival order), solves them
- * with gox_batch_solve, and publishes each result with its latency (submit
- * to completion).  Lanes are independent, so a request's result does not
- * depend on the batch it ran in.  A topology added to a server is used by
- * the server's thread only: do not call it directly while the server runs.
+ * topologies: each of 8 worker threads takes the oldest queued request
+ * whose topology no other worker is solving and up to max_batch of that
+ * topology's requests (arrival order), solves them with gox_batch_solve on
+ * its own stream (batches of different topologies overlap on the GPU), and
+ * publishes each result with its latency (submit to completion).  Lanes
+ * are independent, so a request's result does not depend on the batch it
+ * ran in.  A topology added to a server is used by the server's workers
+ * only: do not call it directly while the server runs.
  * The reference's serving counterpart is the Python `PowerFlowModel.solve_batch`
  * / rayon `BatchSolver` call per batch (src/python.rs:306-341,
  * src/batch.rs:198-289); the queue in front of it is new here. */
