@@ -140,17 +140,21 @@ def serve(gox, rate: float, seconds: float) -> dict:
     `rate` per second for `seconds` over 16 family grids of 100-50,000 buses
     (log-uniform sizes, each request's grid uniform at random), loads x
     lognormal(0, 0.1), 10 % of the requests with one non-bridge branch out,
-    flat start, through the library's serving loop (continuous batching on
-    worker threads, mixed precision, host buffers).  Latency = submit to
-    completion of each request."""
+    warm started from the grid's base-case solution, through the library's
+    serving loop (continuous batching on worker threads, mixed precision,
+    host buffers).  Latency = submit to completion of each request."""
     from gridoxide_gb300 import grids as G
     spec = G.many_topologies(count=16, n_min=100, n_max=50000, seed=5)
-    grids, topos, cand = [], [], []
+    grids, topos, cand, v0 = [], [], [], []
     for (n, gs, _b, _ss) in spec:
         g = G.family_grid(n, gs)
         yb = G.build_ybus(g)
         grids.append((g, yb))
-        topos.append(gox.Topology(yb, g.bus_type))
+        topo = gox.Topology(yb, g.bus_type)
+        base = topo.solve(g.p_spec[None, :], g.q_spec[None, :], g.vm, g.va,
+                          precision=gox.GOX_PRECISION_FP64)
+        v0.append((base.voltage_mag[0].copy(), base.voltage_ang[0].copy()))
+        topos.append(topo)
         cand.append(np.flatnonzero(~G.bridges(g)))
     srv = gox.Server(max_batch=1024, precision=gox.GOX_PRECISION_MIXED,
                      tol=WORKLOAD["tol"], max_iter=WORKLOAD["max_iter"])
@@ -172,7 +176,7 @@ def serve(gox, rate: float, seconds: float) -> dict:
     # warm-up: one request per grid (first-use allocations, pivot orders)
     for t in range(len(spec)):
         g = grids[t][0]
-        srv.wait(srv.submit(ids[t], g.p_spec, g.q_spec, g.vm, g.va), g.n_bus)
+        srv.wait(srv.submit(ids[t], g.p_spec, g.q_spec, *v0[t]), g.n_bus)
     st0 = srv.stats()
     tickets = []
     t0 = time.perf_counter()
@@ -181,8 +185,7 @@ def serve(gox, rate: float, seconds: float) -> dict:
         due += gaps[i]
         while time.perf_counter() < due:
             pass
-        g = grids[t][0]
-        tickets.append(srv.submit(ids[t], p, q, g.vm, g.va, outage=out))
+        tickets.append(srv.submit(ids[t], p, q, *v0[t], outage=out))
     lat, conv = [], 0
     for (t, _, _, _), tk in zip(reqs, tickets):
         r = srv.wait(tk, grids[t][0].n_bus)
@@ -200,7 +203,44 @@ def serve(gox, rate: float, seconds: float) -> dict:
             "grids": len(spec), "buses": [int(min(x[0] for x in spec)), int(max(x[0] for x in spec))],
             "note": "Poisson arrivals of single scenarios over 16 grids (100-50,000 buses), 10 % "
                     "with an N-1 outage, gox_server_* continuous batching on 8 workers, mixed "
-                    "precision, host buffers, flat start"}
+                    "precision, host buffers, warm start from each grid's base case"}
+
+
+def n1_case10000(gox, rounds: int, batch: int = 8192) -> dict:
+    """N-1 leg: the 10,000-bus grid, `batch` scenarios, each with one
+    non-bridge branch out (4-slot Y delta) and loads x lognormal(0, 0.15),
+    warm started from the base case's solution, mixed precision with the
+    pivot-ratio check (a trip re-solves that scenario in FP64); host buffers."""
+    from gridoxide_gb300 import grids as G
+    g = G.config_grid("case10000")
+    yb = G.build_ybus(g)
+    topo = gox.Topology(yb, g.bus_type)
+    base = topo.solve(g.p_spec[None, :], g.q_spec[None, :], g.vm, g.va,
+                      precision=gox.GOX_PRECISION_FP64)
+    vm0, va0 = base.voltage_mag[0], base.voltage_ang[0]
+    p, q = G.load_scenarios(g, batch, 0.15, 2025)
+    rng = np.random.default_rng(2026)
+    br = rng.choice(np.flatnonzero(~G.bridges(g)), size=batch, replace=True)
+    out = G.outage_deltas(g, yb, br)
+
+    def one():
+        return topo.solve(p, q, vm0, va0, tol=WORKLOAD["tol"], max_iter=WORKLOAD["max_iter"],
+                          precision=gox.GOX_PRECISION_MIXED, outage=out)
+
+    res = one()  # warm-up
+    times = []
+    for _ in range(rounds):
+        t0 = time.perf_counter()
+        res = one()
+        times.append(time.perf_counter() - t0)
+    t = float(np.median(times))
+    return {"value": round(batch / t, 1), "unit": "solves/s", "scenarios": batch,
+            "ms_per_step": round(1000 * t, 2), "converged": int(np.sum(res.status == 0)),
+            "max_mismatch_converged": float(np.max(res.max_mismatch[res.status == 0])),
+            "iterations_hist": np.bincount(res.iterations).tolist(),
+            "fp64_fallbacks": int(topo.last_fallbacks()), "rounds": rounds,
+            "note": "case10000, one non-bridge branch out per scenario, warm start from the base "
+                    "case, mixed precision, host buffers (H2D/D2H inside the time)"}
 
 
 def many_topologies(gox, rounds: int) -> dict:
@@ -325,10 +365,10 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--serve-rate", type=float, default=2000.0,
+    ap.add_argument("--serve-rate", type=float, default=1000.0,
                     help="serving leg: Poisson arrivals per second (0 = skip)")
     ap.add_argument("--many-rounds", type=int, default=3,
-                    help="many-topology leg: timed rounds (0 = skip)")
+                    help="N-1 10,000-bus and many-topology legs: timed rounds (0 = skip)")
     ap.add_argument("--serve-seconds", type=float, default=1.0)
     ap.add_argument("--grid", default=WORKLOAD["grid"], help="profiling: another grid")
     ap.add_argument("--scenarios", type=int, default=WORKLOAD["scenarios"],
@@ -516,6 +556,7 @@ def main():
     if rank == 0 and args.serve_rate > 0 and not args.quick:
         line["serving"] = serve(gox, args.serve_rate, args.serve_seconds)
     if rank == 0 and args.many_rounds > 0 and not args.quick:
+        line["n1_case10000"] = n1_case10000(gox, args.many_rounds)
         line["many_topologies"] = many_topologies(gox, args.many_rounds)
     if rank == 0 and not args.no_cpu_baseline:
         threads = os.cpu_count() or 1
