@@ -27,7 +27,7 @@ inline int64_t tagof(int col, int rel) { return ((int64_t)col << 20) | rel; }
 enum { IT_LRUN = 0, IT_FWL = 1, IT_FWY = 2, IT_Y = 3, IT_D = 4, IT_U = 5, IT_X = 6 };
 enum { TK_COL = 0, TK_BWD = 1 };  // task kinds: a refactor column, a backward row
 enum { ST_NONE = 0, ST_GATHERED = 1, ST_RESIDENT = 2 };
-constexpr int kPieceRows = 27;  // longest L run piece placed as one block
+constexpr int kPieceRows = 27;  // longest L run piece placed as one block (large rings)
 
 // One value source of a column: a run of rows of another column's result.
 struct Item {
@@ -90,6 +90,7 @@ struct Builder {
   StreamPlan P;
   int W, R, n;
   int T = 0;  // rows of all rings
+  int piece = kPieceRows;  // longest L run piece: shorter with small rings, so two still fit
   int base(int w) const { return ring_base(P, w); }
   int rsize(int w) const { return ring_size(P, w); }
   std::vector<ColInfo> C;
@@ -132,6 +133,7 @@ struct Builder {
     W = p.nw;
     R = p.ring_rows;
     T = ring_total(p);
+    piece = std::max(9, std::min(kPieceRows, R / 6));
     n = s.n_u;
   }
 
@@ -908,13 +910,13 @@ struct Builder {
         const int e = sc.cu_ptr[k] + p;
         const int j = sc.cu_j[e];
         const int nl = sc.c_llen[j];
-        for (int d = 0; d < nl; d += kPieceRows) {
+        for (int d = 0; d < nl; d += piece) {
           Item it;
           it.kind = IT_LRUN;
           it.j = j;
           it.rel = sc.c_ulen[j] + 1 + d;
           it.src = sc.c_base[j] + it.rel;
-          it.nrows = std::min(kPieceRows, nl - d);
+          it.nrows = std::min(piece, nl - d);
           it.upos = p;
           it.dfirst = d;
           c.items.push_back(it);
