@@ -14,6 +14,8 @@ LIB_PATH = os.path.join(HERE, "libgridoxide_gb300.so")
 GOX_OK = 0
 GOX_SINGULAR = 1
 GOX_PENDING = 2
+GOX_GUESS_GIVEN = 0
+GOX_GUESS_LINEAR = 1
 GOX_E_OUT_OF_MEMORY = -2
 GOX_E_INVALID = -3
 GOX_E_BUS_RANGE = -4
@@ -82,6 +84,7 @@ SIGNATURES = {
     "gox_last_timing": (C.c_int, [vp, f64p]),
     "gox_last_launches": (C.c_int64, [vp]),
     "gox_set_pivot_tolerance": (C.c_int, [vp, C.c_double]),
+    "gox_topo_set_initial_guess": (C.c_int, [vp, C.c_int32]),
     "gox_last_fallbacks": (C.c_int64, [vp]),
     "gox_version": (C.c_char_p, []),
     "gox_server_create": (C.c_int, [C.c_int32, C.c_int32, C.c_double, C.c_int32, C.POINTER(vp)]),

@@ -470,6 +470,23 @@ struct IoStage {
   DevMem p, q, vm, va, ovm, ova, it, st, mm, h, sl, dre, dim;
 };
 
+// The linear initial guess system of a topology (src/network.rs:627-678),
+// built on first use: its pattern, first factor, streams and device buffers.
+struct GuessSys {
+  bool built = false, usable = false;
+  int m = 0, n2 = 0;
+  std::vector<int32_t> pq_bus;
+  Csc csc;
+  Symbolic sym;
+  Numeric num;
+  Schedule sc;
+  Stream s32, s64;
+  DevSchedule dsched;
+  DevMem yp, yi, yre, yim, rec, rhs_ptr, rhs_ej, pqb, pinv, qinv;
+  DevMem lu, off, rhs, sol, sing, piv, gact, err, gvm, gva;
+  GuessDev d{};
+};
+
 struct gox_topo {
   int n_bus = 0;
   std::vector<int32_t> yp, yi, bus_type;
@@ -492,6 +509,9 @@ struct gox_topo {
   // sends a scenario to FP64, and how many the last batch sent
   double piv_tol = 1e-6;
   int64_t fallbacks = 0;
+  // start point: 0 as given, 1 the linear initial guess from it
+  int guess_mode = 0;
+  GuessSys guess;
 };
 
 struct gox_ls {
@@ -648,6 +668,173 @@ static void run_iterations(gox_topo* t, BatchDev D, int max_iter, bool outage, c
 }
 
 // Core of both batch entry points: all arrays on the device.
+// Builds the guess system from scenario 0's injections (host arrays p0, q0):
+// the PQ buses, the 2x2 real blocks of Y' between them, the fixed neighbours
+// of each, the first factorization (partial pivoting) and its streams.
+static void guess_build(gox_topo* t, const double* p0, const double* q0) {
+  GuessSys& G = t->guess;
+  G.built = true;
+  G.usable = false;
+  const int n = t->n_bus;
+  std::vector<int32_t> rpos(n, -1);
+  G.pq_bus.clear();
+  for (int i = 0; i < n; i++)
+    if (t->bus_type[i] == 1) {
+      rpos[i] = (int)G.pq_bus.size();
+      G.pq_bus.push_back(i);
+    }
+  G.m = (int)G.pq_bus.size();
+  G.n2 = 2 * G.m;
+  if (G.m == 0) return;
+  std::vector<int32_t> rows, cols, rp(1, 0);
+  std::vector<int32_t> rec4;  // per triplet {part, Y entry, load bus, 0}
+  std::vector<int32_t> ej;
+  std::vector<double> vals;
+  auto block = [&](int r, int c, int e, int load) {
+    const double yr = (e >= 0 ? t->yre[e] : 0.0) + (load >= 0 ? -p0[load] : 0.0);
+    const double yi = (e >= 0 ? t->yim[e] : 0.0) + (load >= 0 ? q0[load] : 0.0);
+    const int rr[4] = {2 * r, 2 * r, 2 * r + 1, 2 * r + 1}, cc[4] = {2 * c, 2 * c + 1, 2 * c, 2 * c + 1};
+    const int part[4] = {0, 1, 2, 0};
+    const double v[4] = {yr, -yi, yi, yr};
+    for (int k = 0; k < 4; k++) {
+      rows.push_back(rr[k]);
+      cols.push_back(cc[k]);
+      vals.push_back(v[k]);
+      rec4.insert(rec4.end(), {part[k], e, load, 0});
+    }
+  };
+  for (int r = 0; r < G.m; r++) {
+    const int i = G.pq_bus[r];
+    bool diag = false;
+    for (int e = t->yp[i]; e < t->yp[i + 1]; e++) {
+      const int j = t->yi[e];
+      if (j == i) {
+        diag = true;
+        block(r, r, e, i);
+      } else if (rpos[j] >= 0) {
+        block(r, rpos[j], e, -1);
+      } else {
+        ej.insert(ej.end(), {e, j});
+      }
+    }
+    if (!diag) block(r, r, -1, i);
+    rp.push_back((int32_t)(ej.size() / 2));
+  }
+  const int nnz = (int)rows.size();
+  G.csc = build_csc(G.n2, nnz, rows.data(), cols.data());
+  G.sym = klu_analyze(G.n2, G.csc.p.data(), G.csc.i.data());
+  std::vector<double> packed(G.csc.nnz(), 0.0);
+  std::vector<int32_t> trip_of(G.csc.nnz(), -1);
+  for (int e = 0; e < nnz; e++) {
+    packed[G.csc.slot_of[e]] += vals[e];
+    trip_of[G.csc.slot_of[e]] = e;
+  }
+  if (klu_factor(G.csc, packed.data(), G.sym, 0.001, G.num) != 0) return;
+  build_schedule(nullptr, G.csc, G.sym, G.num, G.sc);
+  make_streams(G.sc, G.s32, G.s64);
+  std::vector<int32_t> dummy_p(1, 0), dummy_i;
+  std::vector<double> dummy_x;
+  G.dsched.load(G.sc, dummy_p, dummy_i, dummy_x, dummy_x);
+  G.dsched.load_streams(G.s32, G.s64);
+  // value recipe per LU slot, then per off-diagonal entry
+  const int ns = G.sc.n_slots, no = G.sc.n_off;
+  std::vector<int32_t> rec((size_t)(ns + no) * 4);
+  for (int x = 0; x < ns + no; x++) {
+    const int a = x < ns ? G.sc.slot_a[x] : G.sc.off_a[x - ns];
+    int32_t* r = &rec[(size_t)x * 4];
+    if (a < 0) {
+      r[0] = -1; r[1] = -1; r[2] = -1; r[3] = 0;
+      continue;
+    }
+    const int tr = trip_of[G.sc.a_csc[a]];
+    if (tr < 0) throw std::logic_error("guess system entry without a source");
+    for (int k = 0; k < 4; k++) r[k] = rec4[(size_t)tr * 4 + k];
+  }
+  std::vector<int32_t> pinv(G.n2), qinv(G.n2);
+  for (int k = 0; k < G.n2; k++) {
+    pinv[G.num.Pnum[k]] = k;
+    qinv[G.sym.Q[k]] = k;
+  }
+  upload(G.yp, t->yp);
+  upload(G.yi, t->yi);
+  upload(G.yre, t->yre);
+  upload(G.yim, t->yim);
+  upload(G.rec, rec);
+  upload(G.rhs_ptr, rp);
+  upload(G.rhs_ej, ej);
+  upload(G.pqb, G.pq_bus);
+  upload(G.pinv, pinv);
+  upload(G.qinv, qinv);
+  GuessDev& d = G.d;
+  d.n_bus = n; d.m = G.m; d.n2 = G.n2; d.n_slots = ns; d.n_off = no;
+  d.yp = G.yp.as<int32_t>(); d.yi = G.yi.as<int32_t>(); d.yre = G.yre.as<double>(); d.yim = G.yim.as<double>();
+  d.rec = reinterpret_cast<const int4*>(G.rec.p);
+  d.rhs_ptr = G.rhs_ptr.as<int32_t>();
+  d.rhs_ej = reinterpret_cast<const int2*>(G.rhs_ej.p);
+  d.pq_bus = G.pqb.as<int32_t>();
+  d.pinv = G.pinv.as<int32_t>();
+  d.qinv = G.qinv.as<int32_t>();
+  G.usable = true;
+}
+
+// The linear initial guess of B scenarios (device arrays, start voltages
+// vm0/va0 with stride v_stride): their start points in G.gvm / G.gva [B][N].
+// False when the topology has no PQ bus or its guess system is singular at
+// its first factorization (the start points then stay as given).
+static bool guess_run(gox_topo* t, int B, const double* p_spec, const double* q_spec,
+                      const double* vm0, const double* va0, int v_stride, const int32_t* o_slot,
+                      const double* o_dre, const double* o_dim, cudaStream_t st) {
+  GuessSys& G = t->guess;
+  const int n = t->n_bus;
+  if (!G.built) {
+    std::vector<double> p0(n), q0(n);
+    GOX_CK(cudaMemcpyAsync(p0.data(), p_spec, (size_t)n * 8, cudaMemcpyDeviceToHost, st));
+    GOX_CK(cudaMemcpyAsync(q0.data(), q_spec, (size_t)n * 8, cudaMemcpyDeviceToHost, st));
+    GOX_CK(cudaStreamSynchronize(st));
+    guess_build(t, p0.data(), q0.data());
+  }
+  if (!G.usable) return false;
+  const int Gr = (B + 31) / 32;
+  const SchedDev& S = G.dsched.d;
+  G.lu.ensure((size_t)Gr * S.n_slots * 32 * 8 + 8);
+  G.off.ensure((size_t)Gr * std::max(S.n_off, 1) * 32 * 8);
+  G.rhs.ensure((size_t)Gr * G.n2 * 32 * 8);
+  G.sol.ensure((size_t)Gr * G.n2 * 32 * 8);
+  G.sing.ensure((size_t)Gr * 32 * 4);
+  G.piv.ensure((size_t)Gr * 32 * 4);
+  G.gact.ensure((size_t)Gr * 4);
+  G.err.ensure(16);
+  G.gvm.ensure((size_t)B * n * 8);
+  G.gva.ensure((size_t)B * n * 8);
+  std::vector<int32_t> ones(Gr, 1);
+  GOX_CK(cudaMemcpyAsync(G.gact.p, ones.data(), ones.size() * 4, cudaMemcpyHostToDevice, st));
+  GOX_CK(cudaMemsetAsync(G.sing.p, 0, (size_t)Gr * 32 * 4, st));
+  GOX_CK(cudaMemsetAsync(G.err.p, 0, 16, st));
+  const int items = S.n_slots + S.n_off + G.m;
+  k_guess_fill<<<dim3((items + 7) / 8, Gr), 256, 0, st>>>(G.d, B, p_spec, q_spec, vm0, va0, v_stride,
+                                                          o_slot, o_dre, o_dim, G.lu.as<double>(),
+                                                          G.off.as<double>(), G.rhs.as<double>());
+  BatchDev D{};
+  D.G = Gr;
+  D.jbuf = G.lu.p; D.lu = G.lu.p; D.off = G.off.p; D.rhs = G.rhs.p; D.sol = G.sol.p;
+  D.sing = G.sing.as<int32_t>(); D.piv_flag = G.piv.as<int32_t>(); D.gact = G.gact.as<int32_t>();
+  D.piv_tol = 0.0f;
+  D.err = G.err.as<int32_t>();
+  Iter<double>::refactor(G.dsched, D, st);
+  Iter<double>::solve_rest(G.dsched, D, st);
+  k_guess_start<<<grid1d((size_t)B * n), 256, 0, st>>>(B, n, vm0, va0, v_stride, G.gvm.as<double>(),
+                                                       G.gva.as<double>());
+  k_guess_out<<<grid1d((size_t)B * G.m), 256, 0, st>>>(G.d, B, G.sol.as<double>(), G.sing.as<int32_t>(),
+                                                       G.gvm.as<double>(), G.gva.as<double>());
+  t->launches += 5;
+  int32_t werr = 0;
+  GOX_CK(cudaMemcpyAsync(&werr, G.err.p, 4, cudaMemcpyDeviceToHost, st));
+  GOX_CK(cudaStreamSynchronize(st));
+  GOX_CK(cudaGetLastError());
+  if (werr) throw std::runtime_error("a bounded device wait of the guess refactor gave up");
+  return true;
+}
+
 static int batch_device(gox_topo* t, int B, const double* p_spec, const double* q_spec,
                         const double* vm0, const double* va0, int v_stride,
                         const int32_t* o_slot, const double* o_dre, const double* o_dim,
@@ -659,6 +846,17 @@ static int batch_device(gox_topo* t, int B, const double* p_spec, const double* 
   const int n = t->n_bus;
   const int G = (B + 31) / 32;
   t->launches = 0;
+  // the linear initial guess replaces the start points (BatchSolver runs it
+  // before every scenario, src/batch.rs:268)
+  if (t->guess_mode == 1 &&
+      guess_run(t, B, p_spec, q_spec, vm0, va0, v_stride, o_slot, o_dre, o_dim, st)) {
+    vm0 = t->guess.gvm.as<double>();
+    va0 = t->guess.gva.as<double>();
+    v_stride = n;
+    h_vm = h_va = nullptr;
+    h_p = h_q = nullptr;  // the pivot search reads every input back from the device
+    h_oslot = nullptr; h_odre = nullptr; h_odim = nullptr;
+  }
   std::vector<int> first_singular;
   if (!t->factored) {
     // host copies of the inputs to find the pivot-fixing Jacobian
@@ -799,6 +997,8 @@ static int batch_device(gox_topo* t, int B, const double* p_spec, const double* 
       ovm.ensure(rows * 8); ova.ensure(rows * 8);
       oit.ensure((size_t)Bf * 4); ost.ensure((size_t)Bf * 4); omm.ensure((size_t)Bf * 8);
       if (want_hist) ohi.ensure((size_t)Bf * max_iter * 8);
+      const int gm = t->guess_mode;
+      t->guess_mode = 0;  // the start points are already the guessed ones
       const int rc = batch_device(
           t, Bf, fp.as<double>(), fq.as<double>(), vmf, vaf, v_stride,
           outage ? fsl.as<int32_t>() : nullptr, outage ? fdr.as<double>() : nullptr,
@@ -806,6 +1006,7 @@ static int batch_device(gox_topo* t, int B, const double* p_spec, const double* 
           ova.as<double>(), oit.as<int32_t>(), ost.as<int32_t>(), omm.as<double>(),
           want_hist ? ohi.as<double>() : nullptr, st, nullptr, nullptr, nullptr, nullptr, nullptr,
           nullptr, nullptr);
+      t->guess_mode = gm;
       if (rc != GOX_OK) return rc;
       k_put_rows<double><<<grid1d(rows), 256, 0, st>>>(ovm.as<double>(), n, ix, Bf, vm_out);
       k_put_rows<double><<<grid1d(rows), 256, 0, st>>>(ova.as<double>(), n, ix, Bf, va_out);
@@ -1249,6 +1450,12 @@ int gox_set_pivot_tolerance(gox_topo* t, double tol) {
 }
 
 int64_t gox_last_fallbacks(const gox_topo* t) { return t ? t->fallbacks : -1; }
+
+int gox_topo_set_initial_guess(gox_topo* t, int32_t mode) {
+  if (!t || (mode != GOX_GUESS_GIVEN && mode != GOX_GUESS_LINEAR)) return GOX_E_INVALID;
+  t->guess_mode = mode;
+  return GOX_OK;
+}
 
 // ---- LinearSolver level ----------------------------------------------------
 

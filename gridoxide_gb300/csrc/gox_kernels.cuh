@@ -999,6 +999,120 @@ done:
 }
 
 // ---------------------------------------------------------------------------
+// Linear initial guess (src/network.rs:627-678).  The PQ buses' voltages U_n
+// solve Y'_nn U_n = -Y'_ns U_s, where Y' is the Y-bus with -conj(S_i) added
+// on the diagonal of each PQ bus i (its injection as a constant admittance
+// at |V| = 1) and U_s the fixed voltages of the other buses.  The complex
+// system is solved as the real one with the block [[Re, -Im], [Im, Re]] per
+// entry (unknowns Re U_r, Im U_r at 2r, 2r + 1), refactored in FP64 with the
+// pivot order of its first factorization.
+struct GuessDev {
+  int n_bus, m, n2, n_slots, n_off;
+  const int32_t *yp, *yi;
+  const double *yre, *yim;
+  // per LU slot, then per off-diagonal entry: {part (-1: zero fill-in, 0: Re,
+  // 1: -Im, 2: Im), Y entry (-1: none), PQ bus of the load term (-1: none), 0}
+  const int4* rec;
+  const int32_t* rhs_ptr;  // [m + 1]: per PQ row, its neighbours of fixed voltage
+  const int2* rhs_ej;      // {Y entry, bus}
+  const int32_t* pq_bus;   // [m]
+  const int32_t* pinv;     // [n2]: factor row of real equation q
+  const int32_t* qinv;     // [n2]: factor column of real unknown u
+};
+
+// Y entry e of scenario s, with its outage delta (the scenario's four Y slots)
+__device__ __forceinline__ void guess_y(const GuessDev& L, int e, const int32_t* os, const double* odr,
+                                        const double* odi, double& yr, double& yi) {
+  yr = e >= 0 ? L.yre[e] : 0.0;
+  yi = e >= 0 ? L.yim[e] : 0.0;
+  if (os && e >= 0)
+    for (int c = 0; c < 4; c++)
+      if (os[c] == e) {
+        yr += odr[c];
+        yi += odi[c];
+      }
+}
+
+// Values of the guess system in its factor's layout and its right-hand side
+// in pivot order, per scenario (lane).  grid (ceil(items / 8), G): a warp per
+// item, the LU slots and off-diagonal entries, then the PQ rows.
+__global__ void __launch_bounds__(256) k_guess_fill(GuessDev L, int B, const double* __restrict__ p,
+                                                     const double* __restrict__ q,
+                                                     const double* __restrict__ vm0,
+                                                     const double* __restrict__ va0, int v_stride,
+                                                     const int32_t* __restrict__ o_slot,
+                                                     const double* __restrict__ o_dre,
+                                                     const double* __restrict__ o_dim, double* lu,
+                                                     double* off, double* rhs) {
+  const int g = blockIdx.y, lane = threadIdx.x & 31;
+  const int item = blockIdx.x * 8 + (threadIdx.x >> 5);
+  const int s = min(g * 32 + lane, B - 1);
+  const int N = L.n_bus;
+  const int32_t* os = o_slot ? o_slot + 4 * s : nullptr;
+  const double* odr = o_slot ? o_dre + 4 * s : nullptr;
+  const double* odi = o_slot ? o_dim + 4 * s : nullptr;
+  if (os && os[0] < 0) os = nullptr;
+  const int nv = L.n_slots + L.n_off;
+  if (item < nv) {
+    const int4 r = __ldg(L.rec + item);
+    double v = 0.0;
+    if (r.x >= 0) {
+      double yr, yi;
+      guess_y(L, r.y, os, odr, odi, yr, yi);
+      if (r.z >= 0) {  // + (-conj(p + jq)) = -p + jq
+        yr -= p[(size_t)s * N + r.z];
+        yi += q[(size_t)s * N + r.z];
+      }
+      v = r.x == 0 ? yr : (r.x == 1 ? -yi : yi);
+    }
+    if (item < L.n_slots) lu[((size_t)g * L.n_slots + item) * 32 + lane] = v;
+    else off[((size_t)g * L.n_off + (item - L.n_slots)) * 32 + lane] = v;
+    return;
+  }
+  const int r = item - nv;
+  if (r >= L.m) return;
+  double ar = 0.0, ai = 0.0;  // sum of Y_ij U_j over the fixed neighbours
+  for (int t = __ldg(L.rhs_ptr + r); t < __ldg(L.rhs_ptr + r + 1); t++) {
+    const int2 ej = __ldg(L.rhs_ej + t);
+    double yr, yi;
+    guess_y(L, ej.x, os, odr, odi, yr, yi);
+    const size_t xv = (size_t)s * v_stride + ej.y;
+    double sn, cs;
+    sincos(va0[xv], &sn, &cs);
+    const double ur = vm0[xv] * cs, ui = vm0[xv] * sn;
+    ar += yr * ur - yi * ui;
+    ai += yr * ui + yi * ur;
+  }
+  rhs[((size_t)g * L.n2 + __ldg(L.pinv + 2 * r)) * 32 + lane] = -ar;
+  rhs[((size_t)g * L.n2 + __ldg(L.pinv + 2 * r + 1)) * 32 + lane] = -ai;
+}
+
+// The start point: every bus's given voltage, then the PQ buses' solution
+// where the scenario's guess system was regular and the solution finite
+// (else they keep the given one, as the reference does when its solve fails).
+__global__ void k_guess_start(int B, int N, const double* __restrict__ vm0,
+                              const double* __restrict__ va0, int v_stride, double* gvm, double* gva) {
+  const size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= (size_t)B * N) return;
+  const size_t s = i / N, b = i % N;
+  gvm[i] = vm0[s * v_stride + b];
+  gva[i] = va0[s * v_stride + b];
+}
+__global__ void k_guess_out(GuessDev L, int B, const double* __restrict__ sol,
+                            const int32_t* __restrict__ sing, double* gvm, double* gva) {
+  const size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= (size_t)B * L.m) return;
+  const int s = (int)(i / L.m), r = (int)(i % L.m);
+  const int g = s / 32, lane = s % 32;
+  const double re = sol[((size_t)g * L.n2 + __ldg(L.qinv + 2 * r)) * 32 + lane];
+  const double im = sol[((size_t)g * L.n2 + __ldg(L.qinv + 2 * r + 1)) * 32 + lane];
+  if (sing[s] != 0 || !isfinite(re) || !isfinite(im)) return;
+  const size_t x = (size_t)s * L.n_bus + __ldg(L.pq_bus + r);
+  gvm[x] = hypot(re, im);
+  gva[x] = atan2(im, re);
+}
+
+// ---------------------------------------------------------------------------
 // K4: substitution phases (dependency levels), one CTA per group.  Forward
 // phases (kind 0) fold the off-diagonal terms of later BTF blocks into the
 // right-hand side; backward phases (kind 1) divide by U(k,k).

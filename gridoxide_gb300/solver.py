@@ -325,6 +325,13 @@ class Topology:
         """Scenarios of the last solve that were solved again in FP64."""
         return int(_lib.load().gox_last_fallbacks(self._h))
 
+    def set_initial_guess(self, mode: str) -> None:
+        """Start point of the batched solves: "given" (vm0/va0 as passed) or
+        "linear" (the reference BatchSolver's linear initial guess from them,
+        src/network.rs:627-678, on the GPU)."""
+        code = {"given": _lib.GOX_GUESS_GIVEN, "linear": _lib.GOX_GUESS_LINEAR}[mode]
+        check(_lib.load().gox_topo_set_initial_guess(self._h, code), "gox_topo_set_initial_guess")
+
     def __del__(self):
         try:
             if self._h:

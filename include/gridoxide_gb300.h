@@ -237,6 +237,21 @@ int gox_last_timing(const gox_topo *t, double *out);
 /* Kernel launches issued by the last gox_batch_solve* call. */
 int64_t gox_last_launches(const gox_topo *t);
 
+/* Start point of the batched solves.  GOX_GUESS_GIVEN (default): the
+ * vm0/va0 passed to the call.  GOX_GUESS_LINEAR: the reference BatchSolver's
+ * linear initial guess (src/batch.rs:268 -> linear_initial_guess,
+ * src/network.rs:627-678) computed from them on the GPU: the PQ buses'
+ * voltages solve Y'_nn U_n = -Y'_ns U_s, where Y' adds -conj(p + jq) to the
+ * diagonal of every PQ bus and U_s are the given voltages of the other buses
+ * (a scenario whose system is singular keeps its given start).  The complex
+ * system is solved as its real 2x2-block form, refactored in FP64 with the
+ * pivot order of its first factorization (the reference's faer complex LU,
+ * src/sparse.rs:48-63, pivots per call; the results agree to rounding).
+ * With an outage the guess uses the scenario's modified Y-bus. */
+#define GOX_GUESS_GIVEN 0
+#define GOX_GUESS_LINEAR 1
+int gox_topo_set_initial_guess(gox_topo *t, int32_t mode);
+
 /* Mixed path: the pivot-ratio threshold.  A scenario whose FP32 refactor
  * meets a pivot with |u_kk| < tol * max |L(:, k)| (before scaling) is solved
  * again from its start point on the FP64 path, with the same pivot order,

@@ -359,3 +359,60 @@ class RefKLU:
             self.R.ref_free(self.h)
         except Exception:
             pass
+
+
+def linear_initial_guess(yb, bus_type, p_spec, q_spec, vm, va):
+    """Restatement of the reference's linear_initial_guess
+    (src/network.rs:627-678) for one scenario: returns (vm, va) with the PQ
+    buses' voltages replaced by the solution of Y'_nn U_n = -Y'_ns U_s, where
+    Y' adds y_load = -conj(p + jq) to the diagonal of each PQ bus (:656-657)
+    and U_s = from_polar(vm, va) of every other bus moves to the right-hand
+    side (:666-669); a bus without a diagonal Y entry gets y_load alone
+    (:673-675).  The reference solves the complex system with faer's sparse
+    LU (src/sparse.rs:48-63, faer 0.24.4, not vendored); scipy's splu
+    stands in for it (results agree to rounding, not bit for bit).  A
+    singular or non-finite solve leaves the voltages as they were
+    (:677-678, sparse.rs:58-61)."""
+    import scipy.sparse as sp
+    import scipy.sparse.linalg as spla
+
+    vm = np.array(vm, dtype=np.float64)
+    va = np.array(va, dtype=np.float64)
+    n = yb.n
+    unknown = [i for i in range(n) if int(bus_type[i]) == 1]
+    if not unknown:
+        return vm, va
+    m = len(unknown)
+    pos = -np.ones(n, dtype=np.int64)
+    pos[unknown] = np.arange(m)
+    rows, cols, vals = [], [], []
+    rhs = np.zeros(m, dtype=np.complex128)
+    for r, i in enumerate(unknown):
+        y_load = -np.conj(complex(p_spec[i], q_spec[i]))
+        diag_seen = False
+        for e in range(int(yb.indptr[i]), int(yb.indptr[i + 1])):
+            j = int(yb.indices[e])
+            y = complex(yb.re[e], yb.im[e])
+            if j == i:
+                diag_seen = True
+                y = y + y_load
+            if pos[j] >= 0:
+                rows.append(r)
+                cols.append(int(pos[j]))
+                vals.append(y)
+            else:
+                rhs[r] -= y * (vm[j] * complex(np.cos(va[j]), np.sin(va[j])))
+        if not diag_seen:
+            rows.append(r)
+            cols.append(r)
+            vals.append(y_load)
+    a = sp.csc_matrix((np.array(vals), (rows, cols)), shape=(m, m))
+    try:
+        sol = spla.splu(a).solve(rhs)
+    except RuntimeError:
+        return vm, va
+    if not np.all(np.isfinite(sol)):
+        return vm, va
+    vm[unknown] = np.abs(sol)
+    va[unknown] = np.angle(sol)
+    return vm, va

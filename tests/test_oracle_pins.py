@@ -45,6 +45,25 @@ def test_network3_snapshot(oracle_mod):
         assert abs(res["va"][0][i] - va) < 1e-5
 
 
+def test_network3_snapshot_linear_guess(oracle_mod):
+    """The reference's own setup for the snapshot: the linear initial guess
+    (src/network.rs:627-678) before NR, tol 1e-6."""
+    O = oracle_mod
+    fx = load_fixture("network3")
+    lines = [(int(a), int(b), r, x, bb) for a, b, r, x, bb in [tuple(r) for r in fx["lines"]]]
+    yb = G.ybus_from_lines(3, lines)
+    vm0, va0 = O.linear_initial_guess(yb, fx["bus_type"], fx["p_spec"], fx["q_spec"], fx["vm"], fx["va"])
+    assert vm0[0] == fx["vm"][0] and vm0[1] == fx["vm"][1]  # slack and PV keep their voltage
+    topo = oracle_topology(O, yb, fx["bus_type"], _ordering_for(O, yb, fx["bus_type"]))
+    res = topo.batch_solve(fx["p_spec"][None], fx["q_spec"][None], vm0[None], va0[None], tol=1e-6,
+                           max_iter=20)
+    expected = [(1.06, 0.0), (1.04, 0.014349), (1.003358, -0.043141)]
+    assert res["status"][0] == 0
+    for i, (vm, va) in enumerate(expected):
+        assert abs(res["vm"][0][i] - vm) < 1e-5
+        assert abs(res["va"][0][i] - va) < 1e-5
+
+
 def _mixed_network():
     """jacobian.rs:300-333: bus 0 Slack, bus 1 PV, buses 2-4 PQ."""
     bus_type = np.array([G.BUS_SLACK, G.BUS_PV, G.BUS_PQ, G.BUS_PQ, G.BUS_PQ], np.int32)
