@@ -426,7 +426,7 @@ __global__ void __launch_bounds__(256) k_fill(SchedDev S, BatchDev D, int tw, in
   if (OUTAGE && D.o_bf[s] >= 0) {
     os0 = D.o_slot[4 * s]; os1 = D.o_slot[4 * s + 1]; os2 = D.o_slot[4 * s + 2]; os3 = D.o_slot[4 * s + 3];
   }
-  constexpr int U = 4;  // tasks in flight per warp
+  constexpr int U = 2;  // tasks in flight per warp (2: 48 registers, more warps per SM than 4 in flight)
   for (int ta = t0; ta < t1; ta += U) {
     int4 dst[U], bus[U];
     T G[U], B[U], v[U][5];
