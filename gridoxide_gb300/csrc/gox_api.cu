@@ -512,6 +512,15 @@ struct gox_topo {
   // start point: 0 as given, 1 the linear initial guess from it
   int guess_mode = 0;
   GuessSys guess;
+  // ZIP terms of the effective injection ([4][n]; empty: constant power only)
+  std::vector<double> zip;
+  DevMem dzip;
+  double eff(int part, int i, double s, double vm) const {
+    if (zip.empty()) return s;
+    s += zip[(size_t)part * n_bus + i] * vm * vm;
+    s += zip[(size_t)(2 + part) * n_bus + i] * vm;
+    return s;
+  }
 };
 
 struct gox_ls {
@@ -577,11 +586,11 @@ static int fix_pivots(gox_topo* t, int B, const double* p_spec, const double* q_
     double mx = 0.0;
     for (int a = 0; a < t->jac.n_ang; a++) {
       int i = t->jac.ns_idx[a];
-      mx = std::fmax(mx, std::fabs(p_spec[(size_t)s * n + i] - p[i]));
+      mx = std::fmax(mx, std::fabs(t->eff(0, i, p_spec[(size_t)s * n + i], vm[i]) - p[i]));
     }
     for (int a = 0; a < t->jac.n_pq; a++) {
       int i = t->jac.pq_idx[a];
-      mx = std::fmax(mx, std::fabs(q_spec[(size_t)s * n + i] - q[i]));
+      mx = std::fmax(mx, std::fabs(t->eff(1, i, q_spec[(size_t)s * n + i], vm[i]) - q[i]));
     }
     if (mx < tol) continue;
     host_jac_fill(t->jac, yre.data(), yim.data(), vm, va, p.data(), q.data(), vals.data());
@@ -846,6 +855,9 @@ static int batch_device(gox_topo* t, int B, const double* p_spec, const double* 
   const int n = t->n_bus;
   const int G = (B + 31) / 32;
   t->launches = 0;
+  const double* zipd = t->zip.empty() ? nullptr : t->dzip.as<double>();
+  t->dsched.d.zip = zipd;
+  t->guess.d.zip = zipd;
   // the linear initial guess replaces the start points (BatchSolver runs it
   // before every scenario, src/batch.rs:268)
   if (t->guess_mode == 1 &&
@@ -1172,8 +1184,14 @@ static void host_only_result(gox_topo* t, int B, const double* p_spec, const dou
       for (int c = 0; c < 4; c++) { yre[o_slot[4 * s + c]] += o_dre[4 * s + c]; yim[o_slot[4 * s + c]] += o_dim[4 * s + c]; }
     host_injections(n, t->yp.data(), t->yi.data(), yre.data(), yim.data(), vm, va, p.data(), q.data());
     double mx = 0.0;
-    for (int a = 0; a < t->jac.n_ang; a++) { int i = t->jac.ns_idx[a]; mx = std::fmax(mx, std::fabs(p_spec[(size_t)s * n + i] - p[i])); }
-    for (int a = 0; a < t->jac.n_pq; a++) { int i = t->jac.pq_idx[a]; mx = std::fmax(mx, std::fabs(q_spec[(size_t)s * n + i] - q[i])); }
+    for (int a = 0; a < t->jac.n_ang; a++) {
+      const int i = t->jac.ns_idx[a];
+      mx = std::fmax(mx, std::fabs(t->eff(0, i, p_spec[(size_t)s * n + i], vm[i]) - p[i]));
+    }
+    for (int a = 0; a < t->jac.n_pq; a++) {
+      const int i = t->jac.pq_idx[a];
+      mx = std::fmax(mx, std::fabs(t->eff(1, i, q_spec[(size_t)s * n + i], vm[i]) - q[i]));
+    }
     iters[s] = 1;
     max_mis[s] = mx;
     if (hist) hist[(size_t)s * max_iter] = mx;
@@ -1450,6 +1468,28 @@ int gox_set_pivot_tolerance(gox_topo* t, double tol) {
 }
 
 int64_t gox_last_fallbacks(const gox_topo* t) { return t ? t->fallbacks : -1; }
+
+int gox_topo_set_zip(gox_topo* t, const double* zi_re, const double* zi_im, const double* zc_re,
+                     const double* zc_im) {
+  if (!t) return GOX_E_INVALID;
+  const bool none = !zi_re && !zi_im && !zc_re && !zc_im;
+  if (!none && (!zi_re || !zi_im || !zc_re || !zc_im)) return GOX_E_INVALID;
+  return guard_impl([&]() -> int {
+    const size_t n = (size_t)t->n_bus;
+    if (none) {
+      t->zip.clear();
+      return GOX_OK;
+    }
+    t->zip.resize(4 * n);
+    std::copy(zi_re, zi_re + n, t->zip.begin());
+    std::copy(zi_im, zi_im + n, t->zip.begin() + n);
+    std::copy(zc_re, zc_re + n, t->zip.begin() + 2 * n);
+    std::copy(zc_im, zc_im + n, t->zip.begin() + 3 * n);
+    if (int r = require_device()) return r;
+    upload(t->dzip, t->zip);
+    return GOX_OK;
+  });
+}
 
 int gox_topo_set_initial_guess(gox_topo* t, int32_t mode) {
   if (!t || (mode != GOX_GUESS_GIVEN && mode != GOX_GUESS_LINEAR)) return GOX_E_INVALID;

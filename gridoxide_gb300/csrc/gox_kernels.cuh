@@ -50,7 +50,20 @@ struct SchedDev {
   const int32_t* fz_slot;
   const int32_t *ph_ptr, *ph_rows, *ph_kind, *fw_ptr, *fw_slot, *fw_col, *bw_ptr, *bw_slot,
       *bw_col, *diag_slot;
+  // ZIP terms of the effective injection, or null: [4][n_bus] constant-
+  // impedance re, im, constant-current re, im (per unit at |V| = 1)
+  const double* zip;
 };
+
+// effective_injection (src/network.rs:600-611): s = p + jq, then + s_imp |V|
+// |V| and + s_cur |V|, at the bus's present |V|
+__device__ __forceinline__ double eff_inj(const double* zip, int nb, int i, int part, double s,
+                                          double vm) {
+  if (zip == nullptr) return s;
+  s += zip[(size_t)part * nb + i] * vm * vm;
+  s += zip[(size_t)(2 + part) * nb + i] * vm;
+  return s;
+}
 
 struct BatchDev {
   int G;          // groups of 32 scenarios
@@ -285,7 +298,7 @@ __global__ void __launch_bounds__(256) k_inject(SchedDev S, BatchDev D, int it) 
       // row have Jacobian entries that use them; a PV bus's Q comes from
       // the products, it has no Q row)
       if (rp >= 0) {
-        const double psp = D.psp[x];
+        const double psp = eff_inj(S.zip, N, i, 0, D.psp[x], D.vm[x]);
         const double FP = fma(-fi, ii, fma(-ei, ir, psp));
         const float fp = f32_rn(FP);
         if (active) {
@@ -294,7 +307,7 @@ __global__ void __launch_bounds__(256) k_inject(SchedDev S, BatchDev D, int it) 
         }
         ((float*)D.pT)[x] = f32_rn(psp) - fp;
         if (rq >= 0) {
-          const double qsp = D.qsp[x];
+          const double qsp = eff_inj(S.zip, N, i, 1, D.qsp[x], D.vm[x]);
           const double FQ = fma(ei, ii, fma(-fi, ir, qsp));
           const float fq = f32_rn(FQ);
           if (active) {
@@ -311,12 +324,12 @@ __global__ void __launch_bounds__(256) k_inject(SchedDev S, BatchDev D, int it) 
       const double qc = fi * ir - ei * ii;
       if (active) {
         if (rp >= 0) {
-          const double F = D.psp[x] - pc;
+          const double F = eff_inj(S.zip, N, i, 0, D.psp[x], D.vm[x]) - pc;
           mx = max(mx, abs_bits(F));
           rhs[gidx(g, S.n_u, rp, lane)] = (T)F;
         }
         if (rq >= 0) {
-          const double F = D.qsp[x] - qc;
+          const double F = eff_inj(S.zip, N, i, 1, D.qsp[x], D.vm[x]) - qc;
           mx = max(mx, abs_bits(F));
           rhs[gidx(g, S.n_u, rq, lane)] = (T)F;
         }
@@ -1018,6 +1031,7 @@ struct GuessDev {
   const int32_t* pq_bus;   // [m]
   const int32_t* pinv;     // [n2]: factor row of real equation q
   const int32_t* qinv;     // [n2]: factor column of real unknown u
+  const double* zip;       // ZIP terms as in SchedDev, or null
 };
 
 // Y entry e of scenario s, with its outage delta (the scenario's four Y slots)
@@ -1059,9 +1073,10 @@ __global__ void __launch_bounds__(256) k_guess_fill(GuessDev L, int B, const dou
     if (r.x >= 0) {
       double yr, yi;
       guess_y(L, r.y, os, odr, odi, yr, yi);
-      if (r.z >= 0) {  // + (-conj(p + jq)) = -p + jq
-        yr -= p[(size_t)s * N + r.z];
-        yi += q[(size_t)s * N + r.z];
+      if (r.z >= 0) {  // + (-conj(p + jq)) = -p + jq, the effective injection at the start |V|
+        const double v = vm0[(size_t)s * v_stride + r.z];
+        yr -= eff_inj(L.zip, N, r.z, 0, p[(size_t)s * N + r.z], v);
+        yi += eff_inj(L.zip, N, r.z, 1, q[(size_t)s * N + r.z], v);
       }
       v = r.x == 0 ? yr : (r.x == 1 ? -yi : yi);
     }

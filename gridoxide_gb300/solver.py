@@ -325,6 +325,20 @@ class Topology:
         """Scenarios of the last solve that were solved again in FP64."""
         return int(_lib.load().gox_last_fallbacks(self._h))
 
+    def set_zip(self, imp=None, cur=None) -> None:
+        """ZIP terms of the effective injection (src/network.rs:600-611): per
+        bus complex constant-impedance and constant-current injections (per
+        unit at |V| = 1), added as imp |V|^2 + cur |V| to p_spec + j q_spec in
+        every mismatch; None for both clears them."""
+        L = _lib.load()
+        if imp is None and cur is None:
+            check(L.gox_topo_set_zip(self._h, None, None, None, None), "gox_topo_set_zip")
+            return
+        imp = np.zeros(self.n_bus, np.complex128) if imp is None else np.asarray(imp, np.complex128)
+        cur = np.zeros(self.n_bus, np.complex128) if cur is None else np.asarray(cur, np.complex128)
+        a = [_f64(imp.real), _f64(imp.imag), _f64(cur.real), _f64(cur.imag)]
+        check(L.gox_topo_set_zip(self._h, *[_p(x, _lib.f64p) for x in a]), "gox_topo_set_zip")
+
     def set_initial_guess(self, mode: str) -> None:
         """Start point of the batched solves: "given" (vm0/va0 as passed) or
         "linear" (the reference BatchSolver's linear initial guess from them,

@@ -248,6 +248,17 @@ int64_t gox_last_launches(const gox_topo *t);
  * pivot order of its first factorization (the reference's faer complex LU,
  * src/sparse.rs:48-63, pivots per call; the results agree to rounding).
  * With an outage the guess uses the scenario's modified Y-bus. */
+/* ZIP terms of the effective injection (src/network.rs:600-611): per bus a
+ * constant-impedance and a constant-current complex injection (per unit at
+ * |V| = 1, each the sum of that bus's terms of the kind), added to the
+ * scenario's p_spec + j q_spec as s_imp |V| |V| + s_cur |V| at the present
+ * |V| in every mismatch (and in the linear initial guess).  As in the
+ * reference they are not differentiated in the Jacobian (src/jacobian.rs:
+ * 224-243 uses only the computed injections).  Arrays [n_bus]; all four
+ * NULL clears them. */
+int gox_topo_set_zip(gox_topo *t, const double *zi_re, const double *zi_im, const double *zc_re,
+                     const double *zc_im);
+
 #define GOX_GUESS_GIVEN 0
 #define GOX_GUESS_LINEAR 1
 int gox_topo_set_initial_guess(gox_topo *t, int32_t mode);

@@ -784,6 +784,7 @@ struct gxo_topo {
     int nblocks;
     int32_t *ns_idx, *pq_idx;
     int n_ang, n_pq;
+    double *zip; /* NULL, or [4][n]: impedance re, im; current re, im (per unit at |V| = 1) */
 };
 
 gxo_topo *gxo_topo_new(int n, const int32_t *yp, const int32_t *yi, const double *yre,
@@ -823,8 +824,41 @@ gxo_topo *gxo_topo_new(int n, const int32_t *yp, const int32_t *yi, const double
     return t;
 }
 
+/* ZIP terms of effective_injection (src/network.rs:600-611): per bus one
+ * constant-impedance and one constant-current term (each the sum of the bus's
+ * terms of that kind); NULL clears them. */
+void gxo_topo_set_zip(gxo_topo *t, const double *zi_re, const double *zi_im, const double *zc_re,
+                      const double *zc_im) {
+    free(t->zip);
+    t->zip = NULL;
+    if (!zi_re) return;
+    t->zip = (double *)xmalloc(sizeof(double) * 4 * (size_t)t->n);
+    memcpy(t->zip, zi_re, sizeof(double) * t->n);
+    memcpy(t->zip + t->n, zi_im, sizeof(double) * t->n);
+    memcpy(t->zip + 2 * t->n, zc_re, sizeof(double) * t->n);
+    memcpy(t->zip + 3 * t->n, zc_im, sizeof(double) * t->n);
+}
+
+/* effective_injection (src/network.rs:600-611): s = p + jq; s += s_imp * |V|
+ * * |V| (constant impedance); s += s_cur * |V| (constant current). */
+static double eff_p(const gxo_topo *t, int i, double p, double vm) {
+    if (!t->zip) return p;
+    double s = p;
+    s += t->zip[i] * vm * vm;
+    s += t->zip[2 * t->n + i] * vm;
+    return s;
+}
+static double eff_q(const gxo_topo *t, int i, double q, double vm) {
+    if (!t->zip) return q;
+    double s = q;
+    s += t->zip[t->n + i] * vm * vm;
+    s += t->zip[3 * t->n + i] * vm;
+    return s;
+}
+
 void gxo_topo_free(gxo_topo *t) {
     if (!t) return;
+    free(t->zip);
     free(t->yp); free(t->yi); free(t->yre); free(t->yim); free(t->bus_type);
     gxo_jac_free(t->jac);
     free(t->P); free(t->Q); free(t->R); free(t->ns_idx); free(t->pq_idx);
@@ -849,11 +883,11 @@ int gxo_nr_solve(gxo_topo *t, gxo_lu **cache, const double *yre, const double *y
         int m = 0;
         for (int a = 0; a < t->n_ang; a++) {
             int i = t->ns_idx[a];
-            mis[m++] = p_spec[i] - p[i];
+            mis[m++] = eff_p(t, i, p_spec[i], vm[i]) - p[i];
         }
         for (int a = 0; a < t->n_pq; a++) {
             int i = t->pq_idx[a];
-            mis[m++] = q_spec[i] - q[i];
+            mis[m++] = eff_q(t, i, q_spec[i], vm[i]) - q[i];
         }
         /* fold(0.0, |a, b| a.max(b.abs())); f64::max and fmax both skip NaN */
         double mx = 0.0;

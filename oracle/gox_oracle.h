@@ -7,7 +7,7 @@
  *
  *   Y-bus stamping        gridoxide src/network.rs:225-247, 339-373
  *   power_injections      src/network.rs:680-701 (+ faer SpMV, src/sparse.rs:32-36)
- *   effective_injection   src/network.rs:600-611 (constant-power buses)
+ *   effective_injection   src/network.rs:600-611 (constant power + ZIP terms)
  *   JacobianPattern       src/jacobian.rs:96-171 (analyze), 202-250 (fill)
  *   build_csc_structure   src/klu_native/mod.rs:88-125
  *   KLU numeric factor    src/klu_native/factor.rs:47-131, kernel.rs:32-416
@@ -84,6 +84,9 @@ gxo_topo *gxo_topo_new(int n, const int32_t *yp, const int32_t *yi, const double
                        const double *yim, const int32_t *bus_type, const int32_t *P,
                        const int32_t *Q, const int32_t *R, int nblocks);
 void gxo_topo_free(gxo_topo *t);
+/* ZIP terms of effective_injection (src/network.rs:600-611), [n] each; NULL clears. */
+void gxo_topo_set_zip(gxo_topo *t, const double *zi_re, const double *zi_im, const double *zc_re,
+                      const double *zc_im);
 
 /* newton_raphson_cached for one scenario.  *cache holds the worker's
  * persistent LU (created on the first Jacobian it sees).  yre/yim: this

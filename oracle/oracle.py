@@ -84,6 +84,7 @@ def lib():
         L.gxo_topo_new.argtypes = [C.c_int, _i32p, _i32p, _f64p, _f64p, _i32p, _i32p, _i32p,
                                    _i32p, C.c_int]
         L.gxo_topo_free.argtypes = [C.c_void_p]
+        L.gxo_topo_set_zip.argtypes = [C.c_void_p, _f64p, _f64p, _f64p, _f64p]
         L.gxo_nr_solve.restype = C.c_int
         L.gxo_nr_solve.argtypes = [C.c_void_p, C.POINTER(C.c_void_p), _f64p, _f64p, _f64p, _f64p,
                                    _f64p, _f64p, C.c_double, C.c_int, _f64p, C.POINTER(C.c_int)]
@@ -225,6 +226,18 @@ class Topology:
                                      _p(_i32(bus_type), _i32p), _p(_i32(P), _i32p),
                                      _p(_i32(Q), _i32p), _p(_i32(R), _i32p), len(R) - 1)
 
+    def set_zip(self, imp=None, cur=None):
+        """ZIP terms of effective_injection (src/network.rs:600-611): per bus
+        a constant-impedance and a constant-current complex injection (per
+        unit at |V| = 1); None clears both."""
+        if imp is None and cur is None:
+            self.L.gxo_topo_set_zip(self.h, None, None, None, None)
+            return
+        imp = np.zeros(self.n, np.complex128) if imp is None else np.asarray(imp, np.complex128)
+        cur = np.zeros(self.n, np.complex128) if cur is None else np.asarray(cur, np.complex128)
+        self._zip = [_f64(imp.real), _f64(imp.imag), _f64(cur.real), _f64(cur.imag)]
+        self.L.gxo_topo_set_zip(self.h, *[_p(a, _f64p) for a in self._zip])
+
     def batch_solve(self, p_spec, q_spec, vm0, va0, tol=1e-8, max_iter=20, threads=1,
                     outage=None, history=False):
         """BatchSolver::solve restated.  p_spec/q_spec [B, N]; vm0/va0 [N] (shared)
@@ -361,7 +374,7 @@ class RefKLU:
             pass
 
 
-def linear_initial_guess(yb, bus_type, p_spec, q_spec, vm, va):
+def linear_initial_guess(yb, bus_type, p_spec, q_spec, vm, va, zip_imp=None, zip_cur=None):
     """Restatement of the reference's linear_initial_guess
     (src/network.rs:627-678) for one scenario: returns (vm, va) with the PQ
     buses' voltages replaced by the solution of Y'_nn U_n = -Y'_ns U_s, where
@@ -388,7 +401,12 @@ def linear_initial_guess(yb, bus_type, p_spec, q_spec, vm, va):
     rows, cols, vals = [], [], []
     rhs = np.zeros(m, dtype=np.complex128)
     for r, i in enumerate(unknown):
-        y_load = -np.conj(complex(p_spec[i], q_spec[i]))
+        s_eff = complex(p_spec[i], q_spec[i])  # effective_injection at the bus's |V|
+        if zip_imp is not None:
+            s_eff += complex(zip_imp[i]) * vm[i] * vm[i]
+        if zip_cur is not None:
+            s_eff += complex(zip_cur[i]) * vm[i]
+        y_load = -np.conj(s_eff)
         diag_seen = False
         for e in range(int(yb.indptr[i]), int(yb.indptr[i + 1])):
             j = int(yb.indices[e])
