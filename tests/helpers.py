@@ -39,3 +39,34 @@ def oracle_topology(O, yb, bus_type, ordering=None):
         ordering = S.analyze(jac.n_u, Ap, Ai)
     P, Q, R = ordering
     return O.Topology(yb, bus_type, P, Q, R)
+
+
+# power-grid-model fixtures (tests/golden/pgm/<case>, copied from the
+# reference's tests/data/pgm/powerflow/symmetric by make_pgm_fixtures.py) and
+# the tolerances the reference's own tests give them
+# (tests/klu_native_jacobian_test.rs, tests/pgm_three_winding_transformer_test.rs)
+PGM_CASES = {"basic-node": 1e-5, "node": 1e-5, "line": 1e-5, "shunt": 1e-5, "sym_load": 1e-5,
+             "sym_gen": 1e-5, "source": 1e-5, "transmission-case": 1e-5, "transformer": 1e-4,
+             "distribution-case": 1e-5, "three_winding_transformer": 1e-4}
+
+
+def pgm_runs(case: str):
+    """[(input document, expected node outputs)] of one case: the single input,
+    or every scenario of the update batch merged into the base input."""
+    from gridoxide_gb300 import pgm
+    d = os.path.join(GOLDEN, "pgm", case)
+    base = pgm.load(os.path.join(d, "input.json"))
+    if os.path.exists(os.path.join(d, "sym_output.json")):
+        return [(base, pgm.load(os.path.join(d, "sym_output.json"))["data"]["node"])]
+    upd = pgm.load(os.path.join(d, "update_batch.json"))["data"]
+    exp = pgm.load(os.path.join(d, "sym_output_batch.json"))["data"]
+    return [(pgm.apply_batch_scenario(base, u), e["node"]) for u, e in zip(upd, exp)]
+
+
+def pgm_worst(net, vm, va, nodes) -> float:
+    """Largest |u_pu - vm| or |u_angle - va| over the expected nodes."""
+    worst = 0.0
+    for nd in nodes:
+        k = net.id_to_idx[int(nd["id"])]
+        worst = max(worst, abs(vm[k] - nd["u_pu"]), abs(va[k] - nd["u_angle"]))
+    return worst

@@ -1,0 +1,48 @@
+"""PGM conversion (gridoxide_gb300.pgm, after src/pgm.rs:347-595 and the
+Y-bus stamping of src/network.rs) pinned against power-grid-model's own
+results: every symmetric fixture the reference tests, converted, started from
+the linear initial guess and solved by the oracle's Newton-Raphson with
+tol 1e-6 / 20 iterations, matches the expected node voltages within the
+reference test's tolerance (tests/klu_native_jacobian_test.rs:26-126,
+tests/pgm_three_winding_transformer_test.rs)."""
+import numpy as np
+import pytest
+
+from gridoxide_gb300 import grids as G
+from gridoxide_gb300 import pgm
+from helpers import PGM_CASES, oracle_topology, pgm_runs, pgm_worst
+
+
+@pytest.mark.parametrize("case", sorted(PGM_CASES))
+def test_pgm_case_oracle(oracle_mod, case):
+    O = oracle_mod
+    for doc, nodes in pgm_runs(case):
+        net = pgm.convert(doc)
+        vm0, va0 = O.linear_initial_guess(net.ybus, net.bus_type, net.p_spec, net.q_spec, net.vm,
+                                          net.va, net.zip_imp, net.zip_cur)
+        ot = oracle_topology(O, net.ybus, net.bus_type)
+        ot.set_zip(net.zip_imp, net.zip_cur)
+        r = ot.batch_solve(net.p_spec[None], net.q_spec[None], vm0, va0, tol=1e-6, max_iter=20)
+        assert r["status"][0] == 0
+        assert pgm_worst(net, r["vm"][0], r["va"][0], nodes) < PGM_CASES[case]
+
+
+def test_pgm_conversion_pieces():
+    """Source impedance, island marking and the bus layout of a converted input."""
+    r, x = pgm.source_impedance_pu(1e10, 0.1, 1e6)
+    assert abs(np.hypot(r, x) - 1e-4) < 1e-18 and abs(r / x - 0.1) < 1e-15
+    (doc, _), = pgm_runs("basic-node")
+    net = pgm.convert(doc)
+    # node_1 (PQ), node_2 (no source: a slack at V = 0), the source's slack bus
+    assert list(net.bus_type) == [G.BUS_PQ, G.BUS_SLACK, G.BUS_SLACK]
+    assert net.vm[1] == 0.0 and net.vm[2] == doc["data"]["source"][0]["u_ref"]
+    (doc, _), = pgm_runs("three_winding_transformer")[:1]
+    net = pgm.convert(doc)
+    n_nodes = len(doc["data"]["node"])
+    assert net.n_bus == n_nodes + 1 + len(doc["data"]["source"])
+    star = n_nodes
+    assert net.bus_type[star] == G.BUS_PQ
+    # the star bus connects to the three windings' nodes only
+    cols = set(net.ybus.indices[net.ybus.indptr[star]:net.ybus.indptr[star + 1]])
+    assert cols == {star} | {net.id_to_idx[int(doc["data"]["three_winding_transformer"][0][k])]
+                             for k in ("node_1", "node_2", "node_3")}
