@@ -844,6 +844,46 @@ static bool guess_run(gox_topo* t, int B, const double* p_spec, const double* q_
   return true;
 }
 
+// When no Jacobian is ever needed (every scenario meets tol at its start),
+// or max_iter == 0, the result is computed on the host from the mismatch
+// only; no factorization exists to run on the device.
+static void host_only_result(gox_topo* t, int B, const double* p_spec, const double* q_spec,
+                             const double* vm0, const double* va0, int v_stride,
+                             const int32_t* o_slot, const double* o_dre, const double* o_dim,
+                             double tol, int max_iter, double* vm_out, double* va_out,
+                             int32_t* iters, int32_t* status, double* max_mis, double* hist,
+                             const std::vector<int>& singular_first) {
+  const int n = t->n_bus;
+  std::vector<double> p(n), q(n), yre, yim;
+  for (int s = 0; s < B; s++) {
+    const double* vm = vm0 + (size_t)s * v_stride;
+    const double* va = va0 + (size_t)s * v_stride;
+    std::copy(vm, vm + n, vm_out + (size_t)s * n);
+    std::copy(va, va + n, va_out + (size_t)s * n);
+    if (hist) std::fill(hist + (size_t)s * max_iter, hist + (size_t)(s + 1) * max_iter, 0.0);
+    if (max_iter == 0) { iters[s] = 0; status[s] = GOX_MAX_ITERATIONS; max_mis[s] = 0.0; continue; }
+    yre = t->yre; yim = t->yim;
+    if (o_slot && o_slot[4 * s] >= 0)
+      for (int c = 0; c < 4; c++) { yre[o_slot[4 * s + c]] += o_dre[4 * s + c]; yim[o_slot[4 * s + c]] += o_dim[4 * s + c]; }
+    host_injections(n, t->yp.data(), t->yi.data(), yre.data(), yim.data(), vm, va, p.data(), q.data());
+    double mx = 0.0;
+    for (int a = 0; a < t->jac.n_ang; a++) {
+      const int i = t->jac.ns_idx[a];
+      mx = std::fmax(mx, std::fabs(t->eff(0, i, p_spec[(size_t)s * n + i], vm[i]) - p[i]));
+    }
+    for (int a = 0; a < t->jac.n_pq; a++) {
+      const int i = t->jac.pq_idx[a];
+      mx = std::fmax(mx, std::fabs(t->eff(1, i, q_spec[(size_t)s * n + i], vm[i]) - q[i]));
+    }
+    iters[s] = 1;
+    max_mis[s] = mx;
+    if (hist) hist[(size_t)s * max_iter] = mx;
+    status[s] = mx < tol ? GOX_CONVERGED : GOX_SINGULAR_SCENARIO;
+  }
+  (void)singular_first;
+}
+
+
 static int batch_device(gox_topo* t, int B, const double* p_spec, const double* q_spec,
                         const double* vm0, const double* va0, int v_stride,
                         const int32_t* o_slot, const double* o_dre, const double* o_dim,
@@ -894,26 +934,38 @@ static int batch_device(gox_topo* t, int B, const double* p_spec, const double* 
       pp = hp.data(); qq = hq.data(); vv = hvm.data(); aa = hva.data();
     }
     fix_pivots(t, B, pp, qq, vv, aa, v_stride, ss, dr, di, tol, first_singular);
+    if (!t->factored) {
+      // no Jacobian needed (every scenario meets tol at its start point, e.g.
+      // the linear guess of a network without loads) or every candidate
+      // factorization was singular: the mismatch at the start points decides
+      // Converged or Singular, evaluated on the host copies above (the start
+      // points actually used, the guess included)
+      std::vector<double> ovm((size_t)B * n), ova((size_t)B * n), mm(B),
+          hh(hist ? (size_t)B * max_iter : 0);
+      std::vector<int32_t> it(B), stt(B);
+      host_only_result(t, B, pp, qq, vv, aa, v_stride, ss, dr, di, tol, max_iter, ovm.data(),
+                       ova.data(), it.data(), stt.data(), mm.data(), hist ? hh.data() : nullptr,
+                       first_singular);
+      GOX_CK(cudaMemcpyAsync(vm_out, ovm.data(), ovm.size() * 8, cudaMemcpyHostToDevice, st));
+      GOX_CK(cudaMemcpyAsync(va_out, ova.data(), ova.size() * 8, cudaMemcpyHostToDevice, st));
+      GOX_CK(cudaMemcpyAsync(iters, it.data(), (size_t)B * 4, cudaMemcpyHostToDevice, st));
+      GOX_CK(cudaMemcpyAsync(status, stt.data(), (size_t)B * 4, cudaMemcpyHostToDevice, st));
+      GOX_CK(cudaMemcpyAsync(max_mis, mm.data(), (size_t)B * 8, cudaMemcpyHostToDevice, st));
+      if (hist) GOX_CK(cudaMemcpyAsync(hist, hh.data(), hh.size() * 8, cudaMemcpyHostToDevice, st));
+      GOX_CK(cudaStreamSynchronize(st));
+      return GOX_OK;
+    }
   }
   const bool outage = o_slot != nullptr;
   const bool want_hist = hist != nullptr;
-  if (!t->factored) {
-    // no Jacobian needed (all scenarios converged at their start point) or
-    // every candidate factorization was singular: evaluate the mismatch
-    // only, with a one-iteration budget that never reaches a solve.
-  }
-  if (t->factored && !t->uploaded) {
+  if (!t->uploaded) {
     t->dsched.load(t->sc, t->yp, t->yi, t->yre, t->yim);
     t->dsched.load_streams(t->s32, t->s64);
     t->uploaded = true;
   }
   const SchedDev& S = t->dsched.d;
   DevBatch& DB = t->batch;
-  if (t->factored) {
-    DB.ensure(S, G, precision, max_iter, want_hist);
-  } else {
-    return -1;  // handled by the caller's fallback below
-  }
+  DB.ensure(S, G, precision, max_iter, want_hist);
   BatchDev D = DB.view(want_hist, outage, tol, t->piv_tol);
   // inputs -> interleaved layout
   const size_t tot = (size_t)G * n * 32;
@@ -1161,44 +1213,6 @@ static int check_batch_args(gox_topo* t, int B, const void* p, const void* q, co
   return 1;
 }
 
-// When no Jacobian is ever needed (every scenario meets tol at its start),
-// or max_iter == 0, the result is computed on the host from the mismatch
-// only; no factorization exists to run on the device.
-static void host_only_result(gox_topo* t, int B, const double* p_spec, const double* q_spec,
-                             const double* vm0, const double* va0, int v_stride,
-                             const int32_t* o_slot, const double* o_dre, const double* o_dim,
-                             double tol, int max_iter, double* vm_out, double* va_out,
-                             int32_t* iters, int32_t* status, double* max_mis, double* hist,
-                             const std::vector<int>& singular_first) {
-  const int n = t->n_bus;
-  std::vector<double> p(n), q(n), yre, yim;
-  for (int s = 0; s < B; s++) {
-    const double* vm = vm0 + (size_t)s * v_stride;
-    const double* va = va0 + (size_t)s * v_stride;
-    std::copy(vm, vm + n, vm_out + (size_t)s * n);
-    std::copy(va, va + n, va_out + (size_t)s * n);
-    if (hist) std::fill(hist + (size_t)s * max_iter, hist + (size_t)(s + 1) * max_iter, 0.0);
-    if (max_iter == 0) { iters[s] = 0; status[s] = GOX_MAX_ITERATIONS; max_mis[s] = 0.0; continue; }
-    yre = t->yre; yim = t->yim;
-    if (o_slot && o_slot[4 * s] >= 0)
-      for (int c = 0; c < 4; c++) { yre[o_slot[4 * s + c]] += o_dre[4 * s + c]; yim[o_slot[4 * s + c]] += o_dim[4 * s + c]; }
-    host_injections(n, t->yp.data(), t->yi.data(), yre.data(), yim.data(), vm, va, p.data(), q.data());
-    double mx = 0.0;
-    for (int a = 0; a < t->jac.n_ang; a++) {
-      const int i = t->jac.ns_idx[a];
-      mx = std::fmax(mx, std::fabs(t->eff(0, i, p_spec[(size_t)s * n + i], vm[i]) - p[i]));
-    }
-    for (int a = 0; a < t->jac.n_pq; a++) {
-      const int i = t->jac.pq_idx[a];
-      mx = std::fmax(mx, std::fabs(t->eff(1, i, q_spec[(size_t)s * n + i], vm[i]) - q[i]));
-    }
-    iters[s] = 1;
-    max_mis[s] = mx;
-    if (hist) hist[(size_t)s * max_iter] = mx;
-    status[s] = mx < tol ? GOX_CONVERGED : GOX_SINGULAR_SCENARIO;
-  }
-  (void)singular_first;
-}
 
 int gox_batch_solve_device(gox_topo* t, int32_t B, const double* p_spec, const double* q_spec,
                            const double* vm0, const double* va0, int32_t v_stride,
@@ -1213,40 +1227,10 @@ int gox_batch_solve_device(gox_topo* t, int32_t B, const double* p_spec, const d
   return guard_impl([&]() -> int {
     cudaStream_t st = (cudaStream_t)stream;
     if (max_iter == 0) return GOX_E_INVALID;
-    int r = batch_device(t, B, p_spec, q_spec, vm0, va0, v_stride, o_slot, o_dre, o_dim, tol,
-                         max_iter, precision, vm_out, va_out, iterations, status, max_mismatch,
-                         history, st, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr,
-                         nullptr);
-    if (r == -1) {
-      // no factorization could be fixed: evaluate on the host copy
-      size_t nv = (size_t)(v_stride ? B : 1) * t->n_bus;
-      std::vector<double> hp((size_t)B * t->n_bus), hq(hp.size()), hvm(nv), hva(nv),
-          ovm(hp.size()), ova(hp.size()), mm(B), hh(history ? (size_t)B * max_iter : 0);
-      std::vector<int32_t> it(B), ss(B), hs;
-      std::vector<double> hr, hi;
-      GOX_CK(cudaMemcpy(hp.data(), p_spec, hp.size() * 8, cudaMemcpyDeviceToHost));
-      GOX_CK(cudaMemcpy(hq.data(), q_spec, hq.size() * 8, cudaMemcpyDeviceToHost));
-      GOX_CK(cudaMemcpy(hvm.data(), vm0, nv * 8, cudaMemcpyDeviceToHost));
-      GOX_CK(cudaMemcpy(hva.data(), va0, nv * 8, cudaMemcpyDeviceToHost));
-      if (o_slot) {
-        hs.resize((size_t)B * 4); hr.resize(hs.size()); hi.resize(hs.size());
-        GOX_CK(cudaMemcpy(hs.data(), o_slot, hs.size() * 4, cudaMemcpyDeviceToHost));
-        GOX_CK(cudaMemcpy(hr.data(), o_dre, hr.size() * 8, cudaMemcpyDeviceToHost));
-        GOX_CK(cudaMemcpy(hi.data(), o_dim, hi.size() * 8, cudaMemcpyDeviceToHost));
-      }
-      host_only_result(t, B, hp.data(), hq.data(), hvm.data(), hva.data(), v_stride,
-                       o_slot ? hs.data() : nullptr, hr.data(), hi.data(), tol, max_iter,
-                       ovm.data(), ova.data(), it.data(), ss.data(), mm.data(),
-                       history ? hh.data() : nullptr, {});
-      GOX_CK(cudaMemcpy(vm_out, ovm.data(), ovm.size() * 8, cudaMemcpyHostToDevice));
-      GOX_CK(cudaMemcpy(va_out, ova.data(), ova.size() * 8, cudaMemcpyHostToDevice));
-      GOX_CK(cudaMemcpy(iterations, it.data(), B * 4, cudaMemcpyHostToDevice));
-      GOX_CK(cudaMemcpy(status, ss.data(), B * 4, cudaMemcpyHostToDevice));
-      GOX_CK(cudaMemcpy(max_mismatch, mm.data(), B * 8, cudaMemcpyHostToDevice));
-      if (history) GOX_CK(cudaMemcpy(history, hh.data(), hh.size() * 8, cudaMemcpyHostToDevice));
-      return GOX_OK;
-    }
-    return r;
+    return batch_device(t, B, p_spec, q_spec, vm0, va0, v_stride, o_slot, o_dre, o_dim, tol,
+                        max_iter, precision, vm_out, va_out, iterations, status, max_mismatch,
+                        history, st, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr,
+                        nullptr);
   });
 }
 
@@ -1301,13 +1285,6 @@ int gox_batch_solve(gox_topo* t, int32_t B, const double* p_spec, const double* 
                          dit.as<int32_t>(), dst.as<int32_t>(), dmm.as<double>(),
                          history ? dh.as<double>() : nullptr, st, p_spec, q_spec, vm0, va0,
                          o_slot, o_dre, o_dim);
-    if (r == -1) {
-      std::vector<int> none;
-      GOX_CK(cudaStreamSynchronize(st));
-      host_only_result(t, B, p_spec, q_spec, vm0, va0, v_stride, o_slot, o_dre, o_dim, tol,
-                       max_iter, vm_out, va_out, iterations, status, max_mismatch, history, none);
-      return GOX_OK;
-    }
     if (r != GOX_OK) return r;
     GOX_CK(cudaMemcpyAsync(vm_out, dovm.p, bn * 8, cudaMemcpyDeviceToHost, st));
     GOX_CK(cudaMemcpyAsync(va_out, dova.p, bn * 8, cudaMemcpyDeviceToHost, st));
