@@ -85,6 +85,8 @@ SIGNATURES = {
     "gox_last_launches": (C.c_int64, [vp]),
     "gox_set_pivot_tolerance": (C.c_int, [vp, C.c_double]),
     "gox_topo_set_initial_guess": (C.c_int, [vp, C.c_int32]),
+    "gox_topo_initial_guess": (C.c_int, [vp, C.c_int32, f64p, f64p, f64p, f64p, C.c_int32, f64p,
+                                         f64p]),
     "gox_topo_set_zip": (C.c_int, [vp, f64p, f64p, f64p, f64p]),
     "gox_last_fallbacks": (C.c_int64, [vp]),
     "gox_version": (C.c_char_p, []),

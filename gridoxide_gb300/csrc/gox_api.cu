@@ -1474,6 +1474,44 @@ int gox_topo_set_initial_guess(gox_topo* t, int32_t mode) {
   return GOX_OK;
 }
 
+int gox_topo_initial_guess(gox_topo* t, int32_t B, const double* p_spec, const double* q_spec,
+                           const double* vm0, const double* va0, int32_t v_stride, double* vm_out,
+                           double* va_out) {
+  if (!t || B <= 0 || !p_spec || !q_spec || !vm0 || !va0 || !vm_out || !va_out) return GOX_E_INVALID;
+  if (v_stride != 0 && v_stride != t->n_bus) return GOX_E_INVALID;
+  if (int r = require_device()) return r;
+  return guard_impl([&]() -> int {
+    const int n = t->n_bus;
+    const size_t bn = (size_t)B * n, nv = (size_t)(v_stride ? B : 1) * n;
+    cudaStream_t st = nullptr;
+    GOX_CK(cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking));
+    struct StreamGuard {
+      cudaStream_t s;
+      ~StreamGuard() { cudaStreamDestroy(s); }
+    } sg{st};
+    IoStage& io = t->io;
+    io.p.ensure(bn * 8); io.q.ensure(bn * 8); io.vm.ensure(nv * 8); io.va.ensure(nv * 8);
+    GOX_CK(cudaMemcpyAsync(io.p.p, p_spec, bn * 8, cudaMemcpyHostToDevice, st));
+    GOX_CK(cudaMemcpyAsync(io.q.p, q_spec, bn * 8, cudaMemcpyHostToDevice, st));
+    GOX_CK(cudaMemcpyAsync(io.vm.p, vm0, nv * 8, cudaMemcpyHostToDevice, st));
+    GOX_CK(cudaMemcpyAsync(io.va.p, va0, nv * 8, cudaMemcpyHostToDevice, st));
+    t->guess.d.zip = t->zip.empty() ? nullptr : t->dzip.as<double>();
+    if (guess_run(t, B, io.p.as<double>(), io.q.as<double>(), io.vm.as<double>(), io.va.as<double>(),
+                  v_stride, nullptr, nullptr, nullptr, st)) {
+      GOX_CK(cudaMemcpyAsync(vm_out, t->guess.gvm.p, bn * 8, cudaMemcpyDeviceToHost, st));
+      GOX_CK(cudaMemcpyAsync(va_out, t->guess.gva.p, bn * 8, cudaMemcpyDeviceToHost, st));
+      GOX_CK(cudaStreamSynchronize(st));
+    } else {
+      GOX_CK(cudaStreamSynchronize(st));
+      for (int s = 0; s < B; s++) {
+        std::copy(vm0 + (size_t)s * v_stride, vm0 + (size_t)s * v_stride + n, vm_out + (size_t)s * n);
+        std::copy(va0 + (size_t)s * v_stride, va0 + (size_t)s * v_stride + n, va_out + (size_t)s * n);
+      }
+    }
+    return GOX_OK;
+  });
+}
+
 // ---- LinearSolver level ----------------------------------------------------
 
 int gox_ls_create(int32_t n, int32_t nnz, const int32_t* rows, const int32_t* cols,

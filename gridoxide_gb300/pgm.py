@@ -49,6 +49,10 @@ class Network:
     zip_cur: np.ndarray    # complex, constant current
     ybus: G.YBus
     id_to_idx: dict
+    u_rated: np.ndarray    # V, per bus (a source's slack bus: its node's; a star bus: winding 1's)
+    zip_terms: np.ndarray  # int32, ZIP terms per bus (loads and generators of type 1 or 2)
+    islands: list          # components without a slack bus, pinned to V = 0
+    guess_singular: bool   # the reference's linear guess would meet a singular system
 
 
 def load(path: str) -> dict:
@@ -135,8 +139,11 @@ def source_impedance_pu(sk, rx_ratio, s_base):
     return rx_ratio * x, x
 
 
-def convert(doc: dict, s_base: float = S_BASE_VA, freq_hz: float = FREQ_HZ) -> Network:
-    """pgm_to_buses_and_branches + pgm_shunts_1ph + build_ybus + stamp_shunts."""
+def convert(doc: dict, s_base: float = S_BASE_VA, freq_hz: float = FREQ_HZ,
+            mark_islands: bool = True) -> Network:
+    """pgm_to_buses_and_branches + pgm_shunts_1ph + build_ybus + stamp_shunts;
+    with `mark_islands`, then mark_unreferenced_islands (the start of every
+    solve in the reference)."""
     data = doc["data"]
     id_to_idx = node_id_to_idx(data)
     u_rated = {int(n["id"]): float(n["u_rated"]) for n in data.get("node", [])}
@@ -145,14 +152,17 @@ def convert(doc: dict, s_base: float = S_BASE_VA, freq_hz: float = FREQ_HZ) -> N
     q_inj = np.zeros(n_nodes)
     zimp = np.zeros(n_nodes, np.complex128)
     zcur = np.zeros(n_nodes, np.complex128)
+    nzip = np.zeros(n_nodes, np.int32)
 
     def accumulate(node, load_type, p, q, sign):
         s = complex(p, q) * sign / s_base
         k = id_to_idx[int(node)]
         if load_type == 1:
             zimp[k] += s
+            nzip[k] += 1
         elif load_type == 2:
             zcur[k] += s
+            nzip[k] += 1
         else:
             p_inj[k] += s.real
             q_inj[k] += s.imag
@@ -185,6 +195,11 @@ def convert(doc: dict, s_base: float = S_BASE_VA, freq_hz: float = FREQ_HZ) -> N
     zip_cur = np.zeros(n, np.complex128)
     zip_imp[:n_nodes] = zimp
     zip_cur[:n_nodes] = zcur
+    zip_terms = np.zeros(n, np.int32)
+    zip_terms[:n_nodes] = nzip
+    u_rated_bus = np.zeros(n)
+    for nid, k in id_to_idx.items():
+        u_rated_bus[k] = u_rated[nid]
 
     # voltage regulators: their generator's node becomes PV at u_ref
     gen_node = {int(g["id"]): int(g["node"]) for g in data.get("sym_gen", [])}
@@ -223,6 +238,7 @@ def convert(doc: dict, s_base: float = S_BASE_VA, freq_hz: float = FREQ_HZ) -> N
         v = n_nodes + n_star + i
         bus_type[v] = G.BUS_SLACK
         vm[v] = src["u_ref"]
+        u_rated_bus[v] = u_rated[int(src["node"])]
         r_s, x_s = source_impedance_pu(src["sk"], src["rx_ratio"], s_base)
         lines.append((v, id_to_idx[int(src["node"])], r_s, x_s, 0.0))
     # build_ybus: lines (self-loops as shunts, series branches), then transformers
@@ -247,6 +263,7 @@ def convert(doc: dict, s_base: float = S_BASE_VA, freq_hz: float = FREQ_HZ) -> N
     for i, t3 in enumerate(trafo3):
         star = n_nodes + i
         u1r, u2r, u3r = (u_rated[int(t3[k])] for k in ("node_1", "node_2", "node_3"))
+        u_rated_bus[star] = u1r
         direction = 1.0 if t3["tap_max"] > t3["tap_min"] else -1.0
         delta = direction * (t3["tap_pos"] - t3["tap_nom"]) * t3["tap_size"]
         u1, u2, u3 = t3["u1"], t3["u2"], t3["u3"]
@@ -282,8 +299,10 @@ def convert(doc: dict, s_base: float = S_BASE_VA, freq_hz: float = FREQ_HZ) -> N
         add(k, k, complex(sh["g1"], sh["b1"]) / base_y)
     yb = G.ybus_from_triplets(n, rows, cols, [v.real for v in vals], [v.imag for v in vals])
     net = Network(n_bus=n, bus_type=bus_type, vm=vm, va=va, p_spec=p_spec, q_spec=q_spec,
-                  zip_imp=zip_imp, zip_cur=zip_cur, ybus=yb, id_to_idx=id_to_idx)
-    mark_unreferenced_islands(net)
+                  zip_imp=zip_imp, zip_cur=zip_cur, ybus=yb, id_to_idx=id_to_idx,
+                  u_rated=u_rated_bus, zip_terms=zip_terms, islands=[], guess_singular=False)
+    if mark_islands:
+        mark_unreferenced_islands(net)
     return net
 
 
@@ -309,13 +328,56 @@ def connected_components(yb: G.YBus):
     return comps
 
 
+def _guess_block_singular(net: Network, comp) -> bool:
+    """Whether the linear-guess rows of one slack-free component (its PQ
+    buses, Y + the constant-admittance load on the diagonal, as in
+    src/network.rs:627-671) form a singular system.  The reference builds its
+    guess before it marks islands, so such a component makes its whole guess
+    fail (src/sparse.rs:48-63 returns None) and every bus keeps its start."""
+    from . import solver as S
+    yb = net.ybus
+    pq = [i for i in comp if net.bus_type[i] == G.BUS_PQ]
+    if not pq:
+        return False
+    pos = {b: r for r, b in enumerate(pq)}
+    rows, cols, vals = [], [], []
+
+    def block(r, c, y):
+        rows.extend((2 * r, 2 * r, 2 * r + 1, 2 * r + 1))
+        cols.extend((2 * c, 2 * c + 1, 2 * c, 2 * c + 1))
+        vals.extend((y.real, -y.imag, y.imag, y.real))
+
+    for r, i in enumerate(pq):
+        v = net.vm[i]
+        s_eff = complex(net.p_spec[i], net.q_spec[i]) + net.zip_imp[i] * v * v + net.zip_cur[i] * v
+        y_load = -s_eff.conjugate()
+        diag = False
+        for e in range(int(yb.indptr[i]), int(yb.indptr[i + 1])):
+            j = int(yb.indices[e])
+            y = complex(yb.re[e], yb.im[e])
+            if j == i:
+                diag = True
+                block(r, r, y + y_load)
+            elif j in pos:
+                block(r, pos[j], y)
+        if not diag:
+            block(r, r, y_load)
+    return S.factor_host(2 * len(pq), rows, cols, vals) is None
+
+
 def mark_unreferenced_islands(net: Network) -> None:
     """src/network.rs:142-223: a component without a slack bus is pinned to
-    V = 0 as slack buses with no injection (the reference runs this at the
-    start of Newton; here it runs before the linear guess, which it only
-    changes for systems the guess could not solve anyway)."""
+    V = 0 as slack buses with no injection.  The reference does this at the
+    start of Newton, after its linear guess; here it happens first (the GPU
+    guess then covers the energized part only, which is the same system as
+    long as the island rows are regular) and `guess_singular` records when
+    they are not, so the solve starts from the given voltages instead, as
+    the reference's does."""
     for comp in connected_components(net.ybus):
         if not np.any(net.bus_type[comp] == G.BUS_SLACK):
+            net.islands.append(comp)
+            if not net.guess_singular and _guess_block_singular(net, comp):
+                net.guess_singular = True
             net.bus_type[comp] = G.BUS_SLACK
             net.vm[comp] = 0.0
             net.va[comp] = 0.0
@@ -338,14 +400,21 @@ def apply_batch_scenario(base: dict, scenario: dict) -> dict:
     return doc
 
 
+def topology(gox, net: Network):
+    """The network registered on the GPU: Y-bus, bus types, ZIP terms and the
+    start-point rule (the linear guess unless the reference's would fail)."""
+    topo = gox.Topology(net.ybus, net.bus_type)
+    if np.any(net.zip_imp != 0) or np.any(net.zip_cur != 0):
+        topo.set_zip(net.zip_imp, net.zip_cur)
+    topo.set_initial_guess("given" if net.guess_singular else "linear")
+    return topo
+
+
 def solve(gox, net: Network, tol: float = 1e-6, max_iter: int = 20,
           precision: int | None = None):
     """One scenario of a converted network on the GPU: linear initial guess,
     then Newton-Raphson (FP64 unless `precision` says otherwise)."""
-    topo = gox.Topology(net.ybus, net.bus_type)
-    if np.any(net.zip_imp != 0) or np.any(net.zip_cur != 0):
-        topo.set_zip(net.zip_imp, net.zip_cur)
-    topo.set_initial_guess("linear")
+    topo = topology(gox, net)
     prec = gox.GOX_PRECISION_FP64 if precision is None else precision
     return topo.solve(net.p_spec[None], net.q_spec[None], net.vm, net.va, tol=tol,
                       max_iter=max_iter, precision=prec)

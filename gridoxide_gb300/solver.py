@@ -346,6 +346,23 @@ class Topology:
         code = {"given": _lib.GOX_GUESS_GIVEN, "linear": _lib.GOX_GUESS_LINEAR}[mode]
         check(_lib.load().gox_topo_set_initial_guess(self._h, code), "gox_topo_set_initial_guess")
 
+    def initial_guess(self, p_spec, q_spec, vm0, va0):
+        """The linear initial guess (src/network.rs:627-678) of each scenario,
+        computed on the GPU: ([B, N] |V|, [B, N] theta); the given start where
+        the guess system is singular."""
+        p_spec = _f64(np.atleast_2d(p_spec))
+        q_spec = _f64(np.atleast_2d(q_spec))
+        B, n = p_spec.shape
+        if n != self.n_bus or q_spec.shape != p_spec.shape:
+            raise ValueError("p_spec/q_spec must be [B, n_bus]")
+        vm0, va0 = _f64(vm0), _f64(va0)
+        vm, va = np.empty((B, n)), np.empty((B, n))
+        check(_lib.load().gox_topo_initial_guess(
+            self._h, B, _p(p_spec, _lib.f64p), _p(q_spec, _lib.f64p), _p(vm0, _lib.f64p),
+            _p(va0, _lib.f64p), n if vm0.ndim == 2 else 0, _p(vm, _lib.f64p), _p(va, _lib.f64p)),
+            "gox_topo_initial_guess")
+        return vm, va
+
     def __del__(self):
         try:
             if self._h:
@@ -419,9 +436,10 @@ class PowerFlowReport:
 
 
 class BatchSolver:
-    """batch::BatchSolver with a GB300 backend.  Scenario validation and
-    result order follow src/batch.rs:198-289; the work runs as one GPU
-    batch instead of a rayon work queue."""
+    """batch::BatchSolver with a GB300 backend.  Scenario validation, the
+    linear initial guess before every scenario and result order follow
+    src/batch.rs:198-289; the work runs as one GPU batch instead of a rayon
+    work queue."""
 
     def __init__(self, backend=JacobianBackend.Gb300):
         self.backend = backend
@@ -466,6 +484,7 @@ class BatchSolver:
         topo = self._topos.get(key)
         if topo is None:
             topo = Topology(ybus, buses.bus_type)
+            topo.set_initial_guess("linear")  # every scenario starts from it (src/batch.rs:268)
             self._topos[key] = topo
         res = topo.solve(p, q, vm, va, tol=tol, max_iter=max_iter, precision=self.backend,
                          outage=outage, history=True)

@@ -263,6 +263,17 @@ int gox_topo_set_zip(gox_topo *t, const double *zi_re, const double *zi_im, cons
 #define GOX_GUESS_LINEAR 1
 int gox_topo_set_initial_guess(gox_topo *t, int32_t mode);
 
+/* The linear initial guess itself (what the GOX_GUESS_LINEAR mode starts
+ * Newton from), computed on the GPU for B scenarios: host arrays p_spec,
+ * q_spec [B][n_bus], vm0/va0 [n_bus] (v_stride 0) or [B][n_bus] (v_stride
+ * n_bus); vm_out/va_out [B][n_bus].  Replaces the reference model's
+ * `initial_guess()` (src/python.rs:395-406, one scenario).  When the guess
+ * system is singular at its first factorization the given start is
+ * returned. */
+int gox_topo_initial_guess(gox_topo *t, int32_t B, const double *p_spec, const double *q_spec,
+                           const double *vm0, const double *va0, int32_t v_stride,
+                           double *vm_out, double *va_out);
+
 /* Mixed path: the pivot-ratio threshold.  A scenario whose FP32 refactor
  * meets a pivot with |u_kk| < tol * max |L(:, k)| (before scaling) is solved
  * again from its start point on the FP64 path, with the same pivot order,

@@ -70,3 +70,12 @@ def pgm_worst(net, vm, va, nodes) -> float:
         k = net.id_to_idx[int(nd["id"])]
         worst = max(worst, abs(vm[k] - nd["u_pu"]), abs(va[k] - nd["u_angle"]))
     return worst
+
+
+def pgm_oracle_start(O, net):
+    """The oracle's start point for a converted network: its linear guess,
+    or the given voltages where the reference's guess would be singular."""
+    if net.guess_singular:
+        return net.vm.copy(), net.va.copy()
+    return O.linear_initial_guess(net.ybus, net.bus_type, net.p_spec, net.q_spec, net.vm, net.va,
+                                  net.zip_imp, net.zip_cur)

@@ -13,7 +13,7 @@ import numpy as np
 import pytest
 
 from gridoxide_gb300 import pgm
-from helpers import PGM_CASES, oracle_topology, pgm_runs, pgm_worst
+from helpers import PGM_CASES, oracle_topology, pgm_oracle_start, pgm_runs, pgm_worst
 
 pytestmark = pytest.mark.gpu
 
@@ -28,8 +28,7 @@ def test_pgm_case_gpu(gox, oracle_mod, case):
         res = pgm.solve(gox, net, precision=gox.GOX_PRECISION_FP64)
         assert res.status[0] == gox.GOX_CONVERGED
         assert pgm_worst(net, res.voltage_mag[0], res.voltage_ang[0], nodes) < PGM_CASES[case]
-        vm0, va0 = O.linear_initial_guess(net.ybus, net.bus_type, net.p_spec, net.q_spec, net.vm,
-                                          net.va, net.zip_imp, net.zip_cur)
+        vm0, va0 = pgm_oracle_start(O, net)
         ot = oracle_topology(O, net.ybus, net.bus_type)
         ot.set_zip(net.zip_imp, net.zip_cur)
         ref = ot.batch_solve(net.p_spec[None], net.q_spec[None], vm0, va0, tol=1e-6, max_iter=20)

@@ -10,7 +10,7 @@ import pytest
 
 from gridoxide_gb300 import grids as G
 from gridoxide_gb300 import pgm
-from helpers import PGM_CASES, oracle_topology, pgm_runs, pgm_worst
+from helpers import PGM_CASES, oracle_topology, pgm_oracle_start, pgm_runs, pgm_worst
 
 
 @pytest.mark.parametrize("case", sorted(PGM_CASES))
@@ -18,8 +18,7 @@ def test_pgm_case_oracle(oracle_mod, case):
     O = oracle_mod
     for doc, nodes in pgm_runs(case):
         net = pgm.convert(doc)
-        vm0, va0 = O.linear_initial_guess(net.ybus, net.bus_type, net.p_spec, net.q_spec, net.vm,
-                                          net.va, net.zip_imp, net.zip_cur)
+        vm0, va0 = pgm_oracle_start(O, net)
         ot = oracle_topology(O, net.ybus, net.bus_type)
         ot.set_zip(net.zip_imp, net.zip_cur)
         r = ot.batch_solve(net.p_spec[None], net.q_spec[None], vm0, va0, tol=1e-6, max_iter=20)
