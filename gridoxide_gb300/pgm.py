@@ -418,3 +418,68 @@ def solve(gox, net: Network, tol: float = 1e-6, max_iter: int = 20,
     prec = gox.GOX_PRECISION_FP64 if precision is None else precision
     return topo.solve(net.p_spec[None], net.q_spec[None], net.vm, net.va, tol=tol,
                       max_iter=max_iter, precision=prec)
+
+
+def from_grid(g: G.Grid, u_rated: float = 110e3, sk: float = 1e10, rx_ratio: float = 0.1,
+              s_base: float = S_BASE_VA, freq_hz: float = FREQ_HZ) -> dict:
+    """A generated grid as a power-grid-model input document, so that the
+    PGM path (`PowerFlowModel.from_pgm_json`, the reference's
+    scripts/bench/bench_batch.py workflow) can load it.  Every node is rated
+    `u_rated`; lines keep r, x and charging; a transformer becomes a PGM
+    transformer with the same series impedance (uk = |z|, pk = r s_base,
+    sn = s_base) and its off-nominal ratio as one tap step, its charging as
+    two shunts (b/2k^2 at the tapped end, b/2 at the other); PQ buses carry
+    their net injection as a constant-power load, PV buses as a generator
+    under a voltage regulator at their set-point; the slack bus becomes the
+    node of a source at its set-point with short-circuit power `sk` (its
+    virtual bus is the slack, so the grid's slack bus turns PQ)."""
+    zb = u_rated * u_rated / s_base
+    omega = 2.0 * math.pi * freq_hz
+    next_id = [g.n_bus]
+
+    def new_id():
+        next_id[0] += 1
+        return next_id[0]
+
+    node = [{"id": i + 1, "u_rated": u_rated} for i in range(g.n_bus)]
+    line, transformer, shunt, sym_load, sym_gen, source, regulator = [], [], [], [], [], [], []
+    for b in range(g.n_branch):
+        f, t = int(g.br_from[b]) + 1, int(g.br_to[b]) + 1
+        r, x, bc = float(g.br_r[b]), float(g.br_x[b]), float(g.br_b[b])
+        if not g.br_is_trafo[b]:
+            line.append({"id": new_id(), "from_node": f, "to_node": t, "from_status": 1,
+                         "to_status": 1, "r1": r * zb, "x1": x * zb, "c1": bc / (omega * zb),
+                         "tan1": 0.0, "r0": r * zb, "x0": x * zb, "c0": bc / (omega * zb),
+                         "tan0": 0.0})
+            continue
+        k = float(g.br_tap[b])
+        transformer.append({"id": new_id(), "from_node": f, "to_node": t, "from_status": 1,
+                            "to_status": 1, "u1": u_rated, "u2": u_rated, "sn": s_base,
+                            "uk": math.hypot(r, x), "pk": r * s_base, "i0": 0.0, "p0": 0.0,
+                            "winding_from": 0, "winding_to": 0, "clock": 0, "tap_side": 0,
+                            "tap_pos": 1, "tap_min": 0, "tap_max": 1, "tap_nom": 0,
+                            "tap_size": (k - 1.0) * u_rated})
+        if bc != 0.0:
+            base_y = s_base / (u_rated * u_rated)
+            for nd, y in ((f, bc / 2.0 / (k * k)), (t, bc / 2.0)):
+                shunt.append({"id": new_id(), "node": nd, "status": 1, "g1": 0.0, "b1": y * base_y,
+                              "g0": 0.0, "b0": 0.0})
+    for i in range(g.n_bus):
+        bt = int(g.bus_type[i])
+        if bt == G.BUS_PQ:
+            sym_load.append({"id": new_id(), "node": i + 1, "status": 1, "type": 0,
+                             "p_specified": -float(g.p_spec[i]) * s_base,
+                             "q_specified": -float(g.q_spec[i]) * s_base})
+        elif bt == G.BUS_PV:
+            gid = new_id()
+            sym_gen.append({"id": gid, "node": i + 1, "status": 1, "type": 0,
+                            "p_specified": float(g.p_spec[i]) * s_base, "q_specified": 0.0})
+            regulator.append({"id": new_id(), "regulated_object": gid, "status": 1,
+                              "u_ref": float(g.vm[i])})
+        else:
+            source.append({"id": new_id(), "node": i + 1, "status": 1, "u_ref": float(g.vm[i]),
+                           "sk": sk, "rx_ratio": rx_ratio, "z01_ratio": 1.0})
+    data = {"node": node, "line": line, "transformer": transformer, "shunt": shunt,
+            "sym_load": sym_load, "sym_gen": sym_gen, "source": source,
+            "voltage_regulator": regulator}
+    return {"version": "1.0", "type": "input", "is_batch": False, "attributes": {}, "data": data}

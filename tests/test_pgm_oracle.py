@@ -45,3 +45,31 @@ def test_pgm_conversion_pieces():
     cols = set(net.ybus.indices[net.ybus.indptr[star]:net.ybus.indptr[star + 1]])
     assert cols == {star} | {net.id_to_idx[int(doc["data"]["three_winding_transformer"][0][k])]
                              for k in ("node_1", "node_2", "node_3")}
+
+
+def test_from_grid_round_trip(oracle_mod):
+    """A generated grid written as a PGM document and converted back: the
+    same Y-bus between the grid's buses (to rounding; the slack bus's
+    diagonal gains the source admittance), injections, PV set-points and bus
+    types, one extra slack bus for the source; and it solves."""
+    g = G.config_grid("case118")
+    net = pgm.convert(pgm.from_grid(g))
+    n = g.n_bus
+    assert net.n_bus == n + 1 and net.bus_type[n] == G.BUS_SLACK and net.vm[n] == g.vm[0]
+    a = G.build_ybus(g).dense()
+    b = net.ybus.dense()[:n, :n]
+    d = np.abs(a - b)
+    z_s = complex(*pgm.source_impedance_pu(1e10, 0.1, pgm.S_BASE_VA))
+    assert abs(d[0, 0] - abs(1.0 / z_s)) < 1e-6 * abs(1.0 / z_s)
+    d[0, 0] = 0.0
+    assert d.max() < 1e-14 * np.abs(a).max()
+    expect_type = np.where(g.bus_type == G.BUS_SLACK, G.BUS_PQ, g.bus_type)
+    np.testing.assert_array_equal(net.bus_type[:n], expect_type)
+    ns = g.bus_type != G.BUS_SLACK
+    pq = g.bus_type == G.BUS_PQ
+    assert np.max(np.abs(net.p_spec[:n][ns] - g.p_spec[ns])) < 1e-15
+    assert np.max(np.abs(net.q_spec[:n][pq] - g.q_spec[pq])) < 1e-15
+    np.testing.assert_array_equal(net.vm[:n][g.bus_type == G.BUS_PV], g.vm[g.bus_type == G.BUS_PV])
+    ot = oracle_topology(oracle_mod, net.ybus, net.bus_type)
+    r = ot.batch_solve(net.p_spec[None], net.q_spec[None], net.vm, net.va, tol=1e-8, max_iter=20)
+    assert r["status"][0] == 0
