@@ -99,6 +99,22 @@ __global__ void k_gather_rows(const double* __restrict__ src, int B, int N, int 
   }
 }
 
+// Uniformly scaled injections: p[s][i] = p_base[i] * scale[s] (and q), the
+// scenarios of uniform_load_scaling (src/batch.rs:98-106; a bus with no
+// injection stays at zero either way)
+__global__ void k_scale_rows(const double* __restrict__ p_base, const double* __restrict__ q_base,
+                             const double* __restrict__ scale, int B, int N, double* __restrict__ p,
+                             double* __restrict__ q) {
+  const size_t total = (size_t)B * N;
+  for (size_t t = blockIdx.x * (size_t)blockDim.x + threadIdx.x; t < total;
+       t += (size_t)gridDim.x * blockDim.x) {
+    const int s = (int)(t / N), i = (int)(t % N);
+    const double f = scale[s];
+    p[t] = p_base[i] * f;
+    q[t] = q_base[i] * f;
+  }
+}
+
 // dst row r = src row idx[r] (rows of `w` elements of 4 or 8 bytes), and back
 template <typename E>
 __global__ void k_take_rows(const E* __restrict__ src, int w, const int32_t* __restrict__ idx,
@@ -467,7 +483,7 @@ using namespace gox;
 // opaque handles
 
 struct IoStage {
-  DevMem p, q, vm, va, ovm, ova, it, st, mm, h, sl, dre, dim;
+  DevMem p, q, vm, va, ovm, ova, it, st, mm, h, sl, dre, dim, pb, qb, sc;
 };
 
 // The linear initial guess system of a topology (src/network.rs:627-678),
@@ -1293,6 +1309,73 @@ int gox_batch_solve(gox_topo* t, int32_t B, const double* p_spec, const double* 
     GOX_CK(cudaMemcpyAsync(max_mismatch, dmm.p, (size_t)B * 8, cudaMemcpyDeviceToHost, st));
     if (history)
       GOX_CK(cudaMemcpyAsync(history, dh.p, (size_t)B * max_iter * 8, cudaMemcpyDeviceToHost, st));
+    GOX_CK(cudaStreamSynchronize(st));
+    return GOX_OK;
+  });
+}
+
+int gox_batch_solve_scaled(gox_topo* t, int32_t B, const double* scales, const double* p_base,
+                           const double* q_base, const double* vm0, const double* va0, double tol,
+                           int32_t max_iter, int32_t precision, double* vm_out, double* va_out,
+                           int32_t* iterations, int32_t* status, double* max_mismatch,
+                           double* history) {
+  int c = check_batch_args(t, B, p_base, q_base, vm0, va0, 0, tol, max_iter, precision, vm_out,
+                           va_out, iterations, status, max_mismatch, nullptr, nullptr, nullptr);
+  if (c <= 0) return c;
+  if (!scales) return GOX_E_INVALID;
+  const int n = t->n_bus;
+  if (max_iter == 0) {
+    std::vector<double> hp((size_t)B * n), hq((size_t)B * n);
+    for (int s = 0; s < B; s++)
+      for (int i = 0; i < n; i++) {
+        hp[(size_t)s * n + i] = p_base[i] * scales[s];
+        hq[(size_t)s * n + i] = q_base[i] * scales[s];
+      }
+    std::vector<int> none;
+    host_only_result(t, B, hp.data(), hq.data(), vm0, va0, 0, nullptr, nullptr, nullptr, tol, 0,
+                     vm_out, va_out, iterations, status, max_mismatch, history, none);
+    return GOX_OK;
+  }
+  if (int r = require_device()) return r;
+  return guard_impl([&]() -> int {
+    cudaStream_t st = nullptr;
+    GOX_CK(cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking));
+    struct StreamGuard {
+      cudaStream_t s;
+      ~StreamGuard() { cudaStreamDestroy(s); }
+    } sg{st};
+    const size_t bn = (size_t)B * n;
+    IoStage& io = t->io;
+    io.p.ensure(bn * 8); io.q.ensure(bn * 8); io.vm.ensure((size_t)n * 8); io.va.ensure((size_t)n * 8);
+    io.pb.ensure((size_t)n * 8); io.qb.ensure((size_t)n * 8); io.sc.ensure((size_t)B * 8);
+    io.ovm.ensure(bn * 8); io.ova.ensure(bn * 8); io.it.ensure((size_t)B * 4);
+    io.st.ensure((size_t)B * 4); io.mm.ensure((size_t)B * 8);
+    if (history) io.h.ensure((size_t)B * max_iter * 8);
+    GOX_CK(cudaMemcpyAsync(io.pb.p, p_base, (size_t)n * 8, cudaMemcpyHostToDevice, st));
+    GOX_CK(cudaMemcpyAsync(io.qb.p, q_base, (size_t)n * 8, cudaMemcpyHostToDevice, st));
+    GOX_CK(cudaMemcpyAsync(io.sc.p, scales, (size_t)B * 8, cudaMemcpyHostToDevice, st));
+    GOX_CK(cudaMemcpyAsync(io.vm.p, vm0, (size_t)n * 8, cudaMemcpyHostToDevice, st));
+    GOX_CK(cudaMemcpyAsync(io.va.p, va0, (size_t)n * 8, cudaMemcpyHostToDevice, st));
+    k_scale_rows<<<grid1d(bn), 256, 0, st>>>(io.pb.as<double>(), io.qb.as<double>(),
+                                             io.sc.as<double>(), B, n, io.p.as<double>(),
+                                             io.q.as<double>());
+    GOX_CK(cudaGetLastError());
+    // the pivot search (first call) reads the scaled injections back from the device
+    int r = batch_device(t, B, io.p.as<double>(), io.q.as<double>(), io.vm.as<double>(),
+                         io.va.as<double>(), 0, nullptr, nullptr, nullptr, tol, max_iter, precision,
+                         io.ovm.as<double>(), io.ova.as<double>(), io.it.as<int32_t>(),
+                         io.st.as<int32_t>(), io.mm.as<double>(),
+                         history ? io.h.as<double>() : nullptr, st, nullptr, nullptr, nullptr,
+                         nullptr, nullptr, nullptr, nullptr);
+    t->launches += 1;
+    if (r != GOX_OK) return r;
+    GOX_CK(cudaMemcpyAsync(vm_out, io.ovm.p, bn * 8, cudaMemcpyDeviceToHost, st));
+    GOX_CK(cudaMemcpyAsync(va_out, io.ova.p, bn * 8, cudaMemcpyDeviceToHost, st));
+    GOX_CK(cudaMemcpyAsync(iterations, io.it.p, (size_t)B * 4, cudaMemcpyDeviceToHost, st));
+    GOX_CK(cudaMemcpyAsync(status, io.st.p, (size_t)B * 4, cudaMemcpyDeviceToHost, st));
+    GOX_CK(cudaMemcpyAsync(max_mismatch, io.mm.p, (size_t)B * 8, cudaMemcpyDeviceToHost, st));
+    if (history)
+      GOX_CK(cudaMemcpyAsync(history, io.h.p, (size_t)B * max_iter * 8, cudaMemcpyDeviceToHost, st));
     GOX_CK(cudaStreamSynchronize(st));
     return GOX_OK;
   });

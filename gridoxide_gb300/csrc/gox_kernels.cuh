@@ -1105,26 +1105,31 @@ __global__ void __launch_bounds__(256) k_guess_fill(GuessDev L, int B, const dou
 // The start point: every bus's given voltage, then the PQ buses' solution
 // where the scenario's guess system was regular and the solution finite
 // (else they keep the given one, as the reference does when its solve fails).
+// (grid-stride loops: the launch's grid is capped)
 __global__ void k_guess_start(int B, int N, const double* __restrict__ vm0,
                               const double* __restrict__ va0, int v_stride, double* gvm, double* gva) {
-  const size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= (size_t)B * N) return;
-  const size_t s = i / N, b = i % N;
-  gvm[i] = vm0[s * v_stride + b];
-  gva[i] = va0[s * v_stride + b];
+  const size_t total = (size_t)B * N;
+  for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < total;
+       i += (size_t)gridDim.x * blockDim.x) {
+    const size_t s = i / N, b = i % N;
+    gvm[i] = vm0[s * v_stride + b];
+    gva[i] = va0[s * v_stride + b];
+  }
 }
 __global__ void k_guess_out(GuessDev L, int B, const double* __restrict__ sol,
                             const int32_t* __restrict__ sing, double* gvm, double* gva) {
-  const size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= (size_t)B * L.m) return;
-  const int s = (int)(i / L.m), r = (int)(i % L.m);
-  const int g = s / 32, lane = s % 32;
-  const double re = sol[((size_t)g * L.n2 + __ldg(L.qinv + 2 * r)) * 32 + lane];
-  const double im = sol[((size_t)g * L.n2 + __ldg(L.qinv + 2 * r + 1)) * 32 + lane];
-  if (sing[s] != 0 || !isfinite(re) || !isfinite(im)) return;
-  const size_t x = (size_t)s * L.n_bus + __ldg(L.pq_bus + r);
-  gvm[x] = hypot(re, im);
-  gva[x] = atan2(im, re);
+  const size_t total = (size_t)B * L.m;
+  for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < total;
+       i += (size_t)gridDim.x * blockDim.x) {
+    const int s = (int)(i / L.m), r = (int)(i % L.m);
+    const int g = s / 32, lane = s % 32;
+    const double re = sol[((size_t)g * L.n2 + __ldg(L.qinv + 2 * r)) * 32 + lane];
+    const double im = sol[((size_t)g * L.n2 + __ldg(L.qinv + 2 * r + 1)) * 32 + lane];
+    if (sing[s] != 0 || !isfinite(re) || !isfinite(im)) continue;
+    const size_t x = (size_t)s * L.n_bus + __ldg(L.pq_bus + r);
+    gvm[x] = hypot(re, im);
+    gva[x] = atan2(im, re);
+  }
 }
 
 // ---------------------------------------------------------------------------

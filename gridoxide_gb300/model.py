@@ -115,9 +115,7 @@ class PowerFlowModel:
         net = self._net
         res = self._topology().solve(p, q, net.vm, net.va, tol=self.tol, max_iter=self.max_iter,
                                      precision=self._precision)
-        return [BatchResult(res.voltage_mag[s], res.voltage_ang[s], int(res.iterations[s]),
-                            bool(res.status[s] == GOX_CONVERGED), float(res.max_mismatch[s]))
-                for s in range(p.shape[0])]
+        return _results(res)
 
     def solve_batch(self, scenarios, threads=None) -> list:
         """python.rs:279-321: per scenario a list of (bus, p_spec, q_spec)
@@ -142,10 +140,13 @@ class PowerFlowModel:
         """python.rs:323-343: every scale one scenario with the loaded buses'
         p_spec and q_spec multiplied by it (uniform_load_scaling,
         src/batch.rs:98-106)."""
-        f = np.asarray(scales, np.float64).reshape(-1, 1)
+        f = np.asarray(scales, np.float64).ravel()
         if f.shape[0] == 0:
             return []
-        return self._run_batch(self._net.p_spec[None] * f, self._net.q_spec[None] * f)
+        net = self._net
+        res = self._topology().solve_scaled(f, net.p_spec, net.q_spec, net.vm, net.va, tol=self.tol,
+                                            max_iter=self.max_iter, precision=self._precision)
+        return _results(res)
 
     def ybus_triplets(self):
         """python.rs:351-377: (rows, cols, g, b), row-major, columns ascending."""
@@ -183,6 +184,12 @@ class PowerFlowModel:
     def voltage_kv(self):
         """python.rs:428-434: |V| times the bus's rated voltage, in kV."""
         return (self._vm * self._template.u_rated / 1e3).tolist()
+
+
+def _results(res) -> list:
+    """One BatchResult per scenario (rows of the batch's arrays)."""
+    return list(map(BatchResult, res.voltage_mag, res.voltage_ang, res.iterations.tolist(),
+                    (res.status == GOX_CONVERGED).tolist(), res.max_mismatch.tolist()))
 
 
 def _gox():

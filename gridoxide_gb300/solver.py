@@ -227,6 +227,28 @@ class Topology:
         check(rc, "gox_batch_solve")
         return BatchResult(vm, va, iters, status, mis, hist)
 
+    def solve_scaled(self, scales, p_base, q_base, vm0, va0, tol=1e-8, max_iter=20,
+                     precision=GOX_PRECISION_MIXED, history=False) -> BatchResult:
+        """Batched NR over uniformly scaled injections (gox_batch_solve_scaled):
+        scenario s has p_base * scales[s], q_base * scales[s]; vm0/va0 [N]."""
+        L = _lib.load()
+        scales = _f64(np.ravel(scales))
+        p_base, q_base, vm0, va0 = _f64(p_base), _f64(q_base), _f64(vm0), _f64(va0)
+        B, n = scales.shape[0], self.n_bus
+        if any(a.shape != (n,) for a in (p_base, q_base, vm0, va0)):
+            raise ValueError("p_base/q_base/vm0/va0 must be [n_bus]")
+        vm, va = np.empty((B, n)), np.empty((B, n))
+        iters, status, mis = np.zeros(B, np.int32), np.zeros(B, np.int32), np.zeros(B)
+        hist = np.zeros((B, max_iter)) if history else None
+        check(L.gox_batch_solve_scaled(self._h, B, _p(scales, _lib.f64p), _p(p_base, _lib.f64p),
+                                       _p(q_base, _lib.f64p), _p(vm0, _lib.f64p),
+                                       _p(va0, _lib.f64p), float(tol), int(max_iter),
+                                       int(precision), _p(vm, _lib.f64p), _p(va, _lib.f64p),
+                                       _p(iters, _lib.i32p), _p(status, _lib.i32p),
+                                       _p(mis, _lib.f64p), _p(hist, _lib.f64p)),
+              "gox_batch_solve_scaled")
+        return BatchResult(vm, va, iters, status, mis, hist)
+
     def solve_device(self, p_spec, q_spec, vm0, va0, vm_out, va_out, iters, status, max_mis,
                      tol=1e-8, max_iter=20, precision=GOX_PRECISION_MIXED, outage=None,
                      history=None, stream=None):

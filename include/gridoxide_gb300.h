@@ -161,6 +161,19 @@ int gox_batch_solve_device(gox_topo *t, int32_t B, const double *p_spec, const d
                            int32_t *iterations, int32_t *status, double *max_mismatch,
                            double *history, void *stream);
 
+/* gox_batch_solve for the time-series / Monte Carlo shape: scenario s has
+ * p_spec = p_base * scales[s] and q_spec = q_base * scales[s] (host arrays
+ * p_base, q_base [n_bus], scales [B]; vm0/va0 [n_bus] shared).  Replaces
+ * `BatchSolver::solve` over `uniform_load_scaling` scenarios
+ * (src/batch.rs:98-106, the reference model's `solve_batch_scaled`,
+ * src/python.rs:323-343): the scenarios are expanded on the device, so only
+ * n_bus + B values cross to it.  Outputs as gox_batch_solve. */
+int gox_batch_solve_scaled(gox_topo *t, int32_t B, const double *scales, const double *p_base,
+                           const double *q_base, const double *vm0, const double *va0,
+                           double tol, int32_t max_iter, int32_t precision, double *vm_out,
+                           double *va_out, int32_t *iterations, int32_t *status,
+                           double *max_mismatch, double *history);
+
 /* Fixes the topology's pivot order on the host, without a GPU: the first
  * scenario whose start point misses `tol` has its Jacobian factored with
  * partial pivoting (KluNativeSystem::new on the first Jacobian a

@@ -103,3 +103,25 @@ def test_linear_guess_mixed_case2000(gox, oracle_mod):
     topo.set_initial_guess("given")
     flat = topo.solve(p, q, g.vm, g.va, precision=gox.GOX_PRECISION_MIXED)
     assert np.all(flat.status[ok] == gox.GOX_CONVERGED)
+
+
+def test_linear_guess_large_batch(gox, oracle_mod):
+    """A batch whose scenarios x buses exceed the capped launch grid of the
+    start-point kernels (4,864 blocks x 256 threads): every scenario gets
+    its own guess and converges."""
+    fx = load_fixture("case118")
+    g, yb = grid_from_fixture(fx), ybus_from_fixture(fx)
+    B = 12000
+    assert B * g.n_bus > 4864 * 256
+    p, q = G.load_scenarios(g, B, 0.15, 29)
+    topo = gox.Topology(yb, g.bus_type)
+    topo.set_initial_guess("linear")
+    gvm, gva = topo.initial_guess(p, q, g.vm, g.va)
+    for s in (0, B // 2, B - 1):
+        vm0, va0 = oracle_mod.linear_initial_guess(yb, g.bus_type, p[s], q[s], g.vm, g.va)
+        assert np.max(np.abs(gvm[s] - vm0)) < 1e-12
+        assert np.max(np.abs(gva[s] - va0)) < 1e-12
+    res = topo.solve(p, q, g.vm, g.va, precision=gox.GOX_PRECISION_MIXED)
+    assert np.all(res.status == gox.GOX_CONVERGED)
+    ref = topo.solve(p[-32:], q[-32:], g.vm, g.va, precision=gox.GOX_PRECISION_MIXED)
+    np.testing.assert_array_equal(res.iterations[-32:], ref.iterations)

@@ -75,3 +75,22 @@ def test_model_batch_scaled(gox, oracle_mod):
     ov = m.solve_batch(sc)
     for a, b in zip(ov, out[:8]):
         np.testing.assert_array_equal(a.voltage_mag, b.voltage_mag)
+
+
+def test_solve_scaled_equals_explicit(gox):
+    """gox_batch_solve_scaled (scenarios expanded on the device) gives the
+    results of gox_batch_solve on the same scaled arrays, bit for bit."""
+    from gridoxide_gb300 import grids as G
+    from helpers import grid_from_fixture, load_fixture, ybus_from_fixture
+    fx = load_fixture("case118")
+    g, yb = grid_from_fixture(fx), ybus_from_fixture(fx)
+    f = np.random.default_rng(5).uniform(0.8, 1.2, 200)
+    for prec in (gox.GOX_PRECISION_FP64, gox.GOX_PRECISION_MIXED):
+        topo = gox.Topology(yb, g.bus_type)
+        a = topo.solve_scaled(f, g.p_spec, g.q_spec, g.vm, g.va, precision=prec, history=True)
+        b = topo.solve(g.p_spec[None] * f[:, None], g.q_spec[None] * f[:, None], g.vm, g.va,
+                       precision=prec, history=True)
+        for x, y in ((a.voltage_mag, b.voltage_mag), (a.voltage_ang, b.voltage_ang),
+                     (a.iterations, b.iterations), (a.status, b.status), (a.history, b.history)):
+            np.testing.assert_array_equal(x, y)
+        assert np.all(a.status == gox.GOX_CONVERGED)
