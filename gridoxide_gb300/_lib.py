@@ -68,6 +68,9 @@ SIGNATURES = {
     "gox_batch_solve": (C.c_int, [vp, C.c_int32, f64p, f64p, f64p, f64p, C.c_int32, i32p, f64p,
                                   f64p, C.c_double, C.c_int32, C.c_int32, f64p, f64p, i32p, i32p,
                                   f64p, f64p]),
+    "gox_batch_solve_qlim": (C.c_int, [vp, C.c_int32, f64p, f64p, f64p, f64p, C.c_int32, f64p, f64p,
+                                       C.c_double, C.c_int32, C.c_int32, C.c_int32, f64p, f64p, i32p,
+                                       i32p, f64p, i32p, C.POINTER(C.c_uint8), i32p]),
     "gox_batch_solve_scaled": (C.c_int, [vp, C.c_int32, f64p, f64p, f64p, f64p, f64p, C.c_double,
                                          C.c_int32, C.c_int32, f64p, f64p, i32p, i32p, f64p,
                                          f64p]),

@@ -537,6 +537,12 @@ struct gox_topo {
     s += zip[(size_t)(2 + part) * n_bus + i] * vm;
     return s;
   }
+  // Q-limit enforcement: this topology with PV buses switched to PQ, keyed by
+  // the sorted switched buses (owned; built on first use)
+  std::vector<std::pair<std::vector<int32_t>, gox_topo*>> variants;
+  ~gox_topo() {
+    for (auto& v : variants) delete v.second;
+  }
 };
 
 struct gox_ls {
@@ -1111,6 +1117,67 @@ static int batch_device(gox_topo* t, int B, const double* p_spec, const double* 
   return GOX_OK;
 }
 
+// ---------------------------------------------------------------------------
+// Q-limit enforcement (newton_raphson_enforcing_q_limits, src/solver.rs:545-618)
+// over a batch: scenarios are grouped by the set of PV buses they have
+// switched to PQ, each group solved on the topology variant with those bus
+// types, warm started from its previous state.
+
+// Computed Q of buses `bus[k]` for every scenario, from row-major V [B][N]
+__global__ void k_qcalc(int B, int N, const int32_t* __restrict__ yp, const int32_t* __restrict__ yi,
+                        const double* __restrict__ yre, const double* __restrict__ yim,
+                        const double* __restrict__ vm, const double* __restrict__ va,
+                        const int32_t* __restrict__ bus, int nb, double* __restrict__ qout) {
+  const size_t total = (size_t)B * nb;
+  for (size_t t = blockIdx.x * (size_t)blockDim.x + threadIdx.x; t < total;
+       t += (size_t)gridDim.x * blockDim.x) {
+    const int s = (int)(t / nb), i = bus[t % nb];
+    const double* vms = vm + (size_t)s * N;
+    const double* vas = va + (size_t)s * N;
+    double ir = 0.0, ii = 0.0;
+    for (int p = yp[i]; p < yp[i + 1]; p++) {
+      const int j = yi[p];
+      double sn, cs;
+      sincos(vas[j], &sn, &cs);
+      const double e = vms[j] * cs, f = vms[j] * sn;
+      ir += yre[p] * e - yim[p] * f;
+      ii += yre[p] * f + yim[p] * e;
+    }
+    double sn, cs;
+    sincos(vas[i], &sn, &cs);
+    const double e = vms[i] * cs, f = vms[i] * sn;
+    qout[t] = f * ir - e * ii;
+  }
+}
+
+// q[s][bus] = value for each pinned (scenario, bus, value)
+__global__ void k_pin(int m, const int32_t* __restrict__ sb, const double* __restrict__ val, int N,
+                      double* __restrict__ q) {
+  const int k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k < m) q[(size_t)sb[2 * k] * N + sb[2 * k + 1]] = val[k];
+}
+
+// The variant of `t` with `switched` (sorted) PV buses made PQ
+static gox_topo* topo_variant(gox_topo* t, const std::vector<int32_t>& switched) {
+  if (switched.empty()) return t;
+  for (auto& v : t->variants)
+    if (v.first == switched) return v.second;
+  std::unique_ptr<gox_topo> v(new gox_topo());
+  v->n_bus = t->n_bus;
+  v->yp = t->yp; v->yi = t->yi; v->yre = t->yre; v->yim = t->yim;
+  v->bus_type = t->bus_type;
+  for (int b : switched) v->bus_type[b] = 1;
+  v->jac = jac_analyze(v->n_bus, v->yp.data(), v->yi.data(), v->bus_type.data());
+  v->csc = build_csc(v->jac.n_u, v->jac.nnz(), v->jac.rows.data(), v->jac.cols.data());
+  v->sym = klu_analyze(v->jac.n_u, v->csc.p.data(), v->csc.i.data());
+  v->device = t->device;
+  v->piv_tol = t->piv_tol;
+  v->zip = t->zip;
+  if (!v->zip.empty()) upload(v->dzip, v->zip);
+  t->variants.emplace_back(switched, v.get());
+  return v.release();
+}
+
 extern "C" {
 
 const char* gox_version(void) { return "gridoxide_gb300 0.1.0 (sm_103a)"; }
@@ -1377,6 +1444,159 @@ int gox_batch_solve_scaled(gox_topo* t, int32_t B, const double* scales, const d
     if (history)
       GOX_CK(cudaMemcpyAsync(history, io.h.p, (size_t)B * max_iter * 8, cudaMemcpyDeviceToHost, st));
     GOX_CK(cudaStreamSynchronize(st));
+    return GOX_OK;
+  });
+}
+
+int gox_batch_solve_qlim(gox_topo* t, int32_t B, const double* p_spec, const double* q_spec,
+                         const double* vm0, const double* va0, int32_t v_stride,
+                         const double* q_min, const double* q_max, double tol, int32_t max_iter,
+                         int32_t max_outer, int32_t precision, double* vm_out, double* va_out,
+                         int32_t* iterations, int32_t* status, double* max_mismatch,
+                         int32_t* n_switched, uint8_t* switched, int32_t* stabilized) {
+  int c = check_batch_args(t, B, p_spec, q_spec, vm0, va0, v_stride, tol, max_iter, precision,
+                           vm_out, va_out, iterations, status, max_mismatch, nullptr, nullptr,
+                           nullptr);
+  if (c <= 0) return c;
+  if (!q_min || !q_max || !n_switched || !stabilized || max_outer < 1 || max_iter < 1)
+    return GOX_E_INVALID;
+  if (int r = require_device()) return r;
+  return guard_impl([&]() -> int {
+    const int n = t->n_bus;
+    cudaStream_t st = nullptr;
+    GOX_CK(cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking));
+    struct StreamGuard {
+      cudaStream_t s;
+      ~StreamGuard() { cudaStreamDestroy(s); }
+    } sg{st};
+    const size_t bn = (size_t)B * n, nv = (size_t)(v_stride ? B : 1) * n;
+    // the batch's state on the device: injections (q pinned as buses switch), V
+    DevMem dp, dq, dv0m, dv0a, dvm, dva, dit, dst, dmm;
+    dp.ensure(bn * 8); dq.ensure(bn * 8); dv0m.ensure(nv * 8); dv0a.ensure(nv * 8);
+    dvm.ensure(bn * 8); dva.ensure(bn * 8);
+    dit.ensure((size_t)B * 4); dst.ensure((size_t)B * 4); dmm.ensure((size_t)B * 8);
+    GOX_CK(cudaMemcpyAsync(dp.p, p_spec, bn * 8, cudaMemcpyHostToDevice, st));
+    GOX_CK(cudaMemcpyAsync(dq.p, q_spec, bn * 8, cudaMemcpyHostToDevice, st));
+    GOX_CK(cudaMemcpyAsync(dv0m.p, vm0, nv * 8, cudaMemcpyHostToDevice, st));
+    GOX_CK(cudaMemcpyAsync(dv0a.p, va0, nv * 8, cudaMemcpyHostToDevice, st));
+    // pass 1: every scenario on the topology as given (its own start rule)
+    int r = batch_device(t, B, dp.as<double>(), dq.as<double>(), dv0m.as<double>(),
+                         dv0a.as<double>(), v_stride, nullptr, nullptr, nullptr, tol, max_iter,
+                         precision, dvm.as<double>(), dva.as<double>(), dit.as<int32_t>(),
+                         dst.as<int32_t>(), dmm.as<double>(), nullptr, st, p_spec, q_spec, vm0,
+                         va0, nullptr, nullptr, nullptr);
+    if (r != GOX_OK) return r;
+    std::vector<int32_t> pv;  // the PV buses of the given topology
+    for (int i = 0; i < n; i++)
+      if (t->bus_type[i] == 2) pv.push_back(i);
+    const int npv = (int)pv.size();
+    std::vector<std::vector<int32_t>> sw(B);  // switched buses per scenario, sorted
+    std::vector<uint8_t> done(B, 0);
+    std::vector<int32_t> hst(B);
+    std::vector<double> hq((size_t)B * std::max(npv, 1));
+    DevMem dyp, dyi, dyre, dyim, dpv, dqc, dix, sp, sq, svm, sva, ovm, ova, oit, ost, omm, dsb, dval;
+    upload(dyp, t->yp); upload(dyi, t->yi); upload(dyre, t->yre); upload(dyim, t->yim);
+    upload(dpv, pv);
+    dqc.ensure((size_t)B * std::max(npv, 1) * 8);
+    for (int s = 0; s < B; s++) stabilized[s] = 1;
+    for (int pass = 1;; pass++) {
+      GOX_CK(cudaMemcpyAsync(hst.data(), dst.p, (size_t)B * 4, cudaMemcpyDeviceToHost, st));
+      if (npv > 0) {
+        k_qcalc<<<grid1d((size_t)B * npv), 256, 0, st>>>(
+            B, n, dyp.as<int32_t>(), dyi.as<int32_t>(), dyre.as<double>(), dyim.as<double>(),
+            dvm.as<double>(), dva.as<double>(), dpv.as<int32_t>(), npv, dqc.as<double>());
+        GOX_CK(cudaGetLastError());
+        GOX_CK(cudaMemcpyAsync(hq.data(), dqc.p, (size_t)B * npv * 8, cudaMemcpyDeviceToHost, st));
+      }
+      GOX_CK(cudaStreamSynchronize(st));
+      // PV -> PQ switching of every settled scenario, pinning Q at the violated limit
+      std::vector<int32_t> pin_sb;
+      std::vector<double> pin_val;
+      std::map<std::vector<int32_t>, std::vector<int32_t>> groups;
+      for (int s = 0; s < B; s++) {
+        if (done[s]) continue;
+        if (hst[s] != GOX_CONVERGED) {  // not settled: that pass's report stands
+          done[s] = 1;
+          continue;
+        }
+        bool any = false;
+        std::vector<int32_t>& w = sw[s];
+        const std::vector<int32_t> before = w;
+        for (int k = 0; k < npv; k++) {
+          const int b = pv[k];
+          if (std::binary_search(before.begin(), before.end(), b)) continue;  // already PQ
+          const double qc = hq[(size_t)s * npv + k];
+          double lim;
+          if (qc < q_min[b]) lim = q_min[b];
+          else if (qc > q_max[b]) lim = q_max[b];
+          else continue;
+          pin_sb.insert(pin_sb.end(), {s, b});
+          pin_val.push_back(lim);
+          w.push_back(b);
+          any = true;
+        }
+        if (!any) {
+          done[s] = 1;
+          continue;
+        }
+        std::sort(w.begin(), w.end());
+        if (pass == max_outer) {  // outer budget spent: the last solve's report, not stabilized
+          done[s] = 1;
+          stabilized[s] = 0;
+          continue;
+        }
+        groups[w].push_back(s);
+      }
+      if (!pin_val.empty()) {
+        upload(dsb, pin_sb);
+        upload(dval, pin_val);
+        const int m = (int)pin_val.size();
+        k_pin<<<(m + 255) / 256, 256, 0, st>>>(m, dsb.as<int32_t>(), dval.as<double>(), n,
+                                               dq.as<double>());
+        GOX_CK(cudaGetLastError());
+      }
+      if (groups.empty()) break;
+      // re-solve each group on its variant, warm started from its state
+      for (auto& gk : groups) {
+        gox_topo* v = topo_variant(t, gk.first);
+        const std::vector<int32_t>& idx = gk.second;
+        const int Bg = (int)idx.size();
+        const size_t rows = (size_t)Bg * n;
+        upload(dix, idx);
+        const int32_t* ix = dix.as<int32_t>();
+        sp.ensure(rows * 8); sq.ensure(rows * 8); svm.ensure(rows * 8); sva.ensure(rows * 8);
+        ovm.ensure(rows * 8); ova.ensure(rows * 8);
+        oit.ensure((size_t)Bg * 4); ost.ensure((size_t)Bg * 4); omm.ensure((size_t)Bg * 8);
+        k_take_rows<double><<<grid1d(rows), 256, 0, st>>>(dp.as<double>(), n, ix, Bg, sp.as<double>());
+        k_take_rows<double><<<grid1d(rows), 256, 0, st>>>(dq.as<double>(), n, ix, Bg, sq.as<double>());
+        k_take_rows<double><<<grid1d(rows), 256, 0, st>>>(dvm.as<double>(), n, ix, Bg, svm.as<double>());
+        k_take_rows<double><<<grid1d(rows), 256, 0, st>>>(dva.as<double>(), n, ix, Bg, sva.as<double>());
+        r = batch_device(v, Bg, sp.as<double>(), sq.as<double>(), svm.as<double>(), sva.as<double>(),
+                         n, nullptr, nullptr, nullptr, tol, max_iter, precision, ovm.as<double>(),
+                         ova.as<double>(), oit.as<int32_t>(), ost.as<int32_t>(), omm.as<double>(),
+                         nullptr, st, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr);
+        if (r != GOX_OK) return r;
+        k_put_rows<double><<<grid1d(rows), 256, 0, st>>>(ovm.as<double>(), n, ix, Bg, dvm.as<double>());
+        k_put_rows<double><<<grid1d(rows), 256, 0, st>>>(ova.as<double>(), n, ix, Bg, dva.as<double>());
+        k_put_rows<int32_t><<<grid1d(Bg), 256, 0, st>>>(oit.as<int32_t>(), 1, ix, Bg, dit.as<int32_t>());
+        k_put_rows<int32_t><<<grid1d(Bg), 256, 0, st>>>(ost.as<int32_t>(), 1, ix, Bg, dst.as<int32_t>());
+        k_put_rows<double><<<grid1d(Bg), 256, 0, st>>>(omm.as<double>(), 1, ix, Bg, dmm.as<double>());
+        GOX_CK(cudaGetLastError());
+        GOX_CK(cudaStreamSynchronize(st));  // the staging buffers are reused by the next group
+      }
+    }
+    GOX_CK(cudaMemcpyAsync(vm_out, dvm.p, bn * 8, cudaMemcpyDeviceToHost, st));
+    GOX_CK(cudaMemcpyAsync(va_out, dva.p, bn * 8, cudaMemcpyDeviceToHost, st));
+    GOX_CK(cudaMemcpyAsync(iterations, dit.p, (size_t)B * 4, cudaMemcpyDeviceToHost, st));
+    GOX_CK(cudaMemcpyAsync(status, dst.p, (size_t)B * 4, cudaMemcpyDeviceToHost, st));
+    GOX_CK(cudaMemcpyAsync(max_mismatch, dmm.p, (size_t)B * 8, cudaMemcpyDeviceToHost, st));
+    GOX_CK(cudaStreamSynchronize(st));
+    for (int s = 0; s < B; s++) n_switched[s] = (int32_t)sw[s].size();
+    if (switched) {
+      std::fill(switched, switched + bn, (uint8_t)0);
+      for (int s = 0; s < B; s++)
+        for (int b : sw[s]) switched[(size_t)s * n + b] = 1;
+    }
     return GOX_OK;
   });
 }

@@ -227,6 +227,38 @@ class Topology:
         check(rc, "gox_batch_solve")
         return BatchResult(vm, va, iters, status, mis, hist)
 
+    def solve_qlim(self, p_spec, q_spec, vm0, va0, q_min, q_max, tol=1e-8, max_iter=20,
+                   max_outer=10, precision=GOX_PRECISION_MIXED):
+        """Batched NR enforcing the PV buses' reactive limits
+        (gox_batch_solve_qlim; newton_raphson_enforcing_q_limits,
+        src/solver.rs:545-618).  q_min/q_max [N] per unit.  Returns
+        (BatchResult of the last solves, switched [B, N] bool,
+        stabilized [B] bool)."""
+        L = _lib.load()
+        p_spec = _f64(np.atleast_2d(p_spec))
+        q_spec = _f64(np.atleast_2d(q_spec))
+        B, n = p_spec.shape
+        if n != self.n_bus or q_spec.shape != p_spec.shape:
+            raise ValueError("p_spec/q_spec must be [B, n_bus]")
+        vm0, va0, q_min, q_max = _f64(vm0), _f64(va0), _f64(q_min), _f64(q_max)
+        if q_min.shape != (n,) or q_max.shape != (n,):
+            raise ValueError("q_min/q_max must be [n_bus]")
+        vm, va = np.empty((B, n)), np.empty((B, n))
+        iters, status, mis = np.zeros(B, np.int32), np.zeros(B, np.int32), np.zeros(B)
+        nsw, stab = np.zeros(B, np.int32), np.zeros(B, np.int32)
+        sw = np.zeros((B, n), np.uint8)
+        check(L.gox_batch_solve_qlim(self._h, B, _p(p_spec, _lib.f64p), _p(q_spec, _lib.f64p),
+                                     _p(vm0, _lib.f64p), _p(va0, _lib.f64p),
+                                     n if vm0.ndim == 2 else 0, _p(q_min, _lib.f64p),
+                                     _p(q_max, _lib.f64p), float(tol), int(max_iter),
+                                     int(max_outer), int(precision), _p(vm, _lib.f64p),
+                                     _p(va, _lib.f64p), _p(iters, _lib.i32p), _p(status, _lib.i32p),
+                                     _p(mis, _lib.f64p), _p(nsw, _lib.i32p),
+                                     sw.ctypes.data_as(C.POINTER(C.c_uint8)), _p(stab, _lib.i32p)),
+              "gox_batch_solve_qlim")
+        assert np.array_equal(nsw, sw.sum(axis=1))
+        return BatchResult(vm, va, iters, status, mis, None), sw.astype(bool), stab.astype(bool)
+
     def solve_scaled(self, scales, p_base, q_base, vm0, va0, tol=1e-8, max_iter=20,
                      precision=GOX_PRECISION_MIXED, history=False) -> BatchResult:
         """Batched NR over uniformly scaled injections (gox_batch_solve_scaled):

@@ -174,6 +174,26 @@ int gox_batch_solve_scaled(gox_topo *t, int32_t B, const double *scales, const d
                            double *va_out, int32_t *iterations, int32_t *status,
                            double *max_mismatch, double *history);
 
+/* Batched solve with reactive-power limits on the PV buses: per scenario
+ * the reference's newton_raphson_enforcing_q_limits (src/solver.rs:545-618).
+ * After a converged solve, every PV bus whose computed Q lies outside
+ * [q_min[b], q_max[b]] (per unit, arrays [n_bus]; -inf/+inf for none)
+ * becomes PQ with q_spec pinned at the violated limit, and the scenario is
+ * solved again from its converged state; repeated until no bus switches
+ * (stabilized = 1) or max_outer solves have run (stabilized = 0, the last
+ * solve's report).  A scenario whose solve did not converge stops with that
+ * report.  Switching is one-way.  Scenarios with the same switched set are
+ * solved together on a cached variant of the topology with those bus types.
+ * iterations / status / max_mismatch describe the last solve; n_switched [B]
+ * counts the switched buses and `switched` ([B][n_bus] bytes, or NULL)
+ * marks them.  Inputs and outputs are host arrays as in gox_batch_solve. */
+int gox_batch_solve_qlim(gox_topo *t, int32_t B, const double *p_spec, const double *q_spec,
+                         const double *vm0, const double *va0, int32_t v_stride,
+                         const double *q_min, const double *q_max, double tol, int32_t max_iter,
+                         int32_t max_outer, int32_t precision, double *vm_out, double *va_out,
+                         int32_t *iterations, int32_t *status, double *max_mismatch,
+                         int32_t *n_switched, uint8_t *switched, int32_t *stabilized);
+
 /* Fixes the topology's pivot order on the host, without a GPU: the first
  * scenario whose start point misses `tol` has its Jacobian factored with
  * partial pivoting (KluNativeSystem::new on the first Jacobian a

@@ -79,3 +79,40 @@ def pgm_oracle_start(O, net):
         return net.vm.copy(), net.va.copy()
     return O.linear_initial_guess(net.ybus, net.bus_type, net.p_spec, net.q_spec, net.vm, net.va,
                                   net.zip_imp, net.zip_cur)
+
+
+def oracle_qlim(O, yb, bus_type, p, q, vm0, va0, q_min, q_max, tol, max_iter, max_outer):
+    """newton_raphson_enforcing_q_limits_with_stats (src/solver.rs:569-618)
+    for one scenario on the oracle: solve; stop unless converged; switch
+    every PV bus whose computed Q (src/network.rs power_injections) leaves
+    [q_min, q_max] to PQ with Q pinned at the limit; solve again from the
+    converged state with a fresh pivot order (PersistentSolver::reset);
+    repeat until nothing switches or max_outer solves ran.  Returns
+    (report dict of the last solve, switched buses, stabilized)."""
+    types = np.array(bus_type, np.int32).copy()
+    q = np.array(q, np.float64).copy()
+    vm, va = np.array(vm0, np.float64), np.array(va0, np.float64)
+    switches = []
+    r = None
+    for _ in range(max_outer):
+        ot = oracle_topology(O, yb, types)
+        r = ot.batch_solve(np.asarray(p)[None], q[None], vm, va, tol=tol, max_iter=max_iter)
+        vm, va = r["vm"][0], r["va"][0]
+        if r["status"][0] != 0:
+            return r, switches, True
+        _, qc = O.injections(yb, vm, va)
+        switched = False
+        for b in range(len(types)):
+            if types[b] != G.BUS_PV:
+                continue
+            if qc[b] < q_min[b]:
+                types[b], q[b] = G.BUS_PQ, q_min[b]
+            elif qc[b] > q_max[b]:
+                types[b], q[b] = G.BUS_PQ, q_max[b]
+            else:
+                continue
+            switches.append(b)
+            switched = True
+        if not switched:
+            return r, switches, True
+    return r, switches, False
