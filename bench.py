@@ -322,6 +322,65 @@ def pgm_batch(gox, rounds: int, batch: int = 4096) -> dict:
     return out
 
 
+def qlim_case2000(gox, rounds: int, batch: int = 4096) -> dict:
+    """Q-limit leg: case2000 x `batch` (loads x lognormal(0, 0.15), flat
+    start), reactive limits on the six PV buses with the largest |Q| at the
+    25 % / 75 % quantiles of their unconstrained Q over the batch (floor for
+    the three most negative, ceiling for the three most positive), so each
+    scenario trips its own subset; gox_batch_solve_qlim, mixed precision,
+    host buffers.  The first call builds a topology variant per switched set;
+    the timed calls reuse them."""
+    from gridoxide_gb300 import grids as G
+    g = G.config_grid("case2000")
+    yb = G.build_ybus(g)
+    p, q = G.load_scenarios(g, batch, WORKLOAD["sigma"], 2031)
+    plain = gox.Topology(yb, g.bus_type).solve(p, q, g.vm, g.va, tol=WORKLOAD["tol"],
+                                               max_iter=WORKLOAD["max_iter"],
+                                               precision=gox.GOX_PRECISION_MIXED)
+    # unconstrained Q of the PV buses: Im(V conj(Y V)) per scenario
+    n = g.n_bus
+    rows = np.repeat(np.arange(n), np.diff(yb.indptr))
+    pv = np.flatnonzero(g.bus_type == G.BUS_PV)
+    sel = np.isin(rows, pv)
+    v = plain.voltage_mag * np.exp(1j * plain.voltage_ang)
+    col = {b: k for k, b in enumerate(pv)}
+    cur = np.zeros((batch, pv.size), np.complex128)
+    yv = (yb.re + 1j * yb.im)[sel]
+    for r_, c_, yy in zip(rows[sel], yb.indices[sel], yv):
+        cur[:, col[r_]] += yy * v[:, c_]
+    qpv = (v[:, pv] * np.conj(cur)).imag
+    med = np.median(qpv, axis=0)
+    lo, hi = np.argsort(med)[:3], np.argsort(med)[-3:]
+    q_min = np.full(n, -np.inf)
+    q_max = np.full(n, np.inf)
+    q_min[pv[lo]] = np.quantile(qpv[:, lo], 0.25, axis=0)
+    q_max[pv[hi]] = np.quantile(qpv[:, hi], 0.75, axis=0)
+    topo = gox.Topology(yb, g.bus_type)
+
+    def one():
+        return topo.solve_qlim(p, q, g.vm, g.va, q_min, q_max, tol=WORKLOAD["tol"],
+                               max_iter=WORKLOAD["max_iter"], max_outer=10,
+                               precision=gox.GOX_PRECISION_MIXED)
+
+    t0 = time.perf_counter()
+    res, sw, stab = one()  # builds the variants
+    t_first = time.perf_counter() - t0
+    times = []
+    for _ in range(rounds):
+        t0 = time.perf_counter()
+        res, sw, stab = one()
+        times.append(time.perf_counter() - t0)
+    t = float(np.median(times))
+    return {"value": round(batch / t, 1), "unit": "solves/s", "scenarios": batch,
+            "ms_per_step": round(1000 * t, 2), "first_call_ms": round(1000 * t_first, 1),
+            "switched_sets": len({tuple(np.flatnonzero(r)) for r in sw}),
+            "scenarios_switching": int(sw.any(axis=1).sum()),
+            "converged": int(np.sum(res.status == 0)), "stabilized": int(stab.sum()),
+            "rounds": rounds,
+            "note": "case2000, six PV buses with reactive limits at quantiles of their Q, "
+                    "PV->PQ switching per scenario, mixed precision, host buffers"}
+
+
 _ORACLE_TOPO = {}
 
 
@@ -598,6 +657,7 @@ def main():
         line["n1_case10000"] = n1_case10000(gox, args.many_rounds)
         line["many_topologies"] = many_topologies(gox, args.many_rounds)
         line["pgm_batch"] = pgm_batch(gox, args.many_rounds)
+        line["qlim_case2000"] = qlim_case2000(gox, args.many_rounds)
     if rank == 0 and not args.no_cpu_baseline:
         threads = os.cpu_count() or 1
         v, dt, passes = cpu_baseline(g, yb, p, q, threads)

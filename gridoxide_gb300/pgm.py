@@ -53,6 +53,8 @@ class Network:
     zip_terms: np.ndarray  # int32, ZIP terms per bus (loads and generators of type 1 or 2)
     islands: list          # components without a slack bus, pinned to V = 0
     guess_singular: bool   # the reference's linear guess would meet a singular system
+    q_min: np.ndarray      # per unit, the voltage regulators' reactive limits (-inf: none)
+    q_max: np.ndarray      # per unit (+inf: none)
 
 
 def load(path: str) -> dict:
@@ -201,7 +203,10 @@ def convert(doc: dict, s_base: float = S_BASE_VA, freq_hz: float = FREQ_HZ,
     for nid, k in id_to_idx.items():
         u_rated_bus[k] = u_rated[nid]
 
-    # voltage regulators: their generator's node becomes PV at u_ref
+    # voltage regulators: their generator's node becomes PV at u_ref, with
+    # the regulator's reactive limits (NaN or absent: none)
+    q_min = np.full(n, -np.inf)
+    q_max = np.full(n, np.inf)
     gen_node = {int(g["id"]): int(g["node"]) for g in data.get("sym_gen", [])}
     for vr in data.get("voltage_regulator", []):
         if vr["status"] == 0 or int(vr["regulated_object"]) not in gen_node:
@@ -210,6 +215,9 @@ def convert(doc: dict, s_base: float = S_BASE_VA, freq_hz: float = FREQ_HZ,
         if bus_type[k] == G.BUS_PQ:
             bus_type[k] = G.BUS_PV
             vm[k] = vr["u_ref"]
+            lo, hi = vr.get("q_min", math.nan), vr.get("q_max", math.nan)
+            q_min[k] = -np.inf if lo is None or math.isnan(lo) else lo / s_base
+            q_max[k] = np.inf if hi is None or math.isnan(hi) else hi / s_base
 
     rows, cols, vals = [], [], []
 
@@ -300,7 +308,8 @@ def convert(doc: dict, s_base: float = S_BASE_VA, freq_hz: float = FREQ_HZ,
     yb = G.ybus_from_triplets(n, rows, cols, [v.real for v in vals], [v.imag for v in vals])
     net = Network(n_bus=n, bus_type=bus_type, vm=vm, va=va, p_spec=p_spec, q_spec=q_spec,
                   zip_imp=zip_imp, zip_cur=zip_cur, ybus=yb, id_to_idx=id_to_idx,
-                  u_rated=u_rated_bus, zip_terms=zip_terms, islands=[], guess_singular=False)
+                  u_rated=u_rated_bus, zip_terms=zip_terms, islands=[], guess_singular=False,
+                  q_min=q_min, q_max=q_max)
     if mark_islands:
         mark_unreferenced_islands(net)
     return net

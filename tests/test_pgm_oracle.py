@@ -73,3 +73,20 @@ def test_from_grid_round_trip(oracle_mod):
     ot = oracle_topology(oracle_mod, net.ybus, net.bus_type)
     r = ot.batch_solve(net.p_spec[None], net.q_spec[None], net.vm, net.va, tol=1e-8, max_iter=20)
     assert r["status"][0] == 0
+
+
+def test_voltage_regulator_limits():
+    """A voltage regulator's q_min / q_max become the PV bus's reactive limits
+    in per unit (src/pgm.rs:431-441); NaN or absent means none."""
+    g = G.config_grid("case118")
+    doc = pgm.from_grid(g)
+    regs = doc["data"]["voltage_regulator"]
+    regs[0]["q_min"], regs[0]["q_max"] = -5e6, 7e6
+    regs[1]["q_min"], regs[1]["q_max"] = float("nan"), 2e6
+    net = pgm.convert(doc)
+    gen_node = {x["id"]: x["node"] for x in doc["data"]["sym_gen"]}
+    k0 = net.id_to_idx[gen_node[regs[0]["regulated_object"]]]
+    k1 = net.id_to_idx[gen_node[regs[1]["regulated_object"]]]
+    assert (net.q_min[k0], net.q_max[k0]) == (-5.0, 7.0)
+    assert net.q_min[k1] == -np.inf and net.q_max[k1] == 2.0
+    assert np.isfinite(net.q_min).sum() == 1 and np.isfinite(net.q_max).sum() == 2
