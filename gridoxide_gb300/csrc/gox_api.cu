@@ -4,6 +4,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <atomic>
 #include <cmath>
 #include <functional>
 #include <map>
@@ -14,6 +15,7 @@
 #include <new>
 #include <stdexcept>
 #include <string>
+#include <thread>
 #include <vector>
 
 #include "../../include/gridoxide_gb300.h"
@@ -1157,6 +1159,8 @@ __global__ void k_pin(int m, const int32_t* __restrict__ sb, const double* __res
   if (k < m) q[(size_t)sb[2 * k] * N + sb[2 * k + 1]] = val[k];
 }
 
+static constexpr int kQlimWorkers = 8;  // host threads solving switched-set groups
+
 // The variant of `t` with `switched` (sorted) PV buses made PQ
 static gox_topo* topo_variant(gox_topo* t, const std::vector<int32_t>& switched) {
   if (switched.empty()) return t;
@@ -1494,7 +1498,7 @@ int gox_batch_solve_qlim(gox_topo* t, int32_t B, const double* p_spec, const dou
     std::vector<uint8_t> done(B, 0);
     std::vector<int32_t> hst(B);
     std::vector<double> hq((size_t)B * std::max(npv, 1));
-    DevMem dyp, dyi, dyre, dyim, dpv, dqc, dix, sp, sq, svm, sva, ovm, ova, oit, ost, omm, dsb, dval;
+    DevMem dyp, dyi, dyre, dyim, dpv, dqc, dsb, dval;
     upload(dyp, t->yp); upload(dyi, t->yi); upload(dyre, t->yre); upload(dyim, t->yim);
     upload(dpv, pv);
     dqc.ensure((size_t)B * std::max(npv, 1) * 8);
@@ -1556,34 +1560,65 @@ int gox_batch_solve_qlim(gox_topo* t, int32_t B, const double* p_spec, const dou
         GOX_CK(cudaGetLastError());
       }
       if (groups.empty()) break;
-      // re-solve each group on its variant, warm started from its state
-      for (auto& gk : groups) {
-        gox_topo* v = topo_variant(t, gk.first);
-        const std::vector<int32_t>& idx = gk.second;
-        const int Bg = (int)idx.size();
-        const size_t rows = (size_t)Bg * n;
-        upload(dix, idx);
-        const int32_t* ix = dix.as<int32_t>();
-        sp.ensure(rows * 8); sq.ensure(rows * 8); svm.ensure(rows * 8); sva.ensure(rows * 8);
-        ovm.ensure(rows * 8); ova.ensure(rows * 8);
-        oit.ensure((size_t)Bg * 4); ost.ensure((size_t)Bg * 4); omm.ensure((size_t)Bg * 8);
-        k_take_rows<double><<<grid1d(rows), 256, 0, st>>>(dp.as<double>(), n, ix, Bg, sp.as<double>());
-        k_take_rows<double><<<grid1d(rows), 256, 0, st>>>(dq.as<double>(), n, ix, Bg, sq.as<double>());
-        k_take_rows<double><<<grid1d(rows), 256, 0, st>>>(dvm.as<double>(), n, ix, Bg, svm.as<double>());
-        k_take_rows<double><<<grid1d(rows), 256, 0, st>>>(dva.as<double>(), n, ix, Bg, sva.as<double>());
-        r = batch_device(v, Bg, sp.as<double>(), sq.as<double>(), svm.as<double>(), sva.as<double>(),
-                         n, nullptr, nullptr, nullptr, tol, max_iter, precision, ovm.as<double>(),
-                         ova.as<double>(), oit.as<int32_t>(), ost.as<int32_t>(), omm.as<double>(),
-                         nullptr, st, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr);
-        if (r != GOX_OK) return r;
-        k_put_rows<double><<<grid1d(rows), 256, 0, st>>>(ovm.as<double>(), n, ix, Bg, dvm.as<double>());
-        k_put_rows<double><<<grid1d(rows), 256, 0, st>>>(ova.as<double>(), n, ix, Bg, dva.as<double>());
-        k_put_rows<int32_t><<<grid1d(Bg), 256, 0, st>>>(oit.as<int32_t>(), 1, ix, Bg, dit.as<int32_t>());
-        k_put_rows<int32_t><<<grid1d(Bg), 256, 0, st>>>(ost.as<int32_t>(), 1, ix, Bg, dst.as<int32_t>());
-        k_put_rows<double><<<grid1d(Bg), 256, 0, st>>>(omm.as<double>(), 1, ix, Bg, dmm.as<double>());
-        GOX_CK(cudaGetLastError());
-        GOX_CK(cudaStreamSynchronize(st));  // the staging buffers are reused by the next group
-      }
+      // re-solve each group on its variant, warm started from its state: the
+      // variants are built here (host analysis, in order), then the groups run
+      // concurrently, up to kQlimWorkers host threads with a stream and staging
+      // buffers each, on disjoint rows of the batch state
+      std::vector<std::pair<gox_topo*, const std::vector<int32_t>*>> jobs;
+      for (auto& gk : groups) jobs.emplace_back(topo_variant(t, gk.first), &gk.second);
+      GOX_CK(cudaStreamSynchronize(st));  // the pins are in dq
+      std::atomic<int> next{0}, err{GOX_OK};
+      auto work = [&]() {
+        const int rc = guard_impl([&]() -> int {
+          GOX_CK(cudaSetDevice(t->device));
+          cudaStream_t ws = nullptr;
+          GOX_CK(cudaStreamCreateWithFlags(&ws, cudaStreamNonBlocking));
+          struct WorkStream {
+            cudaStream_t s;
+            ~WorkStream() { cudaStreamDestroy(s); }
+          } wsg{ws};
+          DevMem dix, sp, sq, svm, sva, ovm, ova, oit, ost, omm;
+          for (int j = next++; j < (int)jobs.size() && err.load() == GOX_OK; j = next++) {
+            gox_topo* v = jobs[j].first;
+            const std::vector<int32_t>& idx = *jobs[j].second;
+            const int Bg = (int)idx.size();
+            const size_t rows = (size_t)Bg * n;
+            upload(dix, idx);
+            const int32_t* ix = dix.as<int32_t>();
+            sp.ensure(rows * 8); sq.ensure(rows * 8); svm.ensure(rows * 8); sva.ensure(rows * 8);
+            ovm.ensure(rows * 8); ova.ensure(rows * 8);
+            oit.ensure((size_t)Bg * 4); ost.ensure((size_t)Bg * 4); omm.ensure((size_t)Bg * 8);
+            k_take_rows<double><<<grid1d(rows), 256, 0, ws>>>(dp.as<double>(), n, ix, Bg, sp.as<double>());
+            k_take_rows<double><<<grid1d(rows), 256, 0, ws>>>(dq.as<double>(), n, ix, Bg, sq.as<double>());
+            k_take_rows<double><<<grid1d(rows), 256, 0, ws>>>(dvm.as<double>(), n, ix, Bg, svm.as<double>());
+            k_take_rows<double><<<grid1d(rows), 256, 0, ws>>>(dva.as<double>(), n, ix, Bg, sva.as<double>());
+            const int rg = batch_device(v, Bg, sp.as<double>(), sq.as<double>(), svm.as<double>(),
+                                        sva.as<double>(), n, nullptr, nullptr, nullptr, tol, max_iter,
+                                        precision, ovm.as<double>(), ova.as<double>(),
+                                        oit.as<int32_t>(), ost.as<int32_t>(), omm.as<double>(), nullptr,
+                                        ws, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr);
+            if (rg != GOX_OK) return rg;
+            k_put_rows<double><<<grid1d(rows), 256, 0, ws>>>(ovm.as<double>(), n, ix, Bg, dvm.as<double>());
+            k_put_rows<double><<<grid1d(rows), 256, 0, ws>>>(ova.as<double>(), n, ix, Bg, dva.as<double>());
+            k_put_rows<int32_t><<<grid1d(Bg), 256, 0, ws>>>(oit.as<int32_t>(), 1, ix, Bg, dit.as<int32_t>());
+            k_put_rows<int32_t><<<grid1d(Bg), 256, 0, ws>>>(ost.as<int32_t>(), 1, ix, Bg, dst.as<int32_t>());
+            k_put_rows<double><<<grid1d(Bg), 256, 0, ws>>>(omm.as<double>(), 1, ix, Bg, dmm.as<double>());
+            GOX_CK(cudaGetLastError());
+            GOX_CK(cudaStreamSynchronize(ws));  // the staging buffers are reused by the next group
+          }
+          return GOX_OK;
+        });
+        if (rc != GOX_OK) {
+          int ok = GOX_OK;
+          err.compare_exchange_strong(ok, rc);
+        }
+      };
+      const int nw = std::min<int>(kQlimWorkers, (int)jobs.size());
+      std::vector<std::thread> pool;
+      for (int w = 1; w < nw; w++) pool.emplace_back(work);
+      work();
+      for (auto& th : pool) th.join();
+      if (err.load() != GOX_OK) return err.load();
     }
     GOX_CK(cudaMemcpyAsync(vm_out, dvm.p, bn * 8, cudaMemcpyDeviceToHost, st));
     GOX_CK(cudaMemcpyAsync(va_out, dva.p, bn * 8, cudaMemcpyDeviceToHost, st));
