@@ -14,6 +14,7 @@ LIB_PATH = os.path.join(HERE, "libgridoxide_gb300.so")
 GOX_OK = 0
 GOX_SINGULAR = 1
 GOX_PENDING = 2
+GOX_ISLAND_SOLVABLE, GOX_ISLAND_NO_REFERENCE, GOX_ISLAND_AMBIGUOUS = 0, 1, 2
 GOX_GUESS_GIVEN = 0
 GOX_GUESS_LINEAR = 1
 GOX_E_OUT_OF_MEMORY = -2
@@ -68,6 +69,7 @@ SIGNATURES = {
     "gox_batch_solve": (C.c_int, [vp, C.c_int32, f64p, f64p, f64p, f64p, C.c_int32, i32p, f64p,
                                   f64p, C.c_double, C.c_int32, C.c_int32, f64p, f64p, i32p, i32p,
                                   f64p, f64p]),
+    "gox_outage_islands": (C.c_int, [vp, C.c_int32, i32p, f64p, f64p, i32p, i32p, i32p]),
     "gox_batch_solve_qlim": (C.c_int, [vp, C.c_int32, f64p, f64p, f64p, f64p, C.c_int32, f64p, f64p,
                                        C.c_double, C.c_int32, C.c_int32, C.c_int32, f64p, f64p, i32p,
                                        i32p, f64p, i32p, C.POINTER(C.c_uint8), i32p]),

@@ -542,6 +542,12 @@ struct gox_topo {
   // Q-limit enforcement: this topology with PV buses switched to PQ, keyed by
   // the sorted switched buses (owned; built on first use)
   std::vector<std::pair<std::vector<int32_t>, gox_topo*>> variants;
+  // bridges of the Y-bus graph and the components without each bridge that
+  // an outage has removed (built on first use)
+  bool bridges_found = false;
+  std::vector<std::pair<int, int>> bridges;
+  std::map<std::pair<int, int>, std::vector<int32_t>> splits;
+  std::vector<int32_t> base_label;  // components of the graph as registered
   ~gox_topo() {
     for (auto& v : variants) delete v.second;
   }
@@ -1161,16 +1167,19 @@ __global__ void k_pin(int m, const int32_t* __restrict__ sb, const double* __res
 
 static constexpr int kQlimWorkers = 8;  // host threads solving switched-set groups
 
-// The variant of `t` with `switched` (sorted) PV buses made PQ
-static gox_topo* topo_variant(gox_topo* t, const std::vector<int32_t>& switched) {
-  if (switched.empty()) return t;
+// The variant of `t` whose buses `changes` (sorted, each bus * 4 + its new
+// type) have other types: PV buses switched to PQ by their reactive limits,
+// the buses of a sourceless island pinned as slack buses.  Built on first use
+// (analysis of its own Jacobian) and kept by `t`.
+static gox_topo* topo_variant(gox_topo* t, const std::vector<int32_t>& changes) {
+  if (changes.empty()) return t;
   for (auto& v : t->variants)
-    if (v.first == switched) return v.second;
+    if (v.first == changes) return v.second;
   std::unique_ptr<gox_topo> v(new gox_topo());
   v->n_bus = t->n_bus;
   v->yp = t->yp; v->yi = t->yi; v->yre = t->yre; v->yim = t->yim;
   v->bus_type = t->bus_type;
-  for (int b : switched) v->bus_type[b] = 1;
+  for (int c : changes) v->bus_type[c >> 2] = c & 3;
   v->jac = jac_analyze(v->n_bus, v->yp.data(), v->yi.data(), v->bus_type.data());
   v->csc = build_csc(v->jac.n_u, v->jac.nnz(), v->jac.rows.data(), v->jac.cols.data());
   v->sym = klu_analyze(v->jac.n_u, v->csc.p.data(), v->csc.i.data());
@@ -1178,8 +1187,225 @@ static gox_topo* topo_variant(gox_topo* t, const std::vector<int32_t>& switched)
   v->piv_tol = t->piv_tol;
   v->zip = t->zip;
   if (!v->zip.empty()) upload(v->dzip, v->zip);
-  t->variants.emplace_back(switched, v.get());
+  t->variants.emplace_back(changes, v.get());
   return v.release();
+}
+
+// ---------------------------------------------------------------------------
+// Islands of outage scenarios (network::connected_components / classify /
+// mark_unreferenced_islands, src/network.rs:121-223): an outage whose
+// off-diagonal Y entries become exactly zero removes its edge from the
+// graph; when that edge is a bridge the grid splits, and every component
+// without a slack bus is pinned to V = 0 (slack type, no injection) for
+// that scenario.
+
+// Bridges of the Y-bus graph (iterative Tarjan), as sorted (min, max) pairs
+static void find_bridges(gox_topo* t) {
+  const int n = t->n_bus;
+  std::vector<int32_t> disc(n, -1), low(n, 0), parent_edge(n, -1);
+  std::vector<std::pair<int, int>> stack;  // (bus, next entry position)
+  int timer = 0;
+  t->bridges.clear();
+  for (int r = 0; r < n; r++) {
+    if (disc[r] >= 0) continue;
+    disc[r] = low[r] = timer++;
+    stack.push_back({r, t->yp[r]});
+    while (!stack.empty()) {
+      const int u = stack.back().first;
+      int& pos = stack.back().second;
+      if (pos < t->yp[u + 1]) {
+        const int e = pos++;
+        const int w = t->yi[e];
+        if (w == u) continue;
+        if (disc[w] < 0) {
+          parent_edge[w] = u;
+          disc[w] = low[w] = timer++;
+          stack.push_back({w, t->yp[w]});
+        } else if (w != parent_edge[u]) {
+          low[u] = std::min(low[u], disc[w]);
+        }
+      } else {
+        stack.pop_back();
+        const int pu = parent_edge[u];
+        if (pu >= 0) {
+          low[pu] = std::min(low[pu], low[u]);
+          if (low[u] > disc[pu]) t->bridges.push_back({std::min(pu, u), std::max(pu, u)});
+        }
+      }
+    }
+  }
+  std::sort(t->bridges.begin(), t->bridges.end());
+  t->bridges_found = true;
+}
+
+// Components (connected_components order: by smallest member) of the graph
+// without edge (a, b): label per bus
+static std::vector<int32_t> components_without(const gox_topo* t, int a, int b) {
+  const int n = t->n_bus;
+  std::vector<int32_t> label(n, -1), stack;
+  int nc = 0;
+  for (int r = 0; r < n; r++) {
+    if (label[r] >= 0) continue;
+    label[r] = nc;
+    stack.push_back(r);
+    while (!stack.empty()) {
+      const int u = stack.back();
+      stack.pop_back();
+      for (int e = t->yp[u]; e < t->yp[u + 1]; e++) {
+        const int w = t->yi[e];
+        if (label[w] >= 0 || (u == a && w == b) || (u == b && w == a)) continue;
+        label[w] = nc;
+        stack.push_back(w);
+      }
+    }
+    nc++;
+  }
+  return label;
+}
+
+// The pinned buses (sorted) of one outage scenario, and its components
+// (labels, or empty when the outage does not split the grid)
+static const std::vector<int32_t>& outage_split(gox_topo* t, const int32_t* slot, const double* dre,
+                                               const double* dim, std::vector<int32_t>* pinned) {
+  static const std::vector<int32_t> none;
+  pinned->clear();
+  if (slot[0] < 0) return none;
+  const int nnz = (int)t->yi.size();
+  for (int c = 0; c < 4; c++)
+    if (slot[c] < 0 || slot[c] >= nnz) throw std::runtime_error("bad outage slot");
+  // slots: ff, ft, tf, tt; the edge is gone when both off-diagonals vanish
+  if (t->yre[slot[1]] + dre[1] != 0.0 || t->yim[slot[1]] + dim[1] != 0.0 ||
+      t->yre[slot[2]] + dre[2] != 0.0 || t->yim[slot[2]] + dim[2] != 0.0)
+    return none;
+  const int b = t->yi[slot[1]];
+  int a = -1;
+  for (int i = 0; i < t->n_bus && a < 0; i++)
+    if (slot[1] >= t->yp[i] && slot[1] < t->yp[i + 1]) a = i;
+  if (!t->bridges_found) find_bridges(t);
+  const std::pair<int, int> key{std::min(a, b), std::max(a, b)};
+  if (!std::binary_search(t->bridges.begin(), t->bridges.end(), key)) return none;
+  auto it = t->splits.find(key);
+  if (it == t->splits.end()) it = t->splits.emplace(key, components_without(t, a, b)).first;
+  const std::vector<int32_t>& label = it->second;
+  const int nc = 1 + *std::max_element(label.begin(), label.end());
+  std::vector<int32_t> slacks(nc, 0);
+  for (int i = 0; i < t->n_bus; i++)
+    if (t->bus_type[i] == 3) slacks[label[i]]++;
+  for (int i = 0; i < t->n_bus; i++)
+    if (slacks[label[i]] == 0) pinned->push_back(i);
+  return label;
+}
+
+// q[s][bus] = 0, p likewise, and V = 0 for the pinned buses of every row
+__global__ void k_pin_island(int Bg, int N, const int32_t* __restrict__ bus, int nb, double* p,
+                             double* q, double* vm, double* va) {
+  const size_t total = (size_t)Bg * nb;
+  for (size_t t = blockIdx.x * (size_t)blockDim.x + threadIdx.x; t < total;
+       t += (size_t)gridDim.x * blockDim.x) {
+    const size_t x = (t / nb) * N + bus[t % nb];
+    p[x] = 0.0;
+    q[x] = 0.0;
+    vm[x] = 0.0;
+    va[x] = 0.0;
+  }
+}
+
+// batch_device with the islands of outage scenarios: scenarios are grouped
+// by the buses their outage leaves without a slack bus; a group with pinned
+// buses runs on the variant of `t` where they are slack buses at V = 0 with
+// no injection (its start rule is t's).  Without splitting outages this is
+// batch_device itself.
+static int batch_any(gox_topo* t, int B, const double* p_spec, const double* q_spec,
+                     const double* vm0, const double* va0, int v_stride, const int32_t* o_slot,
+                     const double* o_dre, const double* o_dim, double tol, int max_iter,
+                     int precision, double* vm_out, double* va_out, int32_t* iters,
+                     int32_t* status, double* max_mis, double* hist, cudaStream_t st,
+                     const double* h_p, const double* h_q, const double* h_vm, const double* h_va,
+                     const int32_t* h_oslot, const double* h_odre, const double* h_odim) {
+  auto whole = [&]() {
+    return batch_device(t, B, p_spec, q_spec, vm0, va0, v_stride, o_slot, o_dre, o_dim, tol,
+                        max_iter, precision, vm_out, va_out, iters, status, max_mis, hist, st, h_p,
+                        h_q, h_vm, h_va, h_oslot, h_odre, h_odim);
+  };
+  if (!o_slot) return whole();
+  std::vector<int32_t> hs;
+  std::vector<double> hr, hi;
+  const int32_t* ss = h_oslot;
+  const double *dr = h_odre, *di = h_odim;
+  if (!ss) {
+    hs.resize((size_t)B * 4); hr.resize(hs.size()); hi.resize(hs.size());
+    GOX_CK(cudaMemcpyAsync(hs.data(), o_slot, hs.size() * 4, cudaMemcpyDeviceToHost, st));
+    GOX_CK(cudaMemcpyAsync(hr.data(), o_dre, hr.size() * 8, cudaMemcpyDeviceToHost, st));
+    GOX_CK(cudaMemcpyAsync(hi.data(), o_dim, hi.size() * 8, cudaMemcpyDeviceToHost, st));
+    GOX_CK(cudaStreamSynchronize(st));
+    ss = hs.data(); dr = hr.data(); di = hi.data();
+  }
+  std::map<std::vector<int32_t>, std::vector<int32_t>> groups;  // pinned buses -> scenarios
+  std::vector<int32_t> pinned;
+  for (int s = 0; s < B; s++) {
+    outage_split(t, ss + 4 * s, dr + 4 * s, di + 4 * s, &pinned);
+    groups[pinned].push_back(s);
+  }
+  if (groups.size() == 1 && groups.begin()->first.empty()) return whole();
+  const int n = t->n_bus;
+  int64_t launches = 0;
+  DevMem dix, dzero, dpin, sp, sq, svm, sva, ssl, sdr, sdi, ovm, ova, oit, ost, omm, ohi;
+  for (auto& gk : groups) {
+    const std::vector<int32_t>& idx = gk.second;
+    const int Bg = (int)idx.size();
+    const size_t rows = (size_t)Bg * n;
+    upload(dix, idx);
+    const int32_t* ix = dix.as<int32_t>();
+    sp.ensure(rows * 8); sq.ensure(rows * 8); svm.ensure(rows * 8); sva.ensure(rows * 8);
+    ssl.ensure((size_t)Bg * 16); sdr.ensure((size_t)Bg * 32); sdi.ensure((size_t)Bg * 32);
+    ovm.ensure(rows * 8); ova.ensure(rows * 8);
+    oit.ensure((size_t)Bg * 4); ost.ensure((size_t)Bg * 4); omm.ensure((size_t)Bg * 8);
+    if (hist) ohi.ensure((size_t)Bg * max_iter * 8);
+    k_take_rows<double><<<grid1d(rows), 256, 0, st>>>(p_spec, n, ix, Bg, sp.as<double>());
+    k_take_rows<double><<<grid1d(rows), 256, 0, st>>>(q_spec, n, ix, Bg, sq.as<double>());
+    const int32_t* vix = ix;
+    if (!v_stride) {  // one shared start row
+      upload(dzero, std::vector<int32_t>(Bg, 0));
+      vix = dzero.as<int32_t>();
+    }
+    k_take_rows<double><<<grid1d(rows), 256, 0, st>>>(vm0, n, vix, Bg, svm.as<double>());
+    k_take_rows<double><<<grid1d(rows), 256, 0, st>>>(va0, n, vix, Bg, sva.as<double>());
+    k_take_rows<int32_t><<<grid1d((size_t)Bg * 4), 256, 0, st>>>(o_slot, 4, ix, Bg, ssl.as<int32_t>());
+    k_take_rows<double><<<grid1d((size_t)Bg * 4), 256, 0, st>>>(o_dre, 4, ix, Bg, sdr.as<double>());
+    k_take_rows<double><<<grid1d((size_t)Bg * 4), 256, 0, st>>>(o_dim, 4, ix, Bg, sdi.as<double>());
+    gox_topo* v = t;
+    if (!gk.first.empty()) {
+      std::vector<int32_t> changes(gk.first.size());
+      for (size_t c = 0; c < changes.size(); c++) changes[c] = gk.first[c] * 4 + 3;  // -> slack
+      v = topo_variant(t, changes);
+      v->guess_mode = t->guess_mode;
+      upload(dpin, gk.first);
+      k_pin_island<<<grid1d((size_t)Bg * gk.first.size()), 256, 0, st>>>(
+          Bg, n, dpin.as<int32_t>(), (int)gk.first.size(), sp.as<double>(), sq.as<double>(),
+          svm.as<double>(), sva.as<double>());
+    }
+    GOX_CK(cudaGetLastError());
+    const int r = batch_device(v, Bg, sp.as<double>(), sq.as<double>(), svm.as<double>(),
+                               sva.as<double>(), n, ssl.as<int32_t>(), sdr.as<double>(),
+                               sdi.as<double>(), tol, max_iter, precision, ovm.as<double>(),
+                               ova.as<double>(), oit.as<int32_t>(), ost.as<int32_t>(),
+                               omm.as<double>(), hist ? ohi.as<double>() : nullptr, st, nullptr,
+                               nullptr, nullptr, nullptr, nullptr, nullptr, nullptr);
+    if (r != GOX_OK) return r;
+    launches += v->launches + 13;
+    k_put_rows<double><<<grid1d(rows), 256, 0, st>>>(ovm.as<double>(), n, ix, Bg, vm_out);
+    k_put_rows<double><<<grid1d(rows), 256, 0, st>>>(ova.as<double>(), n, ix, Bg, va_out);
+    k_put_rows<int32_t><<<grid1d(Bg), 256, 0, st>>>(oit.as<int32_t>(), 1, ix, Bg, iters);
+    k_put_rows<int32_t><<<grid1d(Bg), 256, 0, st>>>(ost.as<int32_t>(), 1, ix, Bg, status);
+    k_put_rows<double><<<grid1d(Bg), 256, 0, st>>>(omm.as<double>(), 1, ix, Bg, max_mis);
+    if (hist)
+      k_put_rows<double><<<grid1d((size_t)Bg * max_iter), 256, 0, st>>>(ohi.as<double>(), max_iter, ix,
+                                                                        Bg, hist);
+    GOX_CK(cudaGetLastError());
+    GOX_CK(cudaStreamSynchronize(st));  // the staging buffers are reused by the next group
+  }
+  t->launches = launches;
+  return GOX_OK;
 }
 
 extern "C" {
@@ -1314,10 +1540,9 @@ int gox_batch_solve_device(gox_topo* t, int32_t B, const double* p_spec, const d
   return guard_impl([&]() -> int {
     cudaStream_t st = (cudaStream_t)stream;
     if (max_iter == 0) return GOX_E_INVALID;
-    return batch_device(t, B, p_spec, q_spec, vm0, va0, v_stride, o_slot, o_dre, o_dim, tol,
-                        max_iter, precision, vm_out, va_out, iterations, status, max_mismatch,
-                        history, st, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr,
-                        nullptr);
+    return batch_any(t, B, p_spec, q_spec, vm0, va0, v_stride, o_slot, o_dre, o_dim, tol,
+                     max_iter, precision, vm_out, va_out, iterations, status, max_mismatch,
+                     history, st, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr);
   });
 }
 
@@ -1365,7 +1590,7 @@ int gox_batch_solve(gox_topo* t, int32_t B, const double* p_spec, const double* 
       GOX_CK(cudaMemcpyAsync(dre.p, o_dre, (size_t)B * 32, cudaMemcpyHostToDevice, st));
       GOX_CK(cudaMemcpyAsync(dim.p, o_dim, (size_t)B * 32, cudaMemcpyHostToDevice, st));
     }
-    int r = batch_device(t, B, dp.as<double>(), dq.as<double>(), dvm.as<double>(),
+    int r = batch_any(t, B, dp.as<double>(), dq.as<double>(), dvm.as<double>(),
                          dva.as<double>(), v_stride, o_slot ? dsl.as<int32_t>() : nullptr,
                          o_slot ? dre.as<double>() : nullptr, o_slot ? dim.as<double>() : nullptr,
                          tol, max_iter, precision, dovm.as<double>(), dova.as<double>(),
@@ -1565,7 +1790,11 @@ int gox_batch_solve_qlim(gox_topo* t, int32_t B, const double* p_spec, const dou
       // concurrently, up to kQlimWorkers host threads with a stream and staging
       // buffers each, on disjoint rows of the batch state
       std::vector<std::pair<gox_topo*, const std::vector<int32_t>*>> jobs;
-      for (auto& gk : groups) jobs.emplace_back(topo_variant(t, gk.first), &gk.second);
+      for (auto& gk : groups) {
+        std::vector<int32_t> changes(gk.first.size());
+        for (size_t k = 0; k < changes.size(); k++) changes[k] = gk.first[k] * 4 + 1;  // PV -> PQ
+        jobs.emplace_back(topo_variant(t, changes), &gk.second);
+      }
       GOX_CK(cudaStreamSynchronize(st));  // the pins are in dq
       std::atomic<int> next{0}, err{GOX_OK};
       auto work = [&]() {
@@ -1631,6 +1860,36 @@ int gox_batch_solve_qlim(gox_topo* t, int32_t B, const double* p_spec, const dou
       std::fill(switched, switched + bn, (uint8_t)0);
       for (int s = 0; s < B; s++)
         for (int b : sw[s]) switched[(size_t)s * n + b] = 1;
+    }
+    return GOX_OK;
+  });
+}
+
+int gox_outage_islands(gox_topo* t, int32_t B, const int32_t* out_slot, const double* out_dre,
+                       const double* out_dim, int32_t* n_islands, int32_t* island_of,
+                       int32_t* verdict) {
+  if (!t || B < 0 || !out_slot || !out_dre || !out_dim || !n_islands) return GOX_E_INVALID;
+  return guard_impl([&]() -> int {
+    const int n = t->n_bus;
+    if (t->base_label.empty()) t->base_label = components_without(t, -1, -1);
+    std::vector<int32_t> pinned;
+    for (int s = 0; s < B; s++) {
+      const std::vector<int32_t>& split =
+          outage_split(t, out_slot + 4 * s, out_dre + 4 * s, out_dim + 4 * s, &pinned);
+      const std::vector<int32_t>& label = split.empty() ? t->base_label : split;
+      const int nc = 1 + *std::max_element(label.begin(), label.end());
+      n_islands[s] = nc;
+      std::vector<int32_t> slacks(nc, 0);
+      for (int i = 0; i < n; i++)
+        if (t->bus_type[i] == 3) slacks[label[i]]++;
+      for (int i = 0; i < n; i++) {
+        if (island_of) island_of[(size_t)s * n + i] = label[i];
+        if (verdict) {
+          const int k = slacks[label[i]];
+          verdict[(size_t)s * n + i] = k == 1 ? GOX_ISLAND_SOLVABLE
+                                              : (k == 0 ? GOX_ISLAND_NO_REFERENCE : GOX_ISLAND_AMBIGUOUS);
+        }
+      }
     }
     return GOX_OK;
   });

@@ -227,6 +227,21 @@ class Topology:
         check(rc, "gox_batch_solve")
         return BatchResult(vm, va, iters, status, mis, hist)
 
+    def outage_islands(self, outage):
+        """Components of each outage scenario's grid (gox_outage_islands):
+        (n_islands [B], island_of [B, N], verdict [B, N]) with verdict 0 =
+        one slack bus, 1 = none (pinned to V = 0 by the solves), 2 = several."""
+        sl, dr, di = _i32(outage[0]), _f64(outage[1]), _f64(outage[2])
+        B, n = sl.shape[0], self.n_bus
+        nis = np.zeros(B, np.int32)
+        lab = np.zeros((B, n), np.int32)
+        ver = np.zeros((B, n), np.int32)
+        check(_lib.load().gox_outage_islands(self._h, B, _p(sl, _lib.i32p), _p(dr, _lib.f64p),
+                                             _p(di, _lib.f64p), _p(nis, _lib.i32p),
+                                             _p(lab, _lib.i32p), _p(ver, _lib.i32p)),
+              "gox_outage_islands")
+        return nis, lab, ver
+
     def solve_qlim(self, p_spec, q_spec, vm0, va0, q_min, q_max, tol=1e-8, max_iter=20,
                    max_outer=10, precision=GOX_PRECISION_MIXED):
         """Batched NR enforcing the PV buses' reactive limits

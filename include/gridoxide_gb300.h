@@ -194,6 +194,25 @@ int gox_batch_solve_qlim(gox_topo *t, int32_t B, const double *p_spec, const dou
                          int32_t *iterations, int32_t *status, double *max_mismatch,
                          int32_t *n_switched, uint8_t *switched, int32_t *stabilized);
 
+/* Islands of outage scenarios (network::connected_components / classify,
+ * src/network.rs:121-194).  An outage whose off-diagonal Y entries become
+ * exactly zero removes its branch from the graph; when that branch is a
+ * bridge the grid splits.  The batched solves (gox_batch_solve,
+ * gox_batch_solve_device, the server) pin every component without a slack
+ * bus to V = 0 with no injection (mark_unreferenced_islands,
+ * src/network.rs:196-223) and solve the rest, so such a scenario reports
+ * Converged for its energized part.  This call describes the split without
+ * solving: per scenario the number of components (n_islands [B]), each bus's
+ * component in connected_components order (island_of [B][n_bus] or NULL)
+ * and its component's verdict (verdict [B][n_bus] or NULL, classify's
+ * Verdict: one slack bus, none, or several).  Host arrays, no GPU needed. */
+#define GOX_ISLAND_SOLVABLE 0
+#define GOX_ISLAND_NO_REFERENCE 1
+#define GOX_ISLAND_AMBIGUOUS 2
+int gox_outage_islands(gox_topo *t, int32_t B, const int32_t *out_slot, const double *out_dre,
+                       const double *out_dim, int32_t *n_islands, int32_t *island_of,
+                       int32_t *verdict);
+
 /* Fixes the topology's pivot order on the host, without a GPU: the first
  * scenario whose start point misses `tol` has its Jacobian factored with
  * partial pivoting (KluNativeSystem::new on the first Jacobian a
