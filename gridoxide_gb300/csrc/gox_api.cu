@@ -442,8 +442,14 @@ struct Iter {
     k_update<T><<<gu, 256, 0, st>>>(S, D, it, mode);
     if (mode == 0) {
       dim3 gi((S.n_bus + 8 * BPW - 1) / (8 * BPW), D.G);
-      if (outage) k_inject<T, true, BPW><<<gi, 256, 0, st>>>(S, D, it);
-      else k_inject<T, false, BPW><<<gi, 256, 0, st>>>(S, D, it);
+      // ZIP terms and outages are compiled in only where a batch has them
+      if (S.zip) {
+        if (outage) k_inject<T, true, BPW, true><<<gi, 256, 0, st>>>(S, D, it);
+        else k_inject<T, false, BPW, true><<<gi, 256, 0, st>>>(S, D, it);
+      } else {
+        if (outage) k_inject<T, true, BPW, false><<<gi, 256, 0, st>>>(S, D, it);
+        else k_inject<T, false, BPW, false><<<gi, 256, 0, st>>>(S, D, it);
+      }
     }
     k_decide<<<D.G, 32, 0, st>>>(D, it, mode);
     return mode == 0 ? 3 : 2;

@@ -246,7 +246,7 @@ __device__ __forceinline__ unsigned long long abs_bits(double v) {
   return b > 0x7ff0000000000000ull ? 0ull : b;  // NaN: skipped
 }
 
-template <typename T, bool OUTAGE, int BPW>
+template <typename T, bool OUTAGE, int BPW, bool ZIP>
 __global__ void __launch_bounds__(256) k_inject(SchedDev S, BatchDev D, int it) {
   const int g = blockIdx.y;
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
@@ -298,7 +298,7 @@ __global__ void __launch_bounds__(256) k_inject(SchedDev S, BatchDev D, int it) 
       // row have Jacobian entries that use them; a PV bus's Q comes from
       // the products, it has no Q row)
       if (rp >= 0) {
-        const double psp = eff_inj(S.zip, N, i, 0, D.psp[x], D.vm[x]);
+        const double psp = ZIP ? eff_inj(S.zip, N, i, 0, D.psp[x], D.vm[x]) : D.psp[x];
         const double FP = fma(-fi, ii, fma(-ei, ir, psp));
         const float fp = f32_rn(FP);
         if (active) {
@@ -307,7 +307,7 @@ __global__ void __launch_bounds__(256) k_inject(SchedDev S, BatchDev D, int it) 
         }
         ((float*)D.pT)[x] = f32_rn(psp) - fp;
         if (rq >= 0) {
-          const double qsp = eff_inj(S.zip, N, i, 1, D.qsp[x], D.vm[x]);
+          const double qsp = ZIP ? eff_inj(S.zip, N, i, 1, D.qsp[x], D.vm[x]) : D.qsp[x];
           const double FQ = fma(ei, ii, fma(-fi, ir, qsp));
           const float fq = f32_rn(FQ);
           if (active) {
@@ -324,12 +324,12 @@ __global__ void __launch_bounds__(256) k_inject(SchedDev S, BatchDev D, int it) 
       const double qc = fi * ir - ei * ii;
       if (active) {
         if (rp >= 0) {
-          const double F = eff_inj(S.zip, N, i, 0, D.psp[x], D.vm[x]) - pc;
+          const double F = (ZIP ? eff_inj(S.zip, N, i, 0, D.psp[x], D.vm[x]) : D.psp[x]) - pc;
           mx = max(mx, abs_bits(F));
           rhs[gidx(g, S.n_u, rp, lane)] = (T)F;
         }
         if (rq >= 0) {
-          const double F = eff_inj(S.zip, N, i, 1, D.qsp[x], D.vm[x]) - qc;
+          const double F = (ZIP ? eff_inj(S.zip, N, i, 1, D.qsp[x], D.vm[x]) : D.qsp[x]) - qc;
           mx = max(mx, abs_bits(F));
           rhs[gidx(g, S.n_u, rq, lane)] = (T)F;
         }
