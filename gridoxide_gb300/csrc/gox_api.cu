@@ -394,6 +394,7 @@ struct DevBatch {
     D.o_dim = outage ? o_dim.as<double>() : nullptr;
     D.piv_tol = prec == GOX_PRECISION_MIXED ? (float)piv_tol : 0.0f;
     D.err = err.as<int32_t>() + 1;
+    D.itp = nactive.as<int32_t>() + 1;
     return D;
   }
 };
@@ -511,6 +512,14 @@ struct GuessSys {
   GuessDev d{};
 };
 
+// A Newton loop captured as a CUDA graph (conditional while / if nodes),
+// keyed by every value its launches bake in
+struct LoopGraph {
+  std::vector<unsigned char> key;
+  cudaGraphExec_t exec = nullptr;
+  int uses = 0;
+};
+
 struct gox_topo {
   int n_bus = 0;
   std::vector<int32_t> yp, yi, bus_type;
@@ -554,8 +563,14 @@ struct gox_topo {
   std::vector<std::pair<int, int>> bridges;
   std::map<std::pair<int, int>, std::vector<int32_t>> splits;
   std::vector<int32_t> base_label;  // components of the graph as registered
+  // captured Newton loops (a few keys, oldest replaced) and how many solves used one
+  std::vector<LoopGraph> loop_graphs;
+  bool graphs_off = false;
+  int64_t graph_solves = 0;
   ~gox_topo() {
     for (auto& v : variants) delete v.second;
+    for (auto& lg : loop_graphs)
+      if (lg.exec) cudaGraphExecDestroy(lg.exec);
   }
 };
 
@@ -647,11 +662,145 @@ static int fix_pivots(gox_topo* t, int B, const double* p_spec, const double* q_
   return -1;
 }
 
+// The sink (node without dependents) of a graph captured from one stream
+static cudaGraphNode_t graph_sink(cudaGraph_t g) {
+  size_t n = 0;
+  GOX_CK(cudaGraphGetNodes(g, nullptr, &n));
+  std::vector<cudaGraphNode_t> nodes(n);
+  GOX_CK(cudaGraphGetNodes(g, nodes.data(), &n));
+  for (cudaGraphNode_t v : nodes) {
+    size_t m = 0;
+    GOX_CK(cudaGraphNodeGetDependentNodes(v, nullptr, nullptr, &m));
+    if (m == 0) return v;
+  }
+  throw std::runtime_error("captured graph without a sink");
+}
+
+// Adds a conditional node of `type` on `handle` after `dep` (or at the root)
+// and returns its body graph
+static cudaGraph_t add_conditional(cudaGraph_t g, cudaGraphNode_t* dep, cudaGraphConditionalHandle h,
+                                   cudaGraphConditionalNodeType type, cudaGraphNode_t* out) {
+  cudaGraphNodeParams np{};
+  np.type = cudaGraphNodeTypeConditional;
+  np.conditional.handle = h;
+  np.conditional.type = type;
+  np.conditional.size = 1;
+  GOX_CK(cudaGraphAddNode(out, g, dep, nullptr, dep ? 1 : 0, &np));
+  return np.conditional.phGraph_out[0];
+}
+
+// The whole Newton loop as one graph: it = 0; while (running) { mismatch;
+// decision; if (running) { fill; refactor; solves } }; if (budget spent)
+// { final mismatch }.  Kernels read the iteration from D.itp.
+template <typename T>
+static cudaGraphExec_t build_loop_graph(gox_topo* t, const BatchDev& D, int max_iter, bool outage,
+                                        cudaStream_t st) {
+  const SchedDev& S = t->dsched.d;
+  cudaGraph_t g = nullptr;
+  GOX_CK(cudaGraphCreate(&g, 0));
+  struct GraphGuard {
+    cudaGraph_t g;
+    ~GraphGuard() { cudaGraphDestroy(g); }
+  } gg{g};
+  cudaGraphConditionalHandle hw, hif, hmax;
+  GOX_CK(cudaGraphConditionalHandleCreate(&hw, g, 1, cudaGraphCondAssignDefault));
+  GOX_CK(cudaGraphConditionalHandleCreate(&hif, g, 0, cudaGraphCondAssignDefault));
+  GOX_CK(cudaGraphConditionalHandleCreate(&hmax, g, 0, cudaGraphCondAssignDefault));
+  cudaGraphNode_t n0, nw, nif, nmax;
+  cudaMemsetParams mp{};
+  mp.dst = D.itp; mp.value = 0; mp.elementSize = 4; mp.width = 1; mp.height = 1;
+  GOX_CK(cudaGraphAddMemsetNode(&n0, g, nullptr, 0, &mp));
+  cudaGraph_t body = add_conditional(g, &n0, hw, cudaGraphCondTypeWhile, &nw);
+  cudaGraph_t cap = nullptr;
+  GOX_CK(cudaStreamBeginCaptureToGraph(st, body, nullptr, nullptr, 0, cudaStreamCaptureModeRelaxed));
+  GOX_CK(cudaMemsetAsync(D.nactive, 0, sizeof(int32_t), st));
+  Iter<T>::mismatch(S, D, -1, 0, outage, st);
+  k_cond<<<1, 1, 0, st>>>(D.nactive, D.itp, max_iter, hw, hif, hmax);
+  GOX_CK(cudaStreamEndCapture(st, &cap));
+  cudaGraphNode_t sink = graph_sink(body);
+  cudaGraph_t ifb = add_conditional(body, &sink, hif, cudaGraphCondTypeIf, &nif);
+  GOX_CK(cudaStreamBeginCaptureToGraph(st, ifb, nullptr, nullptr, 0, cudaStreamCaptureModeRelaxed));
+  Iter<T>::fill(S, D, outage, st);
+  Iter<T>::refactor(t->dsched, D, st);
+  Iter<T>::solve_rest(t->dsched, D, st);
+  GOX_CK(cudaStreamEndCapture(st, &cap));
+  cudaGraph_t mb = add_conditional(g, &nw, hmax, cudaGraphCondTypeIf, &nmax);
+  GOX_CK(cudaStreamBeginCaptureToGraph(st, mb, nullptr, nullptr, 0, cudaStreamCaptureModeRelaxed));
+  Iter<T>::mismatch(S, D, -1, 1, outage, st);
+  GOX_CK(cudaStreamEndCapture(st, &cap));
+  cudaGraphExec_t ex = nullptr;
+  GOX_CK(cudaGraphInstantiate(&ex, g, 0));
+  return ex;
+}
+
+// Runs the loop from a cached graph when this exact configuration was seen
+// before (the first sighting runs the host loop and records the key);
+// false: run the host loop.
+template <typename T>
+static bool run_loop_graph(gox_topo* t, const BatchDev& D, int max_iter, bool outage,
+                           cudaStream_t st) {
+  if (t->graphs_off) return false;
+  std::vector<unsigned char> key;
+  auto put = [&](const void* p, size_t n) {
+    const unsigned char* c = static_cast<const unsigned char*>(p);
+    key.insert(key.end(), c, c + n);
+  };
+  const int prec = (int)sizeof(T), i = sizeof(T) == 4 ? 0 : 1;
+  const unsigned char o = outage ? 1 : 0;
+  put(&prec, sizeof prec); put(&max_iter, sizeof max_iter); put(&o, 1);
+  put(&D, sizeof D); put(&t->dsched.d, sizeof(SchedDev));
+  put(&t->dsched.st[i], sizeof(StreamDev)); put(&t->dsched.st_nw[i], sizeof(int));
+  put(&t->dsched.st_smem[i], sizeof(size_t)); put(&t->dsched.st_bwd[i], sizeof(bool));
+  LoopGraph* lg = nullptr;
+  for (auto& x : t->loop_graphs)
+    if (x.key == key) lg = &x;
+  if (!lg) {
+    if (t->loop_graphs.size() >= 4) {
+      if (t->loop_graphs.front().exec) cudaGraphExecDestroy(t->loop_graphs.front().exec);
+      t->loop_graphs.erase(t->loop_graphs.begin());
+    }
+    t->loop_graphs.push_back(LoopGraph{key, nullptr, 1});
+    return false;
+  }
+  if (!lg->exec) {
+    try {
+      lg->exec = build_loop_graph<T>(t, D, max_iter, outage, st);
+    } catch (...) {
+      // a capture that failed leaves the stream capturing: end it, and keep
+      // this topology on the host loop
+      cudaGraph_t junk = nullptr;
+      cudaStreamCaptureStatus cs;
+      if (cudaStreamIsCapturing(st, &cs) == cudaSuccess && cs != cudaStreamCaptureStatusNone)
+        cudaStreamEndCapture(st, &junk);
+      if (junk) cudaGraphDestroy(junk);
+      cudaGetLastError();
+      t->graphs_off = true;
+      return false;
+    }
+  }
+  lg->uses++;
+  GOX_CK(cudaGraphLaunch(lg->exec, st));
+  t->graph_solves++;
+  return true;
+}
+
 template <typename T>
 static void run_iterations(gox_topo* t, BatchDev D, int max_iter, bool outage, cudaStream_t st,
                            int32_t* h_nactive) {
   const SchedDev& S = t->dsched.d;
   const bool timing = t->timing.on;
+  if (!timing && run_loop_graph<T>(t, D, max_iter, outage, st)) {
+    // launches: per iteration 3 + 1 (decision) and, while running, fill,
+    // refactor and the separate solve; the final mismatch when the budget ran out
+    int32_t h[2] = {0, 0};
+    GOX_CK(cudaMemcpyAsync(h, D.nactive, 8, cudaMemcpyDeviceToHost, st));
+    GOX_CK(cudaStreamSynchronize(st));
+    const int its = h[1], ran_out = (h[0] > 0 && its >= max_iter) ? 1 : 0;
+    const int fills = h[0] > 0 ? its : its - 1;
+    const int ns = t->dsched.st_bwd[sizeof(T) == 4 ? 0 : 1] ? 0 : 1;
+    t->launches += (int64_t)its * 4 + (int64_t)fills * (2 + ns) + ran_out * 2;
+    return;
+  }
   // events: per iteration [k1 start, k1 end, k2 end, k3 end, k4 end]; read once at the end
   std::vector<cudaEvent_t> ev;
   auto rec = [&]() {
@@ -1999,6 +2148,7 @@ int gox_topo_info(const gox_topo* t, int64_t* info) {
   info[25] = (int64_t)a.words.size();
   info[28] = a.n_pre;
   info[29] = a.rows_helper;
+  info[30] = t->graph_solves;
   info[26] = a.has_bwd ? 1 : 0;
   info[27] = b.has_bwd ? 1 : 0;
   return GOX_OK;

@@ -89,6 +89,7 @@ struct BatchDev {
   const double *o_dre, *o_dim;
   float piv_tol;                   // pivot-ratio threshold (mixed path)
   int32_t* err;                    // [0] set when a bounded device wait gave up
+  int32_t* itp;                    // [1] iteration of the graph-captured loop (kernels given it < 0)
 };
 
 __device__ __forceinline__ size_t gidx(int g, int n, int e, int lane) {
@@ -141,6 +142,7 @@ __device__ __forceinline__ double from_T(T v) {
 // mode 0: iteration `it`; mode 1: the update after the last iteration.
 template <typename T>
 __global__ void __launch_bounds__(256) k_update(SchedDev S, BatchDev D, int it, int mode) {
+  if (it < 0) it = *D.itp;
   const int g = blockIdx.y;
   const int lane = threadIdx.x & 31;
   const int i = blockIdx.x * 8 + (threadIdx.x >> 5);
@@ -248,6 +250,7 @@ __device__ __forceinline__ unsigned long long abs_bits(double v) {
 
 template <typename T, bool OUTAGE, int BPW, bool ZIP>
 __global__ void __launch_bounds__(256) k_inject(SchedDev S, BatchDev D, int it) {
+  if (it < 0) it = *D.itp;
   const int g = blockIdx.y;
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   const int s = g * 32 + lane;
@@ -349,6 +352,7 @@ __global__ void __launch_bounds__(256) k_inject(SchedDev S, BatchDev D, int it) 
 }
 
 __global__ void k_decide(BatchDev D, int it, int mode) {
+  if (it < 0) it = *D.itp;
   const int g = blockIdx.x, lane = threadIdx.x;
   const int s = g * 32 + lane;
   bool running = D.status[s] == ST_RUNNING;
@@ -378,6 +382,21 @@ __global__ void k_decide(BatchDev D, int it, int mode) {
     D.gact[g] = any ? 1 : 0;
     if (any) atomicAdd(D.nactive, 1);
   }
+}
+
+// The graph-captured Newton loop's decision, one thread after k_decide: run
+// this iteration's Jacobian, refactor and solves while a scenario is running
+// (hif), iterate again while one is and the budget allows (hw), or evaluate
+// the final MaxIterations mismatch when the budget is spent (hmax).
+__global__ void k_cond(const int32_t* __restrict__ nactive, int32_t* itp, int max_iter,
+                       cudaGraphConditionalHandle hw, cudaGraphConditionalHandle hif,
+                       cudaGraphConditionalHandle hmax) {
+  const unsigned any = *nactive > 0 ? 1u : 0u;
+  const int next = *itp + 1;
+  cudaGraphSetConditional(hif, any);
+  cudaGraphSetConditional(hw, any && next < max_iter ? 1u : 0u);
+  cudaGraphSetConditional(hmax, any && next >= max_iter ? 1u : 0u);
+  *itp = next;
 }
 
 // ---------------------------------------------------------------------------

@@ -348,7 +348,7 @@ class Topology:
         return dx
 
     def info(self) -> dict:
-        a = np.zeros(30, np.int64)
+        a = np.zeros(31, np.int64)
         check(_lib.load().gox_topo_info(self._h, _p(a, _lib.i64p)), "gox_topo_info")
         keys = ["n_u", "nnz_j", "nnz_l", "nnz_u", "nnz_off", "nblocks", "levels", "phases",
                 "lu_slots", "max_collen", "rf32_warps", "rf32_ring_rows", "rf32_est_cycles",
@@ -356,7 +356,7 @@ class Topology:
                 "rf32_rows_just_in_time", "rf32_steps", "rf32_waits", "rf64_warps",
                 "rf64_ring_rows", "rf64_est_cycles", "rf64_rows_in_place", "rf32_column_cmds",
                 "rf32_stream_words", "rf32_with_bwd", "rf64_with_bwd", "rf32_pre_columns",
-                "rf32_rows_by_helpers"]
+                "rf32_rows_by_helpers", "graph_solves"]
         return dict(zip(keys, [int(v) for v in a]))
 
     def structure(self) -> dict:

@@ -265,8 +265,10 @@ int gox_factor_host(int32_t n, int32_t nnz, const int32_t *rows, const int32_t *
  * stream words; [26] / [27] 1 when the FP32 / FP64 refactor also runs the
  * backward substitution (no separate solve launch); [28] columns of the FP32
  * plan whose update prefix runs one level early; [29] rows of the FP32 plan
- * copied by warps idle in a level for another warp's next column.  info
- * must hold 30 entries.  Returns GOX_E_INVALID before the first solve. */
+ * copied by warps idle in a level for another warp's next column; [30]
+ * solves of this topology whose Newton loop ran as one captured CUDA graph
+ * (a configuration seen before: same batch buffers, precision, budget).
+ * info must hold 31 entries.  Returns GOX_E_INVALID before the first solve. */
 int gox_topo_info(const gox_topo *t, int64_t *info);
 
 /* The fixed factorization structure (klu_extract layout without values):
