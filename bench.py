@@ -497,7 +497,6 @@ def main():
     g, yb, p, q = make_inputs()
     B, N = p.shape
     topo = gox.Topology(yb, g.bus_type)
-    topo.set_timing(True)
     stream = torch.cuda.Stream(device=dev)
     tp = torch.from_numpy(p).to(dev)
     tq = torch.from_numpy(q).to(dev)
@@ -515,7 +514,11 @@ def main():
         topo.solve_device(tp, tq, tvm0, tva0, ovm, ova, oit, ost, omm, tol=WORKLOAD["tol"],
                           max_iter=WORKLOAD["max_iter"], precision=precision, stream=stream)
 
-    def timed(precision, steps, clocks=None):
+    def timed(precision, steps, clocks=None, kernel_timing=False):
+        """`steps` timed steps.  Without kernel_timing the library runs each
+        solve's Newton loop as its captured CUDA graph; with it, the
+        host-driven loop records CUDA events around every phase."""
+        topo.set_timing(kernel_timing)
         ms, kern, launches = [], {"mismatch": 0.0, "fill": 0.0, "refactor": 0.0, "solve": 0.0}, 0
         iters_run = []
         if world > 1:
@@ -533,12 +536,15 @@ def main():
             e1.record(stream)
             e1.synchronize()
             ms.append(e0.elapsed_time(e1))
-            t = topo.last_timing()
-            kern["mismatch"] += t["mismatch_ms"]
-            kern["fill"] += t["fill_ms"]
-            kern["refactor"] += t["refactor_ms"]
-            kern["solve"] += t["solve_ms"]
-            iters_run.append(int(t["iterations"]))
+            if kernel_timing:
+                t = topo.last_timing()
+                kern["mismatch"] += t["mismatch_ms"]
+                kern["fill"] += t["fill_ms"]
+                kern["refactor"] += t["refactor_ms"]
+                kern["solve"] += t["solve_ms"]
+                iters_run.append(int(t["iterations"]))
+            else:
+                iters_run.append(int(oit.max().item()))
             launches += topo.last_launches()
         torch.cuda.synchronize()
         cl = clocks.stop() if clocks else None
@@ -557,13 +563,18 @@ def main():
     mm = omm.cpu().numpy()
 
     clocks = ClockSampler(local)
-    ms_mx, kern_mx, launches_mx, iters_mx, cl = timed(gox.GOX_PRECISION_MIXED, args.steps, clocks)
+    ms_mx, _, launches_mx, iters_mx, cl = timed(gox.GOX_PRECISION_MIXED, args.steps, clocks)
     st_mx = ost.cpu().numpy().copy()
     mm_mx = omm.cpu().numpy().copy()
     it_mx = oit.cpu().numpy().copy()
+    # the same steps again with CUDA events around every phase (host-driven
+    # loop): the per-kernel times and the roofline
+    ms_k, kern_mx, _, iters_k, _ = timed(gox.GOX_PRECISION_MIXED, args.steps, kernel_timing=True)
     if args.quick:
         print(json.dumps({"quick": True, "ms_per_step": float(np.mean(ms_mx)),
-                          "kernels_ms": kern_mx, "iterations": iters_mx}), flush=True)
+                          "ms_per_step_events": float(np.mean(ms_k)), "kernels_ms": kern_mx,
+                          "iterations": iters_mx, "graph_solves": topo.info()["graph_solves"]}),
+              flush=True)
         return
     ms_64, kern_64, launches_64, iters_64, _ = timed(gox.GOX_PRECISION_FP64,
                                                      max(3, args.steps // 2))
@@ -608,7 +619,7 @@ def main():
         abytes["refactor"] += abytes.pop("solve")
         kern_mx["refactor"] += kern_mx.pop("solve")
     dom = max(kern_mx, key=lambda k: kern_mx[k])
-    n_launch = sum(iters_mx) if dom != "mismatch" else sum(iters_mx) + args.steps
+    n_launch = sum(iters_k) if dom != "mismatch" else sum(iters_k) + args.steps
     per_launch_bytes = abytes[dom] * B
     avg_launch_ms = kern_mx[dom] / max(n_launch, 1)
     achieved = per_launch_bytes / (avg_launch_ms / 1000.0) / 1e9
@@ -621,7 +632,7 @@ def main():
             "avg_launch_ms": round(avg_launch_ms, 4)}
     kernels = {}
     for k in kern_mx:
-        nl = sum(iters_mx) + (args.steps if k == "mismatch" else 0)
+        nl = sum(iters_k) + (args.steps if k == "mismatch" else 0)
         t_ms = kern_mx[k] / max(nl, 1)
         kernels[k] = {"ms_per_launch": round(t_ms, 4),
                       "GB/s": round(abytes[k] * B / (t_ms / 1000.0) / 1e9, 1) if t_ms > 0 else None,
@@ -647,6 +658,12 @@ def main():
         "e2e": {"value": round(e2e_value, 1), "unit": "solves/s", "h2d_bytes_per_step": h2d,
                 "d2h_bytes_per_step": d2h},
         "gpu_launches": int(launches_mx),
+        "newton_loop": {"graph_solves": int(topo.info()["graph_solves"]),
+                        "kernel_timing": "kernels and roofline from a second pass of the same "
+                                         "steps with CUDA events around every phase (host-driven "
+                                         "loop); the timed steps run each solve's loop as its "
+                                         "captured CUDA graph",
+                        "ms_per_step_with_events": round(float(np.mean(ms_k)), 4)},
         "roofline": roof,
         "kernels": kernels,
         "clocks": cl,
