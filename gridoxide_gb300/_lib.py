@@ -93,6 +93,7 @@ SIGNATURES = {
     "gox_last_launches": (C.c_int64, [vp]),
     "gox_set_pivot_tolerance": (C.c_int, [vp, C.c_double]),
     "gox_topo_set_initial_guess": (C.c_int, [vp, C.c_int32]),
+    "gox_topo_set_graph": (C.c_int, [vp, C.c_int32]),
     "gox_topo_initial_guess": (C.c_int, [vp, C.c_int32, f64p, f64p, f64p, f64p, C.c_int32, f64p,
                                          f64p]),
     "gox_topo_set_zip": (C.c_int, [vp, f64p, f64p, f64p, f64p]),

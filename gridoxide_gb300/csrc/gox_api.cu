@@ -565,7 +565,8 @@ struct gox_topo {
   std::vector<int32_t> base_label;  // components of the graph as registered
   // captured Newton loops (a few keys, oldest replaced) and how many solves used one
   std::vector<LoopGraph> loop_graphs;
-  bool graphs_off = false;
+  bool graphs_off = false;   // a capture failed: the host-driven loop only
+  bool graphs_wanted = true;  // gox_topo_set_graph
   int64_t graph_solves = 0;
   ~gox_topo() {
     for (auto& v : variants) delete v.second;
@@ -662,6 +663,8 @@ static int fix_pivots(gox_topo* t, int B, const double* p_spec, const double* q_
   return -1;
 }
 
+static constexpr int kGraphMinGroups = 64;  // batches of >= 2,048 scenarios
+
 // The sink (node without dependents) of a graph captured from one stream
 static cudaGraphNode_t graph_sink(cudaGraph_t g) {
   size_t n = 0;
@@ -739,7 +742,9 @@ static cudaGraphExec_t build_loop_graph(gox_topo* t, const BatchDev& D, int max_
 template <typename T>
 static bool run_loop_graph(gox_topo* t, const BatchDev& D, int max_iter, bool outage,
                            cudaStream_t st) {
-  if (t->graphs_off) return false;
+  // small batches stay on the host-driven loop: measured, their graphs ran
+  // slower when many topologies solve concurrently from several threads
+  if (t->graphs_off || !t->graphs_wanted || D.G < kGraphMinGroups) return false;
   std::vector<unsigned char> key;
   auto put = [&](const void* p, size_t n) {
     const unsigned char* c = static_cast<const unsigned char*>(p);
@@ -1433,9 +1438,7 @@ static const std::vector<int32_t>& outage_split(gox_topo* t, const int32_t* slot
       t->yre[slot[2]] + dre[2] != 0.0 || t->yim[slot[2]] + dim[2] != 0.0)
     return none;
   const int b = t->yi[slot[1]];
-  int a = -1;
-  for (int i = 0; i < t->n_bus && a < 0; i++)
-    if (slot[1] >= t->yp[i] && slot[1] < t->yp[i + 1]) a = i;
+  const int a = (int)(std::upper_bound(t->yp.begin(), t->yp.end(), slot[1]) - t->yp.begin()) - 1;
   if (!t->bridges_found) find_bridges(t);
   const std::pair<int, int> key{std::min(a, b), std::max(a, b)};
   if (!std::binary_search(t->bridges.begin(), t->bridges.end(), key)) return none;
@@ -2219,6 +2222,12 @@ int gox_topo_set_zip(gox_topo* t, const double* zi_re, const double* zi_im, cons
     upload(t->dzip, t->zip);
     return GOX_OK;
   });
+}
+
+int gox_topo_set_graph(gox_topo* t, int32_t on) {
+  if (!t) return GOX_E_INVALID;
+  t->graphs_wanted = on != 0;
+  return GOX_OK;
 }
 
 int gox_topo_set_initial_guess(gox_topo* t, int32_t mode) {

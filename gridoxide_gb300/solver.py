@@ -408,6 +408,10 @@ class Topology:
         a = [_f64(imp.real), _f64(imp.imag), _f64(cur.real), _f64(cur.imag)]
         check(L.gox_topo_set_zip(self._h, *[_p(x, _lib.f64p) for x in a]), "gox_topo_set_zip")
 
+    def set_graph(self, on: bool) -> None:
+        """Run the Newton loop as a captured CUDA graph (default) or host-driven."""
+        check(_lib.load().gox_topo_set_graph(self._h, 1 if on else 0), "gox_topo_set_graph")
+
     def set_initial_guess(self, mode: str) -> None:
         """Start point of the batched solves: "given" (vm0/va0 as passed) or
         "linear" (the reference BatchSolver's linear initial guess from them,

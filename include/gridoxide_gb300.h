@@ -313,6 +313,16 @@ int64_t gox_last_launches(const gox_topo *t);
 int gox_topo_set_zip(gox_topo *t, const double *zi_re, const double *zi_im, const double *zc_re,
                      const double *zc_im);
 
+/* Newton loop as a captured CUDA graph (default on): from the second solve
+ * of a configuration (same batch buffers, precision, budget, outage use)
+ * the whole loop is one graph launch with conditional while / if nodes and
+ * the iteration on the device, instead of host-driven launches with one
+ * synchronization per iteration; results are the same bit for bit.  Only
+ * batches of at least 2,048 scenarios use it (smaller ones measured slower
+ * as graphs when many topologies solve concurrently).  0 keeps this
+ * topology on the host-driven loop. */
+int gox_topo_set_graph(gox_topo *t, int32_t on);
+
 #define GOX_GUESS_GIVEN 0
 #define GOX_GUESS_LINEAR 1
 int gox_topo_set_initial_guess(gox_topo *t, int32_t mode);

@@ -27,7 +27,7 @@ def _same(a, b):
 def test_graph_loop_equals_host_loop(gox, prec, outage, max_iter):
     fx = load_fixture("case118")
     g, yb = grid_from_fixture(fx), ybus_from_fixture(fx)
-    B = 96
+    B = 2048  # batches of 64+ groups of 32 scenarios use the graph
     p, q = G.load_scenarios(g, B, 0.15, 41)
     out = None
     if outage:
@@ -49,3 +49,8 @@ def test_graph_loop_equals_host_loop(gox, prec, outage, max_iter):
         assert np.all(first.status == gox.GOX_MAX_ITERATIONS)
     else:
         assert np.all(first.status == gox.GOX_CONVERGED)
+    # a small batch stays on the host-driven loop
+    small = gox.Topology(yb, g.bus_type)
+    for _ in range(3):
+        small.solve(p[:64], q[:64], g.vm, g.va, precision=precision, max_iter=max_iter)
+    assert small.info()["graph_solves"] == 0
