@@ -353,6 +353,21 @@ struct DevBatch {
   DevMem o_slot, o_bf, o_bt, o_dre, o_dim;
   DevMem in_stage, out_stage;  // host I/O staging (row-major)
 
+  std::vector<DevMem*> all() {
+    return {&vm, &va, &e, &f, &psp, &qsp, &cth, &sth, &eT, &fT, &ivT, &pT, &qT, &jbuf, &lu, &off,
+            &rhs, &sol, &status, &iters, &sing, &piv, &maxmis, &maxacc, &hist, &gact, &nactive,
+            &err, &o_slot, &o_bf, &o_bt, &o_dre, &o_dim, &in_stage, &out_stage};
+  }
+  size_t bytes() {
+    size_t b = 0;
+    for (DevMem* m : all()) b += m->bytes;
+    return b;
+  }
+  void release() {
+    for (DevMem* m : all()) m->release();
+    G = 0;
+  }
+
   void ensure(const SchedDev& S, int G_, int prec_, int max_iter_, bool want_hist) {
     const size_t nb = (size_t)G_ * S.n_bus * 32, w = prec_ == GOX_PRECISION_FP64 ? 8 : 4;
     vm.ensure(nb * 8); va.ensure(nb * 8); e.ensure(nb * 8); f.ensure(nb * 8);
@@ -493,6 +508,17 @@ using namespace gox;
 
 struct IoStage {
   DevMem p, q, vm, va, ovm, ova, it, st, mm, h, sl, dre, dim, pb, qb, sc;
+  std::vector<DevMem*> all() {
+    return {&p, &q, &vm, &va, &ovm, &ova, &it, &st, &mm, &h, &sl, &dre, &dim, &pb, &qb, &sc};
+  }
+  size_t bytes() {
+    size_t b = 0;
+    for (DevMem* m : all()) b += m->bytes;
+    return b;
+  }
+  void release() {
+    for (DevMem* m : all()) m->release();
+  }
 };
 
 // The linear initial guess system of a topology (src/network.rs:627-678),
@@ -2553,6 +2579,23 @@ struct gox_server {
   int64_t next_ticket = 1;
   bool stop = false;
   int64_t batches = 0, solved = 0;
+  // HBM budget (0: none): the per-scenario device bytes of each topology's
+  // batch buffers bound the batch a worker admits; buffers of idle topologies
+  // are released when the reserved total would exceed the budget
+  int64_t budget = 0, peak_reserved = 0;
+  std::vector<int64_t> reserved;  // per topology: its batch and staging buffers
+  int64_t reserved_total() const {
+    int64_t r = 0;
+    for (int64_t v : reserved) r += v;
+    return r;
+  }
+  // Device bytes one scenario of topology t takes in its batch buffers (an
+  // upper bound: FP64 width for the typed arrays)
+  static int64_t scenario_bytes(const gox_topo* t) {
+    const int64_t n = t->n_bus, na = t->jac.nnz(), nu = t->jac.n_u;
+    const int64_t slots = t->factored ? (int64_t)t->sc.n_slots + (int64_t)t->sc.n_off : 4 * na;
+    return 8 * (8 * n + 5 * n + na + slots + 2 * nu) + 8 * 8 * n + 8 * 64 + 128;
+  }
   // Workers: each takes the oldest queued request whose topology no other
   // worker is solving, with up to max_batch queued requests of that
   // topology, so batches of different topologies run concurrently (each
@@ -2581,7 +2624,23 @@ struct gox_server {
           if (!busy[r->topo]) { tp = r->topo; break; }
         busy[tp] = 1;
         t = topos[tp];
-        for (auto it = queue.begin(); it != queue.end() && (int)batch.size() < max_batch;) {
+        int cap = max_batch;
+        if (budget > 0) {
+          // what fits beside the other topologies' buffers; idle ones give
+          // theirs back first when it does not
+          const int64_t per = scenario_bytes(t);
+          auto others = [&]() { return reserved_total() - reserved[tp]; };
+          for (size_t o = 0; o < topos.size() && others() + per > budget; o++)
+            if ((int)o != tp && !busy[o] && reserved[o] > 0) {
+              topos[o]->batch.release();
+              topos[o]->io.release();
+              reserved[o] = 0;
+            }
+          // buffers hold whole groups of 32 scenarios
+          const int64_t groups = (budget - others()) / (32 * per);
+          cap = (int)std::max<int64_t>(1, std::min<int64_t>(max_batch, groups * 32));
+        }
+        for (auto it = queue.begin(); it != queue.end() && (int)batch.size() < cap;) {
           if ((*it)->topo == tp) {
             batch.push_back(*it);
             it = queue.erase(it);
@@ -2593,6 +2652,8 @@ struct gox_server {
       solve(t, batch);
       {
         std::lock_guard<std::mutex> lk(mu);
+        reserved[tp] = (int64_t)(t->batch.bytes() + t->io.bytes());
+        peak_reserved = std::max(peak_reserved, reserved_total());
         busy[tp] = 0;
         batches++;
         solved += (int64_t)batch.size();
@@ -2683,6 +2744,7 @@ int gox_server_add_topology(gox_server* s, gox_topo* t, int32_t* topo_id) {
   std::lock_guard<std::mutex> lk(s->mu);
   s->topos.push_back(t);
   s->busy.push_back(0);
+  s->reserved.push_back(0);
   *topo_id = (int32_t)s->topos.size() - 1;
   return GOX_OK;
 }
@@ -2755,6 +2817,15 @@ int gox_server_stats(gox_server* s, int64_t* out) {
   out[0] = s->batches;
   out[1] = s->solved;
   out[2] = (int64_t)s->queue.size();
+  out[3] = s->reserved_total();
+  out[4] = s->peak_reserved;
+  return GOX_OK;
+}
+
+int gox_server_set_budget(gox_server* s, int64_t bytes) {
+  if (!s || bytes < 0) return GOX_E_INVALID;
+  std::lock_guard<std::mutex> lk(s->mu);
+  s->budget = bytes;
   return GOX_OK;
 }
 

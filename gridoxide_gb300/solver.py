@@ -665,9 +665,14 @@ class Server:
             time.sleep(1e-4)
 
     def stats(self) -> dict:
-        a = np.zeros(3, np.int64)
+        a = np.zeros(5, np.int64)
         check(_lib.load().gox_server_stats(self._h, _p(a, _lib.i64p)), "gox_server_stats")
-        return dict(batches=int(a[0]), solved=int(a[1]), queued=int(a[2]))
+        return dict(batches=int(a[0]), solved=int(a[1]), queued=int(a[2]),
+                    reserved_bytes=int(a[3]), peak_reserved_bytes=int(a[4]))
+
+    def set_budget(self, nbytes: int) -> None:
+        """Admit batches by an HBM budget in bytes (0: none)."""
+        check(_lib.load().gox_server_set_budget(self._h, int(nbytes)), "gox_server_set_budget")
 
     def close(self) -> None:
         if getattr(self, "_h", None):

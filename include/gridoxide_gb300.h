@@ -384,8 +384,15 @@ int gox_server_submit(gox_server *s, int32_t topo_id, const double *p_spec, cons
  * pointers may be NULL. */
 int gox_server_poll(gox_server *s, int64_t ticket, double *vm, double *va, int32_t *iterations,
                     int32_t *status, double *max_mismatch, double *latency_s);
-/* [0] batches run, [1] requests solved, [2] requests queued. */
+/* [0] batches run, [1] requests solved, [2] requests queued, [3] device
+ * bytes the topologies' batch buffers hold now, [4] their peak. */
 int gox_server_stats(gox_server *s, int64_t *out);
+/* Admission by HBM budget (bytes; 0, the default: none).  A worker admits
+ * at most the batch whose buffers fit in the budget beside the other
+ * topologies' buffers (by each topology's per-scenario device bytes),
+ * releasing the buffers of idle topologies first when they do not; one
+ * request is always admitted. */
+int gox_server_set_budget(gox_server *s, int64_t bytes);
 /* Finishes the queued requests, stops the worker, frees the server. */
 void gox_server_destroy(gox_server *s);
 

@@ -1,6 +1,7 @@
 """GPU: the serving loop (gox_server_*).  Requests arrive one scenario at a
 time (Poisson arrivals from a client thread) over three topologies, some
-with an N-1 outage; the worker batches them per topology.  Every report
+with an N-1 outage; the workers batch them per topology, with or without
+an HBM budget (the buffers held then stay within it).  Every report
 must equal, bit for bit, a direct batched solve of the same scenario on the
 same topology (lanes are independent, so the batch a request ran in does
 not change its result), and carry a positive latency."""
@@ -24,8 +25,8 @@ def _grids():
     return [(g1, y1), (g2, G.build_ybus(g2)), (g3, G.build_ybus(g3))]
 
 
-@pytest.mark.parametrize("precision", [0, 1])
-def test_server_reports_equal_direct_solves(gox, precision):
+@pytest.mark.parametrize("precision,budget", [(0, 0), (1, 0), (1, 16 << 20)])
+def test_server_reports_equal_direct_solves(gox, precision, budget):
     grids = _grids()
     topos = [gox.Topology(yb, g.bus_type) for g, yb in grids]
     rng = np.random.default_rng(40)
@@ -41,6 +42,8 @@ def test_server_reports_equal_direct_solves(gox, precision):
         reqs.append((t, p[0], q[0], out))
     srv = gox.Server(max_batch=64, precision=precision)
     ids = [srv.add_topology(tp) for tp in topos]
+    if budget:
+        srv.set_budget(budget)
     tickets = [None] * len(reqs)
 
     def client():
@@ -56,6 +59,8 @@ def test_server_reports_equal_direct_solves(gox, precision):
     st = srv.stats()
     srv.close()
     assert st["solved"] == len(reqs) and st["queued"] == 0 and st["batches"] >= 3
+    if budget:  # admitted batches kept the topologies' buffers within the budget
+        assert 0 < st["peak_reserved_bytes"] <= budget
     lat = np.array([r["latency_s"] for r in reports])
     assert np.all(lat > 0)
     # the same scenarios solved directly on the same topologies
