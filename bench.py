@@ -135,14 +135,16 @@ def read_traffic(kernel: str):
     return None
 
 
-def serve(gox, rate: float, seconds: float) -> dict:
+def serve(gox, rates, seconds: float) -> dict:
     """Serving leg: single-scenario requests arrive as a Poisson process at
-    `rate` per second for `seconds` over 16 family grids of 100-50,000 buses
-    (log-uniform sizes, each request's grid uniform at random), loads x
-    lognormal(0, 0.1), 10 % of the requests with one non-bridge branch out,
-    warm started from the grid's base-case solution, through the library's
-    serving loop (continuous batching on worker threads, mixed precision,
-    host buffers).  Latency = submit to completion of each request."""
+    each rate of `rates` per second for `seconds` over 16 family grids of
+    100-50,000 buses (log-uniform sizes, each request's grid uniform at
+    random), loads x lognormal(0, 0.1), 10 % of the requests with one
+    non-bridge branch out, warm started from the grid's base-case solution,
+    through the library's serving loop (continuous batching on worker
+    threads, mixed precision, host buffers).  Latency = submit to completion
+    of each request.  The last rate is the reported one; every rate is in
+    `sweep`, with p50 latency by grid size."""
     from gridoxide_gb300 import grids as G
     spec = G.many_topologies(count=16, n_min=100, n_max=50000, seed=5)
     grids, topos, cand, v0 = [], [], [], []
@@ -156,54 +158,70 @@ def serve(gox, rate: float, seconds: float) -> dict:
         v0.append((base.voltage_mag[0].copy(), base.voltage_ang[0].copy()))
         topos.append(topo)
         cand.append(np.flatnonzero(~G.bridges(g)))
-    srv = gox.Server(max_batch=1024, precision=gox.GOX_PRECISION_MIXED,
-                     tol=WORKLOAD["tol"], max_iter=WORKLOAD["max_iter"])
-    ids = [srv.add_topology(t) for t in topos]
-    rng = np.random.default_rng(7)
-    n_req = max(1, int(rate * seconds))
-    gaps = rng.exponential(1.0 / rate, size=n_req)
-    which = rng.integers(0, len(spec), size=n_req)
-    reqs = []
-    for i in range(n_req):
-        t = int(which[i])
-        g, yb = grids[t]
-        p, q = G.load_scenarios(g, 1, 0.1, 5000 + i)
-        out = None
-        if rng.random() < 0.1:
-            br = rng.choice(cand[t], size=1)
-            out = tuple(a[0] for a in G.outage_deltas(g, yb, br))
-        reqs.append((t, p[0], q[0], out))
-    # warm-up: one request per grid (first-use allocations, pivot orders)
-    for t in range(len(spec)):
-        g = grids[t][0]
-        srv.wait(srv.submit(ids[t], g.p_spec, g.q_spec, *v0[t]), g.n_bus)
-    st0 = srv.stats()
-    tickets = []
-    t0 = time.perf_counter()
-    due = t0
-    for i, (t, p, q, out) in enumerate(reqs):
-        due += gaps[i]
-        while time.perf_counter() < due:
-            pass
-        tickets.append(srv.submit(ids[t], p, q, *v0[t], outage=out))
-    lat, conv = [], 0
-    for (t, _, _, _), tk in zip(reqs, tickets):
-        r = srv.wait(tk, grids[t][0].n_bus)
-        lat.append(r["latency_s"])
-        conv += int(r["status"] == 0 and r["max_mismatch"] < WORKLOAD["tol"])
-    t1 = time.perf_counter()
-    st = srv.stats()
-    srv.close()
-    lat = np.array(lat) * 1000.0
-    nb = st["batches"] - st0["batches"]
-    return {"offered_rps": rate, "requests": n_req, "completed_rps": round(n_req / (t1 - t0), 1),
-            "p50_ms": round(float(np.percentile(lat, 50)), 3),
-            "p99_ms": round(float(np.percentile(lat, 99)), 3), "batches": nb,
-            "mean_batch": round(n_req / max(nb, 1), 1), "converged": conv,
-            "grids": len(spec), "buses": [int(min(x[0] for x in spec)), int(max(x[0] for x in spec))],
-            "note": "Poisson arrivals of single scenarios over 16 grids (100-50,000 buses), 10 % "
-                    "with an N-1 outage, gox_server_* continuous batching on 8 workers, mixed "
-                    "precision, host buffers, warm start from each grid's base case"}
+    sizes = np.array([x[0] for x in spec])
+    bins = [("<1k", sizes < 1000), ("1k-10k", (sizes >= 1000) & (sizes < 10000)),
+            (">=10k", sizes >= 10000)]
+    sweep = []
+    for k, rate in enumerate(rates):
+        srv = gox.Server(max_batch=1024, precision=gox.GOX_PRECISION_MIXED,
+                         tol=WORKLOAD["tol"], max_iter=WORKLOAD["max_iter"])
+        ids = [srv.add_topology(t) for t in topos]
+        rng = np.random.default_rng(7 + k)
+        n_req = max(1, int(rate * seconds))
+        gaps = rng.exponential(1.0 / rate, size=n_req)
+        which = rng.integers(0, len(spec), size=n_req)
+        reqs = []
+        for i in range(n_req):
+            t = int(which[i])
+            g, yb = grids[t]
+            p, q = G.load_scenarios(g, 1, 0.1, 5000 + 100000 * k + i)
+            out = None
+            if rng.random() < 0.1:
+                br = rng.choice(cand[t], size=1)
+                out = tuple(a[0] for a in G.outage_deltas(g, yb, br))
+            reqs.append((t, p[0], q[0], out))
+        # warm-up: one request per grid (first-use allocations, pivot orders)
+        for t in range(len(spec)):
+            g = grids[t][0]
+            srv.wait(srv.submit(ids[t], g.p_spec, g.q_spec, *v0[t]), g.n_bus)
+        st0 = srv.stats()
+        tickets = []
+        t0 = time.perf_counter()
+        due = t0
+        for i, (t, p, q, out) in enumerate(reqs):
+            due += gaps[i]
+            while time.perf_counter() < due:
+                pass
+            tickets.append(srv.submit(ids[t], p, q, *v0[t], outage=out))
+        lat, conv = [], 0
+        for (t, _, _, _), tk in zip(reqs, tickets):
+            r = srv.wait(tk, grids[t][0].n_bus)
+            lat.append(r["latency_s"])
+            conv += int(r["status"] == 0 and r["max_mismatch"] < WORKLOAD["tol"])
+        t1 = time.perf_counter()
+        st = srv.stats()
+        srv.close()
+        lat = np.array(lat) * 1000.0
+        nb = st["batches"] - st0["batches"]
+        grid_of = np.array([r[0] for r in reqs])
+        by_size = {}
+        for name, sel in bins:
+            m = np.isin(grid_of, np.flatnonzero(sel))
+            if m.any():
+                by_size[name] = round(float(np.percentile(lat[m], 50)), 3)
+        sweep.append({"offered_rps": rate, "requests": n_req,
+                      "completed_rps": round(n_req / (t1 - t0), 1),
+                      "p50_ms": round(float(np.percentile(lat, 50)), 3),
+                      "p99_ms": round(float(np.percentile(lat, 99)), 3), "batches": nb,
+                      "mean_batch": round(n_req / max(nb, 1), 1), "converged": conv,
+                      "p50_ms_by_buses": by_size})
+    out = dict(sweep[-1])
+    out.update({"sweep": sweep, "grids": len(spec),
+                "buses": [int(sizes.min()), int(sizes.max())],
+                "note": "Poisson arrivals of single scenarios over 16 grids (100-50,000 buses), 10 % "
+                        "with an N-1 outage, gox_server_* continuous batching on 8 workers, mixed "
+                        "precision, host buffers, warm start from each grid's base case"})
+    return out
 
 
 def n1_case10000(gox, rounds: int, batch: int = 8192) -> dict:
@@ -669,7 +687,8 @@ def main():
         "clocks": cl,
     }
     if rank == 0 and args.serve_rate > 0 and not args.quick:
-        line["serving"] = serve(gox, args.serve_rate, args.serve_seconds)
+        rates = sorted({r for r in (100.0, 300.0, args.serve_rate) if r <= args.serve_rate})
+        line["serving"] = serve(gox, rates, args.serve_seconds)
     if rank == 0 and args.many_rounds > 0 and not args.quick:
         line["n1_case10000"] = n1_case10000(gox, args.many_rounds)
         line["many_topologies"] = many_topologies(gox, args.many_rounds)
