@@ -25,6 +25,10 @@ import time
 
 import numpy as np
 
+# more hardware work queues than the 8 by default, for the legs that solve
+# from several host threads at once (read when the CUDA context is created)
+os.environ.setdefault("CUDA_DEVICE_MAX_CONNECTIONS", "32")
+
 ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
@@ -209,7 +213,10 @@ def serve(gox, rates, seconds: float) -> dict:
             m = np.isin(grid_of, np.flatnonzero(sel))
             if m.any():
                 by_size[name] = round(float(np.percentile(lat[m], 50)), 3)
+        dq = (st["queue_us"] - st0["queue_us"]) / 1000.0 / n_req
+        ds = (st["solve_us"] - st0["solve_us"]) / 1000.0 / n_req
         sweep.append({"offered_rps": rate, "requests": n_req,
+                      "mean_queued_ms": round(dq, 3), "mean_in_solve_ms": round(ds, 3),
                       "completed_rps": round(n_req / (t1 - t0), 1),
                       "p50_ms": round(float(np.percentile(lat, 50)), 3),
                       "p99_ms": round(float(np.percentile(lat, 99)), 3), "batches": nb,

@@ -36,24 +36,44 @@ struct CudaError : std::runtime_error {
       throw CudaError(std::string(#x) + ": " + cudaGetErrorString(e_));                    \
   } while (0)
 
+// The stream of the entry point running on this thread: device buffers are
+// allocated and freed in its order (cudaMallocAsync / cudaFreeAsync) while it
+// is set.  A plain cudaFree synchronizes the whole device, which would stall
+// every other solve in flight (concurrent topologies, the server's workers).
+static thread_local cudaStream_t tl_alloc_stream = nullptr;
+struct AllocStreamScope {
+  cudaStream_t prev;
+  explicit AllocStreamScope(cudaStream_t s) : prev(tl_alloc_stream) { tl_alloc_stream = s; }
+  ~AllocStreamScope() { tl_alloc_stream = prev; }
+};
+
 // Owning device allocation.
 struct DevMem {
   void* p = nullptr;
   size_t bytes = 0;
+  bool pooled = false;  // from cudaMallocAsync: may be freed in stream order
   DevMem() = default;
   DevMem(const DevMem&) = delete;
   DevMem& operator=(const DevMem&) = delete;
   ~DevMem() { release(); }
   void release() {
-    if (p) cudaFree(p);
+    if (p) {
+      if (pooled && tl_alloc_stream) cudaFreeAsync(p, tl_alloc_stream);
+      else cudaFree(p);
+    }
     p = nullptr;
     bytes = 0;
+    pooled = false;
   }
   void ensure(size_t b) {
     if (b <= bytes && p) return;
+    // a buffer that has to grow grows by half again at least: fewer
+    // reallocations as batches vary
+    if (p) b = std::max(b, bytes + bytes / 2);
     release();
     if (b == 0) b = 16;
-    cudaError_t e = cudaMalloc(&p, b);
+    pooled = tl_alloc_stream != nullptr;
+    cudaError_t e = pooled ? cudaMallocAsync(&p, b, tl_alloc_stream) : cudaMalloc(&p, b);
     if (e == cudaErrorMemoryAllocation) {
       cudaGetLastError();
       throw std::bad_alloc();
@@ -68,7 +88,14 @@ struct DevMem {
 template <typename T>
 static void upload(DevMem& m, const std::vector<T>& v) {
   m.ensure(sizeof(T) * std::max<size_t>(v.size(), 1));
-  if (!v.empty()) GOX_CK(cudaMemcpy(m.p, v.data(), sizeof(T) * v.size(), cudaMemcpyHostToDevice));
+  if (v.empty()) return;
+  if (m.pooled) {  // usable in the order of the stream it was allocated on
+    GOX_CK(cudaMemcpyAsync(m.p, v.data(), sizeof(T) * v.size(), cudaMemcpyHostToDevice,
+                           tl_alloc_stream));
+    GOX_CK(cudaStreamSynchronize(tl_alloc_stream));
+  } else {
+    GOX_CK(cudaMemcpy(m.p, v.data(), sizeof(T) * v.size(), cudaMemcpyHostToDevice));
+  }
 }
 
 // ---------------------------------------------------------------------------
@@ -480,11 +507,16 @@ struct Iter {
   }
   static void refactor(const DevSchedule& ds, const BatchDev& D, cudaStream_t st) {
     const int i = sizeof(T) == 4 ? 0 : 1;
-    // the budget every plan fits in, the same value from every thread (calls
-    // on different topologies may run concurrently; a plan-sized value set
-    // by one could undercut another's launch)
-    GOX_CK(cudaFuncSetAttribute(k_refactor<T>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                (int)kRefactorSmem));
+    // the budget every plan fits in, set once per device (the same value for
+    // every plan; setting an attribute per launch would put a driver call
+    // between concurrent solves' launches)
+    static std::once_flag once[64];
+    int dev = 0;
+    GOX_CK(cudaGetDevice(&dev));
+    std::call_once(once[dev & 63], [] {
+      GOX_CK(cudaFuncSetAttribute(k_refactor<T>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                  (int)kRefactorSmem));
+    });
     k_refactor<T><<<D.G, 32 * ds.st_nw[i], ds.st_smem[i], st>>>(ds.st[i], ds.d, D);
   }
   static void solve(const SchedDev& S, const BatchDev& D, cudaStream_t st) {
@@ -536,6 +568,11 @@ struct GuessSys {
   DevMem yp, yi, yre, yim, rec, rhs_ptr, rhs_ej, pqb, pinv, qinv;
   DevMem lu, off, rhs, sol, sing, piv, gact, err, gvm, gva;
   GuessDev d{};
+};
+
+// Staging of the mixed path's FP64 re-solves (rows of the flagged scenarios)
+struct FallbackBufs {
+  DevMem idx, p, q, vm, va, sl, dr, di, ovm, ova, it, st, mm, hi;
 };
 
 // A Newton loop captured as a CUDA graph (conditional while / if nodes),
@@ -591,10 +628,13 @@ struct gox_topo {
   std::vector<int32_t> base_label;  // components of the graph as registered
   // captured Newton loops (a few keys, oldest replaced) and how many solves used one
   std::vector<LoopGraph> loop_graphs;
+  int32_t* h_nactive = nullptr;  // pinned
+  FallbackBufs fb;
   bool graphs_off = false;   // a capture failed: the host-driven loop only
   bool graphs_wanted = true;  // gox_topo_set_graph
   int64_t graph_solves = 0;
   ~gox_topo() {
+    if (h_nactive) cudaFreeHost(h_nactive);
     for (auto& v : variants) delete v.second;
     for (auto& lg : loop_graphs)
       if (lg.exec) cudaGraphExecDestroy(lg.exec);
@@ -626,6 +666,40 @@ static int guard_impl(const std::function<int()>& f) {
     std::fprintf(stderr, "gridoxide_gb300: %s\n", e.what());
     return GOX_E_INVALID;
   }
+}
+
+// The calling thread's stream for the host-array entry points: created once
+// per thread (and device), so that concurrent callers keep distinct streams
+// (and hardware queues) instead of a new stream per call
+static cudaStream_t thread_stream() {
+  struct ThreadStream {
+    cudaStream_t s = nullptr;
+    int dev = -1;
+    ~ThreadStream() {
+      if (s) cudaStreamDestroy(s);
+    }
+  };
+  thread_local ThreadStream ts;
+  int dev = 0;
+  GOX_CK(cudaGetDevice(&dev));
+  static std::once_flag pool_once[64];
+  std::call_once(pool_once[dev & 63], [dev] {
+    // stream-ordered frees keep their memory in the device's pool for the
+    // next allocation instead of returning it at every synchronization
+    cudaMemPool_t pool;
+    if (cudaDeviceGetDefaultMemPool(&pool, dev) == cudaSuccess) {
+      uint64_t keep = UINT64_MAX;
+      cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &keep);
+    }
+    cudaGetLastError();
+  });
+  if (!ts.s || ts.dev != dev) {
+    if (ts.s) cudaStreamDestroy(ts.s);
+    ts.s = nullptr;
+    GOX_CK(cudaStreamCreateWithFlags(&ts.s, cudaStreamNonBlocking));
+    ts.dev = dev;
+  }
+  return ts.s;
 }
 
 static int require_device() {
@@ -1213,16 +1287,12 @@ static int batch_device(gox_topo* t, int B, const double* p_spec, const double* 
     GOX_CK(cudaStreamSynchronize(st));
   }
   GOX_CK(cudaMemsetAsync(DB.err.p, 0, 16, st));
-  int32_t* h_nactive = nullptr;
-  GOX_CK(cudaMallocHost(&h_nactive, sizeof(int32_t)));
-  try {
-    if (precision == GOX_PRECISION_FP64) run_iterations<double>(t, D, max_iter, outage, st, h_nactive);
-    else run_iterations<float>(t, D, max_iter, outage, st, h_nactive);
-  } catch (...) {
-    cudaFreeHost(h_nactive);
-    throw;
-  }
-  cudaFreeHost(h_nactive);
+  // the running-group count read back every iteration: pinned, kept by the
+  // topology (freeing pinned memory synchronizes the whole device, which
+  // would stall every other topology's solve in flight)
+  if (!t->h_nactive) GOX_CK(cudaMallocHost(&t->h_nactive, sizeof(int32_t)));
+  if (precision == GOX_PRECISION_FP64) run_iterations<double>(t, D, max_iter, outage, st, t->h_nactive);
+  else run_iterations<float>(t, D, max_iter, outage, st, t->h_nactive);
   {
     int32_t herr[2] = {0, 0};
     GOX_CK(cudaMemcpyAsync(herr, DB.err.p, 8, cudaMemcpyDeviceToHost, st));
@@ -1252,7 +1322,11 @@ static int batch_device(gox_topo* t, int B, const double* p_spec, const double* 
       const int Bf = (int)idx.size();
       const int64_t launches0 = t->launches;
       const Timing timing0 = t->timing;
-      DevMem didx, fp, fq, fvm, fva, fsl, fdr, fdi, ovm, ova, oit, ost, omm, ohi;
+      // staging kept by the topology (grow-only): freeing device memory per
+      // call would synchronize the whole device under concurrent solves
+      FallbackBufs& F = t->fb;
+      DevMem &didx = F.idx, &fp = F.p, &fq = F.q, &fvm = F.vm, &fva = F.va, &fsl = F.sl, &fdr = F.dr,
+             &fdi = F.di, &ovm = F.ovm, &ova = F.ova, &oit = F.it, &ost = F.st, &omm = F.mm, &ohi = F.hi;
       upload(didx, idx);
       const int32_t* ix = didx.as<int32_t>();
       const size_t rows = (size_t)Bf * n;
@@ -1723,6 +1797,7 @@ int gox_batch_solve_device(gox_topo* t, int32_t B, const double* p_spec, const d
   if (int r = require_device()) return r;
   return guard_impl([&]() -> int {
     cudaStream_t st = (cudaStream_t)stream;
+    AllocStreamScope alloc_scope(st);
     if (max_iter == 0) return GOX_E_INVALID;
     return batch_any(t, B, p_spec, q_spec, vm0, va0, v_stride, o_slot, o_dre, o_dim, tol,
                      max_iter, precision, vm_out, va_out, iterations, status, max_mismatch,
@@ -1748,12 +1823,8 @@ int gox_batch_solve(gox_topo* t, int32_t B, const double* p_spec, const double* 
   if (int r = require_device()) return r;
   return guard_impl([&]() -> int {
     const int n = t->n_bus;
-    cudaStream_t st = nullptr;
-    GOX_CK(cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking));
-    struct StreamGuard {
-      cudaStream_t s;
-      ~StreamGuard() { cudaStreamDestroy(s); }
-    } sg{st};
+    cudaStream_t st = thread_stream();
+    AllocStreamScope alloc_scope(st);
     const size_t bn = (size_t)B * n, nv = (size_t)(v_stride ? B : 1) * n;
     // device copies of the host arrays, kept by the topology between calls
     IoStage& io = t->io;
@@ -1818,12 +1889,8 @@ int gox_batch_solve_scaled(gox_topo* t, int32_t B, const double* scales, const d
   }
   if (int r = require_device()) return r;
   return guard_impl([&]() -> int {
-    cudaStream_t st = nullptr;
-    GOX_CK(cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking));
-    struct StreamGuard {
-      cudaStream_t s;
-      ~StreamGuard() { cudaStreamDestroy(s); }
-    } sg{st};
+    cudaStream_t st = thread_stream();
+    AllocStreamScope alloc_scope(st);
     const size_t bn = (size_t)B * n;
     IoStage& io = t->io;
     io.p.ensure(bn * 8); io.q.ensure(bn * 8); io.vm.ensure((size_t)n * 8); io.va.ensure((size_t)n * 8);
@@ -1876,12 +1943,8 @@ int gox_batch_solve_qlim(gox_topo* t, int32_t B, const double* p_spec, const dou
   if (int r = require_device()) return r;
   return guard_impl([&]() -> int {
     const int n = t->n_bus;
-    cudaStream_t st = nullptr;
-    GOX_CK(cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking));
-    struct StreamGuard {
-      cudaStream_t s;
-      ~StreamGuard() { cudaStreamDestroy(s); }
-    } sg{st};
+    cudaStream_t st = thread_stream();
+    AllocStreamScope alloc_scope(st);
     const size_t bn = (size_t)B * n, nv = (size_t)(v_stride ? B : 1) * n;
     // the batch's state on the device: injections (q pinned as buses switch), V
     DevMem dp, dq, dv0m, dv0a, dvm, dva, dit, dst, dmm;
@@ -1990,6 +2053,7 @@ int gox_batch_solve_qlim(gox_topo* t, int32_t B, const double* p_spec, const dou
             cudaStream_t s;
             ~WorkStream() { cudaStreamDestroy(s); }
           } wsg{ws};
+          AllocStreamScope alloc_scope(ws);
           DevMem dix, sp, sq, svm, sva, ovm, ova, oit, ost, omm;
           for (int j = next++; j < (int)jobs.size() && err.load() == GOX_OK; j = next++) {
             gox_topo* v = jobs[j].first;
@@ -2271,12 +2335,8 @@ int gox_topo_initial_guess(gox_topo* t, int32_t B, const double* p_spec, const d
   return guard_impl([&]() -> int {
     const int n = t->n_bus;
     const size_t bn = (size_t)B * n, nv = (size_t)(v_stride ? B : 1) * n;
-    cudaStream_t st = nullptr;
-    GOX_CK(cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking));
-    struct StreamGuard {
-      cudaStream_t s;
-      ~StreamGuard() { cudaStreamDestroy(s); }
-    } sg{st};
+    cudaStream_t st = thread_stream();
+    AllocStreamScope alloc_scope(st);
     IoStage& io = t->io;
     io.p.ensure(bn * 8); io.q.ensure(bn * 8); io.vm.ensure(nv * 8); io.va.ensure(nv * 8);
     GOX_CK(cudaMemcpyAsync(io.p.p, p_spec, bn * 8, cudaMemcpyHostToDevice, st));
@@ -2583,6 +2643,7 @@ struct gox_server {
   // batch buffers bound the batch a worker admits; buffers of idle topologies
   // are released when the reserved total would exceed the budget
   int64_t budget = 0, peak_reserved = 0;
+  double queue_s = 0.0, solve_s = 0.0;  // summed over requests: waiting, being solved
   std::vector<int64_t> reserved;  // per topology: its batch and staging buffers
   int64_t reserved_total() const {
     int64_t r = 0;
@@ -2649,9 +2710,14 @@ struct gox_server {
           }
         }
       }
+      const auto t_pick = std::chrono::steady_clock::now();
       solve(t, batch);
+      const auto t_done = std::chrono::steady_clock::now();
       {
         std::lock_guard<std::mutex> lk(mu);
+        for (const auto& r : batch)
+          queue_s += std::chrono::duration<double>(t_pick - r->t_submit).count();
+        solve_s += std::chrono::duration<double>(t_done - t_pick).count() * (double)batch.size();
         reserved[tp] = (int64_t)(t->batch.bytes() + t->io.bytes());
         peak_reserved = std::max(peak_reserved, reserved_total());
         busy[tp] = 0;
@@ -2819,6 +2885,8 @@ int gox_server_stats(gox_server* s, int64_t* out) {
   out[2] = (int64_t)s->queue.size();
   out[3] = s->reserved_total();
   out[4] = s->peak_reserved;
+  out[5] = (int64_t)(s->queue_s * 1e6);
+  out[6] = (int64_t)(s->solve_s * 1e6);
   return GOX_OK;
 }
 

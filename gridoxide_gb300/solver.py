@@ -665,10 +665,11 @@ class Server:
             time.sleep(1e-4)
 
     def stats(self) -> dict:
-        a = np.zeros(5, np.int64)
+        a = np.zeros(7, np.int64)
         check(_lib.load().gox_server_stats(self._h, _p(a, _lib.i64p)), "gox_server_stats")
         return dict(batches=int(a[0]), solved=int(a[1]), queued=int(a[2]),
-                    reserved_bytes=int(a[3]), peak_reserved_bytes=int(a[4]))
+                    reserved_bytes=int(a[3]), peak_reserved_bytes=int(a[4]),
+                    queue_us=int(a[5]), solve_us=int(a[6]))
 
     def set_budget(self, nbytes: int) -> None:
         """Admit batches by an HBM budget in bytes (0: none)."""

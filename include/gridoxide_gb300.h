@@ -385,7 +385,9 @@ int gox_server_submit(gox_server *s, int32_t topo_id, const double *p_spec, cons
 int gox_server_poll(gox_server *s, int64_t ticket, double *vm, double *va, int32_t *iterations,
                     int32_t *status, double *max_mismatch, double *latency_s);
 /* [0] batches run, [1] requests solved, [2] requests queued, [3] device
- * bytes the topologies' batch buffers hold now, [4] their peak. */
+ * bytes the topologies' batch buffers hold now, [4] their peak, [5] / [6]
+ * microseconds summed over the solved requests spent queued / in their
+ * batch's solve. */
 int gox_server_stats(gox_server *s, int64_t *out);
 /* Admission by HBM budget (bytes; 0, the default: none).  A worker admits
  * at most the batch whose buffers fit in the budget beside the other
