@@ -49,6 +49,14 @@ def test_graph_loop_equals_host_loop(gox, prec, outage, max_iter):
         assert np.all(first.status == gox.GOX_MAX_ITERATIONS)
     else:
         assert np.all(first.status == gox.GOX_CONVERGED)
+    # switched off, the same configuration stays on the host-driven loop
+    off = gox.Topology(yb, g.bus_type)
+    off.set_graph(False)
+    for _ in range(3):
+        r = off.solve(p, q, g.vm, g.va, precision=precision, outage=out, history=True,
+                      max_iter=max_iter)
+    assert off.info()["graph_solves"] == 0
+    _same(first, r)
     # a small batch stays on the host-driven loop
     small = gox.Topology(yb, g.bus_type)
     for _ in range(3):
