@@ -94,6 +94,7 @@ SIGNATURES = {
     "gox_set_pivot_tolerance": (C.c_int, [vp, C.c_double]),
     "gox_topo_set_initial_guess": (C.c_int, [vp, C.c_int32]),
     "gox_topo_set_graph": (C.c_int, [vp, C.c_int32]),
+    "gox_topo_set_split": (C.c_int, [vp, C.c_int32]),
     "gox_topo_initial_guess": (C.c_int, [vp, C.c_int32, f64p, f64p, f64p, f64p, C.c_int32, f64p,
                                          f64p]),
     "gox_topo_set_zip": (C.c_int, [vp, f64p, f64p, f64p, f64p]),

@@ -630,10 +630,18 @@ struct gox_topo {
   std::vector<LoopGraph> loop_graphs;
   int32_t* h_nactive = nullptr;  // pinned
   FallbackBufs fb;
+  // split solves: a second instance of this topology (same pivot order, own
+  // device buffers and stream) that solves the second half of a large batch
+  // concurrently with the first
+  int split_parts = 1;
+  std::unique_ptr<gox_topo> twin;
+  cudaStream_t own_stream = nullptr;
   bool graphs_off = false;   // a capture failed: the host-driven loop only
   bool graphs_wanted = true;  // gox_topo_set_graph
   int64_t graph_solves = 0;
   ~gox_topo() {
+    twin.reset();
+    if (own_stream) cudaStreamDestroy(own_stream);
     if (h_nactive) cudaFreeHost(h_nactive);
     for (auto& v : variants) delete v.second;
     for (auto& lg : loop_graphs)
@@ -1666,6 +1674,90 @@ static int batch_any(gox_topo* t, int B, const double* p_spec, const double* q_s
   return GOX_OK;
 }
 
+// The twin of a factored topology: the same pattern, pivot order, schedule
+// and settings; its own device state
+static gox_topo* split_twin(gox_topo* t) {
+  if (t->twin) return t->twin.get();
+  std::unique_ptr<gox_topo> v(new gox_topo());
+  v->n_bus = t->n_bus;
+  v->yp = t->yp; v->yi = t->yi; v->yre = t->yre; v->yim = t->yim; v->bus_type = t->bus_type;
+  v->jac = t->jac; v->csc = t->csc; v->sym = t->sym; v->num = t->num; v->sc = t->sc;
+  v->s32 = t->s32; v->s64 = t->s64;
+  v->factored = true;
+  v->uploaded = false;
+  v->device = t->device;
+  v->piv_tol = t->piv_tol;
+  v->graphs_wanted = t->graphs_wanted;
+  v->zip = t->zip;
+  if (!v->zip.empty()) upload(v->dzip, v->zip);
+  t->twin = std::move(v);
+  return t->twin.get();
+}
+
+static constexpr int kSplitMinScenarios = 4096;
+
+// batch_any, or -- when the topology is set to split, its pivot order is
+// fixed, the start is given and the batch is large -- its two halves (split
+// at a multiple of 32 scenarios, so every group and result is the same)
+// solved concurrently, the first on `st` and the second by the twin on its
+// own stream from a second host thread
+static int batch_split(gox_topo* t, int B, const double* p_spec, const double* q_spec,
+                       const double* vm0, const double* va0, int v_stride, const int32_t* o_slot,
+                       const double* o_dre, const double* o_dim, double tol, int max_iter,
+                       int precision, double* vm_out, double* va_out, int32_t* iters,
+                       int32_t* status, double* max_mis, double* hist, cudaStream_t st,
+                       const double* h_p, const double* h_q, const double* h_vm, const double* h_va,
+                       const int32_t* h_oslot, const double* h_odre, const double* h_odim) {
+  if (t->split_parts < 2 || !t->factored || t->guess_mode != 0 || t->timing.on ||
+      B < kSplitMinScenarios)
+    return batch_any(t, B, p_spec, q_spec, vm0, va0, v_stride, o_slot, o_dre, o_dim, tol, max_iter,
+                     precision, vm_out, va_out, iters, status, max_mis, hist, st, h_p, h_q, h_vm,
+                     h_va, h_oslot, h_odre, h_odim);
+  gox_topo* tw = split_twin(t);
+  if (!tw->own_stream) GOX_CK(cudaStreamCreateWithFlags(&tw->own_stream, cudaStreamNonBlocking));
+  const int n = t->n_bus;
+  const int B1 = ((B / 2 + 31) / 32) * 32, B2 = B - B1;
+  const size_t off = (size_t)B1 * n, voff = v_stride ? off : 0;
+  cudaEvent_t ready;
+  GOX_CK(cudaEventCreateWithFlags(&ready, cudaEventDisableTiming));
+  GOX_CK(cudaEventRecord(ready, st));  // the inputs, as the caller's stream has them
+  int r2 = GOX_OK;
+  std::thread second([&] {
+    r2 = guard_impl([&]() -> int {
+      GOX_CK(cudaSetDevice(t->device));
+      cudaStream_t s2 = tw->own_stream;
+      AllocStreamScope scope(s2);
+      GOX_CK(cudaStreamWaitEvent(s2, ready, 0));
+      return batch_any(tw, B2, p_spec + off, q_spec + off, vm0 + voff, va0 + voff, v_stride,
+                       o_slot ? o_slot + 4 * (size_t)B1 : nullptr,
+                       o_dre ? o_dre + 4 * (size_t)B1 : nullptr,
+                       o_dim ? o_dim + 4 * (size_t)B1 : nullptr, tol, max_iter, precision,
+                       vm_out + off, va_out + off, iters + B1, status + B1, max_mis + B1,
+                       hist ? hist + (size_t)B1 * max_iter : nullptr, s2,
+                       h_p ? h_p + off : nullptr, h_q ? h_q + off : nullptr,
+                       h_vm ? h_vm + voff : nullptr, h_va ? h_va + voff : nullptr,
+                       h_oslot ? h_oslot + 4 * (size_t)B1 : nullptr,
+                       h_odre ? h_odre + 4 * (size_t)B1 : nullptr,
+                       h_odim ? h_odim + 4 * (size_t)B1 : nullptr);
+    });
+  });
+  int r1 = GOX_OK;
+  try {
+    r1 = batch_any(t, B1, p_spec, q_spec, vm0, va0, v_stride, o_slot, o_dre, o_dim, tol, max_iter,
+                   precision, vm_out, va_out, iters, status, max_mis, hist, st, h_p, h_q, h_vm,
+                   h_va, h_oslot, h_odre, h_odim);
+  } catch (...) {
+    second.join();
+    cudaEventDestroy(ready);
+    throw;
+  }
+  second.join();
+  cudaEventDestroy(ready);
+  t->launches += tw->launches;
+  t->fallbacks += tw->fallbacks;
+  return r1 != GOX_OK ? r1 : r2;
+}
+
 extern "C" {
 
 const char* gox_version(void) { return "gridoxide_gb300 0.1.0 (sm_103a)"; }
@@ -1761,6 +1853,7 @@ int gox_topo_register(int32_t n_bus, const int32_t* yp, const int32_t* yi, const
 
 int gox_topo_reset(gox_topo* t) {
   if (!t) return GOX_E_INVALID;
+  t->twin.reset();
   t->factored = false;
   t->uploaded = false;
   t->num = Numeric();
@@ -1799,9 +1892,9 @@ int gox_batch_solve_device(gox_topo* t, int32_t B, const double* p_spec, const d
     cudaStream_t st = (cudaStream_t)stream;
     AllocStreamScope alloc_scope(st);
     if (max_iter == 0) return GOX_E_INVALID;
-    return batch_any(t, B, p_spec, q_spec, vm0, va0, v_stride, o_slot, o_dre, o_dim, tol,
-                     max_iter, precision, vm_out, va_out, iterations, status, max_mismatch,
-                     history, st, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr);
+    return batch_split(t, B, p_spec, q_spec, vm0, va0, v_stride, o_slot, o_dre, o_dim, tol,
+                       max_iter, precision, vm_out, va_out, iterations, status, max_mismatch,
+                       history, st, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr);
   });
 }
 
@@ -1845,7 +1938,7 @@ int gox_batch_solve(gox_topo* t, int32_t B, const double* p_spec, const double* 
       GOX_CK(cudaMemcpyAsync(dre.p, o_dre, (size_t)B * 32, cudaMemcpyHostToDevice, st));
       GOX_CK(cudaMemcpyAsync(dim.p, o_dim, (size_t)B * 32, cudaMemcpyHostToDevice, st));
     }
-    int r = batch_any(t, B, dp.as<double>(), dq.as<double>(), dvm.as<double>(),
+    int r = batch_split(t, B, dp.as<double>(), dq.as<double>(), dvm.as<double>(),
                          dva.as<double>(), v_stride, o_slot ? dsl.as<int32_t>() : nullptr,
                          o_slot ? dre.as<double>() : nullptr, o_slot ? dim.as<double>() : nullptr,
                          tol, max_iter, precision, dovm.as<double>(), dova.as<double>(),
@@ -2287,6 +2380,7 @@ int64_t gox_last_launches(const gox_topo* t) { return t ? t->launches : -1; }
 int gox_set_pivot_tolerance(gox_topo* t, double tol) {
   if (!t || !(tol >= 0.0) || !std::isfinite(tol)) return GOX_E_INVALID;
   t->piv_tol = tol;
+  if (t->twin) t->twin->piv_tol = tol;
   return GOX_OK;
 }
 
@@ -2295,6 +2389,7 @@ int64_t gox_last_fallbacks(const gox_topo* t) { return t ? t->fallbacks : -1; }
 int gox_topo_set_zip(gox_topo* t, const double* zi_re, const double* zi_im, const double* zc_re,
                      const double* zc_im) {
   if (!t) return GOX_E_INVALID;
+  t->twin.reset();  // rebuilt with the new terms when next needed
   const bool none = !zi_re && !zi_im && !zc_re && !zc_im;
   if (!none && (!zi_re || !zi_im || !zc_re || !zc_im)) return GOX_E_INVALID;
   return guard_impl([&]() -> int {
@@ -2314,9 +2409,16 @@ int gox_topo_set_zip(gox_topo* t, const double* zi_re, const double* zi_im, cons
   });
 }
 
+int gox_topo_set_split(gox_topo* t, int32_t parts) {
+  if (!t || parts < 1 || parts > 2) return GOX_E_INVALID;
+  t->split_parts = parts;
+  return GOX_OK;
+}
+
 int gox_topo_set_graph(gox_topo* t, int32_t on) {
   if (!t) return GOX_E_INVALID;
   t->graphs_wanted = on != 0;
+  if (t->twin) t->twin->graphs_wanted = on != 0;
   return GOX_OK;
 }
 

@@ -408,6 +408,10 @@ class Topology:
         a = [_f64(imp.real), _f64(imp.imag), _f64(cur.real), _f64(cur.imag)]
         check(L.gox_topo_set_zip(self._h, *[_p(x, _lib.f64p) for x in a]), "gox_topo_set_zip")
 
+    def set_split(self, parts: int) -> None:
+        """Solve large batches as 1 or 2 concurrent halves (gox_topo_set_split)."""
+        check(_lib.load().gox_topo_set_split(self._h, int(parts)), "gox_topo_set_split")
+
     def set_graph(self, on: bool) -> None:
         """Run the Newton loop as a captured CUDA graph (default) or host-driven."""
         check(_lib.load().gox_topo_set_graph(self._h, 1 if on else 0), "gox_topo_set_graph")
