@@ -323,12 +323,13 @@ int gox_topo_set_zip(gox_topo *t, const double *zi_re, const double *zi_im, cons
  * topology on the host-driven loop. */
 int gox_topo_set_graph(gox_topo *t, int32_t on);
 
-/* Split solves (parts 1, the default, or 2): once the pivot order is fixed,
+/* Split solves (parts 2, the default, or 1): once the pivot order is fixed,
  * a batch of 4,096+ scenarios with the given start is solved as two halves
  * (split at a multiple of 32 scenarios) at the same time, the second by a
  * second instance of the topology on its own stream from a second host
- * thread, so one half's mismatch and fill overlap the other's refactor.
- * Every result is the same as unsplit, bit for bit. */
+ * thread, started a fraction of an iteration later so that one half's
+ * mismatch and fill overlap the other's refactor.  Every result is the same
+ * as unsplit, bit for bit. */
 int gox_topo_set_split(gox_topo *t, int32_t parts);
 
 #define GOX_GUESS_GIVEN 0

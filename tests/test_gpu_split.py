@@ -23,6 +23,8 @@ def test_split_equals_unsplit(gox, prec, outage):
         out = G.outage_deltas(g, yb, rng.choice(np.flatnonzero(~G.bridges(g)), B))
     precision = gox.GOX_PRECISION_MIXED if prec == "mixed" else gox.GOX_PRECISION_FP64
     topo = gox.Topology(yb, g.bus_type)
+    topo.set_split(1)
+    ref = topo.solve(p, q, g.vm, g.va, precision=precision, outage=out, history=True)
     ref = topo.solve(p, q, g.vm, g.va, precision=precision, outage=out, history=True)
     topo.set_split(2)
     for _ in range(2):
@@ -41,6 +43,7 @@ def test_split_device_entry(gox):
     B = 4096
     p, q = G.load_scenarios(g, B, 0.15, 53)
     topo = gox.Topology(yb, g.bus_type)
+    topo.set_split(1)
     ref = topo.solve(p, q, g.vm, g.va)
     topo.set_split(2)
     d = lambda a: torch.as_tensor(np.ascontiguousarray(a), dtype=torch.float64, device="cuda")
