@@ -1728,8 +1728,10 @@ static int batch_split(gox_topo* t, int B, const double* p_spec, const double* q
                        int32_t* status, double* max_mis, double* hist, cudaStream_t st,
                        const double* h_p, const double* h_q, const double* h_vm, const double* h_va,
                        const int32_t* h_oslot, const double* h_odre, const double* h_odim) {
+  // (FP64 solves stay whole: their refactor is bound by the FP64 pipe, which
+  // the halves would share; measured slower split)
   if (t->split_parts < 2 || !t->factored || t->guess_mode != 0 || t->timing.on ||
-      B < kSplitMinScenarios)
+      B < kSplitMinScenarios || precision != GOX_PRECISION_MIXED)
     return batch_any(t, B, p_spec, q_spec, vm0, va0, v_stride, o_slot, o_dre, o_dim, tol, max_iter,
                      precision, vm_out, va_out, iters, status, max_mis, hist, st, h_p, h_q, h_vm,
                      h_va, h_oslot, h_odre, h_odim);

@@ -324,7 +324,7 @@ int gox_topo_set_zip(gox_topo *t, const double *zi_re, const double *zi_im, cons
 int gox_topo_set_graph(gox_topo *t, int32_t on);
 
 /* Split solves (parts 2, the default, or 1): once the pivot order is fixed,
- * a batch of 4,096+ scenarios with the given start is solved as two halves
+ * a mixed-precision batch of 4,096+ scenarios with the given start is solved as two halves
  * (split at a multiple of 32 scenarios) at the same time, the second by a
  * second instance of the topology on its own stream from a second host
  * thread, started a fraction of an iteration later so that one half's

@@ -1,6 +1,6 @@
 """GPU: split solves (gox_topo_set_split).  A batch of 4,096+ scenarios solved
 as two concurrent halves (the second by a twin instance of the topology on
-its own stream) gives the unsplit results bit for bit: mixed and FP64, with
+its own stream) gives the unsplit results bit for bit: mixed precision, with
 outages, through the host and the device entries."""
 import numpy as np
 import pytest
@@ -11,7 +11,7 @@ from helpers import grid_from_fixture, load_fixture, ybus_from_fixture
 pytestmark = pytest.mark.gpu
 
 
-@pytest.mark.parametrize("prec,outage", [("mixed", False), ("fp64", False), ("mixed", True)])
+@pytest.mark.parametrize("prec,outage", [("mixed", False), ("mixed", True)])
 def test_split_equals_unsplit(gox, prec, outage):
     fx = load_fixture("case118")
     g, yb = grid_from_fixture(fx), ybus_from_fixture(fx)
