@@ -226,7 +226,7 @@ def serve(gox, rates, seconds: float) -> dict:
     out.update({"sweep": sweep, "grids": len(spec),
                 "buses": [int(sizes.min()), int(sizes.max())],
                 "note": "Poisson arrivals of single scenarios over 16 grids (100-50,000 buses), 10 % "
-                        "with an N-1 outage, gox_server_* continuous batching on 8 workers, mixed "
+                        "with an N-1 outage, gox_server_* continuous batching on 16 workers, mixed "
                         "precision, host buffers, warm start from each grid's base case"})
     return out
 

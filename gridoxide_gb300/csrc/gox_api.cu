@@ -2788,7 +2788,7 @@ struct gox_server {
   // topology, so batches of different topologies run concurrently (each
   // solve has its own stream) while one topology's state is used by one
   // worker at a time.
-  static constexpr int kWorkers = 8;
+  static constexpr int kWorkers = 16;
   std::vector<std::thread> workers;
   std::vector<char> busy;  // per topology
 

@@ -365,7 +365,7 @@ const char *gox_version(void);
 
 /* ---- serving --------------------------------------------------------------
  * Continuous batching of single-scenario requests over registered
- * topologies: each of 8 worker threads takes the oldest queued request
+ * topologies: each of 16 worker threads takes the oldest queued request
  * whose topology no other worker is solving and up to max_batch of that
  * topology's requests (arrival order), solves them with gox_batch_solve on
  * its own stream (batches of different topologies overlap on the GPU), and
