@@ -2599,6 +2599,8 @@ void gox_ls_destroy(gox_ls* h) { delete h; }
 // process (per device), so the call never allocates.  Host code must not take
 // its address directly (that is a host-side stand-in); it asks the runtime
 // for the device address once per device and passes that to the kernels.
+// The address is valid for the device's context; a process that resets the
+// device (cudaDeviceReset) must not call this entry afterwards.
 namespace gox {
 static __device__ __align__(256) unsigned char g_static_scratch[GOX_STATIC_SCRATCH_BYTES];
 static void* g_static_addr[256];
@@ -2776,6 +2778,52 @@ struct gox_server {
     for (int64_t v : reserved) r += v;
     return r;
   }
+  // Device bytes a topology's per-batch buffers hold now: its batch and
+  // staging buffers, its split twin's, the linear guess system's and the
+  // FP64 re-solve staging
+  static int64_t held_bytes(gox_topo* t) {
+    int64_t b = (int64_t)(t->batch.bytes() + t->io.bytes());
+    if (t->twin) b += (int64_t)(t->twin->batch.bytes() + t->twin->io.bytes());
+    for (const gox::DevMem* m : {&t->guess.lu, &t->guess.off, &t->guess.rhs, &t->guess.sol,
+                                 &t->guess.sing, &t->guess.piv, &t->guess.gact, &t->guess.err,
+                                 &t->guess.gvm, &t->guess.gva, &t->fb.idx, &t->fb.p, &t->fb.q,
+                                 &t->fb.vm, &t->fb.va, &t->fb.sl, &t->fb.dr, &t->fb.di, &t->fb.ovm,
+                                 &t->fb.ova, &t->fb.it, &t->fb.st, &t->fb.mm, &t->fb.hi})
+      b += (int64_t)m->bytes;
+    return b;
+  }
+  static void release_buffers(gox_topo* t) {
+    t->batch.release();
+    t->io.release();
+    if (t->twin) {
+      t->twin->batch.release();
+      t->twin->io.release();
+    }
+    for (gox::DevMem* m : {&t->guess.lu, &t->guess.off, &t->guess.rhs, &t->guess.sol,
+                           &t->guess.gvm, &t->guess.gva, &t->fb.idx, &t->fb.p, &t->fb.q, &t->fb.vm,
+                           &t->fb.va, &t->fb.sl, &t->fb.dr, &t->fb.di, &t->fb.ovm, &t->fb.ova,
+                           &t->fb.it, &t->fb.st, &t->fb.mm, &t->fb.hi})
+      m->release();
+  }
+  // The batch a worker may admit for topology tp under the budget (0: none
+  // fits now).  Idle topologies' buffers are released first while one group
+  // of 32 scenarios does not fit beside the others'.  Buffers hold whole
+  // groups, so the cap is a multiple of 32 (or max_batch); when no other
+  // topology holds buffers, one group is admitted even if it exceeds the
+  // budget (else the request could never run).
+  int admit_cap(int tp) {
+    if (budget <= 0) return max_batch;
+    const int64_t per = scenario_bytes(topos[tp]);
+    auto others = [&]() { return reserved_total() - reserved[tp]; };
+    for (size_t o = 0; o < topos.size() && others() + 32 * per > budget; o++)
+      if ((int)o != tp && !busy[o] && reserved[o] > 0) {
+        release_buffers(topos[o]);
+        reserved[o] = 0;
+      }
+    const int64_t groups = (budget - others()) / (32 * per);
+    if (groups <= 0) return others() > 0 ? 0 : std::min(max_batch, 32);
+    return (int)std::min<int64_t>(max_batch, groups * 32);
+  }
   // Device bytes one scenario of topology t takes in its batch buffers (an
   // upper bound: FP64 width for the typed arrays)
   static int64_t scenario_bytes(const gox_topo* t) {
@@ -2800,33 +2848,36 @@ struct gox_server {
       gox_topo* t = nullptr;
       {
         std::unique_lock<std::mutex> lk(mu);
-        cv.wait(lk, [&] {
-          if (stop && queue.empty()) return true;
-          for (const auto& r : queue)
-            if (!busy[r->topo]) return true;
-          return false;
-        });
-        if (stop && queue.empty()) return;
-        for (const auto& r : queue)
-          if (!busy[r->topo]) { tp = r->topo; break; }
+        int cap = 0;
+        for (;;) {
+          cv.wait(lk, [&] {
+            if (stop && queue.empty()) return true;
+            for (const auto& r : queue)
+              if (!busy[r->topo]) return true;
+            return false;
+          });
+          if (stop && queue.empty()) return;
+          // topologies in the order of their oldest queued request; the
+          // first whose batch fits the budget now
+          std::vector<char> tried(topos.size(), 0);
+          for (const auto& r : queue) {
+            const int c = r->topo;
+            if (busy[c] || tried[c]) continue;
+            tried[c] = 1;
+            cap = admit_cap(c);
+            if (cap > 0) {
+              tp = c;
+              break;
+            }
+          }
+          if (tp >= 0) break;
+          // nothing fits beside the batches being solved: wait for one of
+          // them to finish (their buffers then become releasable)
+          const int64_t seen = batches;
+          cv.wait(lk, [&] { return stop || batches != seen; });
+        }
         busy[tp] = 1;
         t = topos[tp];
-        int cap = max_batch;
-        if (budget > 0) {
-          // what fits beside the other topologies' buffers; idle ones give
-          // theirs back first when it does not
-          const int64_t per = scenario_bytes(t);
-          auto others = [&]() { return reserved_total() - reserved[tp]; };
-          for (size_t o = 0; o < topos.size() && others() + per > budget; o++)
-            if ((int)o != tp && !busy[o] && reserved[o] > 0) {
-              topos[o]->batch.release();
-              topos[o]->io.release();
-              reserved[o] = 0;
-            }
-          // buffers hold whole groups of 32 scenarios
-          const int64_t groups = (budget - others()) / (32 * per);
-          cap = (int)std::max<int64_t>(1, std::min<int64_t>(max_batch, groups * 32));
-        }
         for (auto it = queue.begin(); it != queue.end() && (int)batch.size() < cap;) {
           if ((*it)->topo == tp) {
             batch.push_back(*it);
@@ -2835,6 +2886,10 @@ struct gox_server {
             ++it;
           }
         }
+        // what this batch's buffers will hold (whole groups), counted until
+        // its solve reports the real size
+        const int64_t groups = ((int64_t)batch.size() + 31) / 32;
+        if (budget > 0) reserved[tp] = std::max(reserved[tp], groups * 32 * scenario_bytes(t));
       }
       const auto t_pick = std::chrono::steady_clock::now();
       solve(t, batch);
@@ -2844,7 +2899,7 @@ struct gox_server {
         for (const auto& r : batch)
           queue_s += std::chrono::duration<double>(t_pick - r->t_submit).count();
         solve_s += std::chrono::duration<double>(t_done - t_pick).count() * (double)batch.size();
-        reserved[tp] = (int64_t)(t->batch.bytes() + t->io.bytes());
+        reserved[tp] = held_bytes(t);
         peak_reserved = std::max(peak_reserved, reserved_total());
         busy[tp] = 0;
         batches++;
@@ -2949,12 +3004,15 @@ int gox_server_submit(gox_server* s, int32_t topo_id, const double* p_spec, cons
     return GOX_E_INVALID;
   return guard_impl([&]() -> int {
     auto r = std::make_shared<gox::ServerReq>();
+    int n = 0;
     {
+      // the topology list may grow (and move) under gox_server_add_topology:
+      // read the bus count while holding the lock that validates the id
       std::lock_guard<std::mutex> lk(s->mu);
       if (topo_id < 0 || topo_id >= (int32_t)s->topos.size()) return GOX_E_INVALID;
       r->topo = topo_id;
+      n = s->topos[topo_id]->n_bus;
     }
-    const int n = s->topos[topo_id]->n_bus;
     r->p.assign(p_spec, p_spec + n);
     r->q.assign(q_spec, q_spec + n);
     r->vm0.assign(vm0, vm0 + n);

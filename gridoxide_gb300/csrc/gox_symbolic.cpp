@@ -2,6 +2,25 @@
 // See gox_symbolic.hpp.  Each routine follows the reference step for step
 // where its output must be identical (orderings, pivot rows, patterns); the
 // file:line each one follows is given at the routine.
+//
+// Provenance and licences.  The ordering and first-factor routines restate
+// SuiteSparse (v7.12.2) closely, because their outputs must equal KLU's bit
+// for bit, so they carry the upstream packages' notices:
+//   * btf_maxtrans, btf_strongcomp, btf_order -- from BTF/Source/btf_*.c:
+//       BTF, Copyright (c) 2004-2022, University of Florida.  All Rights Reserved.
+//       SPDX-License-Identifier: LGPL-2.1+
+//   * clear_w, amd_postorder, amd_eliminate, amd_order -- from
+//     AMD/Source/amd_{order,aat,1,2,postorder,post_tree}.c:
+//       AMD, Copyright (c) 1996-2022, Timothy A. Davis, Patrick R. Amestoy,
+//       and Iain S. Duff.  All Rights Reserved.
+//       SPDX-License-Identifier: BSD-3-clause
+//   * klu_analyze, klu_factor -- from KLU/Source/klu_analyze.c, klu_factor.c,
+//     klu_kernel.c:
+//       KLU, Copyright (c) 2004-2022, University of Florida.  All Rights Reserved.
+//       SPDX-License-Identifier: LGPL-2.1+
+// jac_analyze and build_csc restate the reference's own Rust
+// (src/jacobian.rs, src/klu_native/mod.rs).  libgridoxide_gb300.so therefore
+// contains code derived from LGPL-2.1+ sources (BTF, KLU).
 #include "gox_symbolic.hpp"
 
 #include <algorithm>

@@ -96,8 +96,9 @@ class Gb300LinearSolver:
 
     def factor_and_solve_values_static(self, values, rhs) -> Optional[np.ndarray]:
         """As factor_and_solve_values, allocating no device memory: for callers
-        that cannot allocate at solve time (inside a stream capture, under an
-        allocator that owns all device memory, or in a latency-critical loop).
+        that cannot allocate at solve time (a process whose device memory is
+        held by another allocator's pool, or a control loop with a deadline
+        per Newton step, where cudaMalloc/cudaFree synchronize the device).
         Its scratch is a fixed array inside the library, shared by every call
         (serialize calls; see gox_ls_factor_solve_values_static)."""
         L = _lib.load()

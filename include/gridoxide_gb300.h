@@ -81,21 +81,25 @@ int gox_ls_factor_solve(gox_ls *h, int32_t nnz, const int32_t *rows, const int32
 void gox_ls_destroy(gox_ls *h);
 
 /* No counterpart in the reference.  gox_ls_factor_solve_values for callers
- * that cannot allocate device memory at solve time -- code running while a
- * CUDA stream is being captured (an allocation inside capture is not
- * allowed), processes whose device memory is owned up front by another
- * allocator, or loops that cannot afford an allocation's latency.  The
- * refactor and solve use no device buffer of the handle: their scratch (the
- * factor values, right-hand side, solution and flags) lives in one fixed
- * array compiled into the library, GOX_STATIC_SCRATCH_BYTES per device,
- * held by every process that loads the library until it exits.  Nothing is
- * allocated or freed on the device by this call.
+ * that cannot allocate device memory at solve time: a process whose device
+ * memory was handed up front to another allocator (a framework's caching
+ * pool, a serving process that reserves HBM at start-up), where cudaMalloc
+ * fails or takes memory the pool counted on; and a control loop with a
+ * deadline per Newton step, where cudaMalloc / cudaFree synchronize the
+ * device and take unbounded time.  The refactor and solve use no device
+ * buffer of the handle: their scratch (the factor values, right-hand side,
+ * solution and flags) lives in one fixed array compiled into the library,
+ * GOX_STATIC_SCRATCH_BYTES per device, held by every process that loads the
+ * library until it exits.  Nothing is allocated or freed on the device by
+ * this call.
  *   - Limit: 32 * 8 * (LU slots + off-diagonal entries + 2 n) plus
  *     12 * nnz + 16 * n bytes must fit in GOX_STATIC_SCRATCH_BYTES
  *     (GOX_E_TOO_LARGE otherwise; about 260k factor entries).
  *   - The first call on a device looks up the array's device address
- *     (cudaGetSymbolAddress) with that device current; make that first call
- *     before any stream capture.
+ *     (cudaGetSymbolAddress) with that device current and keeps it for the
+ *     process; make that first call before any stream capture.  The address
+ *     belongs to the device's CUDA context: after cudaDeviceReset the
+ *     process must not call this entry again.
  *   - All calls share the one array and leave the last call's values in
  *     it; calls that overlap on the GPU (other host threads, other handles)
  *     overwrite each other's scratch: serialize them.

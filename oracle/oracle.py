@@ -19,7 +19,10 @@ import numpy as np
 HERE = os.path.dirname(os.path.abspath(__file__))
 LIB = os.path.join(HERE, "liboracle.so")
 REF_LIB = os.path.join(HERE, "_ref", "libklu_ref.so")
-REF_SRC = "/root/reference/vendor/suitesparse"
+# The reference checkout the recipe compiles from (its vendored SuiteSparse):
+# $GRIDOXIDE_REFERENCE, else the read-only mount of this build environment.
+REF_ROOT = os.environ.get("GRIDOXIDE_REFERENCE", "/root/reference")
+REF_SRC = os.path.join(REF_ROOT, "vendor", "suitesparse")
 
 _i32p = C.POINTER(C.c_int32)
 _f64p = C.POINTER(C.c_double)
@@ -30,7 +33,10 @@ def build(ref: bool | None = None) -> None:
     """make -C oracle [ref]: the reference build only where its sources exist."""
     if ref is None:
         ref = os.path.isdir(REF_SRC)
-    subprocess.run(["make", "-s", "-C", HERE] + (["ref"] if ref else []), check=True)
+    cmd = ["make", "-s", "-C", HERE]
+    if ref:
+        cmd += ["ref", f"REF={REF_SRC}"]
+    subprocess.run(cmd, check=True)
 
 
 def _p(a, t):

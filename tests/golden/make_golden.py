@@ -29,7 +29,7 @@ sys.path.insert(0, os.path.join(ROOT, "oracle"))
 from gridoxide_gb300 import grids as G  # noqa: E402
 import oracle as O  # noqa: E402
 
-REF_NETWORK = "/root/reference/tests/data/network.json"
+REF_NETWORK = os.path.join(O.REF_ROOT, "tests", "data", "network.json")
 
 
 def nr_with_ref_klu(yb, bus_type, jac, Ap, Ai, order, p_spec, q_spec, vm0, va0, tol, max_iter):

@@ -25,7 +25,9 @@ def _grids():
     return [(g1, y1), (g2, G.build_ybus(g2)), (g3, G.build_ybus(g3))]
 
 
-@pytest.mark.parametrize("precision,budget", [(0, 0), (1, 0), (1, 16 << 20)])
+# 2 MB is below one group of 32 scenarios of the two larger grids: such a
+# batch waits until no other topology holds buffers, then runs alone
+@pytest.mark.parametrize("precision,budget", [(0, 0), (1, 0), (1, 16 << 20), (1, 2 << 20)])
 def test_server_reports_equal_direct_solves(gox, precision, budget):
     grids = _grids()
     topos = [gox.Topology(yb, g.bus_type) for g, yb in grids]
@@ -59,7 +61,7 @@ def test_server_reports_equal_direct_solves(gox, precision, budget):
     st = srv.stats()
     srv.close()
     assert st["solved"] == len(reqs) and st["queued"] == 0 and st["batches"] >= 3
-    if budget:  # admitted batches kept the topologies' buffers within the budget
+    if budget >= 16 << 20:  # admitted batches kept the topologies' buffers within the budget
         assert 0 < st["peak_reserved_bytes"] <= budget
     lat = np.array([r["latency_s"] for r in reports])
     assert np.all(lat > 0)

@@ -1,8 +1,10 @@
 """The LinearSolver refactor + solve without device allocation.
 
-Some callers cannot allocate device memory when they solve: code running
-while a CUDA stream is being captured, processes whose device memory is all
-owned by another allocator, or latency-critical loops.  For them
+Some callers cannot allocate device memory when they solve: a process
+whose device memory another allocator's pool already holds (cudaMalloc
+would fail or take memory the pool counted on), or a control loop with a
+deadline per Newton step (cudaMalloc and cudaFree synchronize the device
+and take unbounded time).  For them
 gox_ls_factor_solve_values_static keeps its scratch in a fixed array inside
 the library.  Its results must equal gox_ls_factor_solve_values' on the same
 handle, call after call (the array keeps the previous call's contents, so
