@@ -102,12 +102,93 @@ class ClockSampler:
                 "samples": len(sm)}
 
 
-def make_inputs():
+def make_inputs(world: int = 1, rank: int = 0):
+    """The workload grid and this rank's scenarios.  With `world` ranks the
+    job is `world` x the single-GPU batch (weak scaling), drawn as one
+    global batch and cut into contiguous shards (replicas.shard_bounds)."""
     from gridoxide_gb300 import grids as G
+    from gridoxide_gb300 import replicas
     g = G.config_grid(WORKLOAD["grid"])
     yb = G.build_ybus(g)
-    p, q = G.load_scenarios(g, WORKLOAD["scenarios"], WORKLOAD["sigma"], WORKLOAD["seed"])
-    return g, yb, p, q
+    total = WORKLOAD["scenarios"] * world
+    p, q = G.load_scenarios(g, total, WORKLOAD["sigma"], WORKLOAD["seed"])
+    if world == 1:
+        return g, yb, p, q
+    lo, hi = replicas.shard_bounds(total, world, rank)
+    make_inputs.global_batch = (p, q)
+    return g, yb, p[lo:hi].copy(), q[lo:hi].copy()
+
+
+def workload_config(world: int = 1) -> dict:
+    """The `config` of both arms' JSON lines: the workload and the two value
+    scales of the generated grid (its loads and resistances; the pattern is
+    the literal one)."""
+    from gridoxide_gb300 import grids as G
+    n, npv, nbr, gseed, ls, rs = G.CONFIGS[WORKLOAD["grid"]]
+    return {"workload": f"{WORKLOAD['grid']} x {WORKLOAD['scenarios']} scenarios per GPU, "
+                        f"lognormal(0,{WORKLOAD['sigma']}) loads, flat start, tol "
+                        f"{WORKLOAD['tol']:g} pu, mixed precision (FP64 timed beside it)",
+            "buses": n, "pv": npv, "branches": nbr, "grid_seed": gseed,
+            "load_scale": ls, "r_scale": rs,
+            "l2": "inputs > L2 and 256 MB flush per step",
+            "parallelism": f"replicas x{world} (scenario shards)", **WORKLOAD}
+
+
+def physical_cores() -> int:
+    """Physical cores (not SMT siblings), counted as the reference's
+    scripts/bench/bench_batch.py:37-59 does, from the sysfs topology first
+    (Arm hosts list no `core id` in /proc/cpuinfo)."""
+    ids = set()
+    base = "/sys/devices/system/cpu"
+    try:
+        for d in os.listdir(base):
+            if not (d.startswith("cpu") and d[3:].isdigit()):
+                continue
+            t = os.path.join(base, d, "topology")
+            with open(os.path.join(t, "core_id")) as fh:
+                core = fh.read().strip()
+            with open(os.path.join(t, "physical_package_id")) as fh:
+                pkg = fh.read().strip()
+            ids.add((pkg, core))
+    except OSError:
+        ids = set()
+    if ids:
+        return len(ids)
+    try:
+        core, pkg = None, None
+        with open("/proc/cpuinfo") as fh:
+            for line in fh:
+                if line.startswith("core id"):
+                    core = line.split(":")[1].strip()
+                elif line.startswith("physical id"):
+                    pkg = line.split(":")[1].strip()
+                elif not line.strip() and core is not None:
+                    ids.add((pkg, core))
+                    core, pkg = None, None
+        if core is not None:
+            ids.add((pkg, core))
+    except OSError:
+        pass
+    return len(ids) or (os.cpu_count() or 1)
+
+
+def cpu_model() -> str:
+    try:
+        out = subprocess.run(["lscpu"], capture_output=True, text=True, timeout=10).stdout
+        for line in out.splitlines():
+            if line.startswith("Model name:"):
+                return line.split(":", 1)[1].strip()
+    except Exception:
+        pass
+    try:
+        with open("/proc/cpuinfo") as fh:
+            for line in fh:
+                if line.startswith("model name"):
+                    return line.split(":", 1)[1].strip()
+    except OSError:
+        pass
+    import platform
+    return platform.processor() or platform.machine()
 
 
 def algorithmic_bytes(info: dict, n_bus: int, w: int) -> dict:
@@ -410,43 +491,80 @@ _ORACLE_TOPO = {}
 
 
 def _oracle_topology(g, yb):
-    """The oracle port's topology for the workload grid (built once)."""
+    """The oracle port's topology for the workload grid (built once).  Its
+    symbolic ordering is the reference's own klu_analyze output for this
+    grid, committed as a fixture (tests/golden/); nothing of the product
+    library is loaded on this path."""
     key = id(yb)
     if key not in _ORACLE_TOPO:
         sys.path.insert(0, os.path.join(ROOT, "oracle"))
         import oracle as O
-        from gridoxide_gb300 import solver as S
         O.build(ref=False) if not os.path.exists(O.LIB) else None
-        jac = O.Jacobian(yb, g.bus_type)
-        Ap, Ai, _ = jac.csc_pattern()
-        _ORACLE_TOPO[key] = O.Topology(yb, g.bus_type, *S.analyze(jac.n_u, Ap, Ai))
+        order = O.fixture_ordering(WORKLOAD["grid"], yb, g.bus_type)
+        _ORACLE_TOPO[key] = O.Topology(yb, g.bus_type, *order)
     return _ORACLE_TOPO[key]
 
 
 def cpu_pass(g, yb, p, q, threads: int):
     """One pass of the oracle port (C restatement of BatchSolver + KLU, one
     persistent solver per worker thread) over every scenario of p, q;
-    returns (solves/s, seconds)."""
+    returns (solves/s, seconds, reports)."""
     topo = _oracle_topology(g, yb)
     t0 = time.perf_counter()
-    topo.batch_solve(p, q, g.vm, g.va, tol=WORKLOAD["tol"], max_iter=WORKLOAD["max_iter"],
-                     threads=threads)
+    res = topo.batch_solve(p, q, g.vm, g.va, tol=WORKLOAD["tol"], max_iter=WORKLOAD["max_iter"],
+                           threads=threads)
     dt = time.perf_counter() - t0
-    return p.shape[0] / dt, dt
+    return p.shape[0] / dt, dt, res
+
+
+def thread_sweep(g, yb, p, q, per_thread: int = 32, repeats: int = 3) -> dict:
+    """The reference's scripts/bench/bench_batch.py method on the oracle
+    port: thread counts 1, 2, 4, ... up to the logical cores, each on a
+    sample of `per_thread` x threads scenarios (bounded time): one warm-up
+    call, then the minimum of `repeats` timed calls; every thread count's
+    voltages must equal the 1-thread run's on the shared scenarios."""
+    logical = os.cpu_count() or 1
+    counts = [t for t in (1, 2, 4, 8, 16, 32, 64, 128) if t <= logical]
+    if logical not in counts:
+        counts.append(logical)
+    out, first = {}, None
+    for t in counts:
+        n = min(p.shape[0], per_thread * t)
+        _, _, res = cpu_pass(g, yb, p[:n], q[:n], t)
+        m = per_thread if first is None else min(first.shape[0], n)
+        if first is None:
+            first = res["vm"][:m].copy()
+        else:
+            worst = float(np.max(np.abs(res["vm"][:m] - first[:m])))
+            assert worst < 1e-12, f"threads={t} disagrees with threads=1 by {worst:.3e}"
+        best = min(cpu_pass(g, yb, p[:n], q[:n], t)[1] for _ in range(repeats))
+        out[str(t)] = round(n / best, 1)
+    return out
 
 
 def cpu_baseline(g, yb, p, q, threads: int, min_seconds: float = 10.0):
     """The oracle port on the host's cores: passes over the whole workload
     until at least `min_seconds` have run (after one warm-up pass over a
-    slice).  Returns (solves/s, seconds, passes)."""
+    slice).  Returns (solves/s, seconds, passes, reports of the last pass)."""
     cpu_pass(g, yb, p[:threads * 4], q[:threads * 4], threads)  # warm-up
-    n, t, passes = 0, 0.0, 0
+    n, t, passes, res = 0, 0.0, 0, None
     while t < min_seconds:
-        v, dt = cpu_pass(g, yb, p, q, threads)
+        v, dt, res = cpu_pass(g, yb, p, q, threads)
         n += p.shape[0]
         t += dt
         passes += 1
-    return n / t, t, passes
+    return n / t, t, passes, res
+
+
+def error_vs_oracle(vm, va, iters, status, ref) -> dict:
+    """max |dV| (pu) and |dtheta| (rad) of a GPU result against the oracle's
+    reports of the same scenarios, and how many iteration counts / statuses
+    agree."""
+    return {"max_abs_dvm": float(np.max(np.abs(vm - ref["vm"]))),
+            "max_abs_dva": float(np.max(np.abs(va - ref["va"]))),
+            "iterations_equal": int(np.sum(iters == ref["iters"])),
+            "status_equal": int(np.sum(status == ref["status"])),
+            "scenarios": int(vm.shape[0])}
 
 
 def run_reference_arm(args):
@@ -461,7 +579,7 @@ def run_reference_arm(args):
         cpu_pass(g, yb, p[:threads * 4], q[:threads * 4], threads)
     vals, secs = [], []
     for _ in range(args.steps):
-        v, dt = cpu_pass(g, yb, p, q, threads)
+        v, dt, _ = cpu_pass(g, yb, p, q, threads)
         vals.append(v)
         secs.append(dt)
     value = float(np.median(vals))
@@ -471,10 +589,12 @@ def run_reference_arm(args):
         "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": round(1000.0 * float(np.median(secs)), 3), "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-        "config": {"workload": f"{WORKLOAD['grid']} x {B} scenarios, one pass per step", **WORKLOAD},
+        "config": workload_config(args.gpus),
         "cpu_baseline": {"value": round(value, 1), "unit": "solves/s", "cores": threads,
-                         "kind": "port",
-                         "sample": f"the whole {B}-scenario workload per step, {threads} threads"},
+                         "kind": "port", "cpu": cpu_model(), "physical_cores": physical_cores(),
+                         "ordering": "the reference's compiled klu_analyze (committed fixture)",
+                         "sample": f"the whole {B}-scenario workload per step (one GPU's share), "
+                                   f"{threads} threads"},
         "e2e": {"value": round(value, 1), "unit": "solves/s", "h2d_bytes_per_step": 0,
                 "d2h_bytes_per_step": 0},
     }
@@ -519,7 +639,7 @@ def main():
     dev = torch.device("cuda", local)
     gox.build.build()
 
-    g, yb, p, q = make_inputs()
+    g, yb, p, q = make_inputs(world, rank)
     B, N = p.shape
     topo = gox.Topology(yb, g.bus_type)
     stream = torch.cuda.Stream(device=dev)
@@ -592,6 +712,8 @@ def main():
     st_mx = ost.cpu().numpy().copy()
     mm_mx = omm.cpu().numpy().copy()
     it_mx = oit.cpu().numpy().copy()
+    vm_mx = ovm.cpu().numpy().copy()
+    va_mx = ova.cpu().numpy().copy()
     # the same steps again with CUDA events around every phase (host-driven
     # loop): the per-kernel times and the roofline
     ms_k, kern_mx, _, iters_k, _ = timed(gox.GOX_PRECISION_MIXED, args.steps, kernel_timing=True)
@@ -604,12 +726,12 @@ def main():
     ms_64, kern_64, launches_64, iters_64, _ = timed(gox.GOX_PRECISION_FP64,
                                                      max(3, args.steps // 2))
     it_64 = oit.cpu().numpy().copy()
+    st_64 = ost.cpu().numpy().copy()
+    vm_64 = ovm.cpu().numpy().copy()
+    va_64 = ova.cpu().numpy().copy()
 
-    total_ms = float(ms_mx.sum())
-    if world > 1:
-        t = torch.tensor([total_ms], device=dev)
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        total_ms = float(t.item())
+    from gridoxide_gb300 import replicas
+    total_ms = replicas.max_over_ranks(float(ms_mx.sum()))
     value = world * B * args.steps / (total_ms / 1000.0)
     fp64_value = B * len(ms_64) / (ms_64.sum() / 1000.0)
 
@@ -626,12 +748,25 @@ def main():
                               _pinned((B,), torch.float64))
     e2e_ms = []
     for k in range(max(3, args.steps // 2)):
+        if world > 1:
+            # the replicas path: every rank solves its shard of the global
+            # batch and the reports are gathered on the host
+            pg, qg = make_inputs.global_batch
+            torch.distributed.barrier()
+            t0 = time.perf_counter()
+            rep = replicas.solve_replicas(
+                replicas.topology_solver(topo, gox.GOX_PRECISION_MIXED), pg, qg, g.vm, g.va,
+                tol=WORKLOAD["tol"], max_iter=WORKLOAD["max_iter"])
+            e2e_ms.append(replicas.max_over_ranks(1000.0 * (time.perf_counter() - t0)))
+            assert int(np.sum(rep["status"] == 0)) == world * B
+            continue
         t0 = time.perf_counter()
         topo.solve(hp, hq, g.vm, g.va, tol=WORKLOAD["tol"], max_iter=WORKLOAD["max_iter"],
                    precision=gox.GOX_PRECISION_MIXED, out=res_buf)
         e2e_ms.append(1000.0 * (time.perf_counter() - t0))
-    assert int(np.sum(res_buf.status == 0)) == B
-    e2e_value = B / (np.median(e2e_ms) / 1000.0)
+    if world == 1:
+        assert int(np.sum(res_buf.status == 0)) == B
+    e2e_value = world * B / (np.median(e2e_ms) / 1000.0)
     h2d = 2 * B * N * 8 + 2 * N * 8
     d2h = 2 * B * N * 8 + B * (4 + 4 + 8)
 
@@ -669,9 +804,7 @@ def main():
         "ms_per_step": round(float(np.mean(ms_mx)), 4), "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f32 LU/solve + f64 mismatch",
         "data": "synthetic",
-        "config": {"workload": "case2000 x 4096 scenarios, lognormal(0,0.15) loads, flat start, "
-                               "mixed precision", "l2": "inputs > L2 and 256 MB flush per step",
-                   "parallelism": f"replicas x{world}", **WORKLOAD},
+        "config": workload_config(world),
         "latency_ms": {"p50": round(float(np.percentile(ms_mx, 50)), 4),
                        "p99": round(float(np.percentile(ms_mx, 99)), 4)},
         "fp64": {"value": round(fp64_value, 1), "unit": "solves/s",
@@ -703,11 +836,23 @@ def main():
         line["qlim_case2000"] = qlim_case2000(gox, args.many_rounds)
     if rank == 0 and not args.no_cpu_baseline:
         threads = os.cpu_count() or 1
-        v, dt, passes = cpu_baseline(g, yb, p, q, threads)
+        v, dt, passes, ref = cpu_baseline(g, yb, p, q, threads)
         line["cpu_baseline"] = {"value": round(v, 1), "unit": "solves/s", "cores": threads,
-                                "kind": "port",
+                                "kind": "port", "cpu": cpu_model(),
+                                "physical_cores": physical_cores(),
+                                "threads_sweep_solves_per_s": thread_sweep(g, yb, p, q),
+                                "ordering": "the reference's compiled klu_analyze (committed "
+                                            "fixture)",
                                 "sample": f"{passes} passes over the {p.shape[0]}-scenario "
                                           f"workload ({dt:.1f} s)"}
+        # every result states its error against the FP64 oracle: the timed
+        # steps' results (the last step of each precision) against the
+        # oracle's reports of the same scenarios
+        line["err_vs_oracle"] = {
+            "fp64": error_vs_oracle(vm_64, va_64, it_64, st_64, ref),
+            "mixed": error_vs_oracle(vm_mx, va_mx, it_mx, st_mx, ref),
+            "note": "max over all scenarios of the timed configuration; the FP64 path must match "
+                    "the oracle's iteration counts and |V|, theta within 1e-9"}
     if rank == 0:
         print(json.dumps(line), flush=True)
     if world > 1:

@@ -282,6 +282,42 @@ class Topology:
 
 
 # ---------------------------------------------------------------------------
+# the reference's orderings as committed fixtures (usable where the
+# reference's KLU cannot be built)
+
+GOLDEN = os.path.join(os.path.dirname(HERE), "tests", "golden")
+
+
+def pattern_fingerprint(yb, bus_type) -> str:
+    """sha256 of the Y-bus pattern and bus types: all the symbolic ordering
+    of the Jacobian depends on."""
+    import hashlib
+    h = hashlib.sha256()
+    for a in (yb.indptr, yb.indices, bus_type):
+        h.update(np.ascontiguousarray(a, dtype="<i4").tobytes())
+    return h.hexdigest()
+
+
+def fixture_ordering(name: str, yb, bus_type):
+    """(P, Q, R) of the reference's compiled klu_analyze for grid `name`, as
+    tests/golden/make_golden.py stored it (<name>.npz or <name>_order.npz).
+    Raises if the fixture belongs to another Y-bus pattern or bus types."""
+    path = os.path.join(GOLDEN, f"{name}.npz")
+    if not os.path.exists(path):
+        path = os.path.join(GOLDEN, f"{name}_order.npz")
+    with np.load(path) as z:
+        if "pattern_sha256" in z.files:
+            same = str(z["pattern_sha256"]) == pattern_fingerprint(yb, bus_type)
+        else:
+            same = (np.array_equal(z["y_indptr"], yb.indptr)
+                    and np.array_equal(z["y_indices"], yb.indices)
+                    and np.array_equal(z["bus_type"], bus_type))
+        if not same:
+            raise ValueError(f"{path}: the fixture's ordering belongs to another pattern")
+        return z["ref_P"].copy(), z["ref_Q"].copy(), z["ref_R"].copy()
+
+
+# ---------------------------------------------------------------------------
 # the reference's compiled KLU (only where it was built)
 
 _ref = None

@@ -100,6 +100,19 @@ def grid_fixture(name: str, n_scen: int, sigma: float, seed: int):
     print(name, "iters", res["iters"], "status", res["status"])
 
 
+def ordering_fixture(name: str):
+    """Only the reference's klu_analyze ordering of a grid too large to
+    store whole, with a fingerprint of the pattern it belongs to."""
+    g = G.config_grid(name)
+    yb = G.build_ybus(g)
+    jac = O.Jacobian(yb, g.bus_type)
+    Ap, Ai, _ = jac.csc_pattern()
+    P, Q, R = O.ref_analyze(jac.n_u, Ap, Ai)
+    np.savez_compressed(os.path.join(HERE, f"{name}_order.npz"), ref_P=P, ref_Q=Q, ref_R=R,
+                        pattern_sha256=O.pattern_fingerprint(yb, g.bus_type))
+    print(name, "ordering: blocks", len(R) - 1)
+
+
 def network3_fixture():
     with open(REF_NETWORK) as fh:
         net = json.load(fh)
@@ -122,3 +135,4 @@ if __name__ == "__main__":
     network3_fixture()
     grid_fixture("case118", 8, 0.15, 101)
     grid_fixture("case2000", 4, 0.15, 102)
+    ordering_fixture("case10000")

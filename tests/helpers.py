@@ -28,10 +28,24 @@ def ybus_from_fixture(fx: dict) -> G.YBus:
                   re=fx["y_re"], im=fx["y_im"])
 
 
+def reference_ordering(O, yb, bus_type):
+    """The reference's compiled klu_analyze ordering of one of the workload
+    grids (committed fixture), or None for other grids."""
+    for name in ("case118", "case2000", "case10000"):
+        try:
+            return O.fixture_ordering(name, yb, bus_type)
+        except ValueError:
+            continue
+    return None
+
+
 def oracle_topology(O, yb, bus_type, ordering=None):
-    """Oracle topology.  The symbolic ordering is an input of the oracle;
-    by default it is taken from the library's klu_analyze, whose output the
-    CPU tests pin bit for bit against the reference's compiled KLU."""
+    """Oracle topology.  The symbolic ordering is an input of the oracle: the
+    reference's own (a committed fixture) for the workload grids, else the
+    library's klu_analyze, whose output the CPU tests pin bit for bit
+    against the reference's compiled KLU."""
+    if ordering is None:
+        ordering = reference_ordering(O, yb, bus_type)
     if ordering is None:
         from gridoxide_gb300 import solver as S
         jac = O.Jacobian(yb, bus_type)
