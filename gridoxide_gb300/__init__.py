@@ -13,7 +13,7 @@ The GPU engine lives in ``libgridoxide_gb300.so`` (C ABI:
 """
 from . import build, grids, pgm, replicas  # noqa: F401
 from ._lib import (GOX_CONVERGED, GOX_MAX_ITERATIONS, GOX_PRECISION_FP64,  # noqa: F401
-                   GOX_PRECISION_MIXED, GOX_SINGULAR_SCENARIO, GoxError)
+                   GOX_E_DEVICE_WAIT, GOX_PRECISION_MIXED, GOX_SINGULAR_SCENARIO, GoxError)
 from .solver import (BatchError, BatchResult, BatchSolver, Buses, BusOverride,  # noqa: F401
                      Gb300LinearSolver, JacobianBackend, PowerFlowReport, Scenario, Server,
                      SolveStatus, Topology, analyze, factor_host, uniform_load_scaling)

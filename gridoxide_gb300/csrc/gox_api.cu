@@ -2334,6 +2334,125 @@ int gox_topo_emulate_step(const gox_topo* t, const double* jac_vals, const doubl
   });
 }
 
+}  // extern "C"
+
+// One mismatch, fill and refactor of the batch path at given voltages, with
+// the Jacobian image (after the fill) and the factor (after the refactor)
+// read back: the per-entry view the parity tests compare with the oracle.
+template <typename T>
+static void factor_values_run(gox_topo* t, const BatchDev& D, int B, cudaStream_t st,
+                              double* jac_vals, double* lu_vals) {
+  const SchedDev& S = t->dsched.d;
+  const Schedule& sc = t->sc;
+  const size_t nl = (size_t)D.G * S.n_slots * 32, no = (size_t)D.G * S.n_off * 32;
+  std::vector<T> img(nl), offv(no);
+  GOX_CK(cudaMemsetAsync(D.nactive, 0, sizeof(int32_t), st));
+  Iter<T>::mismatch(S, D, 0, 0, false, st);
+  Iter<T>::fill(S, D, false, st);
+  if (jac_vals) {
+    GOX_CK(cudaMemcpyAsync(img.data(), D.lu, nl * sizeof(T), cudaMemcpyDeviceToHost, st));
+    GOX_CK(cudaMemcpyAsync(offv.data(), D.off, no * sizeof(T), cudaMemcpyDeviceToHost, st));
+    GOX_CK(cudaStreamSynchronize(st));
+    // emission entry e -> CSC slot -> A entry (consumption order) -> LU slot
+    // or off-diagonal entry of the image
+    std::vector<int32_t> a_of_csc(t->csc.nnz(), -1), slot_of_a(sc.n_a, -1);
+    for (int a = 0; a < sc.n_a; a++) a_of_csc[sc.a_csc[a]] = a;
+    for (int x = 0; x < sc.n_slots; x++)
+      if (sc.slot_a[x] >= 0) slot_of_a[sc.slot_a[x]] = x;
+    const int nj = t->jac.nnz();
+    for (int e = 0; e < nj; e++) {
+      const int a = a_of_csc[t->csc.slot_of[e]];
+      const int x = slot_of_a[a];
+      for (int sn = 0; sn < B; sn++) {
+        const int g = sn / 32, l = sn % 32;
+        const T v = sc.a_dst[a] >= 0 ? img[((size_t)g * S.n_slots + x) * 32 + l]
+                                     : offv[((size_t)g * S.n_off + (-sc.a_dst[a] - 1)) * 32 + l];
+        jac_vals[(size_t)sn * nj + e] = (double)v;
+      }
+    }
+  }
+  Iter<T>::refactor(t->dsched, D, st);
+  GOX_CK(cudaGetLastError());
+  if (lu_vals) {
+    GOX_CK(cudaMemcpyAsync(img.data(), D.lu, nl * sizeof(T), cudaMemcpyDeviceToHost, st));
+    GOX_CK(cudaStreamSynchronize(st));
+    for (int sn = 0; sn < B; sn++) {
+      const int g = sn / 32, l = sn % 32;
+      for (int x = 0; x < S.n_slots; x++)
+        lu_vals[(size_t)sn * S.n_slots + x] = (double)img[((size_t)g * S.n_slots + x) * 32 + l];
+    }
+  }
+  GOX_CK(cudaStreamSynchronize(st));
+}
+
+extern "C" {
+
+int gox_topo_factor_values(gox_topo* t, int32_t B, const double* p_spec, const double* q_spec,
+                           const double* vm, const double* va, int32_t precision,
+                           double* jac_vals, double* lu_vals) {
+  if (!t || B <= 0 || !p_spec || !q_spec || !vm || !va || !t->factored) return GOX_E_INVALID;
+  if (precision != GOX_PRECISION_FP64 && precision != GOX_PRECISION_MIXED) return GOX_E_INVALID;
+  if (int r = require_device()) return r;
+  return guard_impl([&]() -> int {
+    cudaStream_t st = thread_stream();
+    AllocStreamScope alloc_scope(st);
+    const int n = t->n_bus, G = (B + 31) / 32;
+    if (!t->uploaded) {
+      t->dsched.load(t->sc, t->yp, t->yi, t->yre, t->yim);
+      t->dsched.load_streams(t->s32, t->s64);
+      t->uploaded = true;
+    }
+    t->dsched.d.zip = t->zip.empty() ? nullptr : t->dzip.as<double>();
+    const SchedDev& S = t->dsched.d;
+    DevBatch& DB = t->batch;
+    DB.ensure(S, G, precision, 1, false);
+    // tol 0: no scenario counts as converged, so every group is filled and
+    // refactored
+    BatchDev D = DB.view(false, false, 0.0, 0.0);
+    IoStage& io = t->io;
+    const size_t bn = (size_t)B * n;
+    io.p.ensure(bn * 8); io.q.ensure(bn * 8); io.vm.ensure(bn * 8); io.va.ensure(bn * 8);
+    GOX_CK(cudaMemcpyAsync(io.p.p, p_spec, bn * 8, cudaMemcpyHostToDevice, st));
+    GOX_CK(cudaMemcpyAsync(io.q.p, q_spec, bn * 8, cudaMemcpyHostToDevice, st));
+    GOX_CK(cudaMemcpyAsync(io.vm.p, vm, bn * 8, cudaMemcpyHostToDevice, st));
+    GOX_CK(cudaMemcpyAsync(io.va.p, va, bn * 8, cudaMemcpyHostToDevice, st));
+    const size_t tot = (size_t)G * n * 32;
+    k_scatter_rows<<<grid1d(tot), 256, 0, st>>>(io.p.as<double>(), B, n, n, D.psp, G);
+    k_scatter_rows<<<grid1d(tot), 256, 0, st>>>(io.q.as<double>(), B, n, n, D.qsp, G);
+    k_scatter_rows<<<grid1d(tot), 256, 0, st>>>(io.vm.as<double>(), B, n, n, D.vm, G);
+    k_scatter_rows<<<grid1d(tot), 256, 0, st>>>(io.va.as<double>(), B, n, n, D.va, G);
+    k_init_scen<<<(G * 32 + 255) / 256, 256, 0, st>>>(B, G, D.status, D.iters, D.sing,
+                                                       D.piv_flag, D.maxmis, D.maxacc);
+    GOX_CK(cudaMemsetAsync(DB.err.p, 0, 16, st));
+    if (precision == GOX_PRECISION_FP64) factor_values_run<double>(t, D, B, st, jac_vals, lu_vals);
+    else factor_values_run<float>(t, D, B, st, jac_vals, lu_vals);
+    int32_t herr[2] = {0, 0};
+    GOX_CK(cudaMemcpyAsync(herr, DB.err.p, 8, cudaMemcpyDeviceToHost, st));
+    GOX_CK(cudaStreamSynchronize(st));
+    return herr[1] ? GOX_E_DEVICE_WAIT : GOX_OK;
+  });
+}
+
+int gox_topo_stream_word(gox_topo* t, int32_t precision, int32_t warp, int32_t index,
+                         int32_t value, int32_t* old_value) {
+  if (!t || !t->factored || !t->uploaded) return GOX_E_INVALID;
+  if (precision != GOX_PRECISION_FP64 && precision != GOX_PRECISION_MIXED) return GOX_E_INVALID;
+  const Stream& s = precision == GOX_PRECISION_MIXED ? t->s32 : t->s64;
+  if (warp < 0 || warp >= s.plan.nw || index < 0 ||
+      (int64_t)index >= (int64_t)s.nchunks[warp] * s.plan.chunk_words)
+    return GOX_E_INVALID;
+  return guard_impl([&]() -> int {
+    const int i = precision == GOX_PRECISION_MIXED ? 0 : 1;
+    int32_t* w = t->dsched.sw[i].as<int32_t>() + (size_t)s.chunk0[warp] * s.plan.chunk_words + index;
+    int32_t old = 0;
+    GOX_CK(cudaDeviceSynchronize());
+    GOX_CK(cudaMemcpy(&old, w, 4, cudaMemcpyDeviceToHost));
+    GOX_CK(cudaMemcpy(w, &value, 4, cudaMemcpyHostToDevice));
+    if (old_value) *old_value = old;
+    return GOX_OK;
+  });
+}
+
 int gox_topo_info(const gox_topo* t, int64_t* info) {
   if (!t || !info || !t->factored) return GOX_E_INVALID;
   const Schedule& sc = t->sc;

@@ -875,8 +875,13 @@ __global__ void __launch_bounds__(sizeof(T) == 4 ? 32 * kMaxRefactorWarps : 256,
     bulk_load(cbuf, gw, (unsigned)CW * 4u, &mbar[warp][0]);
     if (nch > 1) bulk_load(cbuf + CW, gw + CW, (unsigned)CW * 4u, &mbar[warp][1]);
   }
+  // bulk copies issued into / completions waited for, per chunk buffer (warp
+  // uniform): a warp that stops early waits for the copies still in flight
+  // before the CTA can exit
+  int issued0 = 1, issued1 = nch > 1 ? 1 : 0, waited0 = 0, waited1 = 0;
   unsigned par0 = 0u, par1 = 0u;
   bool ok = mbar_wait(&mbar[warp][0], par0);
+  if (ok) waited0++;
   par0 ^= 1u;
   int chunk = 0, buf = 0, pc = 0, bars = 0;
   const int32_t* cb = cbuf;
@@ -987,9 +992,13 @@ __global__ void __launch_bounds__(sizeof(T) == 4 ? 32 * kMaxRefactorWarps : 256,
           break;
         case CMD_NEXT:
           __syncwarp();
-          if (lane == 0 && chunk + 2 < nch)
-            bulk_load(cbuf + (size_t)buf * CW, gw + (size_t)(chunk + 2) * CW, (unsigned)CW * 4u,
-                      &mbar[warp][buf]);
+          if (chunk + 2 < nch) {
+            if (lane == 0)
+              bulk_load(cbuf + (size_t)buf * CW, gw + (size_t)(chunk + 2) * CW, (unsigned)CW * 4u,
+                        &mbar[warp][buf]);
+            if (buf == 0) issued0++;
+            else issued1++;
+          }
           chunk++;
           buf ^= 1;
           if (chunk >= nch) {
@@ -998,9 +1007,11 @@ __global__ void __launch_bounds__(sizeof(T) == 4 ? 32 * kMaxRefactorWarps : 256,
           }
           if (buf == 0) {
             ok = mbar_wait(&mbar[warp][0], par0);
+            if (ok) waited0++;
             par0 ^= 1u;
           } else {
             ok = mbar_wait(&mbar[warp][1], par1);
+            if (ok) waited1++;
             par1 ^= 1u;
           }
           cb = cbuf + (size_t)buf * CW;
@@ -1018,6 +1029,12 @@ done:
   if (!ok) {
     if (lane == 0) atomicExch(&timed_out, 1);
     asm volatile("cp.async.wait_all;\n" ::: "memory");
+    // stream chunks still being copied into this warp's buffers: wait for
+    // them (each wait bounded) so no copy lands after the CTA has exited
+    for (unsigned pr = (unsigned)waited0 & 1u; waited0 < issued0; waited0++, pr ^= 1u)
+      if (!mbar_wait(&mbar[warp][0], pr)) break;
+    for (unsigned pr = (unsigned)waited1 & 1u; waited1 < issued1; waited1++, pr ^= 1u)
+      if (!mbar_wait(&mbar[warp][1], pr)) break;
     for (; bars < P.n_bars; bars++) __syncthreads();
   }
   if (bad) atomicOr(&flags[0][lane], 1);

@@ -348,6 +348,34 @@ class Topology:
         check(rc, "gox_topo_emulate_step")
         return dx
 
+    def factor_values(self, p_spec, q_spec, vm, va, precision=GOX_PRECISION_FP64):
+        """The device's Jacobian (emission order) and factor (LU slot layout:
+        per factor column its U entries, diagonal, L entries) at the given
+        voltages, [B, nnzJ] and [B, slots]; see gox_topo_factor_values."""
+        L = _lib.load()
+        p_spec, q_spec = _f64(np.atleast_2d(p_spec)), _f64(np.atleast_2d(q_spec))
+        vm, va = _f64(np.atleast_2d(vm)), _f64(np.atleast_2d(va))
+        B = p_spec.shape[0]
+        if not (q_spec.shape == vm.shape == va.shape == p_spec.shape and p_spec.shape[1] == self.n_bus):
+            raise ValueError("factor_values: arrays must be [B, n_bus]")
+        inf = self.info()
+        jac = np.zeros((B, inf["nnz_j"]))
+        lu = np.zeros((B, inf["lu_slots"]))
+        check(L.gox_topo_factor_values(self._h, B, _p(p_spec, _lib.f64p), _p(q_spec, _lib.f64p),
+                                       _p(vm, _lib.f64p), _p(va, _lib.f64p), int(precision),
+                                       _p(jac, _lib.f64p), _p(lu, _lib.f64p)),
+              "gox_topo_factor_values")
+        return jac, lu
+
+    def stream_word(self, precision: int, warp: int, index: int, value: int) -> int:
+        """Test hook: replace one word of the device refactor stream; returns the
+        old word (gox_topo_stream_word)."""
+        old = np.zeros(1, np.int32)
+        check(_lib.load().gox_topo_stream_word(self._h, int(precision), int(warp), int(index),
+                                               int(value), _p(old, _lib.i32p)),
+              "gox_topo_stream_word")
+        return int(old[0])
+
     def info(self) -> dict:
         a = np.zeros(31, np.int64)
         check(_lib.load().gox_topo_info(self._h, _p(a, _lib.i64p)), "gox_topo_info")

@@ -237,6 +237,31 @@ int gox_topo_emulate_step(const gox_topo *t, const double *jac_vals, const doubl
 
 /* ---- inspection (klu_analyze / klu_extract analogues) ------------------ */
 
+/* The device path's Jacobian and factor values at given voltages (the
+ * per-entry view of JacobianPattern::fill, src/jacobian.rs:202-250, and of
+ * the refactor, src/klu_native/refactor.rs:68-152, that klu_extract gives
+ * for KLU): for B scenarios (host arrays p_spec, q_spec, vm, va
+ * [B][n_bus]) one injection + mismatch, one Jacobian fill and one refactor
+ * with the fixed pivot order run on the GPU in `precision`.  jac_vals
+ * [B][nnz J] (emission order, or NULL) receives the filled Jacobian;
+ * lu_vals [B][LU slots] (or NULL) the factor, column by column in factor
+ * order: the column's U entries (gox_topo_structure's Ui order), its
+ * diagonal, then its L entries (Li order, divided by the pivot).  Needs a
+ * fixed pivot order. */
+int gox_topo_factor_values(gox_topo *t, int32_t B, const double *p_spec, const double *q_spec,
+                           const double *vm, const double *va, int32_t precision,
+                           double *jac_vals, double *lu_vals);
+
+/* Test hook, no counterpart in the reference: replaces word `index` of warp
+ * `warp`'s refactor command stream (FP32 plan for GOX_PRECISION_MIXED, FP64
+ * plan otherwise) on the device with `value` and returns the old word, so a
+ * test can plant a malformed command and restore the stream.  A refactor
+ * that meets a malformed command stops that warp, drains its copies, keeps
+ * the CTA's barriers and makes the solve return GOX_E_DEVICE_WAIT.  The
+ * stream must have been uploaded (a solve ran). */
+int gox_topo_stream_word(gox_topo *t, int32_t precision, int32_t warp, int32_t index,
+                         int32_t value, int32_t *old_value);
+
 /* klu_analyze on a CSC pattern (BTF + AMD): P, Q [n], R [n+1]; returns the
  * number of blocks or < 0. */
 int gox_analyze(int32_t n, const int32_t *Ap, const int32_t *Ai, int32_t *P, int32_t *Q,

@@ -993,14 +993,14 @@ int gxo_batch_solve(gxo_topo *t, int B, const double *p_spec, const double *q_sp
     pthread_mutex_init(&J.mu, NULL);
     if (nthreads < 1) nthreads = 1;
     if (nthreads > B) nthreads = B;
-    if (nthreads == 1) {
-        batch_worker(&J);
-    } else {
-        pthread_t *th = (pthread_t *)xmalloc(sizeof(pthread_t) * nthreads);
-        for (int w = 0; w < nthreads; w++) pthread_create(&th[w], NULL, batch_worker, &J);
-        for (int w = 0; w < nthreads; w++) pthread_join(th[w], NULL);
-        free(th);
-    }
+    /* every worker, a single one included, runs on a thread of its own: the
+       calling thread's allocator arena behaves differently (on the Arm host
+       it ran one worker 2.7x slower), and a thread count of 1 must measure
+       the same worker as the others */
+    pthread_t *th = (pthread_t *)xmalloc(sizeof(pthread_t) * nthreads);
+    for (int w = 0; w < nthreads; w++) pthread_create(&th[w], NULL, batch_worker, &J);
+    for (int w = 0; w < nthreads; w++) pthread_join(th[w], NULL);
+    free(th);
     pthread_mutex_destroy(&J.mu);
     return 0;
 }
