@@ -22,6 +22,7 @@
 #include "gox_engine.hpp"
 #include "gox_stream.hpp"
 #include "gox_kernels.cuh"
+#include "gox_pivot.cuh"
 
 namespace gox {
 
@@ -575,6 +576,17 @@ struct FallbackBufs {
   DevMem idx, p, q, vm, va, sl, dr, di, ovm, ova, it, st, mm, hi;
 };
 
+// The partial-pivoting factorization of the FP64 re-solves (gox_pivot.cuh):
+// each factor column's A entries with their BTF-permuted rows and fill-image
+// locations, the right-hand-side positions, and the per-CTA scratch
+// (built on first use)
+struct PivotPlan {
+  bool built = false;
+  DevMem R, cp, ci, csrc, rhs_pos, scratch;
+  PivotDev d{};
+  int max_ctas = 0;
+};
+
 // A Newton loop captured as a CUDA graph (conditional while / if nodes),
 // keyed by every value its launches bake in
 struct LoopGraph {
@@ -630,6 +642,10 @@ struct gox_topo {
   std::vector<LoopGraph> loop_graphs;
   int32_t* h_nactive = nullptr;  // pinned
   FallbackBufs fb;
+  // FP64 re-solves of flagged mixed scenarios factor each Jacobian with
+  // threshold partial pivoting (set only during those re-solves)
+  PivotPlan pplan;
+  bool pivot_pass = false;
   // split solves: a second instance of this topology (same pivot order, own
   // device buffers and stream) that solves the second half of a large batch
   // concurrently with the first
@@ -897,12 +913,73 @@ static bool run_loop_graph(gox_topo* t, const BatchDev& D, int max_iter, bool ou
   return true;
 }
 
+// Scratch bound of a scenario's pivoting factor: the static pattern three
+// times over plus four entries per column (partial pivoting changes the
+// pattern; a factor that outgrows this marks its scenario singular).
+static void pivot_plan_build(gox_topo* t) {
+  PivotPlan& PP = t->pplan;
+  const Schedule& sc = t->sc;
+  const Symbolic& S = t->sym;
+  const Csc& A = t->csc;
+  const int n = sc.n_u;
+  std::vector<int32_t> psinv(n), a_of_csc(A.nnz(), -1), cp(n + 1, 0), ci, csrc, rhs_pos(n);
+  for (int i = 0; i < n; i++) psinv[S.P[i]] = i;
+  for (int a = 0; a < sc.n_a; a++) a_of_csc[sc.a_csc[a]] = a;
+  for (int k = 0; k < n; k++) {
+    const int oc = S.Q[k];
+    for (int p = A.p[oc]; p < A.p[oc + 1]; p++) {
+      const int a = a_of_csc[p];
+      if (a < 0) throw std::runtime_error("pivot plan: an A entry without a fill destination");
+      ci.push_back(psinv[A.i[p]]);
+      csrc.push_back(sc.a_dst[a] >= 0 ? sc.c_base[k] + sc.a_dst[a] : sc.a_dst[a]);
+    }
+    cp[k + 1] = (int)ci.size();
+  }
+  for (int i = 0; i < n; i++) rhs_pos[i] = t->num.Pinv[S.P[i]];
+  upload(PP.R, S.R);
+  upload(PP.cp, cp);
+  upload(PP.ci, ci);
+  upload(PP.csrc, csrc);
+  upload(PP.rhs_pos, rhs_pos);
+  PivotDev& d = PP.d;
+  d.n = n;
+  d.nblocks = S.nblocks;
+  d.n_slots = sc.n_slots;
+  d.n_off = sc.n_off;
+  const int nlu = (int)(t->num.Li.size() + t->num.Ui.size());
+  d.lcap = 3 * nlu + 4 * n;
+  d.ucap = 3 * nlu + 4 * n;
+  d.ocap = std::max(sc.n_off, 1);
+  d.R = PP.R.as<int32_t>();
+  d.cp = PP.cp.as<int32_t>();
+  d.ci = PP.ci.as<int32_t>();
+  d.csrc = PP.csrc.as<int32_t>();
+  d.rhs_pos = PP.rhs_pos.as<int32_t>();
+  d.tol = 0.001;  // KLU's default pivot tolerance (klu_defaults.c), as KluNative
+  d.stride = pivot_stride(n, d.lcap, d.ucap, d.ocap);
+  // as many CTAs as 4 GB of scratch hold (at least one per SM)
+  PP.max_ctas = (int)std::max<size_t>(152, ((size_t)4 << 30) / d.stride);
+  PP.built = true;
+}
+
+// The pivoting factorization + solve of every running scenario of the batch
+// (FP64 buffers), in place of the static refactor and substitutions.
+static void pivot_run(gox_topo* t, BatchDev& D, cudaStream_t st) {
+  PivotPlan& PP = t->pplan;
+  if (!PP.built) pivot_plan_build(t);
+  const int ctas = std::min(D.G * 32, PP.max_ctas);
+  PP.scratch.ensure((size_t)ctas * PP.d.stride);
+  PP.d.scratch = PP.scratch.as<unsigned char>();
+  k_factor_pivot<<<ctas, 32, 0, st>>>(PP.d, D);
+}
+
 template <typename T>
 static void run_iterations(gox_topo* t, BatchDev D, int max_iter, bool outage, cudaStream_t st,
                            int32_t* h_nactive) {
   const SchedDev& S = t->dsched.d;
   const bool timing = t->timing.on;
-  if (!timing && run_loop_graph<T>(t, D, max_iter, outage, st)) {
+  const bool pivoting = sizeof(T) == 8 && t->pivot_pass;
+  if (!timing && !pivoting && run_loop_graph<T>(t, D, max_iter, outage, st)) {
     // launches: per iteration 3 + 1 (decision) and, while running, fill,
     // refactor and the separate solve; the final mismatch when the budget ran out
     int32_t h[2] = {0, 0};
@@ -936,9 +1013,15 @@ static void run_iterations(gox_topo* t, BatchDev D, int max_iter, bool outage, c
     if (*h_nactive == 0) break;
     Iter<T>::fill(S, D, outage, st);
     rec();
-    Iter<T>::refactor(t->dsched, D, st);
-    rec();
-    const int ns = Iter<T>::solve_rest(t->dsched, D, st);
+    int ns = 0;
+    if (pivoting) {
+      pivot_run(t, D, st);
+      rec();
+    } else {
+      Iter<T>::refactor(t->dsched, D, st);
+      rec();
+      ns = Iter<T>::solve_rest(t->dsched, D, st);
+    }
     rec();
     t->launches += 2 + ns;
     GOX_CK(cudaGetLastError());
@@ -1361,6 +1444,13 @@ static int batch_device(gox_topo* t, int B, const double* p_spec, const double* 
       if (want_hist) ohi.ensure((size_t)Bf * max_iter * 8);
       const int gm = t->guess_mode;
       t->guess_mode = 0;  // the start points are already the guessed ones
+      // their static pivot order is poor for their own Jacobians: every
+      // Newton step of the re-solve factors with threshold partial pivoting
+      struct PivotPass {
+        gox_topo* t;
+        explicit PivotPass(gox_topo* t_) : t(t_) { t->pivot_pass = true; }
+        ~PivotPass() { t->pivot_pass = false; }
+      } pivot_scope(t);
       const int rc = batch_device(
           t, Bf, fp.as<double>(), fq.as<double>(), vmf, vaf, v_stride,
           outage ? fsl.as<int32_t>() : nullptr, outage ? fdr.as<double>() : nullptr,
@@ -2430,6 +2520,53 @@ int gox_topo_factor_values(gox_topo* t, int32_t B, const double* p_spec, const d
     GOX_CK(cudaMemcpyAsync(herr, DB.err.p, 8, cudaMemcpyDeviceToHost, st));
     GOX_CK(cudaStreamSynchronize(st));
     return herr[1] ? GOX_E_DEVICE_WAIT : GOX_OK;
+  });
+}
+
+int gox_topo_pivot_solve(gox_topo* t, const double* jac_vals, const double* rhs, double* dx) {
+  if (!t || !t->factored || !jac_vals || !rhs || !dx) return GOX_E_INVALID;
+  if (int r = require_device()) return r;
+  return guard_impl([&]() -> int {
+    cudaStream_t st = thread_stream();
+    AllocStreamScope alloc_scope(st);
+    const Schedule& sc = t->sc;
+    const int n = sc.n_u;
+    if (!t->uploaded) {
+      t->dsched.load(t->sc, t->yp, t->yi, t->yre, t->yim);
+      t->dsched.load_streams(t->s32, t->s64);
+      t->uploaded = true;
+    }
+    const SchedDev& S = t->dsched.d;
+    DevBatch& DB = t->batch;
+    DB.ensure(S, 1, GOX_PRECISION_FP64, 1, false);
+    BatchDev D = DB.view(false, false, 0.0, 0.0);
+    // the fill image of one group: the Jacobian in lane 0 (the other lanes
+    // are unused scenarios), the right-hand side in the static pivot order
+    std::vector<double> packed(t->csc.nnz(), 0.0);
+    for (int e = 0; e < t->jac.nnz(); e++) packed[t->csc.slot_of[e]] += jac_vals[e];
+    std::vector<double> img((size_t)S.n_slots * 32, 0.0), off((size_t)S.n_off * 32, 0.0),
+        b((size_t)n * 32, 0.0), x((size_t)n * 32, 0.0);
+    for (int xs = 0; xs < sc.n_slots; xs++)
+      if (sc.slot_a[xs] >= 0) img[(size_t)xs * 32] = packed[sc.a_csc[sc.slot_a[xs]]];
+    for (int a = 0; a < sc.n_a; a++)
+      if (sc.a_dst[a] < 0) off[(size_t)(-sc.a_dst[a] - 1) * 32] = packed[sc.a_csc[a]];
+    for (int u = 0; u < n; u++) b[(size_t)t->num.Pinv[u] * 32] = rhs[u];
+    std::vector<int32_t> status(32, ST_UNUSED), zeros(32, 0), one(1, 1);
+    status[0] = ST_RUNNING;
+    GOX_CK(cudaMemcpyAsync(D.lu, img.data(), img.size() * 8, cudaMemcpyHostToDevice, st));
+    GOX_CK(cudaMemcpyAsync(D.off, off.data(), off.size() * 8, cudaMemcpyHostToDevice, st));
+    GOX_CK(cudaMemcpyAsync(D.rhs, b.data(), b.size() * 8, cudaMemcpyHostToDevice, st));
+    GOX_CK(cudaMemcpyAsync(D.status, status.data(), 128, cudaMemcpyHostToDevice, st));
+    GOX_CK(cudaMemcpyAsync(D.sing, zeros.data(), 128, cudaMemcpyHostToDevice, st));
+    GOX_CK(cudaMemcpyAsync(D.gact, one.data(), 4, cudaMemcpyHostToDevice, st));
+    pivot_run(t, D, st);
+    GOX_CK(cudaGetLastError());
+    int32_t sing = 0;
+    GOX_CK(cudaMemcpyAsync(x.data(), D.sol, x.size() * 8, cudaMemcpyDeviceToHost, st));
+    GOX_CK(cudaMemcpyAsync(&sing, D.sing, 4, cudaMemcpyDeviceToHost, st));
+    GOX_CK(cudaStreamSynchronize(st));
+    for (int k = 0; k < n; k++) dx[t->sym.Q[k]] = x[(size_t)k * 32];
+    return sing ? GOX_SINGULAR : GOX_OK;
   });
 }
 

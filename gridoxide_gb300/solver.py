@@ -367,6 +367,19 @@ class Topology:
               "gox_topo_factor_values")
         return jac, lu
 
+    def pivot_solve(self, jac_vals, rhs) -> Optional[np.ndarray]:
+        """dx of J dx = rhs with J factored afresh with threshold partial
+        pivoting on the GPU (the mixed path's repair of a poor static pivot
+        order; gox_topo_pivot_solve); None when singular."""
+        L = _lib.load()
+        dx = np.zeros(len(rhs))
+        rc = L.gox_topo_pivot_solve(self._h, _p(_f64(jac_vals), _lib.f64p),
+                                    _p(_f64(rhs), _lib.f64p), _p(dx, _lib.f64p))
+        if rc == GOX_SINGULAR:
+            return None
+        check(rc, "gox_topo_pivot_solve")
+        return dx
+
     def stream_word(self, precision: int, warp: int, index: int, value: int) -> int:
         """Test hook: replace one word of the device refactor stream; returns the
         old word (gox_topo_stream_word)."""

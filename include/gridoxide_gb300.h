@@ -252,6 +252,18 @@ int gox_topo_factor_values(gox_topo *t, int32_t B, const double *p_spec, const d
                            const double *vm, const double *va, int32_t precision,
                            double *jac_vals, double *lu_vals);
 
+/* The mixed path's repair of a poor static pivot order, on one Jacobian:
+ * the FP64 threshold-partial-pivoting factorization the GPU runs for the
+ * Newton steps of scenarios that trip the pivot-ratio check (Gilbert-Peierls
+ * per BTF block with KLU's lpivot, tol 0.001 and diagonal preference --
+ * src/klu_native/kernel.rs:187-262, 341-416 -- pivots chosen afresh for
+ * these values, then the block substitutions of src/klu_native/solve.rs:
+ * 56-102).  jac_vals in emission order, rhs and dx in unknown order.  Needs
+ * a fixed (static) pivot order, which only lays out the inputs.  Returns
+ * GOX_SINGULAR on a zero pivot, a factor above its fill bound (three times
+ * the static factor plus 4 n entries) or a non-finite dx. */
+int gox_topo_pivot_solve(gox_topo *t, const double *jac_vals, const double *rhs, double *dx);
+
 /* Test hook, no counterpart in the reference: replaces word `index` of warp
  * `warp`'s refactor command stream (FP32 plan for GOX_PRECISION_MIXED, FP64
  * plan otherwise) on the device with `value` and returns the old word, so a
@@ -378,11 +390,12 @@ int gox_topo_initial_guess(gox_topo *t, int32_t B, const double *p_spec, const d
 
 /* Mixed path: the pivot-ratio threshold.  A scenario whose FP32 refactor
  * meets a pivot with |u_kk| < tol * max |L(:, k)| (before scaling) is solved
- * again from its start point on the FP64 path, with the same pivot order,
- * and that report replaces its mixed one.  Default 1e-6; 0 disables.
- * No counterpart in the reference (its refactor is FP64 only); the FP64
- * path it falls back to is the reference's static-pivot refactor,
- * KLU_refactor (KLU/Source/klu_refactor.c:24). */
+ * again from its start point on the FP64 path, each of its Newton steps
+ * factoring its Jacobian with threshold partial pivoting on the GPU
+ * (KLU_factor's pivoting, src/klu_native/kernel.rs:187-262, 341-416; see
+ * gox_topo_pivot_solve), and that report replaces its mixed one.  Default
+ * 1e-6; 0 disables.  No counterpart in the reference (its refactor is FP64
+ * only and keeps its pivots). */
 int gox_set_pivot_tolerance(gox_topo *t, double tol);
 
 /* Scenarios of the last gox_batch_solve / gox_batch_solve_device call that
