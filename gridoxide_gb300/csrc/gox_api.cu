@@ -4,11 +4,13 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <array>
 #include <atomic>
 #include <cmath>
 #include <functional>
 #include <map>
 #include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <memory>
 #include <mutex>
@@ -508,6 +510,12 @@ struct Iter {
   }
   static void refactor(const DevSchedule& ds, const BatchDev& D, cudaStream_t st) {
     const int i = sizeof(T) == 4 ? 0 : 1;
+    refactor_with(ds.st[i], ds.st_nw[i], ds.st_smem[i], ds.d, D, D.G, st);
+  }
+  // one launch of the refactor with a given plan's stream over the first
+  // `groups` groups
+  static void refactor_with(const StreamDev& P, int nw, size_t smem, const SchedDev& S,
+                            const BatchDev& D, int groups, cudaStream_t st) {
     // the budget every plan fits in, set once per device (the same value for
     // every plan; setting an attribute per launch would put a driver call
     // between concurrent solves' launches)
@@ -518,7 +526,7 @@ struct Iter {
       GOX_CK(cudaFuncSetAttribute(k_refactor<T>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                   (int)kRefactorSmem));
     });
-    k_refactor<T><<<D.G, 32 * ds.st_nw[i], ds.st_smem[i], st>>>(ds.st[i], ds.d, D);
+    k_refactor<T><<<groups, 32 * nw, smem, st>>>(P, S, D);
   }
   static void solve(const SchedDev& S, const BatchDev& D, cudaStream_t st) {
     k_solve<T><<<D.G, 32 * kWarps, 0, st>>>(S, D);
@@ -646,6 +654,13 @@ struct gox_topo {
   // threshold partial pivoting (set only during those re-solves)
   PivotPlan pplan;
   bool pivot_pass = false;
+  // refactor plan chosen by the autotuner, per precision (FP32, FP64)
+  bool tune_cache_only = false;  // variants: a cached plan or the default, never timed
+  struct Tuning {
+    bool done = false;
+    int source = 0;  // 0 the default (most warps), 1 measured here, 2 from the cache
+    std::vector<std::array<double, 4>> table;  // timed candidates: warps, chunk words, ring rows, ms
+  } tune[2];
   // split solves: a second instance of this topology (same pivot order, own
   // device buffers and stream) that solves the second half of a large batch
   // concurrently with the first
@@ -863,12 +878,11 @@ static cudaGraphExec_t build_loop_graph(gox_topo* t, const BatchDev& D, int max_
 // Runs the loop from a cached graph when this exact configuration was seen
 // before (the first sighting runs the host loop and records the key);
 // false: run the host loop.
+// Everything a captured loop bakes in: precision (first 4 bytes), budget,
+// outage use, buffers, schedule and the refactor stream.
 template <typename T>
-static bool run_loop_graph(gox_topo* t, const BatchDev& D, int max_iter, bool outage,
-                           cudaStream_t st) {
-  // small batches stay on the host-driven loop: measured, their graphs ran
-  // slower when many topologies solve concurrently from several threads
-  if (t->graphs_off || !t->graphs_wanted || D.G < kGraphMinGroups) return false;
+static std::vector<unsigned char> loop_key(const gox_topo* t, const BatchDev& D, int max_iter,
+                                           bool outage) {
   std::vector<unsigned char> key;
   auto put = [&](const void* p, size_t n) {
     const unsigned char* c = static_cast<const unsigned char*>(p);
@@ -880,15 +894,32 @@ static bool run_loop_graph(gox_topo* t, const BatchDev& D, int max_iter, bool ou
   put(&D, sizeof D); put(&t->dsched.d, sizeof(SchedDev));
   put(&t->dsched.st[i], sizeof(StreamDev)); put(&t->dsched.st_nw[i], sizeof(int));
   put(&t->dsched.st_smem[i], sizeof(size_t)); put(&t->dsched.st_bwd[i], sizeof(bool));
+  return key;
+}
+
+// A configuration seen once: its next solve captures and runs the graph.
+static void remember_loop(gox_topo* t, const std::vector<unsigned char>& key) {
+  for (auto& x : t->loop_graphs)
+    if (x.key == key) return;
+  if (t->loop_graphs.size() >= 4) {
+    if (t->loop_graphs.front().exec) cudaGraphExecDestroy(t->loop_graphs.front().exec);
+    t->loop_graphs.erase(t->loop_graphs.begin());
+  }
+  t->loop_graphs.push_back(LoopGraph{key, nullptr, 1});
+}
+
+template <typename T>
+static bool run_loop_graph(gox_topo* t, const BatchDev& D, int max_iter, bool outage,
+                           cudaStream_t st) {
+  // small batches stay on the host-driven loop: measured, their graphs ran
+  // slower when many topologies solve concurrently from several threads
+  if (t->graphs_off || !t->graphs_wanted || D.G < kGraphMinGroups) return false;
+  const std::vector<unsigned char> key = loop_key<T>(t, D, max_iter, outage);
   LoopGraph* lg = nullptr;
   for (auto& x : t->loop_graphs)
     if (x.key == key) lg = &x;
   if (!lg) {
-    if (t->loop_graphs.size() >= 4) {
-      if (t->loop_graphs.front().exec) cudaGraphExecDestroy(t->loop_graphs.front().exec);
-      t->loop_graphs.erase(t->loop_graphs.begin());
-    }
-    t->loop_graphs.push_back(LoopGraph{key, nullptr, 1});
+    remember_loop(t, key);
     return false;
   }
   if (!lg->exec) {
@@ -973,6 +1004,204 @@ static void pivot_run(gox_topo* t, BatchDev& D, cudaStream_t st) {
   k_factor_pivot<<<ctas, 32, 0, st>>>(PP.d, D);
 }
 
+// ---------------------------------------------------------------------------
+// Refactor autotuner.  The plan of a topology's refactor streams (warps per
+// CTA, stream-chunk words, hence ring rows) is chosen by timing the
+// candidate plans on the first batch the topology solves in a precision:
+// after that batch's first Jacobian fill, each candidate's stream (compiled
+// on the host and checked by the host interpreter first) refactors the
+// first min(G, 152) groups of the image, twice, timed with CUDA events on
+// the solve stream; the fastest is kept.  The choice is cached per process
+// (and in the file $GOX_TUNE_CACHE, when set) under (precision, bus-count
+// bucket of half an octave, fill nnz(L+U) / nnz(J) in tenths, batch size
+// in groups: 1, 2-8, 9-38, 39-152, more); a topology with a cached key
+// compiles that plan only.  gox_set_autotune(0) keeps the default plan
+// (the most warps that fit).
+
+static std::mutex g_tune_mu;
+static std::map<std::array<int, 4>, std::array<int, 2>> g_tune;  // key -> {warps, chunk words}
+static bool g_tune_loaded = false;
+static std::atomic<int> g_autotune{1};
+
+static std::array<int, 4> tune_key(const gox_topo* t, int prec, int groups) {
+  const double fill = (double)(t->num.Li.size() + t->num.Ui.size() + t->num.Pnum.size()) /
+                      (double)std::max(1, t->jac.nnz());
+  const int gb = groups <= 1 ? 0 : groups <= 8 ? 1 : groups <= 38 ? 2 : groups <= 152 ? 3 : 4;
+  return {prec, (int)std::lround(2.0 * std::log2((double)std::max(2, t->n_bus))),
+          (int)std::lround(10.0 * fill), gb};
+}
+
+static void tune_cache_load() {
+  if (g_tune_loaded) return;
+  g_tune_loaded = true;
+  const char* path = std::getenv("GOX_TUNE_CACHE");
+  if (!path || !*path) return;
+  FILE* f = std::fopen(path, "r");
+  if (!f) return;
+  int a, b, c, d, nw, cw;
+  while (std::fscanf(f, "gox-tune-1 %d %d %d %d %d %d\n", &a, &b, &c, &d, &nw, &cw) == 6)
+    g_tune[{a, b, c, d}] = {nw, cw};
+  std::fclose(f);
+}
+
+static void tune_cache_store(const std::array<int, 4>& k, int nw, int cw) {
+  g_tune[k] = {nw, cw};
+  const char* path = std::getenv("GOX_TUNE_CACHE");
+  if (!path || !*path) return;
+  if (FILE* f = std::fopen(path, "a")) {
+    std::fprintf(f, "gox-tune-1 %d %d %d %d %d %d\n", k[0], k[1], k[2], k[3], nw, cw);
+    std::fclose(f);
+  }
+}
+
+// Compiles a plan's stream and runs it once through the checking host
+// interpreter (as make_streams does for the default plan).
+static bool compile_checked(const Schedule& sc, const StreamPlan& p, Stream& out) {
+  std::string why;
+  if (!build_plan(sc, p, out, why)) return false;
+  std::vector<double> lu(sc.n_slots, 1.0), rhs(sc.n_u, 0.0), X;
+  bool sing = false;
+  return run_stream_host(sc, out, lu, rhs, X, sing).empty();
+}
+
+// Installs a precision's stream on the topology (and its split twin); the
+// captured Newton loops hold the old stream's device pointers: dropped.
+static void drop_loops(gox_topo* t, int i) {
+  const int prec = i == 0 ? 4 : 8;
+  std::vector<LoopGraph> keep;
+  for (auto& lg : t->loop_graphs) {
+    int kp = 0;
+    std::memcpy(&kp, lg.key.data(), sizeof kp);
+    if (kp == prec) {
+      if (lg.exec) cudaGraphExecDestroy(lg.exec);
+    } else {
+      keep.push_back(std::move(lg));
+    }
+  }
+  t->loop_graphs = std::move(keep);
+}
+
+static void install_stream(gox_topo* t, int i, Stream&& s) {
+  (i == 0 ? t->s32 : t->s64) = std::move(s);
+  t->dsched.load_streams(t->s32, t->s64);
+  drop_loops(t, i);
+  if (t->twin) {
+    t->twin->s32 = t->s32;
+    t->twin->s64 = t->s64;
+    if (t->twin->uploaded) t->twin->dsched.load_streams(t->twin->s32, t->twin->s64);
+    drop_loops(t->twin.get(), i);
+  }
+}
+
+template <typename T>
+static void autotune(gox_topo* t, const BatchDev& D, cudaStream_t st) {
+  const int i = sizeof(T) == 4 ? 0 : 1;
+  gox_topo::Tuning& TU = t->tune[i];
+  TU.done = true;
+  if (!g_autotune.load()) return;
+  const Schedule& sc = t->sc;
+  const int elem = (int)sizeof(T);
+  const std::array<int, 4> key = tune_key(t, i, D.G);
+  {
+    std::lock_guard<std::mutex> lk(g_tune_mu);
+    tune_cache_load();
+    auto it = g_tune.find(key);
+    if (it == g_tune.end() && t->tune_cache_only) return;
+    if (it != g_tune.end()) {
+      const Stream& cur = i == 0 ? t->s32 : t->s64;
+      if (cur.plan.nw == it->second[0] && cur.plan.chunk_words == it->second[1]) {
+        TU.source = 2;
+        return;
+      }
+      for (const StreamPlan& p : candidate_plans(sc, elem, kRefactorSmem))
+        if (p.nw == it->second[0] && p.chunk_words == it->second[1]) {
+          Stream s;
+          if (compile_checked(sc, p, s)) {
+            install_stream(t, i, std::move(s));
+            TU.source = 2;
+          }
+          return;
+        }
+      return;
+    }
+  }
+  // compile and check every candidate (host threads in parallel)
+  std::vector<StreamPlan> cand = candidate_plans(sc, elem, kRefactorSmem);
+  std::vector<Stream> built(cand.size());
+  std::vector<char> ok(cand.size(), 0);
+  {
+    std::vector<std::thread> th;
+    std::atomic<size_t> next{0};
+    const unsigned nt = std::max(1u, std::min(8u, std::thread::hardware_concurrency()));
+    for (unsigned w = 0; w < nt; w++)
+      th.emplace_back([&] {
+        for (size_t c; (c = next++) < cand.size();) ok[c] = compile_checked(sc, cand[c], built[c]);
+      });
+    for (auto& x : th) x.join();
+  }
+  const int Gt = std::min(D.G, 152);
+  const size_t img_bytes = (size_t)Gt * sc.n_slots * 32 * sizeof(T);
+  DevMem bak, words, c0, nc;
+  bak.ensure(img_bytes);
+  GOX_CK(cudaMemcpyAsync(bak.p, D.lu, img_bytes, cudaMemcpyDeviceToDevice, st));
+  cudaEvent_t e0, e1;
+  GOX_CK(cudaEventCreate(&e0));
+  GOX_CK(cudaEventCreate(&e1));
+  double best_ms = 1e30;
+  int best = -1;
+  TU.table.clear();
+  for (size_t c = 0; c < cand.size(); c++) {
+    if (!ok[c]) continue;
+    const Stream& s = built[c];
+    upload(words, s.words);
+    upload(c0, s.chunk0);
+    upload(nc, s.nchunks);
+    StreamDev P{};
+    P.words = words.as<int32_t>();
+    P.chunk0 = c0.as<int32_t>();
+    P.nchunks = nc.as<int32_t>();
+    P.ring_rows = s.plan.ring_rows;
+    P.rows_total = ring_total(s.plan);
+    P.chunk_words = s.plan.chunk_words;
+    P.n_bars = s.n_bars;
+    float ms = 0.0f;
+    for (int rep = 0; rep < 2; rep++) {
+      GOX_CK(cudaMemcpyAsync(D.lu, bak.p, img_bytes, cudaMemcpyDeviceToDevice, st));
+      GOX_CK(cudaEventRecord(e0, st));
+      Iter<T>::refactor_with(P, s.plan.nw, stream_smem_bytes(s.plan), t->dsched.d, D, Gt, st);
+      GOX_CK(cudaEventRecord(e1, st));
+      GOX_CK(cudaEventSynchronize(e1));
+      GOX_CK(cudaEventElapsedTime(&ms, e0, e1));
+    }
+    GOX_CK(cudaGetLastError());
+    int32_t herr[2] = {0, 0};
+    GOX_CK(cudaMemcpyAsync(herr, D.err - 1, 8, cudaMemcpyDeviceToHost, st));
+    GOX_CK(cudaStreamSynchronize(st));
+    if (herr[1]) {  // a bounded wait gave up under this plan: not a candidate
+      const int32_t z[2] = {0, 0};
+      GOX_CK(cudaMemcpyAsync(D.err - 1, z, 8, cudaMemcpyHostToDevice, st));
+      continue;
+    }
+    TU.table.push_back({(double)s.plan.nw, (double)s.plan.chunk_words, (double)s.plan.ring_rows,
+                        (double)ms});
+    if (ms < best_ms) {
+      best_ms = ms;
+      best = (int)c;
+    }
+  }
+  // the image as the fill left it, for the iteration to go on
+  GOX_CK(cudaMemcpyAsync(D.lu, bak.p, img_bytes, cudaMemcpyDeviceToDevice, st));
+  GOX_CK(cudaStreamSynchronize(st));
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  if (best < 0) return;
+  const int nw = cand[best].nw, cw = cand[best].chunk_words;
+  install_stream(t, i, std::move(built[best]));
+  TU.source = 1;
+  std::lock_guard<std::mutex> lk(g_tune_mu);
+  tune_cache_store(key, nw, cw);
+}
+
 template <typename T>
 static void run_iterations(gox_topo* t, BatchDev D, int max_iter, bool outage, cudaStream_t st,
                            int32_t* h_nactive) {
@@ -1001,6 +1230,7 @@ static void run_iterations(gox_topo* t, BatchDev D, int max_iter, bool outage, c
     ev.push_back(e);
   };
   int it = 0;
+  bool tuned_now = false;
   std::vector<int> full;  // iterations that ran K2-K4
   rec();
   for (it = 0; it < max_iter; it++) {
@@ -1012,6 +1242,10 @@ static void run_iterations(gox_topo* t, BatchDev D, int max_iter, bool outage, c
     GOX_CK(cudaStreamSynchronize(st));
     if (*h_nactive == 0) break;
     Iter<T>::fill(S, D, outage, st);
+    if (!pivoting && !t->tune[sizeof(T) == 4 ? 0 : 1].done) {
+      autotune<T>(t, D, st);
+      tuned_now = true;
+    }
     rec();
     int ns = 0;
     if (pivoting) {
@@ -1029,6 +1263,11 @@ static void run_iterations(gox_topo* t, BatchDev D, int max_iter, bool outage, c
   if (it == max_iter) t->launches += Iter<T>::mismatch(S, D, max_iter, 1, outage, st);
   rec();
   GOX_CK(cudaGetLastError());
+  // the plan chosen during this solve changed the loop's key: remember the
+  // new configuration, so that the next solve runs it as a graph
+  if (tuned_now && !timing && !pivoting && !t->graphs_off && t->graphs_wanted &&
+      D.G >= kGraphMinGroups)
+    remember_loop(t, loop_key<T>(t, D, max_iter, outage));
   if (timing) {
     GOX_CK(cudaEventSynchronize(ev.back()));
     auto el = [&](size_t a, size_t b) {
@@ -1545,6 +1784,7 @@ static gox_topo* topo_variant(gox_topo* t, const std::vector<int32_t>& changes) 
   v->piv_tol = t->piv_tol;
   v->zip = t->zip;
   if (!v->zip.empty()) upload(v->dzip, v->zip);
+  v->tune_cache_only = true;  // many variants solve concurrently: no timing of their own
   t->variants.emplace_back(changes, v.get());
   return v.release();
 }
@@ -1780,6 +2020,8 @@ static gox_topo* split_twin(gox_topo* t) {
   v->graphs_wanted = t->graphs_wanted;
   v->zip = t->zip;
   if (!v->zip.empty()) upload(v->dzip, v->zip);
+  // the twin runs the streams its topology chose (install_stream updates it)
+  v->tune[0].done = v->tune[1].done = true;
   t->twin = std::move(v);
   return t->twin.get();
 }
@@ -1820,8 +2062,10 @@ static int batch_split(gox_topo* t, int B, const double* p_spec, const double* q
                        const int32_t* h_oslot, const double* h_odre, const double* h_odim) {
   // (FP64 solves stay whole: their refactor is bound by the FP64 pipe, which
   // the halves would share; measured slower split)
+  // (and not before the topology's plan for this precision is tuned: the
+  // tuning installs streams the twin shares)
   if (t->split_parts < 2 || !t->factored || t->guess_mode != 0 || t->timing.on ||
-      B < kSplitMinScenarios || precision != GOX_PRECISION_MIXED)
+      B < kSplitMinScenarios || precision != GOX_PRECISION_MIXED || !t->tune[0].done)
     return batch_any(t, B, p_spec, q_spec, vm0, va0, v_stride, o_slot, o_dre, o_dim, tol, max_iter,
                      precision, vm_out, va_out, iters, status, max_mis, hist, st, h_p, h_q, h_vm,
                      h_va, h_oslot, h_odre, h_odim);
@@ -1972,6 +2216,8 @@ int gox_topo_reset(gox_topo* t) {
   t->uploaded = false;
   t->num = Numeric();
   t->sc = Schedule();
+  t->tune[0] = gox_topo::Tuning();
+  t->tune[1] = gox_topo::Tuning();
   return GOX_OK;
 }
 
@@ -2588,6 +2834,34 @@ int gox_topo_stream_word(gox_topo* t, int32_t precision, int32_t warp, int32_t i
     if (old_value) *old_value = old;
     return GOX_OK;
   });
+}
+
+int gox_set_autotune(int32_t on) {
+  g_autotune.store(on ? 1 : 0);
+  return GOX_OK;
+}
+
+int gox_topo_tuning(const gox_topo* t, int32_t precision, int64_t* plan, double* table,
+                    int32_t max_rows) {
+  if (!t || !plan || (precision != GOX_PRECISION_FP64 && precision != GOX_PRECISION_MIXED))
+    return GOX_E_INVALID;
+  if (!t->factored) return GOX_E_INVALID;
+  const int i = precision == GOX_PRECISION_MIXED ? 0 : 1;
+  const Stream& s = i == 0 ? t->s32 : t->s64;
+  const gox_topo::Tuning& TU = t->tune[i];
+  plan[0] = s.plan.nw;
+  plan[1] = s.plan.ring_rows;
+  plan[2] = s.plan.big_rows;
+  plan[3] = s.plan.chunk_words;
+  plan[4] = TU.source;
+  plan[5] = (int64_t)TU.table.size();
+  int rows = 0;
+  for (const auto& r : TU.table) {
+    if (!table || rows >= max_rows) break;
+    for (int c = 0; c < 4; c++) table[(size_t)rows * 4 + c] = r[c];
+    rows++;
+  }
+  return rows;
 }
 
 int gox_topo_info(const gox_topo* t, int64_t* info) {

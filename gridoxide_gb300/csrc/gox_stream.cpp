@@ -1210,32 +1210,62 @@ bool choose_stream(const Schedule& sc, int elem, size_t smem_budget, Stream& out
   return false;
 }
 
+// The plan with nw warps and chunk_words-word stream chunks in the budget:
+// the rest of the shared memory split into rings (one larger ring for warp 0
+// when some column's block does not fit an even share).  False when none.
+static bool plan_for(const Schedule& sc, int elem, size_t smem_budget, int nw, int chunk_words,
+                     StreamPlan& p) {
+  int max_brows = 1;
+  for (int k = 0; k < sc.n_u; k++) max_brows = std::max(max_brows, sc.c_ulen[k] + 1 + sc.c_llen[k] + 3);
+  p = StreamPlan{};
+  p.elem = elem;
+  p.nw = nw;
+  p.chunk_words = chunk_words;
+  const size_t fixed = (size_t)nw * 2 * p.chunk_words * 4 + (size_t)kSpareRows * 32 * elem;
+  if (fixed >= smem_budget) return false;
+  const int total = std::min((int)((smem_budget - fixed) / ((size_t)32 * elem)), kMaxRows - kSpareRows);
+  int r = total / nw;
+  int big = 0;
+  if (max_brows > r && nw > 1) {
+    // one large ring (warp 0) for the columns the even split cannot hold
+    big = max_brows + max_brows / 8;
+    r = (total - big) / (nw - 1);
+    if (r < 32 || big <= r) return false;
+  }
+  if (r < 16) return false;
+  p.ring_rows = r;
+  p.big_rows = big;
+  return true;
+}
+
+std::vector<StreamPlan> candidate_plans(const Schedule& sc, int elem, size_t smem_budget) {
+  std::vector<StreamPlan> out;
+  for (int nw : {12, 11, 10, 9, 8, 7, 6, 5, 4}) {
+    if (nw > (elem == 4 ? kMaxRefactorWarps : 8)) continue;
+    for (int cw : {256, 320, 512}) {
+      StreamPlan p;
+      if (plan_for(sc, elem, smem_budget, nw, cw, p)) out.push_back(p);
+    }
+  }
+  return out;
+}
+
+bool build_plan(const Schedule& sc, const StreamPlan& p, Stream& out, std::string& why) {
+  for (bool bwd : {sc.fuse_fwd, false}) {
+    if (build_stream(sc, p, out, why, bwd)) return true;
+    if (!bwd) break;
+  }
+  return false;
+}
+
 static bool choose_stream_1(const Schedule& sc, int elem, size_t smem_budget, Stream& out,
                             std::string& why, bool with_bwd) {
   bool found = false;
   std::string last;
-  int max_brows = 1;
-  for (int k = 0; k < sc.n_u; k++) max_brows = std::max(max_brows, sc.c_ulen[k] + 1 + sc.c_llen[k] + 3);
   for (int nw : {12, 10, 8, 6, 4, 3, 2, 1}) {
     if (nw > (elem == 4 ? kMaxRefactorWarps : 8)) continue;
     StreamPlan p;
-    p.elem = elem;
-    p.nw = nw;
-    p.chunk_words = nw >= 10 ? 320 : 512;
-    const size_t fixed = (size_t)nw * 2 * p.chunk_words * 4 + (size_t)kSpareRows * 32 * elem;
-    if (fixed >= smem_budget) continue;
-    const int total = std::min((int)((smem_budget - fixed) / ((size_t)32 * elem)), kMaxRows - kSpareRows);
-    int r = total / nw;
-    int big = 0;
-    if (max_brows > r && nw > 1) {
-      // one large ring (warp 0) for the columns the even split cannot hold
-      big = max_brows + max_brows / 8;
-      r = (total - big) / (nw - 1);
-      if (r < 32 || big <= r) continue;
-    }
-    if (r < 16) continue;
-    p.ring_rows = r;
-    p.big_rows = big;
+    if (!plan_for(sc, elem, smem_budget, nw, nw >= 10 ? 320 : 512, p)) continue;
     Stream s;
     std::string w;
     if (!build_stream(sc, p, s, w, with_bwd)) {

@@ -147,6 +147,15 @@ bool build_stream(const Schedule& sc, const StreamPlan& plan, Stream& out, std::
 bool choose_stream(const Schedule& sc, int elem, size_t smem_budget, Stream& out,
                    std::string& why);
 
+// The plans an autotuner may time: every warp count (12 down to 4 in FP32,
+// 8 down to 4 in FP64) with stream chunks of 256, 320 and 512 words whose
+// rings fit `smem_budget`, most warps first.
+std::vector<StreamPlan> candidate_plans(const Schedule& sc, int elem, size_t smem_budget);
+
+// Builds one plan's stream, with the backward substitution when the
+// schedule allows it and the plan holds it, else without.
+bool build_plan(const Schedule& sc, const StreamPlan& p, Stream& out, std::string& why);
+
 // Host interpreter of a stream for one scenario in FP64.  lu holds the A
 // image in the factor's layout on entry and the factor on exit; X receives
 // y_k (forward substitution) when the schedule fuses it.  Checks every

@@ -153,6 +153,11 @@ class BatchResult:
         return self.status == GOX_CONVERGED
 
 
+def set_autotune(on: bool) -> None:
+    """Turn the refactor-plan autotuner on (default) or off, process-wide."""
+    check(_lib.load().gox_set_autotune(1 if on else 0), "gox_set_autotune")
+
+
 class Topology:
     """A registered topology: Y-bus (CSR) + bus types, resident on the GPU."""
 
@@ -388,6 +393,19 @@ class Topology:
                                                int(value), _p(old, _lib.i32p)),
               "gox_topo_stream_word")
         return int(old[0])
+
+    def tuning(self, precision=GOX_PRECISION_MIXED) -> dict:
+        """The refactor plan in `precision` and the autotuner's timed
+        candidates (gox_topo_tuning)."""
+        plan = np.zeros(6, np.int64)
+        table = np.zeros((64, 4))
+        rows = check(_lib.load().gox_topo_tuning(self._h, int(precision), _p(plan, _lib.i64p),
+                                                 _p(table, _lib.f64p), 64), "gox_topo_tuning")
+        return {"warps": int(plan[0]), "ring_rows": int(plan[1]), "big_rows": int(plan[2]),
+                "chunk_words": int(plan[3]),
+                "source": ("default", "measured", "cached")[int(plan[4])],
+                "candidates": [dict(warps=int(r[0]), chunk_words=int(r[1]), ring_rows=int(r[2]),
+                                    ms=float(r[3])) for r in table[:rows]]}
 
     def info(self) -> dict:
         a = np.zeros(31, np.int64)

@@ -312,6 +312,31 @@ int gox_factor_host(int32_t n, int32_t nnz, const int32_t *rows, const int32_t *
  * info must hold 31 entries.  Returns GOX_E_INVALID before the first solve. */
 int gox_topo_info(const gox_topo *t, int64_t *info);
 
+/* The refactor plan's autotuner (no counterpart in the reference: its KLU
+ * runs one fixed kernel; the nearest knobs are KLU's fixed Options,
+ * src/klu_native/types.rs:73-99).  A topology's first batch in a precision
+ * times the candidate plans of its refactor streams -- warps per CTA (12
+ * down to 4 in FP32, 8 down to 4 in FP64) x stream chunks of 256 / 320 /
+ * 512 words, each compiled and checked on the host first -- on the first
+ * min(G, 152) groups of that batch's first Jacobian (CUDA events, two runs
+ * each) and keeps the fastest.  Choices are cached per process, and in the
+ * file named by $GOX_TUNE_CACHE when set, under (precision, bus count in
+ * half-octave buckets, fill nnz(L+U) / nnz(J) in tenths, batch-size bucket
+ * of 1 / 2-8 / 9-38 / 39-152 / more groups of 32); a later topology with
+ * the same key compiles the cached plan without timing.  Q-limit and
+ * island variants take a cached plan or the default.  gox_set_autotune(0)
+ * turns it off process-wide: the default plan is the most warps that fit. */
+int gox_set_autotune(int32_t on);
+
+/* The plan a topology's refactor runs in `precision`: plan[0] warps per
+ * CTA, [1] ring rows per warp, [2] rows of warp 0's larger ring (0: none),
+ * [3] stream-chunk words, [4] source (0 default, 1 timed by the autotuner,
+ * 2 from its cache), [5] candidates timed.  With `table`, up to max_rows
+ * rows {warps, chunk words, ring rows, ms} of the timed candidates; returns
+ * the rows written, or < 0.  Needs a fixed pivot order. */
+int gox_topo_tuning(const gox_topo *t, int32_t precision, int64_t *plan, double *table,
+                    int32_t max_rows);
+
 /* The fixed factorization structure (klu_extract layout without values):
  * Pnum, Q [n], R [nblocks+1], L pattern Lp [n+1] / Li (rows in pivot order,
  * no unit diagonal), U pattern Up [n+1] / Ui (DFS order, no diagonal).

@@ -1,0 +1,50 @@
+"""GPU: the refactor-plan autotuner.
+
+A topology's first mixed batch times the candidate plans of its refactor
+streams and keeps the fastest; a second topology with the same key (bus
+count, fill, batch-size bucket) takes the cached plan without timing.  The
+plan only reschedules the same operations: every candidate gives the same
+results, bit for bit, as the default plan."""
+import numpy as np
+import pytest
+
+from gridoxide_gb300 import grids as G
+from gridoxide_gb300 import solver as S
+from helpers import grid_from_fixture, load_fixture, ybus_from_fixture
+
+pytestmark = pytest.mark.gpu
+
+
+def test_autotuner_times_candidates_caches_and_keeps_results(gox):
+    fx = load_fixture("case2000")
+    g, yb = grid_from_fixture(fx), ybus_from_fixture(fx)
+    p, q = G.load_scenarios(g, 256, 0.15, 606)
+    kw = dict(tol=1e-8, max_iter=20, precision=gox.GOX_PRECISION_MIXED)
+    S.set_autotune(False)
+    try:
+        base = gox.Topology(yb, g.bus_type)
+        ref = base.solve(p, q, g.vm, g.va, **kw)
+        assert base.tuning()["source"] == "default"
+    finally:
+        S.set_autotune(True)
+    # the first topology of this key in the process times the candidates,
+    # the next one reuses the choice
+    t1 = gox.Topology(yb, g.bus_type)
+    r1 = t1.solve(p, q, g.vm, g.va, **kw)
+    tu = t1.tuning()
+    if tu["source"] == "measured":
+        ms = [c["ms"] for c in tu["candidates"]]
+        assert len(ms) >= 3
+        chosen = [c for c in tu["candidates"]
+                  if c["warps"] == tu["warps"] and c["chunk_words"] == tu["chunk_words"]]
+        assert chosen and chosen[0]["ms"] == min(ms)
+    else:  # another test of this process tuned this key first
+        assert tu["source"] == "cached"
+    t2 = gox.Topology(yb, g.bus_type)
+    r2 = t2.solve(p, q, g.vm, g.va, **kw)
+    assert t2.tuning()["source"] == "cached"
+    assert (t2.tuning()["warps"], t2.tuning()["chunk_words"]) == (tu["warps"], tu["chunk_words"])
+    for r in (r1, r2):
+        np.testing.assert_array_equal(r.voltage_mag, ref.voltage_mag)
+        np.testing.assert_array_equal(r.voltage_ang, ref.voltage_ang)
+        np.testing.assert_array_equal(r.iterations, ref.iterations)
