@@ -267,6 +267,7 @@ struct DevSchedule {
       st[i].rows_total = ring_total(ss[i]->plan);
       st[i].chunk_words = ss[i]->plan.chunk_words;
       st[i].n_bars = ss[i]->n_bars;
+      st[i].sync = ss[i]->plan.sync;
       st_nw[i] = ss[i]->plan.nw;
       st_smem[i] = stream_smem_bytes(ss[i]->plan);
       st_bwd[i] = ss[i]->has_bwd;
@@ -454,12 +455,17 @@ static constexpr int kWarps = 8;  // warps per CTA of the group kernels
 // Dynamic shared memory the refactor may use per CTA (of 227 KB).
 static constexpr size_t kRefactorSmem = 225 * 1024;
 
+// How the default refactor plan ends its levels: 1 per-warp progress flags,
+// 0 CTA barriers (gox_set_refactor_sync).
+static std::atomic<int> g_refactor_sync{0};
+
 // Compiles the refactor streams of a schedule for both precisions.
 static void make_streams(const Schedule& sc, Stream& s32, Stream& s64) {
   std::string why;
-  if (!choose_stream(sc, 4, kRefactorSmem, s32, why))
+  const int sync = g_refactor_sync.load();
+  if (!choose_stream(sc, 4, kRefactorSmem, s32, why, sync))
     throw std::runtime_error("refactor schedule (FP32): " + why);
-  if (!choose_stream(sc, 8, kRefactorSmem, s64, why))
+  if (!choose_stream(sc, 8, kRefactorSmem, s64, why, sync))
     throw std::runtime_error("refactor schedule (FP64): " + why);
   // every stream runs once through the checking host interpreter before a
   // GPU sees it (indices, copies waited for, no cross-warp conflicts)
@@ -659,7 +665,7 @@ struct gox_topo {
   struct Tuning {
     bool done = false;
     int source = 0;  // 0 the default (most warps), 1 measured here, 2 from the cache
-    std::vector<std::array<double, 4>> table;  // timed candidates: warps, chunk words, ring rows, ms
+    std::vector<std::array<double, 5>> table;  // timed candidates: warps, chunk words, ring rows, ms, sync
   } tune[2];
   // split solves: a second instance of this topology (same pivot order, own
   // device buffers and stream) that solves the second half of a large batch
@@ -1019,7 +1025,7 @@ static void pivot_run(gox_topo* t, BatchDev& D, cudaStream_t st) {
 // (the most warps that fit).
 
 static std::mutex g_tune_mu;
-static std::map<std::array<int, 4>, std::array<int, 2>> g_tune;  // key -> {warps, chunk words}
+static std::map<std::array<int, 4>, std::array<int, 3>> g_tune;  // key -> {warps, chunk words, sync}
 static bool g_tune_loaded = false;
 static std::atomic<int> g_autotune{1};
 
@@ -1038,18 +1044,18 @@ static void tune_cache_load() {
   if (!path || !*path) return;
   FILE* f = std::fopen(path, "r");
   if (!f) return;
-  int a, b, c, d, nw, cw;
-  while (std::fscanf(f, "gox-tune-1 %d %d %d %d %d %d\n", &a, &b, &c, &d, &nw, &cw) == 6)
-    g_tune[{a, b, c, d}] = {nw, cw};
+  int a, b, c, d, nw, cw, sy;
+  while (std::fscanf(f, "gox-tune-2 %d %d %d %d %d %d %d\n", &a, &b, &c, &d, &nw, &cw, &sy) == 7)
+    g_tune[{a, b, c, d}] = {nw, cw, sy};
   std::fclose(f);
 }
 
-static void tune_cache_store(const std::array<int, 4>& k, int nw, int cw) {
-  g_tune[k] = {nw, cw};
+static void tune_cache_store(const std::array<int, 4>& k, int nw, int cw, int sy) {
+  g_tune[k] = {nw, cw, sy};
   const char* path = std::getenv("GOX_TUNE_CACHE");
   if (!path || !*path) return;
   if (FILE* f = std::fopen(path, "a")) {
-    std::fprintf(f, "gox-tune-1 %d %d %d %d %d %d\n", k[0], k[1], k[2], k[3], nw, cw);
+    std::fprintf(f, "gox-tune-2 %d %d %d %d %d %d %d\n", k[0], k[1], k[2], k[3], nw, cw, sy);
     std::fclose(f);
   }
 }
@@ -1109,12 +1115,13 @@ static void autotune(gox_topo* t, const BatchDev& D, cudaStream_t st) {
     if (it == g_tune.end() && t->tune_cache_only) return;
     if (it != g_tune.end()) {
       const Stream& cur = i == 0 ? t->s32 : t->s64;
-      if (cur.plan.nw == it->second[0] && cur.plan.chunk_words == it->second[1]) {
+      if (cur.plan.nw == it->second[0] && cur.plan.chunk_words == it->second[1] &&
+          cur.plan.sync == it->second[2]) {
         TU.source = 2;
         return;
       }
       for (const StreamPlan& p : candidate_plans(sc, elem, kRefactorSmem))
-        if (p.nw == it->second[0] && p.chunk_words == it->second[1]) {
+        if (p.nw == it->second[0] && p.chunk_words == it->second[1] && p.sync == it->second[2]) {
           Stream s;
           if (compile_checked(sc, p, s)) {
             install_stream(t, i, std::move(s));
@@ -1164,6 +1171,7 @@ static void autotune(gox_topo* t, const BatchDev& D, cudaStream_t st) {
     P.rows_total = ring_total(s.plan);
     P.chunk_words = s.plan.chunk_words;
     P.n_bars = s.n_bars;
+    P.sync = s.plan.sync;
     float ms = 0.0f;
     for (int rep = 0; rep < 2; rep++) {
       GOX_CK(cudaMemcpyAsync(D.lu, bak.p, img_bytes, cudaMemcpyDeviceToDevice, st));
@@ -1183,7 +1191,7 @@ static void autotune(gox_topo* t, const BatchDev& D, cudaStream_t st) {
       continue;
     }
     TU.table.push_back({(double)s.plan.nw, (double)s.plan.chunk_words, (double)s.plan.ring_rows,
-                        (double)ms});
+                        (double)ms, (double)s.plan.sync});
     if (ms < best_ms) {
       best_ms = ms;
       best = (int)c;
@@ -1195,11 +1203,11 @@ static void autotune(gox_topo* t, const BatchDev& D, cudaStream_t st) {
   cudaEventDestroy(e0);
   cudaEventDestroy(e1);
   if (best < 0) return;
-  const int nw = cand[best].nw, cw = cand[best].chunk_words;
+  const int nw = cand[best].nw, cw = cand[best].chunk_words, sy = cand[best].sync;
   install_stream(t, i, std::move(built[best]));
   TU.source = 1;
   std::lock_guard<std::mutex> lk(g_tune_mu);
-  tune_cache_store(key, nw, cw);
+  tune_cache_store(key, nw, cw, sy);
 }
 
 template <typename T>
@@ -2841,6 +2849,11 @@ int gox_set_autotune(int32_t on) {
   return GOX_OK;
 }
 
+int gox_set_refactor_sync(int32_t flags) {
+  g_refactor_sync.store(flags ? 1 : 0);
+  return GOX_OK;
+}
+
 int gox_topo_tuning(const gox_topo* t, int32_t precision, int64_t* plan, double* table,
                     int32_t max_rows) {
   if (!t || !plan || (precision != GOX_PRECISION_FP64 && precision != GOX_PRECISION_MIXED))
@@ -2855,10 +2868,11 @@ int gox_topo_tuning(const gox_topo* t, int32_t precision, int64_t* plan, double*
   plan[3] = s.plan.chunk_words;
   plan[4] = TU.source;
   plan[5] = (int64_t)TU.table.size();
+  plan[6] = s.plan.sync;
   int rows = 0;
   for (const auto& r : TU.table) {
     if (!table || rows >= max_rows) break;
-    for (int c = 0; c < 4; c++) table[(size_t)rows * 4 + c] = r[c];
+    for (int c = 0; c < 5; c++) table[(size_t)rows * 5 + c] = r[c];
     rows++;
   }
   return rows;
@@ -2891,6 +2905,9 @@ int gox_topo_info(const gox_topo* t, int64_t* info) {
   info[30] = t->graph_solves;
   info[26] = a.has_bwd ? 1 : 0;
   info[27] = b.has_bwd ? 1 : 0;
+  info[31] = a.plan.sync;
+  info[32] = a.n_waitp;
+  info[33] = a.n_wait_reqs;
   return GOX_OK;
 }
 

@@ -635,7 +635,37 @@ struct StreamDev {
   const int32_t* nchunks;
   int ring_rows, chunk_words, n_bars;
   int rows_total;  // rows of all rings (the zero row follows them)
+  int sync;        // levels end in: 0 CTA barriers, 1 per-warp progress flags
 };
+
+// Progress flags (plans with sync = 1).  A warp that has done its work of
+// the first n levels publishes n: every lane fences its shared and global
+// writes (and the copies it waited for) at CTA scope, the warp meets, and
+// lane 0 stores n with release semantics.  A warp waits for another's count
+// with acquire loads by all lanes, a bounded number of polls, and gives up
+// early once any warp of the CTA has failed.
+__device__ __forceinline__ void publish_level(int* prog, int warp, int lane, int n) {
+  __threadfence_block();
+  __syncwarp();
+  if (lane == 0)
+    asm volatile("st.release.cta.shared.b32 [%0], %1;\n" ::"r"(smem_u32(prog + warp)), "r"(n)
+                 : "memory");
+}
+__device__ __forceinline__ int ld_acquire_s32(const int* p) {
+  int v;
+  asm volatile("ld.acquire.cta.shared.b32 %0, [%1];\n" : "=r"(v) : "r"(smem_u32(p)) : "memory");
+  return v;
+}
+// m words v | n << 8 (warp v has published n levels); false when a wait gave up
+__device__ __forceinline__ bool wait_levels(const int32_t* w, int m, const int* prog,
+                                            const volatile int* failed) {
+  for (int q = 0; q < m; q++) {
+    const int v = w[q] & 0xff, need = (int)(((uint32_t)w[q]) >> 8);
+    for (int it = 0; !__all_sync(0xffffffffu, ld_acquire_s32(prog + v) >= need); it++)
+      if (__any_sync(0xffffffffu, it >= kSpinLimit || *failed != 0)) return false;
+  }
+  return true;
+}
 
 // Pieces of the refactor interpreter.  Every loop below runs over counts the
 // stream compiler padded (gather rows to 2 copies, steps to pairs, forward
@@ -843,7 +873,8 @@ __global__ void __launch_bounds__(sizeof(T) == 4 ? 32 * kMaxRefactorWarps : 256,
   extern __shared__ __align__(128) unsigned char smem_raw[];
   __shared__ __align__(8) uint64_t mbar[kMaxRefactorWarps][2];
   __shared__ int flags[2][32];
-  __shared__ int timed_out;
+  __shared__ int prog[kMaxRefactorWarps];  // levels each warp has published (progress flags)
+  __shared__ volatile int timed_out;
   constexpr uint32_t RB = R::RB;
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
   const int CW = P.chunk_words;
@@ -859,6 +890,7 @@ __global__ void __launch_bounds__(sizeof(T) == 4 ? 32 * kMaxRefactorWarps : 256,
   bool bad = false, tiny = false;
 
   if (threadIdx.x < 64) (&flags[0][0])[threadIdx.x] = 0;
+  if (threadIdx.x < kMaxRefactorWarps) prog[threadIdx.x] = 0;
   if (threadIdx.x == 0) timed_out = 0;
   if (lane == 0) {
     mbar_init(&mbar[warp][0]);
@@ -883,7 +915,7 @@ __global__ void __launch_bounds__(sizeof(T) == 4 ? 32 * kMaxRefactorWarps : 256,
   bool ok = mbar_wait(&mbar[warp][0], par0);
   if (ok) waited0++;
   par0 ^= 1u;
-  int chunk = 0, buf = 0, pc = 0, bars = 0;
+  int chunk = 0, buf = 0, pc = 0, bars = 0, lev = 0;
   const int32_t* cb = cbuf;
   while (ok) {
     const int32_t w0 = cb[pc];
@@ -917,8 +949,12 @@ __global__ void __launch_bounds__(sizeof(T) == 4 ? 32 * kMaxRefactorWarps : 256,
       if (!((w0 >> 10) & 1)) R::finish(k, base, ulen, llen, st_lane, LUg, Xg, lane, fuse, ptol, bad, tiny);
       pc = sw + 4 * nst + nfw;
       if ((w0 >> 8) & 1) {
-        __syncthreads();
-        bars++;
+        if (P.sync) {
+          publish_level(prog, warp, lane, ++lev);
+        } else {
+          __syncthreads();
+          bars++;
+        }
       }
     } else if (op == CMD_BWD) {
       const uint32_t w2 = (uint32_t)cb[pc + 2], w3 = (uint32_t)cb[pc + 3], w4 = (uint32_t)cb[pc + 4];
@@ -942,8 +978,12 @@ __global__ void __launch_bounds__(sizeof(T) == 4 ? 32 * kMaxRefactorWarps : 256,
              Xg + (size_t)k * 32u + lane, bad);
       pc += 5 + nlate + npref + m;
       if ((w0 >> 8) & 1) {
-        __syncthreads();
-        bars++;
+        if (P.sync) {
+          publish_level(prog, warp, lane, ++lev);
+        } else {
+          __syncthreads();
+          bars++;
+        }
       }
     } else {
       switch (op) {
@@ -983,10 +1023,29 @@ __global__ void __launch_bounds__(sizeof(T) == 4 ? 32 * kMaxRefactorWarps : 256,
           break;
         }
         case CMD_BAR:
+          if (P.sync) {  // not in a plan with progress flags
+            ok = false;
+            break;
+          }
           __syncthreads();
           bars++;
           pc++;
           break;
+        case CMD_PUB:
+          lev = (int)(((uint32_t)w0) >> 4);
+          publish_level(prog, warp, lane, lev);
+          pc++;
+          break;
+        case CMD_WAITP: {
+          const int m = (w0 >> 4) & 0xff;
+          if (!P.sync || pc + 1 + m >= CW || !wait_levels(cb + pc + 1, m, prog, &timed_out)) {
+            ok = false;
+            break;
+          }
+          __syncwarp();
+          pc += 1 + m;
+          break;
+        }
         case CMD_NOP:
           pc++;
           break;
@@ -1027,7 +1086,7 @@ __global__ void __launch_bounds__(sizeof(T) == 4 ? 32 * kMaxRefactorWarps : 256,
   }
 done:
   if (!ok) {
-    if (lane == 0) atomicExch(&timed_out, 1);
+    if (lane == 0) atomicExch((int*)&timed_out, 1);
     asm volatile("cp.async.wait_all;\n" ::: "memory");
     // stream chunks still being copied into this warp's buffers: wait for
     // them (each wait bounded) so no copy lands after the CTA has exited

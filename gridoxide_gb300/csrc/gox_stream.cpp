@@ -128,6 +128,10 @@ struct Builder {
   bool with_bwd = false;  // the backward substitution runs in the stream too
   bool with_pre = true;   // narrow levels' columns run their prefix one level early
   bool with_helpers = true;  // idle warps issue the copies of busy warps' next tasks
+  // Plans with progress flags: per warp and level, the WAITP words that open
+  // the warp's work of that level (from the analysis of the barrier form).
+  const std::vector<std::vector<std::vector<int32_t>>>* reqs = nullptr;
+  std::vector<int64_t> last_pub;  // per warp: word index of its last PUB (-1: none to raise)
 
   Builder(const Schedule& s, const StreamPlan& p) : sc(s), P(p) {
     W = p.nw;
@@ -1066,6 +1070,11 @@ struct Builder {
     wcost.assign(W, 0.0);
     pinned.assign(W, 0);
     hpend.assign(W, {});
+    last_pub.assign(W, -1);
+    if (P.sync && (!reqs || (int)reqs->size() != W)) {
+      err = "progress flags without their analysis";
+      return false;
+    }
     std::vector<int> wnext(W, 0);
     for (int L = 0; L < NL; L++) {
       for (int w = 0; w < W; w++) { pos[w] = 0; pinned[w] = 0; }
@@ -1105,13 +1114,41 @@ struct Builder {
       auto bar = [&](int w) {
         helper_wait(w, L);
         Emit& e = em[w];
-        if (last_colhdr[w] >= 0 && last_colend[w] == (int64_t)e.w.size()) {
-          e.w[last_colhdr[w]] |= (1 << 8);  // the level's barrier rides on the last column
+        const bool rides = last_colhdr[w] >= 0 && last_colend[w] == (int64_t)e.w.size();
+        const int64_t rides_at = last_colhdr[w];
+        last_colhdr[w] = -1;
+        if (P.sync == 0) {
+          if (rides) {
+            e.w[rides_at] |= (1 << 8);  // the level's barrier rides on the last column
+          } else {
+            e.need(1);
+            e.w.push_back(CMD_BAR);
+          }
+          return;
+        }
+        // progress flags: L + 1 levels done, published by the last column or
+        // by PUB (an idle stretch of levels takes one PUB, raised in place);
+        // then the waits that open the warp's next level
+        if (rides) {
+          e.w[rides_at] |= (1 << 8);
+          last_pub[w] = -1;
+        } else if (last_pub[w] >= 0 && last_pub[w] + 1 == (int64_t)e.w.size()) {
+          e.w[last_pub[w]] = CMD_PUB | ((L + 1) << 4);
         } else {
           e.need(1);
-          e.w.push_back(CMD_BAR);
+          last_pub[w] = (int64_t)e.w.size();
+          e.w.push_back(CMD_PUB | ((L + 1) << 4));
         }
-        last_colhdr[w] = -1;
+        if (L + 1 < NL) {
+          const std::vector<int32_t>& rq = (*reqs)[w][L + 1];
+          if (!rq.empty()) {
+            e.need(1 + rq.size());
+            e.w.push_back(CMD_WAITP | ((int32_t)rq.size() << 4));
+            for (int32_t x : rq) e.w.push_back(x);
+            out->n_waitp++;
+            out->n_wait_reqs += (int64_t)rq.size();
+          }
+        }
       };
       for (int w = 0; w < W; w++) {
         if (idle[w]) continue;
@@ -1162,7 +1199,8 @@ struct Builder {
       }
       st.est_cycles += *std::max_element(wcost.begin(), wcost.end()) + 120;
     }
-    st.n_bars = NL;
+    st.n_levels = NL;
+    st.n_bars = P.sync ? 0 : NL;
     st.has_bwd = with_bwd;
     // ---- assemble
     st.chunk0.assign(W, 0);
@@ -1182,12 +1220,36 @@ struct Builder {
 }  // namespace
 
 static bool choose_stream_1(const Schedule& sc, int elem, size_t smem_budget, Stream& out,
-                            std::string& why, bool with_bwd);
+                            std::string& why, bool with_bwd, int sync);
+
+using WaitLists = std::vector<std::vector<std::vector<int32_t>>>;
+static std::string interpret(const Schedule& sc, const Stream& st, std::vector<double>& lu,
+                             const std::vector<double>& rhs, std::vector<double>& X,
+                             bool& singular, WaitLists* reqs);
 
 bool build_stream(const Schedule& sc, const StreamPlan& plan, Stream& out, std::string& why,
                   bool with_bwd) {
+  WaitLists reqs;
+  if (plan.sync) {
+    // the barrier form of the same schedule, run through the interpreter to
+    // find each level's waits; the flag form is then emitted with them (the
+    // builder makes the same decisions for both: no placement depends on
+    // where commands fall in the stream chunks)
+    StreamPlan pb = plan;
+    pb.sync = 0;
+    Stream sb;
+    if (!build_stream(sc, pb, sb, why, with_bwd)) return false;
+    std::vector<double> lu(sc.n_slots, 1.0), rhs(sc.n_u, 0.0), X;
+    bool sing = false;
+    const std::string e = interpret(sc, sb, lu, rhs, X, sing, &reqs);
+    if (!e.empty()) {
+      why = "progress-flag analysis: " + e;
+      return false;
+    }
+  }
   Builder b(sc, plan);
   b.with_bwd = with_bwd;
+  if (plan.sync) b.reqs = &reqs;
   bool ok = false;
   try {
     ok = b.build(out);
@@ -1200,11 +1262,11 @@ bool build_stream(const Schedule& sc, const StreamPlan& plan, Stream& out, std::
 }
 
 bool choose_stream(const Schedule& sc, int elem, size_t smem_budget, Stream& out,
-                   std::string& why) {
+                   std::string& why, int sync) {
   // with the backward substitution in the stream when the schedule allows
   // it (no off-diagonal BTF entries), else (or when no plan holds it) without
   for (bool bwd : {sc.fuse_fwd, false}) {
-    if (choose_stream_1(sc, elem, smem_budget, out, why, bwd)) return true;
+    if (choose_stream_1(sc, elem, smem_budget, out, why, bwd, sync)) return true;
     if (!bwd) break;
   }
   return false;
@@ -1244,7 +1306,11 @@ std::vector<StreamPlan> candidate_plans(const Schedule& sc, int elem, size_t sme
     if (nw > (elem == 4 ? kMaxRefactorWarps : 8)) continue;
     for (int cw : {256, 320, 512}) {
       StreamPlan p;
-      if (plan_for(sc, elem, smem_budget, nw, cw, p)) out.push_back(p);
+      if (!plan_for(sc, elem, smem_budget, nw, cw, p)) continue;
+      for (int sync : {1, 0}) {
+        p.sync = sync;
+        out.push_back(p);
+      }
     }
   }
   return out;
@@ -1259,13 +1325,14 @@ bool build_plan(const Schedule& sc, const StreamPlan& p, Stream& out, std::strin
 }
 
 static bool choose_stream_1(const Schedule& sc, int elem, size_t smem_budget, Stream& out,
-                            std::string& why, bool with_bwd) {
+                            std::string& why, bool with_bwd, int sync) {
   bool found = false;
   std::string last;
   for (int nw : {12, 10, 8, 6, 4, 3, 2, 1}) {
     if (nw > (elem == 4 ? kMaxRefactorWarps : 8)) continue;
     StreamPlan p;
     if (!plan_for(sc, elem, smem_budget, nw, nw >= 10 ? 320 : 512, p)) continue;
+    p.sync = sync;
     Stream s;
     std::string w;
     if (!build_stream(sc, p, s, w, with_bwd)) {
@@ -1286,12 +1353,23 @@ static bool choose_stream_1(const Schedule& sc, int elem, size_t smem_budget, St
 std::string run_stream_host(const Schedule& sc, const Stream& st, std::vector<double>& lu,
                             const std::vector<double>& rhs, std::vector<double>& X,
                             bool& singular) {
+  return interpret(sc, st, lu, rhs, X, singular, nullptr);
+}
+
+// The interpreter proper.  With `reqs` it analyses a barrier-form stream:
+// barriers order nothing, and every access that conflicts with an earlier
+// one of another warp not yet ordered before it adds a wait to the warp's
+// current level (reqs[w][L]: words v | n << 8), as the flag form will.
+static std::string interpret(const Schedule& sc, const Stream& st, std::vector<double>& lu,
+                             const std::vector<double>& rhs, std::vector<double>& X,
+                             bool& singular, WaitLists* reqs) {
   const StreamPlan& P = st.plan;
   const int W = P.nw, CW = P.chunk_words, n = sc.n_u;
   const int T = ring_total(P);
   const int rows = T + kSpareRows;
   const int zero_row = T, trash_row = T + 1;
   const int rpi2 = 2 * (512 / (32 * P.elem));
+  const int NLv = st.n_levels;
   std::vector<double> ring(rows, 0.0);
   std::vector<int> pend(rows, -1);  // commit group of a copy not yet waited for
   std::vector<int> col_of_slot(sc.n_slots, -1);
@@ -1300,7 +1378,87 @@ std::string run_stream_host(const Schedule& sc, const Stream& st, std::vector<do
   std::vector<int> colfin(n, -1), xfin(n, -1), bfin(n, -1);  // level of FINISH / BWD
   singular = false;
   if ((int)lu.size() != sc.n_slots || (int)rhs.size() != n) return "buffer sizes";
+  if (NLv <= 0 || NLv >= 32000) return "level count out of range";
   X.assign(n, 0.0);
+  // ---- happens-before between warps (progress-flag plans and the analysis)
+  const bool flags = P.sync != 0, analyze = reqs != nullptr;
+  const bool vcs = flags || analyze;
+  if (flags && analyze) return "analysis of a stream that already has progress flags";
+  // vc[w][v]: levels of warp v known to warp w to be done; pubvc[v][p]: v's
+  // clock when it had published p levels; per access key (ring rows, then
+  // factor slots and solution rows in global memory): the last writer and
+  // its level, and per warp the last level it read the key since
+  const int K = rows + sc.n_slots + n;
+  std::vector<int> vc, pubvc, published(W, 0), lw_w, lw_l;
+  std::vector<int16_t> rdl;
+  if (vcs) {
+    vc.assign((size_t)W * W, 0);
+    pubvc.assign((size_t)W * (NLv + 1) * W, 0);
+    lw_w.assign(K, -1);
+    lw_l.assign(K, -1);
+    rdl.assign((size_t)K * W, -1);
+  }
+  if (analyze) reqs->assign(W, std::vector<std::vector<int32_t>>(NLv));
+  auto join = [&](int w, int v, int p) {
+    const int* src = &pubvc[((size_t)v * (NLv + 1) + p) * W];
+    for (int u = 0; u < W; u++) vc[(size_t)w * W + u] = std::max(vc[(size_t)w * W + u], src[u]);
+  };
+  auto publish = [&](int w, int p) {
+    if (!vcs) return;
+    vc[(size_t)w * W + w] = p;
+    for (int q = published[w] + 1; q <= p; q++)
+      std::copy(&vc[(size_t)w * W], &vc[(size_t)w * W] + W, &pubvc[((size_t)w * (NLv + 1) + q) * W]);
+    published[w] = std::max(published[w], p);
+  };
+  // warp w, in level L, needs warp v's first p levels done
+  std::string vce;
+  auto need = [&](int w, int L, int v, int p) -> bool {
+    if (v == w || p <= 0 || vc[(size_t)w * W + v] >= p) return true;
+    if (p > L) {
+      vce = "conflicts with warp " + std::to_string(v) + " within level " + std::to_string(L);
+      return false;
+    }
+    if (!analyze) {
+      vce = "conflicts with warp " + std::to_string(v) + "'s level " + std::to_string(p - 1) +
+            " without a wait for it";
+      return false;
+    }
+    if (published[v] < p) {
+      vce = "depends on a level of warp " + std::to_string(v) + " not yet published";
+      return false;
+    }
+    std::vector<int32_t>& rq = (*reqs)[w][L];
+    bool found = false;
+    for (int32_t& x : rq)
+      if ((x & 0xff) == v) {
+        x = v | (std::max(x >> 8, p) << 8);
+        found = true;
+      }
+    if (!found) rq.push_back(v | (p << 8));
+    join(w, v, p);
+    return true;
+  };
+  auto acc_r = [&](int key, int w, int L) -> bool {
+    if (!vcs) return true;
+    if (lw_w[key] >= 0 && !need(w, L, lw_w[key], lw_l[key] + 1)) return false;
+    int16_t& r = rdl[(size_t)key * W + w];
+    if (r < L) r = (int16_t)L;
+    return true;
+  };
+  auto acc_w = [&](int key, int w, int L) -> bool {
+    if (!vcs) return true;
+    if (lw_w[key] >= 0 && !need(w, L, lw_w[key], lw_l[key] + 1)) return false;
+    for (int v = 0; v < W; v++) {
+      int16_t& r = rdl[(size_t)key * W + v];
+      if (r >= 0 && !need(w, L, v, r + 1)) return false;
+    }
+    for (int v = 0; v < W; v++) rdl[(size_t)key * W + v] = -1;
+    lw_w[key] = w;
+    lw_l[key] = L;
+    return true;
+  };
+  const int gkey = rows;               // factor slot s: gkey + s
+  const int xkey = rows + sc.n_slots;  // solution row k: xkey + k
   struct WS {
     int chunk = 0, pc = 0, ng = 0, bars = 0;
     bool done = false;
@@ -1310,7 +1468,7 @@ std::string run_stream_host(const Schedule& sc, const Stream& st, std::vector<do
   for (int w = 0; w < W; w++) ws[w].pc = st.chunk0[w] * CW;
   // per level: who touched which row
   std::vector<int> wr_by(rows, -1), rd_by(rows, -1), stamp_w(rows, -1), stamp_r(rows, -1);
-  for (int L = 0; L <= st.n_bars; L++) {
+  for (int L = 0; L <= NLv; L++) {
     for (int w = 0; w < W; w++) {
       WS& s = ws[w];
       if (s.done || s.bars > L) continue;  // finished, or already past this level's barrier
@@ -1322,6 +1480,8 @@ std::string run_stream_host(const Schedule& sc, const Stream& st, std::vector<do
       auto in_ring = [&](int r) { return r >= 0 && r < T; };
       auto note_w = [&](int r) -> bool {
         if (r == zero_row) { e = "writes the zero row"; return false; }
+        if (pend[r] >= 0) { e = "row " + std::to_string(r) + " written while a copy into it is in flight"; return false; }
+        if (!acc_w(r, w, L)) { e = vce + " (row " + std::to_string(r) + ")"; return false; }
         if (stamp_w[r] == L && wr_by[r] != w) { e = "two warps write row " + std::to_string(r); return false; }
         if (stamp_r[r] == L && rd_by[r] != w) {
           e = "row " + std::to_string(r) + " written while warp " + std::to_string(rd_by[r]) +
@@ -1334,6 +1494,7 @@ std::string run_stream_host(const Schedule& sc, const Stream& st, std::vector<do
       };
       auto note_r = [&](int r) -> bool {
         if (pend[r] >= 0) { e = "row " + std::to_string(r) + " read before its copy is waited for"; return false; }
+        if (!acc_r(r, w, L)) { e = vce + " (row " + std::to_string(r) + ")"; return false; }
         if (stamp_w[r] == L && wr_by[r] != w) {
           e = "row " + std::to_string(r) + " read while warp " + std::to_string(wr_by[r]) +
               " writes it (level " + std::to_string(L) + ")";
@@ -1372,6 +1533,10 @@ std::string run_stream_host(const Schedule& sc, const Stream& st, std::vector<do
             e = "source row out of range";
             return false;
           }
+          if (src < sc.n_slots + n && !acc_r(gkey + src, w, L)) {
+            e = vce + " (global row " + std::to_string(src) + ")";
+            return false;
+          }
           if (!note_w(dst)) return false;
           ring[dst] = v;
           pend[dst] = s.ng;
@@ -1384,7 +1549,10 @@ std::string run_stream_host(const Schedule& sc, const Stream& st, std::vector<do
         const int upto = s.ng - 1 - m;
         std::vector<int> keep;
         for (int r : s.pend_rows) {
-          if (pend[r] >= 0 && pend[r] <= upto) pend[r] = -1;
+          if (pend[r] >= 0 && pend[r] <= upto) {
+            pend[r] = -1;
+            if (vcs) lw_l[r] = L;  // the copy's write is complete from here on
+          }
           if (pend[r] >= 0) keep.push_back(r);
         }
         s.pend_rows.swap(keep);
@@ -1399,11 +1567,16 @@ std::string run_stream_host(const Schedule& sc, const Stream& st, std::vector<do
           if (lrow + kStepOps > rows) { e = "step L rows out of range"; return false; }
           if (!in_ring(S0 + jp)) { e = "step pivot row out of range"; return false; }
           const uint32_t dw[3] = {d[1], d[2], d[3]};
-          for (int tt = cnt; tt < kStepOps; tt++)
-            if (!in_ring(S0 + (int)((dw[tt / 3] >> (10 * (tt % 3))) & 0x3ff))) {
+          for (int tt = cnt; tt < kStepOps; tt++) {
+            const int ur = S0 + (int)((dw[tt / 3] >> (10 * (tt % 3))) & 0x3ff);
+            if (!in_ring(ur)) {
               e = "unused step slot outside the ring";
               return false;
             }
+            // FP32 steps run all nine updates: the unused ones write their
+            // (dummy) row, which another warp may copy into later
+            if (P.elem == 4 && !note_w(ur)) return false;
+          }
           if (cnt == 0) continue;  // padding step
           if (!note_r(S0 + jp)) return false;
           const double xj = ring[S0 + jp];
@@ -1452,6 +1625,11 @@ std::string run_stream_host(const Schedule& sc, const Stream& st, std::vector<do
         const double piv = ring[S0 + ulen];
         if (piv == 0.0) singular = true;
         const double inv = 1.0 / piv;
+        for (int p = 0; p < len; p++)
+          if (!acc_w(gkey + base + p, w, L)) {
+            e = vce + " (factor slot " + std::to_string(base + p) + ")";
+            return false;
+          }
         for (int p = 0; p <= ulen; p++) lu[base + p] = ring[S0 + p];
         for (int p = ulen + 1; p < len; p++) {
           if (!note_w(S0 + p)) return false;
@@ -1461,9 +1639,21 @@ std::string run_stream_host(const Schedule& sc, const Stream& st, std::vector<do
         colfin[k] = L;
         if (sc.fuse_fwd) {
           if (!note_r(S0 + len)) return false;
+          if (!acc_w(xkey + k, w, L)) {
+            e = vce + " (solution row " + std::to_string(k) + ")";
+            return false;
+          }
           X[k] = ring[S0 + len];
           xfin[k] = L;
         }
+        return true;
+      };
+      // the end of this warp's work of level L (a barrier, or its progress
+      // flag), and the level count it has then done
+      auto level_end = [&](int p) -> bool {
+        if (p <= s.bars || p > NLv) { e = "level count " + std::to_string(p) + " out of order"; return false; }
+        s.bars = p;
+        publish(w, p);
         return true;
       };
       for (;;) {
@@ -1478,11 +1668,38 @@ std::string run_stream_host(const Schedule& sc, const Stream& st, std::vector<do
           break;  // re-enter with the new chunk bounds
         }
         if (op == CMD_END) {
-          if (s.bars != st.n_bars) return fail("END after a wrong number of barriers");
+          if (s.bars != NLv) return fail("END after a wrong number of levels");
           s.done = true;
           break;
         }
-        if (op == CMD_BAR) { s.pc++; s.bars++; break; }
+        if (op == CMD_BAR) {
+          if (flags) return fail("a barrier in a plan with progress flags");
+          if (!level_end(s.bars + 1)) return fail(e);
+          s.pc++;
+          break;
+        }
+        if (op == CMD_PUB) {
+          if (!flags) return fail("a progress flag in a plan with barriers");
+          if (!level_end((int)(((uint32_t)w0) >> 4))) return fail(e);
+          s.pc++;
+          break;
+        }
+        if (op == CMD_WAITP) {
+          if (!flags) return fail("a progress-flag wait in a plan with barriers");
+          const int m = (w0 >> 4) & 0xff;
+          if (m < 1 || m >= W || s.pc + 1 + m > cend) return fail("bad WAITP command");
+          for (int q = 0; q < m; q++) {
+            const int32_t x = st.words[s.pc + 1 + q];
+            const int v = x & 0xff, p = (int)(((uint32_t)x) >> 8);
+            if (v >= W || v == w || p < 1 || p > s.bars) return fail("bad WAITP entry");
+            // in level order every level waited for is published first, so
+            // no warp waits for one that can only come after its own wait
+            if (published[v] < p) return fail("waits for a level not yet published");
+            join(w, v, p);
+          }
+          s.pc += 1 + m;
+          continue;
+        }
         if (op == CMD_GATHER) {
           const int m = (w0 >> 4) & 0xffff;
           if (s.pc + 1 + m > cend) return fail("GATHER past its chunk");
@@ -1549,11 +1766,15 @@ std::string run_stream_host(const Schedule& sc, const Stream& st, std::vector<do
           const double x = v / ring[dr];
           if (!std::isfinite(x)) singular = true;
           if (!note_w(xr)) return fail(e);
+          if (!acc_w(xkey + k, w, L)) return fail(vce + " (solution row " + std::to_string(k) + ")");
           ring[xr] = x;
           X[k] = x;
           bfin[k] = L;
           s.pc = tb + m;
-          if ((w0 >> 8) & 1) { s.bars++; break; }
+          if ((w0 >> 8) & 1) {
+            if (!level_end(s.bars + 1)) return fail(e);
+            break;
+          }
           continue;
         }
         if (op == CMD_COLUMN) {
@@ -1573,7 +1794,10 @@ std::string run_stream_host(const Schedule& sc, const Stream& st, std::vector<do
           if (!sc.fuse_fwd && nf) return fail("forward terms without fusion");
           if (!((w0 >> 10) & 1) && !finish(k, base, ulen, llen, S0)) return fail(e);
           s.pc = sw + 4 * ns + nf;
-          if ((w0 >> 8) & 1) { s.bars++; break; }
+          if ((w0 >> 8) & 1) {
+            if (!level_end(s.bars + 1)) return fail(e);
+            break;
+          }
           continue;
         }
         return fail("bad opcode " + std::to_string(op));

@@ -27,6 +27,23 @@
 //                       and y_k to the forward-substitution vector
 //   NEXT                continue with the warp's next stream chunk
 //   END
+//   PUB n               (plans with progress flags) this warp has finished
+//                       its work of the first n dependency levels
+//   WAITP               (plans with progress flags) wait until the listed
+//                       warps have published the listed level counts
+//
+// Plans synchronize the levels in one of two ways.  With CTA barriers every
+// warp meets every other at the end of every level.  With progress flags
+// each warp publishes, per level, that its work of that level
+// is done, and before its work of a level waits only for the warps whose
+// earlier work it depends on: a value it reads (in a ring or in global
+// memory) that they wrote, or a row it overwrites that they read or wrote.
+// The compiler finds those dependencies by running the barrier form of the
+// same schedule through the host interpreter and recording, for every row,
+// its last writer and its readers since (vector clocks keep the waits to
+// those not already implied by earlier ones); the flag form then carries
+// exactly those waits, and the interpreter checks it again with the flag
+// semantics.
 //
 // Shared memory: per warp two stream chunks (TMA bulk copies) and a ring of
 // rows; the rings of all warps form one row space, so a step may read the
@@ -51,7 +68,9 @@ enum : int32_t {
   CMD_END = 7,
   CMD_FWD = 8,
   CMD_COLUMN = 9,
-  CMD_BWD = 10
+  CMD_BWD = 10,
+  CMD_PUB = 11,
+  CMD_WAITP = 12
 };
 enum : int32_t { ARR_LU = 0, ARR_X = 1, ARR_RHS = 2 };
 
@@ -92,6 +111,12 @@ constexpr int kMaxRefactorWarps = 12;  // FP32 plans; FP64 plans up to 8 (regist
 //           k, x_row | y_row << 16, d_row | m << 16, nlate | npref << 16; then
 //           the nlate and npref gather words, then m terms u_row | x_row << 16
 //           (U(k, j) and x_j; a multiple of 8, padded on the zero row)
+//   PUB     w0 = op | n << 4: levels 0 .. n-1 of this warp are done (its
+//           writes, and the copies it waited for, are visible to the CTA)
+//   WAITP   w0 = op | m << 4, then m words v | n << 8: wait until warp v
+//           has published at least n levels (bounded waits)
+//   With progress flags, bit 8 of COLUMN / BWD (bar_after) publishes the
+//   next level count instead of a barrier.
 // Gather word counts are multiples of 2 copies (8 rows FP32, 4 FP64), step
 // counts are even, forward term counts multiples of 8 (padding as above);
 // 8 words after a command's last step stay inside its chunk (the step loop
@@ -103,6 +128,7 @@ struct StreamPlan {
   int big_rows = 0;         // ring rows of warp 0 when larger (columns too
                             // long for the other rings run there); 0: ring_rows
   int chunk_words = 512;    // stream chunk, 32-bit words (multiple of 4)
+  int sync = 0;             // levels: 0 CTA barriers, 1 per-warp progress flags
 };
 // The rings in the row space: warp 0's first, then the others'.
 inline int ring_size(const StreamPlan& p, int w) {
@@ -119,12 +145,14 @@ struct Stream {
   StreamPlan plan;
   std::vector<int32_t> words;            // all chunks; warp w owns chunks chunk0[w] ..
   std::vector<int32_t> chunk0, nchunks;  // per warp
-  int n_bars = 0;
+  int n_levels = 0;  // dependency levels (refactor, then backward substitution)
+  int n_bars = 0;    // CTA barriers the stream takes (n_levels, or 0 with progress flags)
   bool has_bwd = false;  // the stream also runs the backward substitution
   // statistics of the schedule
   int64_t rows_gathered = 0, rows_prefetched = 0, rows_resident = 0, rows_late = 0;
   int64_t rows_jit = 0, n_steps = 0, n_waits = 0, n_groups = 0, n_column_cmds = 0, n_pre = 0;
   int64_t rows_helper = 0;  // rows copied by warps idle in the level, for other warps' tasks
+  int64_t n_waitp = 0, n_wait_reqs = 0;  // progress-flag waits: commands, warps waited for
   double est_cycles = 0;  // rough critical-path estimate, used to choose a plan
 };
 
@@ -138,18 +166,20 @@ bool build_stream(const Schedule& sc, const StreamPlan& plan, Stream& out, std::
                   bool with_bwd = false);
 
 // Chooses the plan within `smem_budget` bytes: the most warps (up to 12 in
-// FP32, 8 in FP64) whose rings hold the schedule, and builds its stream.
+// FP32, 8 in FP64) whose rings hold the schedule, with the levels' `sync`
+// (1 progress flags, 0 barriers), and builds its stream.
 // (Measured on GB300, case2000 x 4096 FP32, refactor with both
 // substitutions: 8 / 10 / 11 / 12 warps took 2.31 / 2.23 / 2.20 / 2.17 ms
 // with 512-, 512-, 256- and 320-word chunks; more warps hide more of the
 // latencies of the wide levels and give the narrow ones more idle warps to
 // issue copies, and smaller chunks leave the rings room.)
 bool choose_stream(const Schedule& sc, int elem, size_t smem_budget, Stream& out,
-                   std::string& why);
+                   std::string& why, int sync = 1);
 
 // The plans an autotuner may time: every warp count (12 down to 4 in FP32,
 // 8 down to 4 in FP64) with stream chunks of 256, 320 and 512 words whose
-// rings fit `smem_budget`, most warps first.
+// rings fit `smem_budget`, each with progress flags and with barriers,
+// most warps first.
 std::vector<StreamPlan> candidate_plans(const Schedule& sc, int elem, size_t smem_budget);
 
 // Builds one plan's stream, with the backward substitution when the
@@ -161,8 +191,12 @@ bool build_plan(const Schedule& sc, const StreamPlan& p, Stream& out, std::strin
 // y_k (forward substitution) when the schedule fuses it.  Checks every
 // index, that no row is read before the copy into it is waited for, that
 // no copy reads a value before the level that finishes it, and that no two
-// warps touch a row within one level when one of them writes it.  Returns
-// an empty string, or the first violation.
+// warps touch a row within one level when one of them writes it; for a
+// plan with progress flags also that every access that conflicts with an
+// earlier one of another warp (ring rows, factor values and the solution
+// vector in global memory) comes after a wait that orders the two, and
+// that every wait is for a level published earlier in level order (so no
+// warp can wait forever).  Returns an empty string, or the first violation.
 std::string run_stream_host(const Schedule& sc, const Stream& st, std::vector<double>& lu,
                             const std::vector<double>& rhs, std::vector<double>& X,
                             bool& singular);

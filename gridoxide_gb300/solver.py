@@ -158,6 +158,13 @@ def set_autotune(on: bool) -> None:
     check(_lib.load().gox_set_autotune(1 if on else 0), "gox_set_autotune")
 
 
+def set_refactor_sync(progress_flags: bool) -> None:
+    """How the default refactor plan of topologies analysed from now on ends
+    its dependency levels: per-warp progress flags or CTA barriers (the
+    default; gox_set_refactor_sync); the results are the same bit for bit."""
+    check(_lib.load().gox_set_refactor_sync(1 if progress_flags else 0), "gox_set_refactor_sync")
+
+
 class Topology:
     """A registered topology: Y-bus (CSR) + bus types, resident on the GPU."""
 
@@ -397,18 +404,20 @@ class Topology:
     def tuning(self, precision=GOX_PRECISION_MIXED) -> dict:
         """The refactor plan in `precision` and the autotuner's timed
         candidates (gox_topo_tuning)."""
-        plan = np.zeros(6, np.int64)
-        table = np.zeros((64, 4))
+        plan = np.zeros(7, np.int64)
+        table = np.zeros((128, 5))
         rows = check(_lib.load().gox_topo_tuning(self._h, int(precision), _p(plan, _lib.i64p),
-                                                 _p(table, _lib.f64p), 64), "gox_topo_tuning")
+                                                 _p(table, _lib.f64p), 128), "gox_topo_tuning")
         return {"warps": int(plan[0]), "ring_rows": int(plan[1]), "big_rows": int(plan[2]),
                 "chunk_words": int(plan[3]),
                 "source": ("default", "measured", "cached")[int(plan[4])],
+                "progress_flags": bool(plan[6]),
                 "candidates": [dict(warps=int(r[0]), chunk_words=int(r[1]), ring_rows=int(r[2]),
-                                    ms=float(r[3])) for r in table[:rows]]}
+                                    ms=float(r[3]), progress_flags=bool(r[4]))
+                               for r in table[:rows]]}
 
     def info(self) -> dict:
-        a = np.zeros(31, np.int64)
+        a = np.zeros(34, np.int64)
         check(_lib.load().gox_topo_info(self._h, _p(a, _lib.i64p)), "gox_topo_info")
         keys = ["n_u", "nnz_j", "nnz_l", "nnz_u", "nnz_off", "nblocks", "levels", "phases",
                 "lu_slots", "max_collen", "rf32_warps", "rf32_ring_rows", "rf32_est_cycles",
@@ -416,7 +425,8 @@ class Topology:
                 "rf32_rows_just_in_time", "rf32_steps", "rf32_waits", "rf64_warps",
                 "rf64_ring_rows", "rf64_est_cycles", "rf64_rows_in_place", "rf32_column_cmds",
                 "rf32_stream_words", "rf32_with_bwd", "rf64_with_bwd", "rf32_pre_columns",
-                "rf32_rows_by_helpers", "graph_solves"]
+                "rf32_rows_by_helpers", "graph_solves", "rf32_progress_flags",
+                "rf32_flag_waits", "rf32_flag_warps_waited"]
         return dict(zip(keys, [int(v) for v in a]))
 
     def structure(self) -> dict:

@@ -308,8 +308,11 @@ int gox_factor_host(int32_t n, int32_t nnz, const int32_t *rows, const int32_t *
  * plan whose update prefix runs one level early; [29] rows of the FP32 plan
  * copied by warps idle in a level for another warp's next column; [30]
  * solves of this topology whose Newton loop ran as one captured CUDA graph
- * (a configuration seen before: same batch buffers, precision, budget).
- * info must hold 31 entries.  Returns GOX_E_INVALID before the first solve. */
+ * (a configuration seen before: same batch buffers, precision, budget);
+ * [31] 1 when the FP32 plan's levels end in per-warp progress flags (0: CTA
+ * barriers), [32] its progress-flag wait commands, [33] the warps those
+ * commands wait for, summed.  info must hold 34 entries.  Returns
+ * GOX_E_INVALID before the first solve. */
 int gox_topo_info(const gox_topo *t, int64_t *info);
 
 /* The refactor plan's autotuner (no counterpart in the reference: its KLU
@@ -317,7 +320,8 @@ int gox_topo_info(const gox_topo *t, int64_t *info);
  * src/klu_native/types.rs:73-99).  A topology's first batch in a precision
  * times the candidate plans of its refactor streams -- warps per CTA (12
  * down to 4 in FP32, 8 down to 4 in FP64) x stream chunks of 256 / 320 /
- * 512 words, each compiled and checked on the host first -- on the first
+ * 512 words x the levels' synchronization (per-warp progress flags or CTA
+ * barriers), each compiled and checked on the host first -- on the first
  * min(G, 152) groups of that batch's first Jacobian (CUDA events, two runs
  * each) and keeps the fastest.  Choices are cached per process, and in the
  * file named by $GOX_TUNE_CACHE when set, under (precision, bus count in
@@ -325,15 +329,33 @@ int gox_topo_info(const gox_topo *t, int64_t *info);
  * of 1 / 2-8 / 9-38 / 39-152 / more groups of 32); a later topology with
  * the same key compiles the cached plan without timing.  Q-limit and
  * island variants take a cached plan or the default.  gox_set_autotune(0)
- * turns it off process-wide: the default plan is the most warps that fit. */
+ * turns it off process-wide: the default plan is the most warps that fit,
+ * with the levels' synchronization of gox_set_refactor_sync. */
 int gox_set_autotune(int32_t on);
+
+/* How the default refactor plan (the one used without the autotuner, and
+ * before it has timed anything) ends each dependency level: flags = 1
+ * per-warp progress flags -- each warp publishes the levels it has done
+ * and waits only for the warps whose earlier work it reads or overwrites,
+ * as found by the stream compiler --, 0 (default) CTA barriers.  Both
+ * forms run the same operations in the same order per value, so the
+ * results are bit-identical; the autotuner times both.  (Measured on
+ * case2000 x 4,096, 12 warps: FP32 2.19 ms with barriers, 2.27 ms with
+ * flags -- the critical path is the column chain itself, not the barrier
+ * -- and FP64 7.71 / 7.60 ms at 7 warps.)  Applies to topologies analysed
+ * afterwards.
+ * (No counterpart in the reference: its KLU refactor is sequential per
+ * scenario, src/klu_native/kernel.rs:476-524.) */
+int gox_set_refactor_sync(int32_t flags);
 
 /* The plan a topology's refactor runs in `precision`: plan[0] warps per
  * CTA, [1] ring rows per warp, [2] rows of warp 0's larger ring (0: none),
  * [3] stream-chunk words, [4] source (0 default, 1 timed by the autotuner,
- * 2 from its cache), [5] candidates timed.  With `table`, up to max_rows
- * rows {warps, chunk words, ring rows, ms} of the timed candidates; returns
- * the rows written, or < 0.  Needs a fixed pivot order. */
+ * 2 from its cache), [5] candidates timed, [6] 1 when the levels end in
+ * per-warp progress flags, 0 in CTA barriers (plan must hold 7 entries).
+ * With `table`, up to max_rows rows {warps, chunk words, ring rows, ms,
+ * progress flags} of the timed candidates; returns the rows written, or
+ * < 0.  Needs a fixed pivot order. */
 int gox_topo_tuning(const gox_topo *t, int32_t precision, int64_t *plan, double *table,
                     int32_t max_rows);
 

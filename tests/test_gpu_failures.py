@@ -9,9 +9,11 @@
   bit for bit.
 * A malformed command in the refactor's device stream (planted through the
   gox_topo_stream_word test hook) stops that warp: the kernel drains its
-  copies, keeps the CTA's barriers and reports a device-wait error, so the
-  solve returns GOX_E_DEVICE_WAIT promptly; with the word restored the next
-  solve is correct again.  No wait is left to run out and nothing faults.
+  copies, keeps the CTA's barriers (barrier plans) or makes the other warps'
+  progress-flag waits give up (flag plans), and reports a device-wait
+  error, so the solve returns GOX_E_DEVICE_WAIT promptly; with the word
+  restored the next solve is correct again.  No wait is left to run out and
+  nothing faults.
 """
 import time
 
@@ -57,13 +59,24 @@ def test_bad_scenarios_do_not_poison_the_batch(gox, precision):
 BAD_COMMAND = 15  # no command has this code
 
 
+@pytest.mark.parametrize("progress_flags", [True, False])
 @pytest.mark.parametrize("precision", [0, 1])
-def test_malformed_stream_command_reports_device_wait(gox, precision):
+def test_malformed_stream_command_reports_device_wait(gox, precision, progress_flags):
+    from gridoxide_gb300 import solver as S
     g, yb = _case118()
     p, q = G.load_scenarios(g, 96, 0.15, 78)
-    topo = gox.Topology(yb, g.bus_type)
-    kw = dict(tol=1e-8, max_iter=20, precision=precision)
-    good = topo.solve(p, q, g.vm, g.va, **kw)  # uploads the streams
+    # the default plan in either form (with progress flags, the other warps'
+    # waits for the stopped warp give up at once instead of running out)
+    S.set_autotune(False)
+    S.set_refactor_sync(progress_flags)
+    try:
+        topo = gox.Topology(yb, g.bus_type)
+        kw = dict(tol=1e-8, max_iter=20, precision=precision)
+        good = topo.solve(p, q, g.vm, g.va, **kw)  # uploads the streams
+    finally:
+        S.set_autotune(True)
+        S.set_refactor_sync(False)  # the default
+    assert topo.info()["rf32_progress_flags"] == int(progress_flags)
     old = topo.stream_word(precision, 0, 0, BAD_COMMAND)
     try:
         t0 = time.perf_counter()

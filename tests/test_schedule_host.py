@@ -13,8 +13,14 @@ from gridoxide_gb300 import grids as G
 from helpers import grid_from_fixture, load_fixture, ybus_from_fixture
 
 
+@pytest.mark.parametrize("progress_flags", [False, True])
 @pytest.mark.parametrize("name", ["case118", "case2000", "case10000"])
-def test_schedule_mirror_matches_oracle_lu(gox, oracle_mod, name):
+def test_schedule_mirror_matches_oracle_lu(gox, oracle_mod, name, progress_flags):
+    """Both forms of the levels' synchronization: with progress flags the
+    host interpreter also checks, before the stream is accepted, that every
+    conflicting pair of accesses by two warps is ordered by a flag wait and
+    that every wait is for a level published earlier in level order."""
+    from gridoxide_gb300 import solver as S
     O = oracle_mod
     if name == "case10000":
         g = G.config_grid(name)
@@ -23,9 +29,16 @@ def test_schedule_mirror_matches_oracle_lu(gox, oracle_mod, name):
         fx = load_fixture(name)
         g = grid_from_fixture(fx)
         yb = ybus_from_fixture(fx)
-    topo = gox.Topology(yb, g.bus_type)
-    assert topo.prepare(g.p_spec, g.q_spec, g.vm, g.va)
+    S.set_refactor_sync(progress_flags)
+    try:
+        topo = gox.Topology(yb, g.bus_type)
+        assert topo.prepare(g.p_spec, g.q_spec, g.vm, g.va)
+    finally:
+        S.set_refactor_sync(False)
     info = topo.info()
+    assert info["rf32_progress_flags"] == int(progress_flags)
+    if progress_flags:
+        assert 0 < info["rf32_flag_waits"] <= info["rf32_flag_warps_waited"]
     jac = O.Jacobian(yb, g.bus_type)
     st = topo.structure()
     Ap, Ai, _ = jac.csc_pattern()
