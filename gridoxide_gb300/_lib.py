@@ -90,6 +90,7 @@ SIGNATURES = {
     "gox_topo_pivot_solve": (C.c_int, [vp, f64p, f64p, f64p]),
     "gox_set_autotune": (C.c_int, [C.c_int32]),
     "gox_set_refactor_sync": (C.c_int, [C.c_int32]),
+    "gox_set_refactor_wide": (C.c_int, [C.c_int32]),
     "gox_topo_tuning": (C.c_int, [vp, C.c_int32, i64p, f64p, C.c_int32]),
     "gox_topo_stream_word": (C.c_int, [vp, C.c_int32, C.c_int32, C.c_int32, C.c_int32, i32p]),
     "gox_topo_info": (C.c_int, [vp, i64p]),

@@ -253,6 +253,10 @@ struct DevSchedule {
   int st_nw[2] = {0, 0};
   size_t st_smem[2] = {0, 0};
   bool st_bwd[2] = {false, false};  // the stream runs the backward substitution too
+  int st_wl[2] = {0, 0}, st_wp[2] = {0, 0};  // levels / phases the wide kernels run
+  std::vector<int32_t> lev_ptr_h;  // host copy: columns per refactor level
+  // launches of one refactor (with both substitutions when the stream has them)
+  int refactor_launches(int i) const { return 1 + st_wl[i] + st_wp[i]; }
 
   void load_streams(const Stream& s32, const Stream& s64) {
     const Stream* ss[2] = {&s32, &s64};
@@ -271,6 +275,8 @@ struct DevSchedule {
       st_nw[i] = ss[i]->plan.nw;
       st_smem[i] = stream_smem_bytes(ss[i]->plan);
       st_bwd[i] = ss[i]->has_bwd;
+      st_wl[i] = ss[i]->plan.wide_levels;
+      st_wp[i] = ss[i]->plan.wide_phases;
     }
   }
 
@@ -282,6 +288,7 @@ struct DevSchedule {
     upload(a_kind, sc.a_kind); upload(a_bi, sc.a_bi); upload(a_bk, sc.a_bk);
     upload(a_yslot, sc.a_yslot); upload(a_dst, sc.a_dst);
     upload(lev_ptr, sc.lev_ptr); upload(lev_cols, sc.lev_cols); upload(c_base, sc.c_base);
+    lev_ptr_h = sc.lev_ptr;
     upload(c_ulen, sc.c_ulen); upload(c_llen, sc.c_llen); upload(c_abeg, sc.c_abeg);
     upload(c_aend, sc.c_aend);
     upload(op_ptr, sc.op_ptr); upload(op_slot, sc.op_slot); upload(op_pos, sc.op_pos);
@@ -458,14 +465,17 @@ static constexpr size_t kRefactorSmem = 225 * 1024;
 // How the default refactor plan ends its levels: 1 per-warp progress flags,
 // 0 CTA barriers (gox_set_refactor_sync).
 static std::atomic<int> g_refactor_sync{0};
+// Narrowest refactor level / backward phase the default plan gives the wide
+// kernels (0: none; gox_set_refactor_wide).
+static std::atomic<int> g_refactor_wide{0};
 
 // Compiles the refactor streams of a schedule for both precisions.
 static void make_streams(const Schedule& sc, Stream& s32, Stream& s64) {
   std::string why;
-  const int sync = g_refactor_sync.load();
-  if (!choose_stream(sc, 4, kRefactorSmem, s32, why, sync))
+  const int sync = g_refactor_sync.load(), wide = g_refactor_wide.load();
+  if (!choose_stream(sc, 4, kRefactorSmem, s32, why, sync, wide))
     throw std::runtime_error("refactor schedule (FP32): " + why);
-  if (!choose_stream(sc, 8, kRefactorSmem, s64, why, sync))
+  if (!choose_stream(sc, 8, kRefactorSmem, s64, why, sync, wide))
     throw std::runtime_error("refactor schedule (FP64): " + why);
   // every stream runs once through the checking host interpreter before a
   // GPU sees it (indices, copies waited for, no cross-warp conflicts)
@@ -516,11 +526,38 @@ struct Iter {
   }
   static void refactor(const DevSchedule& ds, const BatchDev& D, cudaStream_t st) {
     const int i = sizeof(T) == 4 ? 0 : 1;
-    refactor_with(ds.st[i], ds.st_nw[i], ds.st_smem[i], ds.d, D, D.G, st);
+    refactor_with(ds, ds.st[i], ds.st_nw[i], ds.st_smem[i], ds.st_wl[i], ds.st_wp[i], D, D.G, st);
   }
-  // one launch of the refactor with a given plan's stream over the first
-  // `groups` groups
-  static void refactor_with(const StreamDev& P, int nw, size_t smem, const SchedDev& S,
+  // the refactor with a given plan's stream over the first `groups` groups:
+  // the wide kernels' levels (one launch each), the stream kernel, the wide
+  // kernels' backward phases (one launch each)
+  static void refactor_with(const DevSchedule& ds, const StreamDev& P, int nw, size_t smem, int wl,
+                            int wp, const BatchDev& D, int groups, cudaStream_t st) {
+    const SchedDev& S = ds.d;
+    for (int L = 0; L < wl; L++) {
+      const long long tasks = (long long)(ds.lev_ptr_h[L + 1] - ds.lev_ptr_h[L]) * groups;
+      const unsigned blocks = (unsigned)((tasks + kWideWarps - 1) / kWideWarps);
+      wide_attr();
+      k_refactor_wide<T><<<blocks, 32 * kWideWarps, kWideSmem, st>>>(S, D, L, groups);
+    }
+    stream_kernel(P, nw, smem, S, D, groups, st);
+    for (int L = wp - 1; L >= 0; L--) {
+      const long long tasks = (long long)(ds.lev_ptr_h[L + 1] - ds.lev_ptr_h[L]) * groups;
+      const unsigned blocks = (unsigned)((tasks + kWideWarps - 1) / kWideWarps);
+      k_solve_wide<T><<<blocks, 32 * kWideWarps, 0, st>>>(S, D, L, groups);
+    }
+  }
+  static constexpr size_t kWideSmem = (size_t)kWideWarps * kWideCap * 32 * sizeof(T);
+  static void wide_attr() {
+    static std::once_flag once[64];
+    int dev = 0;
+    GOX_CK(cudaGetDevice(&dev));
+    std::call_once(once[dev & 63], [] {
+      GOX_CK(cudaFuncSetAttribute(k_refactor_wide<T>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                  (int)kWideSmem));
+    });
+  }
+  static void stream_kernel(const StreamDev& P, int nw, size_t smem, const SchedDev& S,
                             const BatchDev& D, int groups, cudaStream_t st) {
     // the budget every plan fits in, set once per device (the same value for
     // every plan; setting an attribute per launch would put a driver call
@@ -665,7 +702,8 @@ struct gox_topo {
   struct Tuning {
     bool done = false;
     int source = 0;  // 0 the default (most warps), 1 measured here, 2 from the cache
-    std::vector<std::array<double, 5>> table;  // timed candidates: warps, chunk words, ring rows, ms, sync
+    std::vector<std::array<double, 7>> table;  // timed candidates: warps, chunk words, ring rows, ms,
+                                               // sync, wide levels, wide phases
   } tune[2];
   // split solves: a second instance of this topology (same pivot order, own
   // device buffers and stream) that solves the second half of a large batch
@@ -900,6 +938,7 @@ static std::vector<unsigned char> loop_key(const gox_topo* t, const BatchDev& D,
   put(&D, sizeof D); put(&t->dsched.d, sizeof(SchedDev));
   put(&t->dsched.st[i], sizeof(StreamDev)); put(&t->dsched.st_nw[i], sizeof(int));
   put(&t->dsched.st_smem[i], sizeof(size_t)); put(&t->dsched.st_bwd[i], sizeof(bool));
+  put(&t->dsched.st_wl[i], sizeof(int)); put(&t->dsched.st_wp[i], sizeof(int));
   return key;
 }
 
@@ -1025,7 +1064,8 @@ static void pivot_run(gox_topo* t, BatchDev& D, cudaStream_t st) {
 // (the most warps that fit).
 
 static std::mutex g_tune_mu;
-static std::map<std::array<int, 4>, std::array<int, 3>> g_tune;  // key -> {warps, chunk words, sync}
+// key -> {warps, chunk words, sync, wide split (0/1: at kWideMinWidth, per topology)}
+static std::map<std::array<int, 4>, std::array<int, 4>> g_tune;
 static bool g_tune_loaded = false;
 static std::atomic<int> g_autotune{1};
 
@@ -1044,18 +1084,19 @@ static void tune_cache_load() {
   if (!path || !*path) return;
   FILE* f = std::fopen(path, "r");
   if (!f) return;
-  int a, b, c, d, nw, cw, sy;
-  while (std::fscanf(f, "gox-tune-2 %d %d %d %d %d %d %d\n", &a, &b, &c, &d, &nw, &cw, &sy) == 7)
-    g_tune[{a, b, c, d}] = {nw, cw, sy};
+  int a, b, c, d, nw, cw, sy, wd;
+  while (std::fscanf(f, "gox-tune-3 %d %d %d %d %d %d %d %d\n", &a, &b, &c, &d, &nw, &cw, &sy, &wd) == 8)
+    g_tune[{a, b, c, d}] = {nw, cw, sy, wd};
   std::fclose(f);
 }
 
-static void tune_cache_store(const std::array<int, 4>& k, int nw, int cw, int sy) {
-  g_tune[k] = {nw, cw, sy};
+static void tune_cache_store(const std::array<int, 4>& k, const StreamPlan& p) {
+  const int nw = p.nw, cw = p.chunk_words, sy = p.sync, wd = p.wide_levels + p.wide_phases > 0;
+  g_tune[k] = {nw, cw, sy, wd};
   const char* path = std::getenv("GOX_TUNE_CACHE");
   if (!path || !*path) return;
   if (FILE* f = std::fopen(path, "a")) {
-    std::fprintf(f, "gox-tune-2 %d %d %d %d %d %d %d\n", k[0], k[1], k[2], k[3], nw, cw, sy);
+    std::fprintf(f, "gox-tune-3 %d %d %d %d %d %d %d %d\n", k[0], k[1], k[2], k[3], nw, cw, sy, wd);
     std::fclose(f);
   }
 }
@@ -1115,13 +1156,16 @@ static void autotune(gox_topo* t, const BatchDev& D, cudaStream_t st) {
     if (it == g_tune.end() && t->tune_cache_only) return;
     if (it != g_tune.end()) {
       const Stream& cur = i == 0 ? t->s32 : t->s64;
-      if (cur.plan.nw == it->second[0] && cur.plan.chunk_words == it->second[1] &&
-          cur.plan.sync == it->second[2]) {
+      auto same = [&](const StreamPlan& p) {
+        return p.nw == it->second[0] && p.chunk_words == it->second[1] && p.sync == it->second[2] &&
+               (p.wide_levels + p.wide_phases > 0 ? 1 : 0) == it->second[3];
+      };
+      if (same(cur.plan)) {
         TU.source = 2;
         return;
       }
       for (const StreamPlan& p : candidate_plans(sc, elem, kRefactorSmem))
-        if (p.nw == it->second[0] && p.chunk_words == it->second[1] && p.sync == it->second[2]) {
+        if (same(p)) {
           Stream s;
           if (compile_checked(sc, p, s)) {
             install_stream(t, i, std::move(s));
@@ -1176,7 +1220,8 @@ static void autotune(gox_topo* t, const BatchDev& D, cudaStream_t st) {
     for (int rep = 0; rep < 2; rep++) {
       GOX_CK(cudaMemcpyAsync(D.lu, bak.p, img_bytes, cudaMemcpyDeviceToDevice, st));
       GOX_CK(cudaEventRecord(e0, st));
-      Iter<T>::refactor_with(P, s.plan.nw, stream_smem_bytes(s.plan), t->dsched.d, D, Gt, st);
+      Iter<T>::refactor_with(t->dsched, P, s.plan.nw, stream_smem_bytes(s.plan), s.plan.wide_levels,
+                             s.plan.wide_phases, D, Gt, st);
       GOX_CK(cudaEventRecord(e1, st));
       GOX_CK(cudaEventSynchronize(e1));
       GOX_CK(cudaEventElapsedTime(&ms, e0, e1));
@@ -1191,7 +1236,8 @@ static void autotune(gox_topo* t, const BatchDev& D, cudaStream_t st) {
       continue;
     }
     TU.table.push_back({(double)s.plan.nw, (double)s.plan.chunk_words, (double)s.plan.ring_rows,
-                        (double)ms, (double)s.plan.sync});
+                        (double)ms, (double)s.plan.sync, (double)s.plan.wide_levels,
+                        (double)s.plan.wide_phases});
     if (ms < best_ms) {
       best_ms = ms;
       best = (int)c;
@@ -1203,11 +1249,11 @@ static void autotune(gox_topo* t, const BatchDev& D, cudaStream_t st) {
   cudaEventDestroy(e0);
   cudaEventDestroy(e1);
   if (best < 0) return;
-  const int nw = cand[best].nw, cw = cand[best].chunk_words, sy = cand[best].sync;
+  const StreamPlan bestp = cand[best];
   install_stream(t, i, std::move(built[best]));
   TU.source = 1;
   std::lock_guard<std::mutex> lk(g_tune_mu);
-  tune_cache_store(key, nw, cw, sy);
+  tune_cache_store(key, bestp);
 }
 
 template <typename T>
@@ -1225,7 +1271,8 @@ static void run_iterations(gox_topo* t, BatchDev D, int max_iter, bool outage, c
     const int its = h[1], ran_out = (h[0] > 0 && its >= max_iter) ? 1 : 0;
     const int fills = h[0] > 0 ? its : its - 1;
     const int ns = t->dsched.st_bwd[sizeof(T) == 4 ? 0 : 1] ? 0 : 1;
-    t->launches += (int64_t)its * 4 + (int64_t)fills * (2 + ns) + ran_out * 2;
+    const int nr = t->dsched.refactor_launches(sizeof(T) == 4 ? 0 : 1);
+    t->launches += (int64_t)its * 4 + (int64_t)fills * (1 + nr + ns) + ran_out * 2;
     return;
   }
   // events: per iteration [k1 start, k1 end, k2 end, k3 end, k4 end]; read once at the end
@@ -1265,7 +1312,7 @@ static void run_iterations(gox_topo* t, BatchDev D, int max_iter, bool outage, c
       ns = Iter<T>::solve_rest(t->dsched, D, st);
     }
     rec();
-    t->launches += 2 + ns;
+    t->launches += 1 + t->dsched.refactor_launches(sizeof(T) == 4 ? 0 : 1) + ns;
     GOX_CK(cudaGetLastError());
   }
   if (it == max_iter) t->launches += Iter<T>::mismatch(S, D, max_iter, 1, outage, st);
@@ -2854,6 +2901,12 @@ int gox_set_refactor_sync(int32_t flags) {
   return GOX_OK;
 }
 
+int gox_set_refactor_wide(int32_t min_width) {
+  if (min_width < 0) return GOX_E_INVALID;
+  g_refactor_wide.store(min_width);
+  return GOX_OK;
+}
+
 int gox_topo_tuning(const gox_topo* t, int32_t precision, int64_t* plan, double* table,
                     int32_t max_rows) {
   if (!t || !plan || (precision != GOX_PRECISION_FP64 && precision != GOX_PRECISION_MIXED))
@@ -2869,10 +2922,12 @@ int gox_topo_tuning(const gox_topo* t, int32_t precision, int64_t* plan, double*
   plan[4] = TU.source;
   plan[5] = (int64_t)TU.table.size();
   plan[6] = s.plan.sync;
+  plan[7] = s.plan.wide_levels;
+  plan[8] = s.plan.wide_phases;
   int rows = 0;
   for (const auto& r : TU.table) {
     if (!table || rows >= max_rows) break;
-    for (int c = 0; c < 5; c++) table[(size_t)rows * 5 + c] = r[c];
+    for (int c = 0; c < 7; c++) table[(size_t)rows * 7 + c] = r[c];
     rows++;
   }
   return rows;
@@ -2908,6 +2963,8 @@ int gox_topo_info(const gox_topo* t, int64_t* info) {
   info[31] = a.plan.sync;
   info[32] = a.n_waitp;
   info[33] = a.n_wait_reqs;
+  info[34] = a.plan.wide_levels;
+  info[35] = a.plan.wide_phases;
   return GOX_OK;
 }
 

@@ -1107,6 +1107,110 @@ done:
 }
 
 // ---------------------------------------------------------------------------
+// K3 / K4 wide levels.  The first levels of the refactor hold most columns
+// (case2000: 2,900 of 3,698 in levels 0-9), all independent within a level;
+// the last phases of the backward substitution likewise hold most rows.
+// The wide kernels run one such level / phase per launch with one warp per
+// (column or row, group of 32 scenarios), so a level's work spreads over
+// every SM whatever the batch size, where the per-group stream kernel would
+// give it one SM per group.  A column's values are staged in shared memory
+// private to its warp's lanes (row r of lane l at stage[r * 32 + l]); its
+// inputs -- the A image the fill wrote into the factor, the L values and y
+// of earlier columns -- come from global memory, where earlier launches
+// left them.  The arithmetic is the stream kernel's, in the same order per
+// value: KLU's update order (the schedule's hazard-free batches keep each
+// entry's order), the forward terms in order, the pivot's correctly
+// rounded reciprocal, the pivot-ratio check; so both give the same bits.
+constexpr int kWideWarps = 4;  // warps per CTA of the wide kernels
+
+template <typename T>
+__global__ void __launch_bounds__(32 * kWideWarps) k_refactor_wide(SchedDev S, BatchDev D, int lev,
+                                                                   int groups) {
+  extern __shared__ __align__(16) unsigned char wsm[];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const int q0 = S.lev_ptr[lev], ncol = S.lev_ptr[lev + 1] - q0;
+  const long long task = (long long)blockIdx.x * kWideWarps + warp;
+  if (task >= (long long)ncol * groups) return;
+  const int g = (int)(task % groups), q = (int)(task / groups);
+  if (!D.gact[g]) return;
+  T* stg = reinterpret_cast<T*>(wsm) + (size_t)warp * kWideCap * 32 + lane;
+  const int k = S.lev_cols[q0 + q];
+  const int base = S.c_base[k], ulen = S.c_ulen[k], len = ulen + 1 + S.c_llen[k];
+  const T* LUr = (const T*)D.lu + (size_t)g * S.n_slots * 32u + lane;
+  T* LUw = (T*)D.lu + (size_t)g * S.n_slots * 32u + lane;
+  for (int r = 0; r < len; r++) stg[r * 32] = LUr[(size_t)(base + r) * 32];
+  // updates: per hazard-free batch, every load before every store
+  int o = S.op_ptr[k];
+  for (int b = S.bt_ptr[k]; b < S.bt_ptr[k + 1]; b++) {
+    const int cnt = S.bt_cnt[b];
+    T lv[kMaxBatch], uv[kMaxBatch], dv[kMaxBatch];
+    int dp[kMaxBatch];
+#pragma unroll
+    for (int t = 0; t < kMaxBatch; t++)
+      if (t < cnt) {
+        const uint32_t pos = S.op_pos[o + t];
+        dp[t] = (int)(pos & 0xffffu);
+        lv[t] = LUr[(size_t)S.op_slot[o + t] * 32];
+        uv[t] = stg[(pos >> 16) * 32];
+        dv[t] = stg[dp[t] * 32];
+      }
+#pragma unroll
+    for (int t = 0; t < kMaxBatch; t++)
+      if (t < cnt) stg[dp[t] * 32] = dv[t] - lv[t] * uv[t];
+    o += cnt;
+  }
+  T* Xg = (T*)D.sol + (size_t)g * S.n_u * 32u + lane;
+  T y = (T)0;
+  if (S.fuse_fwd) {
+    y = ((const T*)D.rhs)[((size_t)g * S.n_u + k) * 32u + lane];
+    for (int tt = S.fw_ptr[k]; tt < S.fw_ptr[k + 1]; tt++)
+      y -= LUr[(size_t)S.fw_slot[tt] * 32] * Xg[(size_t)S.fw_col[tt] * 32];
+  }
+  // finish: pivot, U and the diagonal as they are, L scaled
+  const T piv = stg[ulen * 32];
+  const bool bad = piv == (T)0;
+  const T inv = rcp_rn(piv);
+  for (int r = 0; r <= ulen; r++) LUw[(size_t)(base + r) * 32] = stg[r * 32];
+  T colmax = fabs(piv);
+  for (int r = ulen + 1; r < len; r++) {
+    T v = stg[r * 32];
+    colmax = fmax(colmax, fabs(v));
+    v *= inv;
+    LUw[(size_t)(base + r) * 32] = v;
+  }
+  const float ptol = D.piv_tol;
+  const bool tiny = (ptol > 0.0f) && ((float)fabs(piv) < ptol * (float)colmax);
+  if (S.fuse_fwd) Xg[(size_t)k * 32] = y;
+  const int s = g * 32 + lane;
+  if (bad) D.sing[s] = 1;
+  if (tiny) D.piv_flag[s] = 1;
+}
+
+// The backward substitution of one wide refactor level's rows: x_k = (y_k -
+// sum U(k, j) x_j) / U(k, k), terms in the stream's order, one warp per
+// (row, group).  A row needs only rows of higher levels, so the levels run
+// from the last wide one down, after the stream kernel has solved the rest.
+template <typename T>
+__global__ void __launch_bounds__(32 * kWideWarps) k_solve_wide(SchedDev S, BatchDev D, int lev,
+                                                                int groups) {
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const int q0 = S.lev_ptr[lev], nrow = S.lev_ptr[lev + 1] - q0;
+  const long long task = (long long)blockIdx.x * kWideWarps + warp;
+  if (task >= (long long)nrow * groups) return;
+  const int g = (int)(task % groups), q = (int)(task / groups);
+  if (!D.gact[g]) return;
+  const int k = S.lev_cols[q0 + q];
+  const T* LUr = (const T*)D.lu + (size_t)g * S.n_slots * 32u + lane;
+  T* Xg = (T*)D.sol + (size_t)g * S.n_u * 32u + lane;
+  T v = Xg[(size_t)k * 32];
+  for (int tt = S.bw_ptr[k]; tt < S.bw_ptr[k + 1]; tt++)
+    v -= LUr[(size_t)S.bw_slot[tt] * 32] * Xg[(size_t)S.bw_col[tt] * 32];
+  const T x = v / LUr[(size_t)S.diag_slot[k] * 32];
+  if (!isfinite(x)) D.sing[g * 32 + lane] = 1;
+  Xg[(size_t)k * 32] = x;
+}
+
+// ---------------------------------------------------------------------------
 // Linear initial guess (src/network.rs:627-678).  The PQ buses' voltages U_n
 // solve Y'_nn U_n = -Y'_ns U_s, where Y' is the Y-bus with -conj(S_i) added
 // on the diagonal of each PQ bus i (its injection as a constant admittance

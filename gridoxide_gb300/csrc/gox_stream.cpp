@@ -894,19 +894,28 @@ struct Builder {
       err = "factor too large for 21-bit row fields";
       return false;
     }
+    // levels the wide kernels run before the stream (their columns are
+    // finished in global memory when it starts: level -1 here) and backward
+    // phases they run after it
+    const int S0 = P.wide_levels, PW = P.wide_phases;
+    if (S0 < 0 || S0 >= sc.n_levels || PW != S0 || (S0 > 0 && !(sc.fuse_fwd && with_bwd))) {
+      err = "bad wide split";
+      return false;
+    }
+    const int NR = sc.n_levels - S0;  // refactor levels in the stream
     // ---- columns and their value sources
     C.assign(n, ColInfo());
     for (int k = 0; k < n; k++) {
       ColInfo& c = C[k];
       c.k = k;
-      c.level = sc.col_level[k];
+      c.level = sc.col_level[k] < S0 ? -1 : sc.col_level[k] - S0;
       c.len = sc.c_ulen[k] + 1 + sc.c_llen[k];
       c.brows = c.len + 3;
-      if (c.len >= 1024) {
+      if (c.level >= 0 && c.len >= 1024) {
         err = "column too long for 10-bit stage rows";
         return false;
       }
-      if (c.brows > rsize(0)) {
+      if (c.level >= 0 && c.brows > rsize(0)) {
         err = "column " + std::to_string(k) + " longer than the ring";
         return false;
       }
@@ -960,17 +969,22 @@ struct Builder {
     std::vector<int32_t> blev_ptr(1, 0), blev_rows;
     if (with_bwd) {
       C.resize(2 * (size_t)n);
+      // phases as scheduled, without the rows of the wide kernels' columns
+      // (solved after the stream, in reverse level order; no row of the
+      // stream needs them: a row needs rows of higher refactor levels only)
       for (int ph = 0; ph < sc.n_phases; ph++) {
         if (sc.ph_kind[ph] != 1) {
           err = "backward tasks need a schedule without forward phases";
           return false;
         }
+        const size_t before = blev_rows.size();
         for (int q = sc.ph_ptr[ph]; q < sc.ph_ptr[ph + 1]; q++) {
           const int k = sc.ph_rows[q];
+          if (sc.col_level[k] < S0) continue;
           ColInfo& c = C[n + k];
           c.kind = TK_BWD;
           c.k = k;
-          c.level = sc.n_levels + ph;
+          c.level = NR + n_blev;
           c.brows = 1;
           const int ulen = sc.c_ulen[k], len = ulen + 1 + sc.c_llen[k];
           Item y;
@@ -991,15 +1005,21 @@ struct Builder {
           c.cost = 100 + fma_cost() * (sc.bw_ptr[k + 1] - sc.bw_ptr[k]);
           blev_rows.push_back(n + k);
         }
+        if (blev_rows.size() == before) continue;  // every row of the phase is a wide one
         blev_ptr.push_back((int32_t)blev_rows.size());
+        n_blev++;
       }
-      n_blev = sc.n_phases;
     }
-    const int NL = sc.n_levels + n_blev;
+    const int NL = NR + n_blev;
+    if (NL <= 0) {
+      err = "no level left for the stream";
+      return false;
+    }
     auto level_tasks = [&](int L) {
-      if (L < sc.n_levels)
-        return std::vector<int>(sc.lev_cols.begin() + sc.lev_ptr[L], sc.lev_cols.begin() + sc.lev_ptr[L + 1]);
-      const int b = L - sc.n_levels;
+      if (L < NR)
+        return std::vector<int>(sc.lev_cols.begin() + sc.lev_ptr[L + S0],
+                                sc.lev_cols.begin() + sc.lev_ptr[L + S0 + 1]);
+      const int b = L - NR;
       return std::vector<int>(blev_rows.begin() + blev_ptr[b], blev_rows.begin() + blev_ptr[b + 1]);
     };
     // ---- columns to warps: per level, longest first to the least loaded
@@ -1032,10 +1052,10 @@ struct Builder {
         }
     }
     // ---- columns of narrow levels run in slices at earlier levels
-    for (int L = 2; L < sc.n_levels; L++) {
-      const int width = sc.lev_ptr[L + 1] - sc.lev_ptr[L];
+    for (int L = 2; L < NR; L++) {
+      const int width = sc.lev_ptr[L + S0 + 1] - sc.lev_ptr[L + S0];
       if (width > std::max(1, W / 4)) continue;
-      for (int q = sc.lev_ptr[L]; q < sc.lev_ptr[L + 1]; q++) {
+      for (int q = sc.lev_ptr[L + S0]; q < sc.lev_ptr[L + S0 + 1]; q++) {
         ColInfo& c = C[sc.lev_cols[q]];
         c.run_early.assign(c.nlr, 0);
         int e = 0;
@@ -1220,7 +1240,7 @@ struct Builder {
 }  // namespace
 
 static bool choose_stream_1(const Schedule& sc, int elem, size_t smem_budget, Stream& out,
-                            std::string& why, bool with_bwd, int sync);
+                            std::string& why, bool with_bwd, int sync, int wl, int wp);
 
 using WaitLists = std::vector<std::vector<std::vector<int32_t>>>;
 static std::string interpret(const Schedule& sc, const Stream& st, std::vector<double>& lu,
@@ -1262,11 +1282,16 @@ bool build_stream(const Schedule& sc, const StreamPlan& plan, Stream& out, std::
 }
 
 bool choose_stream(const Schedule& sc, int elem, size_t smem_budget, Stream& out,
-                   std::string& why, int sync) {
+                   std::string& why, int sync, int wide_min) {
+  // with the wide kernels' split when asked and the schedule has one, then
   // with the backward substitution in the stream when the schedule allows
   // it (no off-diagonal BTF entries), else (or when no plan holds it) without
+  int wl = 0, wp = 0;
+  wide_split(sc, wide_min, wl, wp);
+  if (wl + wp > 0 && choose_stream_1(sc, elem, smem_budget, out, why, true, sync, wl, wp))
+    return true;
   for (bool bwd : {sc.fuse_fwd, false}) {
-    if (choose_stream_1(sc, elem, smem_budget, out, why, bwd, sync)) return true;
+    if (choose_stream_1(sc, elem, smem_budget, out, why, bwd, sync, 0, 0)) return true;
     if (!bwd) break;
   }
   return false;
@@ -1300,16 +1325,38 @@ static bool plan_for(const Schedule& sc, int elem, size_t smem_budget, int nw, i
   return true;
 }
 
+void wide_split(const Schedule& sc, int min_width, int& levels, int& phases) {
+  levels = phases = 0;
+  if (!sc.fuse_fwd || min_width <= 0) return;
+  for (; levels < sc.n_levels - 1; levels++) {
+    if (sc.lev_ptr[levels + 1] - sc.lev_ptr[levels] < min_width) break;
+    bool fits = true;
+    for (int q = sc.lev_ptr[levels]; q < sc.lev_ptr[levels + 1] && fits; q++) {
+      const int k = sc.lev_cols[q];
+      fits = sc.c_ulen[k] + 1 + sc.c_llen[k] <= kWideCap;
+    }
+    if (!fits) break;
+  }
+  phases = levels;  // the rows of those columns, in reverse level order
+}
+
 std::vector<StreamPlan> candidate_plans(const Schedule& sc, int elem, size_t smem_budget) {
   std::vector<StreamPlan> out;
-  for (int nw : {12, 11, 10, 9, 8, 7, 6, 5, 4}) {
+  int wl = 0, wp = 0;
+  wide_split(sc, kWideMinWidth, wl, wp);
+  for (int nw : {12, 10, 8, 7, 6, 5}) {
     if (nw > (elem == 4 ? kMaxRefactorWarps : 8)) continue;
-    for (int cw : {256, 320, 512}) {
+    for (int cw : {320, 512}) {
       StreamPlan p;
       if (!plan_for(sc, elem, smem_budget, nw, cw, p)) continue;
-      for (int sync : {1, 0}) {
-        p.sync = sync;
-        out.push_back(p);
+      for (int wide : {0, 1}) {
+        if (wide && wl + wp == 0) continue;
+        p.wide_levels = wide ? wl : 0;
+        p.wide_phases = wide ? wp : 0;
+        for (int sync : {0, 1}) {
+          p.sync = sync;
+          out.push_back(p);
+        }
       }
     }
   }
@@ -1317,6 +1364,7 @@ std::vector<StreamPlan> candidate_plans(const Schedule& sc, int elem, size_t sme
 }
 
 bool build_plan(const Schedule& sc, const StreamPlan& p, Stream& out, std::string& why) {
+  if (p.wide_levels > 0 || p.wide_phases > 0) return build_stream(sc, p, out, why, true);
   for (bool bwd : {sc.fuse_fwd, false}) {
     if (build_stream(sc, p, out, why, bwd)) return true;
     if (!bwd) break;
@@ -1325,7 +1373,7 @@ bool build_plan(const Schedule& sc, const StreamPlan& p, Stream& out, std::strin
 }
 
 static bool choose_stream_1(const Schedule& sc, int elem, size_t smem_budget, Stream& out,
-                            std::string& why, bool with_bwd, int sync) {
+                            std::string& why, bool with_bwd, int sync, int wl, int wp) {
   bool found = false;
   std::string last;
   for (int nw : {12, 10, 8, 6, 4, 3, 2, 1}) {
@@ -1333,6 +1381,8 @@ static bool choose_stream_1(const Schedule& sc, int elem, size_t smem_budget, St
     StreamPlan p;
     if (!plan_for(sc, elem, smem_budget, nw, nw >= 10 ? 320 : 512, p)) continue;
     p.sync = sync;
+    p.wide_levels = wl;
+    p.wide_phases = wp;
     Stream s;
     std::string w;
     if (!build_stream(sc, p, s, w, with_bwd)) {
@@ -1380,6 +1430,35 @@ static std::string interpret(const Schedule& sc, const Stream& st, std::vector<d
   if ((int)lu.size() != sc.n_slots || (int)rhs.size() != n) return "buffer sizes";
   if (NLv <= 0 || NLv >= 32000) return "level count out of range";
   X.assign(n, 0.0);
+  // ---- the wide kernels' part before the stream: the columns of the first
+  //      wide_levels levels, each as the wide kernel computes it (KLU's
+  //      update order, the forward term, pivot and scaling), finished
+  //      before level 0 of the stream (-2)
+  const int S0 = P.wide_levels, PW = P.wide_phases;
+  if (S0 < 0 || S0 >= sc.n_levels || PW != S0 || (S0 > 0 && !(sc.fuse_fwd && st.has_bwd)))
+    return "bad wide split";
+  for (int L = 0; L < S0; L++)
+    for (int q = sc.lev_ptr[L]; q < sc.lev_ptr[L + 1]; q++) {
+      const int k = sc.lev_cols[q], base = sc.c_base[k], ulen = sc.c_ulen[k];
+      const int len = ulen + 1 + sc.c_llen[k];
+      if (len > kWideCap) return "a wide-kernel column longer than its stage";
+      std::vector<double> stg(lu.begin() + base, lu.begin() + base + len);
+      for (int p = 0; p < ulen; p++) {
+        const int e = sc.cu_ptr[k] + p, j = sc.cu_j[e];
+        if (sc.col_level[j] >= L) return "a wide-kernel column reads one of its own level";
+        const double x = stg[p];
+        const int lb = sc.c_base[j] + sc.c_ulen[j] + 1;
+        for (int i = 0; i < sc.c_llen[j]; i++) stg[sc.cu_dst[sc.cu_dptr[e] + i]] -= lu[lb + i] * x;
+      }
+      double y = rhs[k];
+      for (int tt = sc.fw_ptr[k]; tt < sc.fw_ptr[k + 1]; tt++) y -= lu[sc.fw_slot[tt]] * X[sc.fw_col[tt]];
+      if (stg[ulen] == 0.0) singular = true;
+      const double inv = 1.0 / stg[ulen];
+      for (int p = 0; p <= ulen; p++) lu[base + p] = stg[p];
+      for (int p = ulen + 1; p < len; p++) lu[base + p] = stg[p] * inv;
+      X[k] = y;
+      colfin[k] = xfin[k] = -2;
+    }
   // ---- happens-before between warps (progress-flag plans and the analysis)
   const bool flags = P.sync != 0, analyze = reqs != nullptr;
   const bool vcs = flags || analyze;
@@ -1522,7 +1601,7 @@ static std::string interpret(const Schedule& sc, const Stream& st, std::vector<d
             v = lu[src];
           } else if (src < sc.n_slots + n) {
             const int r = src - sc.n_slots;
-            if (bfin[r] >= 0 ? bfin[r] >= L : (xfin[r] < 0 || xfin[r] >= L)) {
+            if (bfin[r] >= 0 ? bfin[r] >= L : (xfin[r] == -1 || xfin[r] >= L)) {
               e = "copies X before its value is final";
               return false;
             }
@@ -1811,8 +1890,25 @@ static std::string interpret(const Schedule& sc, const Stream& st, std::vector<d
   }
   for (int w = 0; w < W; w++)
     if (!ws[w].done) return "warp " + std::to_string(w) + " did not reach END";
+  // ---- the wide kernels' part after the stream: the backward substitution
+  //      of the wide columns' rows, one refactor level at a time from the
+  //      last wide level down
+  for (int L = PW - 1; L >= 0; L--)
+    for (int q = sc.lev_ptr[L]; q < sc.lev_ptr[L + 1]; q++) {
+      const int k = sc.lev_cols[q];
+      double v = X[k];
+      for (int tt = sc.bw_ptr[k]; tt < sc.bw_ptr[k + 1]; tt++) {
+        const int j = sc.bw_col[tt];
+        if (bfin[j] < 0) return "a wide-kernel row reads x of a row not yet solved";
+        v -= lu[sc.bw_slot[tt]] * X[j];
+      }
+      const double x = v / lu[sc.diag_slot[k]];
+      if (!std::isfinite(x)) singular = true;
+      X[k] = x;
+      bfin[k] = NLv;
+    }
   for (int k = 0; k < n; k++)
-    if (colfin[k] < 0) return "column " + std::to_string(k) + " never finished";
+    if (colfin[k] == -1) return "column " + std::to_string(k) + " never finished";
   if (st.has_bwd)
     for (int k = 0; k < n; k++)
       if (bfin[k] < 0) return "row " + std::to_string(k) + " of the backward substitution never solved";

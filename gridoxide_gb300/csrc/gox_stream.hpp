@@ -129,7 +129,23 @@ struct StreamPlan {
                             // long for the other rings run there); 0: ring_rows
   int chunk_words = 512;    // stream chunk, 32-bit words (multiple of 4)
   int sync = 0;             // levels: 0 CTA barriers, 1 per-warp progress flags
+  // The columns of the first wide_levels refactor levels, and their rows of
+  // the backward substitution, are not in the stream: the wide kernels run
+  // them, one launch per level with one warp per (column or row, group)
+  // across all SMs, before the stream kernel (the columns, level by level)
+  // and after it (the rows, from the last of those levels down).  Their
+  // values reach the stream, and the stream's reach them, through global
+  // memory.  wide_phases equals wide_levels (the backward launches).
+  int wide_levels = 0, wide_phases = 0;
 };
+// Columns the wide kernels stage at once (per warp and lane, in shared memory).
+constexpr int kWideCap = 64;
+// Narrowest level / phase the autotuner's wide candidates give the wide kernels.
+constexpr int kWideMinWidth = 64;
+// The wide split of a schedule: the leading refactor levels with at least
+// min_width columns each, all columns at most kWideCap long (none when the
+// forward substitution is not fused); phases = levels.
+void wide_split(const Schedule& sc, int min_width, int& levels, int& phases);
 // The rings in the row space: warp 0's first, then the others'.
 inline int ring_size(const StreamPlan& p, int w) {
   return w == 0 && p.big_rows > p.ring_rows ? p.big_rows : p.ring_rows;
@@ -145,7 +161,7 @@ struct Stream {
   StreamPlan plan;
   std::vector<int32_t> words;            // all chunks; warp w owns chunks chunk0[w] ..
   std::vector<int32_t> chunk0, nchunks;  // per warp
-  int n_levels = 0;  // dependency levels (refactor, then backward substitution)
+  int n_levels = 0;  // dependency levels in the stream (refactor, then backward substitution)
   int n_bars = 0;    // CTA barriers the stream takes (n_levels, or 0 with progress flags)
   bool has_bwd = false;  // the stream also runs the backward substitution
   // statistics of the schedule
@@ -174,12 +190,13 @@ bool build_stream(const Schedule& sc, const StreamPlan& plan, Stream& out, std::
 // latencies of the wide levels and give the narrow ones more idle warps to
 // issue copies, and smaller chunks leave the rings room.)
 bool choose_stream(const Schedule& sc, int elem, size_t smem_budget, Stream& out,
-                   std::string& why, int sync = 1);
+                   std::string& why, int sync = 0, int wide_min = 0);
 
-// The plans an autotuner may time: every warp count (12 down to 4 in FP32,
-// 8 down to 4 in FP64) with stream chunks of 256, 320 and 512 words whose
-// rings fit `smem_budget`, each with progress flags and with barriers,
-// most warps first.
+// The plans an autotuner may time: warp counts 12, 10, 8, 7, 6, 5 (FP64 up
+// to 8) with stream chunks of 320 and 512 words whose rings fit
+// `smem_budget`, each without and (when the schedule has one) with the
+// wide kernels' split at kWideMinWidth, each with barriers and with
+// progress flags, most warps first.
 std::vector<StreamPlan> candidate_plans(const Schedule& sc, int elem, size_t smem_budget);
 
 // Builds one plan's stream, with the backward substitution when the

@@ -165,6 +165,15 @@ def set_refactor_sync(progress_flags: bool) -> None:
     check(_lib.load().gox_set_refactor_sync(1 if progress_flags else 0), "gox_set_refactor_sync")
 
 
+def set_refactor_wide(min_width: int) -> None:
+    """The wide kernels in the default refactor plan of topologies analysed
+    from now on: leading refactor levels / trailing backward phases with at
+    least `min_width` columns / rows run one level per launch across every
+    SM (0, the default: none; gox_set_refactor_wide); same results bit for
+    bit."""
+    check(_lib.load().gox_set_refactor_wide(int(min_width)), "gox_set_refactor_wide")
+
+
 class Topology:
     """A registered topology: Y-bus (CSR) + bus types, resident on the GPU."""
 
@@ -404,20 +413,22 @@ class Topology:
     def tuning(self, precision=GOX_PRECISION_MIXED) -> dict:
         """The refactor plan in `precision` and the autotuner's timed
         candidates (gox_topo_tuning)."""
-        plan = np.zeros(7, np.int64)
-        table = np.zeros((128, 5))
+        plan = np.zeros(9, np.int64)
+        table = np.zeros((128, 7))
         rows = check(_lib.load().gox_topo_tuning(self._h, int(precision), _p(plan, _lib.i64p),
                                                  _p(table, _lib.f64p), 128), "gox_topo_tuning")
         return {"warps": int(plan[0]), "ring_rows": int(plan[1]), "big_rows": int(plan[2]),
                 "chunk_words": int(plan[3]),
                 "source": ("default", "measured", "cached")[int(plan[4])],
-                "progress_flags": bool(plan[6]),
+                "progress_flags": bool(plan[6]), "wide_levels": int(plan[7]),
+                "wide_phases": int(plan[8]),
                 "candidates": [dict(warps=int(r[0]), chunk_words=int(r[1]), ring_rows=int(r[2]),
-                                    ms=float(r[3]), progress_flags=bool(r[4]))
+                                    ms=float(r[3]), progress_flags=bool(r[4]),
+                                    wide_levels=int(r[5]), wide_phases=int(r[6]))
                                for r in table[:rows]]}
 
     def info(self) -> dict:
-        a = np.zeros(34, np.int64)
+        a = np.zeros(36, np.int64)
         check(_lib.load().gox_topo_info(self._h, _p(a, _lib.i64p)), "gox_topo_info")
         keys = ["n_u", "nnz_j", "nnz_l", "nnz_u", "nnz_off", "nblocks", "levels", "phases",
                 "lu_slots", "max_collen", "rf32_warps", "rf32_ring_rows", "rf32_est_cycles",
@@ -426,7 +437,8 @@ class Topology:
                 "rf64_ring_rows", "rf64_est_cycles", "rf64_rows_in_place", "rf32_column_cmds",
                 "rf32_stream_words", "rf32_with_bwd", "rf64_with_bwd", "rf32_pre_columns",
                 "rf32_rows_by_helpers", "graph_solves", "rf32_progress_flags",
-                "rf32_flag_waits", "rf32_flag_warps_waited"]
+                "rf32_flag_waits", "rf32_flag_warps_waited", "rf32_wide_levels",
+                "rf32_wide_phases"]
         return dict(zip(keys, [int(v) for v in a]))
 
     def structure(self) -> dict:

@@ -311,8 +311,9 @@ int gox_factor_host(int32_t n, int32_t nnz, const int32_t *rows, const int32_t *
  * (a configuration seen before: same batch buffers, precision, budget);
  * [31] 1 when the FP32 plan's levels end in per-warp progress flags (0: CTA
  * barriers), [32] its progress-flag wait commands, [33] the warps those
- * commands wait for, summed.  info must hold 34 entries.  Returns
- * GOX_E_INVALID before the first solve. */
+ * commands wait for, summed; [34] / [35] refactor levels / backward phases
+ * of the FP32 plan the wide kernels run.  info must hold 36 entries.
+ * Returns GOX_E_INVALID before the first solve. */
 int gox_topo_info(const gox_topo *t, int64_t *info);
 
 /* The refactor plan's autotuner (no counterpart in the reference: its KLU
@@ -321,7 +322,8 @@ int gox_topo_info(const gox_topo *t, int64_t *info);
  * times the candidate plans of its refactor streams -- warps per CTA (12
  * down to 4 in FP32, 8 down to 4 in FP64) x stream chunks of 256 / 320 /
  * 512 words x the levels' synchronization (per-warp progress flags or CTA
- * barriers), each compiled and checked on the host first -- on the first
+ * barriers) x without / with the wide kernels (gox_set_refactor_wide),
+ * each compiled and checked on the host first -- on the first
  * min(G, 152) groups of that batch's first Jacobian (CUDA events, two runs
  * each) and keeps the fastest.  Choices are cached per process, and in the
  * file named by $GOX_TUNE_CACHE when set, under (precision, bus count in
@@ -348,14 +350,28 @@ int gox_set_autotune(int32_t on);
  * scenario, src/klu_native/kernel.rs:476-524.) */
 int gox_set_refactor_sync(int32_t flags);
 
+/* The wide kernels in the default refactor plan: min_width > 0 hands the
+ * leading refactor levels with at least min_width columns each (columns of
+ * at most 64 entries) and the trailing backward-substitution phases with
+ * at least min_width rows each to kernels that run one level / phase per
+ * launch with one warp per (column or row, group of 32 scenarios) across
+ * every SM; the per-group refactor kernel runs the levels between.  0
+ * (default) keeps every level in the per-group kernel.  The results are
+ * bit-identical either way; the autotuner times both (at min_width 64).
+ * Applies to topologies analysed afterwards; GOX_E_INVALID for < 0.  (No
+ * counterpart in the reference: KLU's refactor is one sequential sweep per
+ * scenario, src/klu_native/kernel.rs:476-524, solve.rs:56-102.) */
+int gox_set_refactor_wide(int32_t min_width);
+
 /* The plan a topology's refactor runs in `precision`: plan[0] warps per
  * CTA, [1] ring rows per warp, [2] rows of warp 0's larger ring (0: none),
  * [3] stream-chunk words, [4] source (0 default, 1 timed by the autotuner,
  * 2 from its cache), [5] candidates timed, [6] 1 when the levels end in
- * per-warp progress flags, 0 in CTA barriers (plan must hold 7 entries).
- * With `table`, up to max_rows rows {warps, chunk words, ring rows, ms,
- * progress flags} of the timed candidates; returns the rows written, or
- * < 0.  Needs a fixed pivot order. */
+ * per-warp progress flags, 0 in CTA barriers, [7] / [8] refactor levels /
+ * backward phases the wide kernels run (plan must hold 9 entries).  With
+ * `table`, up to max_rows rows {warps, chunk words, ring rows, ms,
+ * progress flags, wide levels, wide phases} of the timed candidates;
+ * returns the rows written, or < 0.  Needs a fixed pivot order. */
 int gox_topo_tuning(const gox_topo *t, int32_t precision, int64_t *plan, double *table,
                     int32_t max_rows);
 

@@ -37,17 +37,20 @@ def test_autotuner_times_candidates_caches_and_keeps_results(gox):
         assert len(ms) >= 3
         chosen = [c for c in tu["candidates"]
                   if c["warps"] == tu["warps"] and c["chunk_words"] == tu["chunk_words"]
-                  and c["progress_flags"] == tu["progress_flags"]]
+                  and c["progress_flags"] == tu["progress_flags"]
+                  and c["wide_levels"] == tu["wide_levels"]]
         # both forms of the levels' synchronization were timed
         assert {c["progress_flags"] for c in tu["candidates"]} == {True, False}
+        # ... and with and without the wide kernels
+        assert {c["wide_levels"] > 0 for c in tu["candidates"]} == {True, False}
         assert chosen and chosen[0]["ms"] == min(ms)
     else:  # another test of this process tuned this key first
         assert tu["source"] == "cached"
     t2 = gox.Topology(yb, g.bus_type)
     r2 = t2.solve(p, q, g.vm, g.va, **kw)
     assert t2.tuning()["source"] == "cached"
-    assert ((t2.tuning()["warps"], t2.tuning()["chunk_words"], t2.tuning()["progress_flags"])
-            == (tu["warps"], tu["chunk_words"], tu["progress_flags"]))
+    key = ("warps", "chunk_words", "progress_flags", "wide_levels", "wide_phases")
+    assert tuple(t2.tuning()[k] for k in key) == tuple(tu[k] for k in key)
     for r in (r1, r2):
         np.testing.assert_array_equal(r.voltage_mag, ref.voltage_mag)
         np.testing.assert_array_equal(r.voltage_ang, ref.voltage_ang)

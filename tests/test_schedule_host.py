@@ -13,13 +13,15 @@ from gridoxide_gb300 import grids as G
 from helpers import grid_from_fixture, load_fixture, ybus_from_fixture
 
 
-@pytest.mark.parametrize("progress_flags", [False, True])
+@pytest.mark.parametrize("progress_flags,wide", [(False, 0), (True, 0), (False, 16), (True, 16)])
 @pytest.mark.parametrize("name", ["case118", "case2000", "case10000"])
-def test_schedule_mirror_matches_oracle_lu(gox, oracle_mod, name, progress_flags):
-    """Both forms of the levels' synchronization: with progress flags the
-    host interpreter also checks, before the stream is accepted, that every
-    conflicting pair of accesses by two warps is ordered by a flag wait and
-    that every wait is for a level published earlier in level order."""
+def test_schedule_mirror_matches_oracle_lu(gox, oracle_mod, name, progress_flags, wide):
+    """Both forms of the levels' synchronization, without and with the wide
+    kernels' levels (run by the host mirror before and after the stream):
+    with progress flags the host interpreter also checks, before the stream
+    is accepted, that every conflicting pair of accesses by two warps is
+    ordered by a flag wait and that every wait is for a level published
+    earlier in level order."""
     from gridoxide_gb300 import solver as S
     O = oracle_mod
     if name == "case10000":
@@ -30,13 +32,18 @@ def test_schedule_mirror_matches_oracle_lu(gox, oracle_mod, name, progress_flags
         g = grid_from_fixture(fx)
         yb = ybus_from_fixture(fx)
     S.set_refactor_sync(progress_flags)
+    S.set_refactor_wide(wide)
     try:
         topo = gox.Topology(yb, g.bus_type)
         assert topo.prepare(g.p_spec, g.q_spec, g.vm, g.va)
     finally:
         S.set_refactor_sync(False)
+        S.set_refactor_wide(0)
     info = topo.info()
     assert info["rf32_progress_flags"] == int(progress_flags)
+    if wide:
+        assert info["rf32_wide_levels"] > 0
+        assert name == "case118" or info["rf32_wide_phases"] > 0
     if progress_flags:
         assert 0 < info["rf32_flag_waits"] <= info["rf32_flag_warps_waited"]
     jac = O.Jacobian(yb, g.bus_type)
