@@ -228,8 +228,13 @@ def serve(gox, rates, seconds: float) -> dict:
     non-bridge branch out, warm started from the grid's base-case solution,
     through the library's serving loop (continuous batching on worker
     threads, mixed precision, host buffers).  Latency = submit to completion
-    of each request.  The last rate is the reported one; every rate is in
-    `sweep`, with p50 latency by grid size."""
+    of each request.  The rates run in increasing order until one
+    saturates (completed < 0.95 x offered, counting the drain after the last
+    arrival); that rate and every one before it are in `sweep`, with p50 and
+    p99 latency by grid size; `saturation_rps` is the highest offered rate
+    the server kept up with.  Each grid's requests draw their load vectors
+    from 32 seeded samples of the grid's distribution (the per-request host
+    copies are the grid's size whatever the sample)."""
     from gridoxide_gb300 import grids as G
     spec = G.many_topologies(count=16, n_min=100, n_max=50000, seed=5)
     grids, topos, cand, v0 = [], [], [], []
@@ -246,7 +251,9 @@ def serve(gox, rates, seconds: float) -> dict:
     sizes = np.array([x[0] for x in spec])
     bins = [("<1k", sizes < 1000), ("1k-10k", (sizes >= 1000) & (sizes < 10000)),
             (">=10k", sizes >= 10000)]
+    loads = [G.load_scenarios(g, 32, 0.1, 5000 + t) for t, (g, _) in enumerate(grids)]
     sweep = []
+    saturation = None
     for k, rate in enumerate(rates):
         srv = gox.Server(max_batch=1024, precision=gox.GOX_PRECISION_MIXED,
                          tol=WORKLOAD["tol"], max_iter=WORKLOAD["max_iter"])
@@ -255,16 +262,17 @@ def serve(gox, rates, seconds: float) -> dict:
         n_req = max(1, int(rate * seconds))
         gaps = rng.exponential(1.0 / rate, size=n_req)
         which = rng.integers(0, len(spec), size=n_req)
+        pick = rng.integers(0, 32, size=n_req)
         reqs = []
         for i in range(n_req):
             t = int(which[i])
             g, yb = grids[t]
-            p, q = G.load_scenarios(g, 1, 0.1, 5000 + 100000 * k + i)
+            p, q = loads[t][0][pick[i]], loads[t][1][pick[i]]
             out = None
             if rng.random() < 0.1:
                 br = rng.choice(cand[t], size=1)
                 out = tuple(a[0] for a in G.outage_deltas(g, yb, br))
-            reqs.append((t, p[0], q[0], out))
+            reqs.append((t, p, q, out))
         # warm-up: one request per grid (first-use allocations, pivot orders)
         for t in range(len(spec)):
             g = grids[t][0]
@@ -289,22 +297,27 @@ def serve(gox, rates, seconds: float) -> dict:
         lat = np.array(lat) * 1000.0
         nb = st["batches"] - st0["batches"]
         grid_of = np.array([r[0] for r in reqs])
-        by_size = {}
+        by_size, by_size99 = {}, {}
         for name, sel in bins:
             m = np.isin(grid_of, np.flatnonzero(sel))
             if m.any():
                 by_size[name] = round(float(np.percentile(lat[m], 50)), 3)
+                by_size99[name] = round(float(np.percentile(lat[m], 99)), 3)
         dq = (st["queue_us"] - st0["queue_us"]) / 1000.0 / n_req
         ds = (st["solve_us"] - st0["solve_us"]) / 1000.0 / n_req
+        done_rps = n_req / (t1 - t0)
         sweep.append({"offered_rps": rate, "requests": n_req,
                       "mean_queued_ms": round(dq, 3), "mean_in_solve_ms": round(ds, 3),
-                      "completed_rps": round(n_req / (t1 - t0), 1),
+                      "completed_rps": round(done_rps, 1),
                       "p50_ms": round(float(np.percentile(lat, 50)), 3),
                       "p99_ms": round(float(np.percentile(lat, 99)), 3), "batches": nb,
                       "mean_batch": round(n_req / max(nb, 1), 1), "converged": conv,
-                      "p50_ms_by_buses": by_size})
+                      "p50_ms_by_buses": by_size, "p99_ms_by_buses": by_size99})
+        if done_rps < 0.95 * rate:
+            break
+        saturation = rate
     out = dict(sweep[-1])
-    out.update({"sweep": sweep, "grids": len(spec),
+    out.update({"sweep": sweep, "grids": len(spec), "saturation_rps": saturation,
                 "buses": [int(sizes.min()), int(sizes.max())],
                 "note": "Poisson arrivals of single scenarios over 16 grids (100-50,000 buses), 10 % "
                         "with an N-1 outage, gox_server_* continuous batching on 16 workers, mixed "
@@ -608,11 +621,11 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--serve-rate", type=float, default=1000.0,
-                    help="serving leg: Poisson arrivals per second (0 = skip)")
+    ap.add_argument("--serve-rate", type=float, default=30000.0,
+                    help="serving leg: highest Poisson arrival rate of the sweep (0 = skip)")
     ap.add_argument("--many-rounds", type=int, default=3,
                     help="N-1 10,000-bus and many-topology legs: timed rounds (0 = skip)")
-    ap.add_argument("--serve-seconds", type=float, default=1.0)
+    ap.add_argument("--serve-seconds", type=float, default=2.0)
     ap.add_argument("--grid", default=WORKLOAD["grid"], help="profiling: another grid")
     ap.add_argument("--scenarios", type=int, default=WORKLOAD["scenarios"],
                     help="profiling: a smaller batch")
@@ -827,7 +840,8 @@ def main():
         "clocks": cl,
     }
     if rank == 0 and args.serve_rate > 0 and not args.quick:
-        rates = sorted({r for r in (100.0, 300.0, args.serve_rate) if r <= args.serve_rate})
+        rates = sorted({r for r in (1000.0, 3000.0, 10000.0, 30000.0, args.serve_rate)
+                        if r <= args.serve_rate})
         line["serving"] = serve(gox, rates, args.serve_seconds)
     if rank == 0 and args.many_rounds > 0 and not args.quick:
         line["n1_case10000"] = n1_case10000(gox, args.many_rounds)

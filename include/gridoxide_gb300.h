@@ -477,7 +477,9 @@ const char *gox_version(void);
  * publishes each result with its latency (submit to completion).  Lanes
  * are independent, so a request's result does not depend on the batch it
  * ran in.  A topology added to a server is used by the server's workers
- * only: do not call it directly while the server runs.
+ * only: do not call it directly while the server runs.  Its refactor plan
+ * is timed by the autotuner on its first batch at most; later batches keep
+ * that plan (or a cached one), so no timing runs inside the serving loop.
  * The reference's serving counterpart is the Python `PowerFlowModel.solve_batch`
  * / rayon `BatchSolver` call per batch (src/python.rs:306-341,
  * src/batch.rs:198-289); the queue in front of it is new here. */
