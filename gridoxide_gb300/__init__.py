@@ -16,7 +16,8 @@ from ._lib import (GOX_CONVERGED, GOX_MAX_ITERATIONS, GOX_PRECISION_FP64,  # noq
                    GOX_E_DEVICE_WAIT, GOX_PRECISION_MIXED, GOX_SINGULAR_SCENARIO, GoxError)
 from .solver import (BatchError, BatchResult, BatchSolver, Buses, BusOverride,  # noqa: F401
                      Gb300LinearSolver, JacobianBackend, PowerFlowReport, Scenario, Server,
-                     SolveStatus, Topology, analyze, factor_host, uniform_load_scaling)
+                     SolveStatus, Topology, analyze, factor_host, multi_solve,
+                     uniform_load_scaling)
 
 from .model import PowerFlowModel  # noqa: F401,E402
 

@@ -55,6 +55,7 @@ i32p = C.POINTER(C.c_int32)
 i64p = C.POINTER(C.c_int64)
 f64p = C.POINTER(C.c_double)
 vp = C.c_void_p
+vpp = C.POINTER(C.c_void_p)
 
 # name -> (restype, argtypes); every symbol include/gridoxide_gb300.h declares
 SIGNATURES = {
@@ -73,6 +74,8 @@ SIGNATURES = {
     "gox_batch_solve_qlim": (C.c_int, [vp, C.c_int32, f64p, f64p, f64p, f64p, C.c_int32, f64p, f64p,
                                        C.c_double, C.c_int32, C.c_int32, C.c_int32, f64p, f64p, i32p,
                                        i32p, f64p, i32p, C.POINTER(C.c_uint8), i32p]),
+    "gox_multi_solve": (C.c_int, [C.c_int32, vpp, i32p, vpp, vpp, vpp, vpp, i32p, C.c_double,
+                                  C.c_int32, C.c_int32, vpp, vpp, vpp, vpp, vpp]),
     "gox_batch_solve_scaled": (C.c_int, [vp, C.c_int32, f64p, f64p, f64p, f64p, f64p, C.c_double,
                                          C.c_int32, C.c_int32, f64p, f64p, i32p, i32p, f64p,
                                          f64p]),

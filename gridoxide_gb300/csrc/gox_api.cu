@@ -533,18 +533,27 @@ struct Iter {
   // kernels' backward phases (one launch each)
   static void refactor_with(const DevSchedule& ds, const StreamDev& P, int nw, size_t smem, int wl,
                             int wp, const BatchDev& D, int groups, cudaStream_t st) {
-    const SchedDev& S = ds.d;
+    wide_pre(ds, wl, D, groups, st);
+    stream_kernel(P, nw, smem, ds.d, D, groups, st);
+    wide_post(ds, wp, D, groups, st);
+  }
+  // the wide kernels' refactor levels (before the stream kernel) and their
+  // backward-substitution levels (after it)
+  static void wide_pre(const DevSchedule& ds, int wl, const BatchDev& D, int groups,
+                       cudaStream_t st) {
     for (int L = 0; L < wl; L++) {
       const long long tasks = (long long)(ds.lev_ptr_h[L + 1] - ds.lev_ptr_h[L]) * groups;
       const unsigned blocks = (unsigned)((tasks + kWideWarps - 1) / kWideWarps);
       wide_attr();
-      k_refactor_wide<T><<<blocks, 32 * kWideWarps, kWideSmem, st>>>(S, D, L, groups);
+      k_refactor_wide<T><<<blocks, 32 * kWideWarps, kWideSmem, st>>>(ds.d, D, L, groups);
     }
-    stream_kernel(P, nw, smem, S, D, groups, st);
+  }
+  static void wide_post(const DevSchedule& ds, int wp, const BatchDev& D, int groups,
+                        cudaStream_t st) {
     for (int L = wp - 1; L >= 0; L--) {
       const long long tasks = (long long)(ds.lev_ptr_h[L + 1] - ds.lev_ptr_h[L]) * groups;
       const unsigned blocks = (unsigned)((tasks + kWideWarps - 1) / kWideWarps);
-      k_solve_wide<T><<<blocks, 32 * kWideWarps, 0, st>>>(S, D, L, groups);
+      k_solve_wide<T><<<blocks, 32 * kWideWarps, 0, st>>>(ds.d, D, L, groups);
     }
   }
   static constexpr size_t kWideSmem = (size_t)kWideWarps * kWideCap * 32 * sizeof(T);
@@ -1566,7 +1575,26 @@ static int batch_device(gox_topo* t, int B, const double* p_spec, const double* 
                         double* va_out, int32_t* iters, int32_t* status, double* max_mis,
                         double* hist, cudaStream_t st, const double* h_p, const double* h_q,
                         const double* h_vm, const double* h_va, const int32_t* h_oslot,
-                        const double* h_odre, const double* h_odim) {
+                        const double* h_odre, const double* h_odim);
+
+// One batch's device state between its set-up and its results.
+struct BatchRun {
+  BatchDev D{};
+  bool outage = false, want_hist = false;
+  bool resolved = false;  // answered without a Newton loop (no Jacobian needed)
+};
+
+// The set-up of a batched solve: the linear guess, the pivot order (the
+// first solve of a topology), the schedule and streams on the device, the
+// batch buffers, the inputs in the interleaved layout, the outages.
+static int batch_prepare(gox_topo* t, int B, const double* p_spec, const double* q_spec,
+                        const double* vm0, const double* va0, int v_stride,
+                        const int32_t* o_slot, const double* o_dre, const double* o_dim,
+                        double tol, int max_iter, int precision, double* vm_out,
+                        double* va_out, int32_t* iters, int32_t* status, double* max_mis,
+                        double* hist, cudaStream_t st, const double* h_p, const double* h_q,
+                        const double* h_vm, const double* h_va, const int32_t* h_oslot,
+                        const double* h_odre, const double* h_odim, BatchRun& R) {
   const int n = t->n_bus;
   const int G = (B + 31) / 32;
   t->launches = 0;
@@ -1628,6 +1656,7 @@ static int batch_device(gox_topo* t, int B, const double* p_spec, const double* 
       GOX_CK(cudaMemcpyAsync(max_mis, mm.data(), (size_t)B * 8, cudaMemcpyHostToDevice, st));
       if (hist) GOX_CK(cudaMemcpyAsync(hist, hh.data(), hh.size() * 8, cudaMemcpyHostToDevice, st));
       GOX_CK(cudaStreamSynchronize(st));
+      R.resolved = true;
       return GOX_OK;
     }
   }
@@ -1676,8 +1705,28 @@ static int batch_device(gox_topo* t, int B, const double* p_spec, const double* 
   // topology (freeing pinned memory synchronizes the whole device, which
   // would stall every other topology's solve in flight)
   if (!t->h_nactive) GOX_CK(cudaMallocHost(&t->h_nactive, sizeof(int32_t)));
-  if (precision == GOX_PRECISION_FP64) run_iterations<double>(t, D, max_iter, outage, st, t->h_nactive);
-  else run_iterations<float>(t, D, max_iter, outage, st, t->h_nactive);
+  R.D = D;
+  R.outage = outage;
+  R.want_hist = want_hist;
+  return GOX_OK;
+}
+
+// The results of a batched solve after its Newton loop: bounded-wait
+// errors, outputs in the row-major layout, the mixed path's FP64 re-solves
+// of scenarios that tripped the pivot-ratio check.
+static int batch_finish(gox_topo* t, int B, const double* p_spec, const double* q_spec,
+                        const double* vm0, const double* va0, int v_stride,
+                        const int32_t* o_slot, const double* o_dre, const double* o_dim,
+                        double tol, int max_iter, int precision, double* vm_out,
+                        double* va_out, int32_t* iters, int32_t* status, double* max_mis,
+                        double* hist, cudaStream_t st, const double* h_p, const double* h_q,
+                        const double* h_vm, const double* h_va, const int32_t* h_oslot,
+                        const double* h_odre, const double* h_odim, BatchRun& R) {
+  const int n = t->n_bus;
+  const int G = (B + 31) / 32;
+  const BatchDev& D = R.D;
+  const bool outage = R.outage, want_hist = R.want_hist;
+  DevBatch& DB = t->batch;
   {
     int32_t herr[2] = {0, 0};
     GOX_CK(cudaMemcpyAsync(herr, DB.err.p, 8, cudaMemcpyDeviceToHost, st));
@@ -1775,6 +1824,281 @@ static int batch_device(gox_topo* t, int B, const double* p_spec, const double* 
     }
   }
   return GOX_OK;
+}
+
+static int batch_device(gox_topo* t, int B, const double* p_spec, const double* q_spec,
+                        const double* vm0, const double* va0, int v_stride,
+                        const int32_t* o_slot, const double* o_dre, const double* o_dim,
+                        double tol, int max_iter, int precision, double* vm_out,
+                        double* va_out, int32_t* iters, int32_t* status, double* max_mis,
+                        double* hist, cudaStream_t st, const double* h_p, const double* h_q,
+                        const double* h_vm, const double* h_va, const int32_t* h_oslot,
+                        const double* h_odre, const double* h_odim) {
+  BatchRun R;
+  int rc = batch_prepare(t, B, p_spec, q_spec, vm0, va0, v_stride, o_slot, o_dre, o_dim, tol,
+                         max_iter, precision, vm_out, va_out, iters, status, max_mis, hist, st, h_p,
+                         h_q, h_vm, h_va, h_oslot, h_odre, h_odim, R);
+  if (rc != GOX_OK || R.resolved) return rc;
+  if (precision == GOX_PRECISION_FP64)
+    run_iterations<double>(t, R.D, max_iter, R.outage, st, t->h_nactive);
+  else
+    run_iterations<float>(t, R.D, max_iter, R.outage, st, t->h_nactive);
+  return batch_finish(t, B, p_spec, q_spec, vm0, va0, v_stride, o_slot, o_dre, o_dim, tol, max_iter,
+                      precision, vm_out, va_out, iters, status, max_mis, hist, st, h_p, h_q, h_vm,
+                      h_va, h_oslot, h_odre, h_odim, R);
+}
+
+// ---------------------------------------------------------------------------
+// Many topologies, one Newton loop (the reference's shared work queue over
+// uneven scenarios, src/batch.rs:230-281, as one launch per phase).  Every
+// topology's batch is set up as for a single solve; then each iteration
+// runs the update, injection and decision kernels once over the work items
+// {job, block, group} of every topology still running, reads every job's
+// running-group count back at once, and runs the fill and the refactor once
+// over the running jobs' items (the refactor's CTAs listed largest job
+// first, so the longest dependency chains start first; each CTA is sized
+// for the largest plan and runs its own job's stream).  A job leaves the
+// loop at the iteration its single solve would have left it, with the same
+// kernels on the same lanes: its results are the single solve's, bit for
+// bit.  The wide kernels' levels run one launch per level over the jobs
+// whose plans have that level; only the separate solve of a topology with
+// off-diagonal BTF blocks runs per job.
+// The lists one iteration's launches run over, for a set of running jobs:
+// per kernel the jobs (the refactor's longest first) and the prefix of
+// their CTAs; per wide level the jobs whose plans have it.  All lists live
+// in one device buffer, rebuilt when a job leaves.
+struct MultiLists {
+  std::vector<int32_t> host;
+  DevMem dev;
+  struct L { size_t off = 0, job = 0; int n = 0, ctas = 0; };
+  L upd, inj, dec, fill, rf;
+  std::vector<L> wide;  // per wide level
+  MultiList view(const L& l) const {
+    MultiList m;
+    m.off = dev.as<int32_t>() + l.off;
+    m.job = dev.as<int32_t>() + l.job;
+    m.n = l.n;
+    return m;
+  }
+};
+
+template <typename T>
+static void build_lists(const std::vector<gox_topo*>& ts, const std::vector<BatchRun>& runs,
+                        const std::vector<int>& act, MultiLists& M, cudaStream_t st) {
+  const int i = sizeof(T) == 4 ? 0 : 1;
+  M.host.clear();
+  auto add = [&](const std::vector<int>& jobs, auto ctas_of) {
+    MultiLists::L l;
+    l.n = (int)jobs.size();
+    l.off = M.host.size();
+    int c = 0;
+    for (int j : jobs) {
+      M.host.push_back(c);
+      c += ctas_of(j);
+    }
+    M.host.push_back(c);
+    l.job = M.host.size();
+    for (int j : jobs) M.host.push_back(j);
+    l.ctas = c;
+    return l;
+  };
+  auto G = [&](int j) { return runs[j].D.G; };
+  M.upd = add(act, [&](int j) { return update_blocks(ts[j]->dsched.d.n_bus) * G(j); });
+  M.inj = add(act, [&](int j) { return inject_blocks(ts[j]->dsched.d.n_bus) * G(j); });
+  M.dec = add(act, [&](int j) { return G(j); });
+  M.fill = add(act, [&](int j) {
+    return fill_blocks(ts[j]->dsched.d.n_ftask, ts[j]->dsched.d.n_fzero) * G(j);
+  });
+  std::vector<int> order(act);
+  std::stable_sort(order.begin(), order.end(), [&](int a, int b) {
+    return (i == 0 ? ts[a]->s32 : ts[a]->s64).est_cycles > (i == 0 ? ts[b]->s32 : ts[b]->s64).est_cycles;
+  });
+  M.rf = add(order, [&](int j) { return G(j); });
+  int maxl = 0;
+  for (int j : act) maxl = std::max(maxl, ts[j]->dsched.st_wl[i]);
+  M.wide.clear();
+  for (int L = 0; L < maxl; L++) {
+    std::vector<int> jl;
+    for (int j : act)
+      if (ts[j]->dsched.st_wl[i] > L) jl.push_back(j);
+    M.wide.push_back(add(jl, [&](int j) {
+      const std::vector<int32_t>& lp = ts[j]->dsched.lev_ptr_h;
+      const long long tasks = (long long)(lp[L + 1] - lp[L]) * G(j);
+      return (int)((tasks + kWideWarps - 1) / kWideWarps);
+    }));
+  }
+  M.dev.ensure(M.host.size() * 4);
+  GOX_CK(cudaMemcpyAsync(M.dev.p, M.host.data(), M.host.size() * 4, cudaMemcpyHostToDevice, st));
+  GOX_CK(cudaStreamSynchronize(st));  // the host vector is rebuilt next time
+}
+
+template <typename T>
+static void upload_jobs(const std::vector<gox_topo*>& ts, const std::vector<BatchRun>& runs,
+                        DevMem& dev, cudaStream_t st) {
+  const int i = sizeof(T) == 4 ? 0 : 1;
+  std::vector<MultiJob> jobs(ts.size());
+  for (size_t j = 0; j < ts.size(); j++) {
+    jobs[j].S = ts[j]->dsched.d;
+    jobs[j].D = runs[j].D;
+    jobs[j].P = ts[j]->dsched.st[i];
+    jobs[j].nw = ts[j]->dsched.st_nw[i];
+  }
+  dev.ensure(jobs.size() * sizeof(MultiJob));
+  GOX_CK(cudaMemcpyAsync(dev.p, jobs.data(), jobs.size() * sizeof(MultiJob), cudaMemcpyHostToDevice,
+                         st));
+  GOX_CK(cudaStreamSynchronize(st));  // the host vector goes out of scope
+}
+
+template <typename T>
+static void run_multi(const std::vector<gox_topo*>& ts, std::vector<BatchRun>& runs, int max_iter,
+                      cudaStream_t st, int64_t& launches) {
+  const int nj = (int)ts.size(), i = sizeof(T) == 4 ? 0 : 1;
+  DevMem jobs, counts;
+  MultiLists M;
+  counts.ensure((size_t)nj * 4);
+  std::vector<int32_t> h_counts(nj, 0);
+  std::vector<int> act(nj);
+  for (int j = 0; j < nj; j++) act[j] = j;
+  upload_jobs<T>(ts, runs, jobs, st);
+  build_lists<T>(ts, runs, act, M, st);
+  // the refactor's CTA: the largest plan among the jobs
+  int nw_max = 1;
+  size_t smem_max = 0;
+  auto plan_size = [&]() {
+    nw_max = 1;
+    smem_max = 0;
+    for (gox_topo* t : ts) {
+      nw_max = std::max(nw_max, t->dsched.st_nw[i]);
+      smem_max = std::max(smem_max, t->dsched.st_smem[i]);
+    }
+  };
+  plan_size();
+  {
+    static std::once_flag once[64];
+    int dev = 0;
+    GOX_CK(cudaGetDevice(&dev));
+    std::call_once(once[dev & 63], [] {
+      GOX_CK(cudaFuncSetAttribute(k_refactor_multi<T>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                  (int)kRefactorSmem));
+      GOX_CK(cudaFuncSetAttribute(k_refactor_wide_multi<T>,
+                                  cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                  (int)Iter<T>::kWideSmem));
+    });
+  }
+  const MultiJob* J = nullptr;
+  auto count = [&](int zero) {
+    k_multi_counts<<<(nj + 127) / 128, 128, 0, st>>>(jobs.as<MultiJob>(), nj, counts.as<int32_t>(),
+                                                       zero);
+    launches++;
+  };
+  auto launch = [&](const MultiLists::L& l, auto kernel_launch) {
+    if (l.n > 0 && l.ctas > 0) {
+      kernel_launch((unsigned)l.ctas, M.view(l));
+      launches++;
+    }
+  };
+  // CUDA events around the phases when the first topology's timing is on:
+  // its report holds the loop's mismatch (k1), fill (k2), shared refactor
+  // launch (k3) and wide levels around it (k4)
+  const bool timing = ts[0]->timing.on;
+  std::vector<cudaEvent_t> ev;
+  auto rec = [&]() {
+    if (!timing) return;
+    cudaEvent_t e;
+    GOX_CK(cudaEventCreate(&e));
+    GOX_CK(cudaEventRecord(e, st));
+    ev.push_back(e);
+  };
+  int it = 0;
+  for (it = 0; it < max_iter && !act.empty(); it++) {
+    J = jobs.as<MultiJob>();
+    rec();
+    count(1);
+    launch(M.upd, [&](unsigned c, MultiList l) { k_update_multi<T><<<c, 256, 0, st>>>(J, l, it, 0); });
+    launch(M.inj, [&](unsigned c, MultiList l) { k_inject_multi<T><<<c, 256, 0, st>>>(J, l, it); });
+    launch(M.dec, [&](unsigned c, MultiList l) { k_decide_multi<<<c, 32, 0, st>>>(J, l, it, 0); });
+    count(0);
+    rec();
+    GOX_CK(cudaMemcpyAsync(h_counts.data(), counts.p, (size_t)nj * 4, cudaMemcpyDeviceToHost, st));
+    GOX_CK(cudaStreamSynchronize(st));
+    std::vector<int> still;
+    for (int j : act)
+      if (h_counts[j] > 0) still.push_back(j);
+    if (still.size() != act.size()) {
+      act.swap(still);
+      if (act.empty()) break;
+      build_lists<T>(ts, runs, act, M, st);
+    }
+    rec();
+    launch(M.fill, [&](unsigned c, MultiList l) { k_fill_multi<T><<<c, 32 * kWarps, 0, st>>>(J, l); });
+    rec();
+    // a job whose plan was not timed yet: the autotuner, as its single
+    // solve would run it here
+    bool retuned = false;
+    for (int j : act)
+      if (!ts[j]->tune[i].done) {
+        autotune<T>(ts[j], runs[j].D, st);
+        retuned = true;
+      }
+    if (retuned) {
+      upload_jobs<T>(ts, runs, jobs, st);
+      build_lists<T>(ts, runs, act, M, st);
+      plan_size();
+      J = jobs.as<MultiJob>();
+    }
+    rec();
+    for (size_t L = 0; L < M.wide.size(); L++)
+      launch(M.wide[L], [&](unsigned c, MultiList l) {
+        k_refactor_wide_multi<T><<<c, 32 * kWideWarps, Iter<T>::kWideSmem, st>>>(J, l, (int)L);
+      });
+    rec();
+    launch(M.rf, [&](unsigned c, MultiList l) {
+      k_refactor_multi<T><<<c, 32 * nw_max, smem_max, st>>>(J, l);
+    });
+    rec();
+    for (size_t L = M.wide.size(); L-- > 0;)
+      launch(M.wide[L], [&](unsigned c, MultiList l) {
+        k_solve_wide_multi<T><<<c, 32 * kWideWarps, 0, st>>>(J, l, (int)L);
+      });
+    for (int j : act) launches += Iter<T>::solve_rest(ts[j]->dsched, runs[j].D, st);
+    rec();
+    GOX_CK(cudaGetLastError());
+  }
+  if (it == max_iter && !act.empty()) {
+    // the budget ran out with scenarios still running: their MaxIterations
+    // mismatch (update and decision, as the single solve's last step)
+    J = jobs.as<MultiJob>();
+    launch(M.upd, [&](unsigned c, MultiList l) {
+      k_update_multi<T><<<c, 256, 0, st>>>(J, l, max_iter, 1);
+    });
+    launch(M.dec, [&](unsigned c, MultiList l) {
+      k_decide_multi<<<c, 32, 0, st>>>(J, l, max_iter, 1);
+    });
+  }
+  GOX_CK(cudaStreamSynchronize(st));
+  GOX_CK(cudaGetLastError());
+  if (timing && ev.size() >= 2) {
+    // per full iteration 8 events: [0] mismatch [1] | [2] fill [3] | [4]
+    // wide levels [5] refactor [6] wide backward levels [7]; the last
+    // iteration may stop after [1]
+    auto el = [&](size_t a, size_t b) {
+      float ms = 0;
+      GOX_CK(cudaEventElapsedTime(&ms, ev[a], ev[b]));
+      return (double)ms;
+    };
+    Timing& T_ = ts[0]->timing;
+    T_.iters = it;
+    T_.total = el(0, ev.size() - 1);
+    T_.k1 = T_.k2 = T_.k3 = T_.k4 = 0;
+    for (size_t b = 0; b + 1 < ev.size(); b += 8) {
+      T_.k1 += el(b, b + 1);
+      if (b + 7 >= ev.size()) break;
+      T_.k2 += el(b + 2, b + 3);
+      T_.k3 += el(b + 5, b + 6);
+      T_.k4 += el(b + 4, b + 5) + el(b + 6, b + 7);
+    }
+    for (auto e : ev) cudaEventDestroy(e);
+  }
 }
 
 // ---------------------------------------------------------------------------
@@ -2368,6 +2692,96 @@ int gox_batch_solve(gox_topo* t, int32_t B, const double* p_spec, const double* 
     GOX_CK(cudaMemcpyAsync(max_mismatch, dmm.p, (size_t)B * 8, cudaMemcpyDeviceToHost, st));
     if (history)
       GOX_CK(cudaMemcpyAsync(history, dh.p, (size_t)B * max_iter * 8, cudaMemcpyDeviceToHost, st));
+    GOX_CK(cudaStreamSynchronize(st));
+    return GOX_OK;
+  });
+}
+
+int gox_multi_solve(int32_t n_topo, gox_topo* const* topos, const int32_t* batch,
+                    const double* const* p_spec, const double* const* q_spec,
+                    const double* const* vm0, const double* const* va0, const int32_t* v_stride,
+                    double tol, int32_t max_iter, int32_t precision, double* const* vm_out,
+                    double* const* va_out, int32_t* const* iterations, int32_t* const* status,
+                    double* const* max_mismatch) {
+  if (n_topo < 0 || (n_topo > 0 && (!topos || !batch || !p_spec || !q_spec || !vm0 || !va0 ||
+                                    !v_stride || !vm_out || !va_out || !iterations || !status ||
+                                    !max_mismatch)))
+    return GOX_E_INVALID;
+  if (max_iter <= 0) return GOX_E_INVALID;
+  std::vector<int> jobs;
+  for (int j = 0; j < n_topo; j++) {
+    gox_topo* t = topos[j];
+    int c = check_batch_args(t, batch[j], p_spec[j], q_spec[j], vm0[j], va0[j], v_stride[j], tol,
+                             max_iter, precision, vm_out[j], va_out[j], iterations[j], status[j],
+                             max_mismatch[j], nullptr, nullptr, nullptr);
+    if (c < 0) return c;
+    if (!t->zip.empty()) return GOX_E_INVALID;  // ZIP terms: one gox_batch_solve per topology
+    for (int k : jobs)
+      if (topos[k] == t) return GOX_E_INVALID;  // a topology's buffers serve one batch
+    if (c > 0) jobs.push_back(j);
+  }
+  if (jobs.empty()) return GOX_OK;
+  if (int r = require_device()) return r;
+  return guard_impl([&]() -> int {
+    cudaStream_t st = thread_stream();
+    AllocStreamScope alloc_scope(st);
+    std::vector<gox_topo*> ts;
+    std::vector<BatchRun> runs;
+    std::vector<int> of;  // job -> argument index
+    for (int j : jobs) {
+      gox_topo* t = topos[j];
+      const int B = batch[j], n = t->n_bus;
+      const size_t bn = (size_t)B * n, nv = (size_t)(v_stride[j] ? B : 1) * n;
+      IoStage& io = t->io;
+      io.p.ensure(bn * 8); io.q.ensure(bn * 8); io.vm.ensure(nv * 8); io.va.ensure(nv * 8);
+      io.ovm.ensure(bn * 8); io.ova.ensure(bn * 8); io.it.ensure((size_t)B * 4);
+      io.st.ensure((size_t)B * 4); io.mm.ensure((size_t)B * 8);
+      GOX_CK(cudaMemcpyAsync(io.p.p, p_spec[j], bn * 8, cudaMemcpyHostToDevice, st));
+      GOX_CK(cudaMemcpyAsync(io.q.p, q_spec[j], bn * 8, cudaMemcpyHostToDevice, st));
+      GOX_CK(cudaMemcpyAsync(io.vm.p, vm0[j], nv * 8, cudaMemcpyHostToDevice, st));
+      GOX_CK(cudaMemcpyAsync(io.va.p, va0[j], nv * 8, cudaMemcpyHostToDevice, st));
+      BatchRun R;
+      const int rc = batch_prepare(
+          t, B, io.p.as<double>(), io.q.as<double>(), io.vm.as<double>(), io.va.as<double>(),
+          v_stride[j], nullptr, nullptr, nullptr, tol, max_iter, precision, io.ovm.as<double>(),
+          io.ova.as<double>(), io.it.as<int32_t>(), io.st.as<int32_t>(), io.mm.as<double>(),
+          nullptr, st, p_spec[j], q_spec[j], vm0[j], va0[j], nullptr, nullptr, nullptr, R);
+      if (rc != GOX_OK) return rc;
+      if (!R.resolved) {
+        ts.push_back(t);
+        runs.push_back(R);
+        of.push_back(j);
+      }
+    }
+    int64_t launches = 0;
+    if (!ts.empty()) {
+      if (precision == GOX_PRECISION_FP64) run_multi<double>(ts, runs, max_iter, st, launches);
+      else run_multi<float>(ts, runs, max_iter, st, launches);
+    }
+    for (size_t k = 0; k < ts.size(); k++) {
+      const int j = of[k];
+      gox_topo* t = ts[k];
+      IoStage& io = t->io;
+      const int rc = batch_finish(
+          t, batch[j], io.p.as<double>(), io.q.as<double>(), io.vm.as<double>(),
+          io.va.as<double>(), v_stride[j], nullptr, nullptr, nullptr, tol, max_iter, precision,
+          io.ovm.as<double>(), io.ova.as<double>(), io.it.as<int32_t>(), io.st.as<int32_t>(),
+          io.mm.as<double>(), nullptr, st, p_spec[j], q_spec[j], vm0[j], va0[j], nullptr, nullptr,
+          nullptr, runs[k]);
+      if (rc != GOX_OK) return rc;
+      t->launches += launches / (int64_t)ts.size();
+    }
+    for (int j : jobs) {
+      gox_topo* t = topos[j];
+      const int B = batch[j];
+      const size_t bn = (size_t)B * t->n_bus;
+      IoStage& io = t->io;
+      GOX_CK(cudaMemcpyAsync(vm_out[j], io.ovm.p, bn * 8, cudaMemcpyDeviceToHost, st));
+      GOX_CK(cudaMemcpyAsync(va_out[j], io.ova.p, bn * 8, cudaMemcpyDeviceToHost, st));
+      GOX_CK(cudaMemcpyAsync(iterations[j], io.it.p, (size_t)B * 4, cudaMemcpyDeviceToHost, st));
+      GOX_CK(cudaMemcpyAsync(status[j], io.st.p, (size_t)B * 4, cudaMemcpyDeviceToHost, st));
+      GOX_CK(cudaMemcpyAsync(max_mismatch[j], io.mm.p, (size_t)B * 8, cudaMemcpyDeviceToHost, st));
+    }
     GOX_CK(cudaStreamSynchronize(st));
     return GOX_OK;
   });

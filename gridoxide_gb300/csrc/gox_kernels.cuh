@@ -141,11 +141,12 @@ __device__ __forceinline__ double from_T(T v) {
 // K5 + K1a.  grid (ceil(N/8), G), 8 warps: warp -> bus, lane -> scenario.
 // mode 0: iteration `it`; mode 1: the update after the last iteration.
 template <typename T>
-__global__ void __launch_bounds__(256) k_update(SchedDev S, BatchDev D, int it, int mode) {
+__device__ __forceinline__ void update_body(const SchedDev& S, const BatchDev& D, int it, int mode,
+                                            int BX, int BY) {
   if (it < 0) it = *D.itp;
-  const int g = blockIdx.y;
+  const int g = BY;
   const int lane = threadIdx.x & 31;
-  const int i = blockIdx.x * 8 + (threadIdx.x >> 5);
+  const int i = BX * 8 + (threadIdx.x >> 5);
   const int N = S.n_bus;
   if (i >= N) return;
   const int s = g * 32 + lane;
@@ -209,6 +210,10 @@ __global__ void __launch_bounds__(256) k_update(SchedDev S, BatchDev D, int it, 
   // costs far more than an FP32 one on this GPU)
   ((T*)D.ivT)[x] = (T)1 / to_T<T>(vm);
 }
+template <typename T>
+__global__ void __launch_bounds__(256) k_update(SchedDev S, BatchDev D, int it, int mode) {
+  update_body<T>(S, D, it, mode, blockIdx.x, blockIdx.y);
+}
 
 // ---------------------------------------------------------------------------
 // K1b: S = V conj(Y V), F, max|F|.  grid (ceil(N / (8*BPW)), G), 8 warps,
@@ -249,9 +254,10 @@ __device__ __forceinline__ unsigned long long abs_bits(double v) {
 }
 
 template <typename T, bool OUTAGE, int BPW, bool ZIP>
-__global__ void __launch_bounds__(256) k_inject(SchedDev S, BatchDev D, int it) {
+__device__ __forceinline__ void inject_body(const SchedDev& S, const BatchDev& D, int it, int BX,
+                                            int BY) {
   if (it < 0) it = *D.itp;
-  const int g = blockIdx.y;
+  const int g = BY;
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   const int s = g * 32 + lane;
   const int N = S.n_bus;
@@ -263,7 +269,7 @@ __global__ void __launch_bounds__(256) k_inject(SchedDev S, BatchDev D, int it) 
   int obf = -1, obt = -1;
   if (OUTAGE) { obf = D.o_bf[s]; obt = D.o_bt[s]; }
   unsigned long long mx = 0ull;
-  const int i0 = (blockIdx.x * 8 + warp) * BPW;
+  const int i0 = (BX * 8 + warp) * BPW;
   for (int i = i0; i < min(N, i0 + BPW); i++) {
     double ir = 0.0, ii = 0.0;
     int p = __ldg(S.yp + i);
@@ -350,10 +356,14 @@ __global__ void __launch_bounds__(256) k_inject(SchedDev S, BatchDev D, int it) 
     if (active && m > 0ull) atomicMax(D.maxacc + s, m);
   }
 }
+template <typename T, bool OUTAGE, int BPW, bool ZIP>
+__global__ void __launch_bounds__(256) k_inject(SchedDev S, BatchDev D, int it) {
+  inject_body<T, OUTAGE, BPW, ZIP>(S, D, it, blockIdx.x, blockIdx.y);
+}
 
-__global__ void k_decide(BatchDev D, int it, int mode) {
+__device__ __forceinline__ void decide_body(const BatchDev& D, int it, int mode, int BX) {
   if (it < 0) it = *D.itp;
-  const int g = blockIdx.x, lane = threadIdx.x;
+  const int g = BX, lane = threadIdx.x;
   const int s = g * 32 + lane;
   bool running = D.status[s] == ST_RUNNING;
   if (running) {
@@ -383,6 +393,7 @@ __global__ void k_decide(BatchDev D, int it, int mode) {
     if (any) atomicAdd(D.nactive, 1);
   }
 }
+__global__ void k_decide(BatchDev D, int it, int mode) { decide_body(D, it, mode, blockIdx.x); }
 
 // The graph-captured Newton loop's decision, one thread after k_decide: run
 // this iteration's Jacobian, refactor and solves while a scenario is running
@@ -419,11 +430,12 @@ __device__ __forceinline__ void fill_store(T* LU, T* OFF, int n_slots, int x, in
 }
 
 template <typename T, bool OUTAGE>
-__global__ void __launch_bounds__(256) k_fill(SchedDev S, BatchDev D, int tw, int per_warp) {
-  const int g = blockIdx.y;
+__device__ __forceinline__ void fill_body(const SchedDev& S, const BatchDev& D, int tw, int per_warp,
+                                          int BX, int BY) {
+  const int g = BY;
   if (!D.gact[g]) return;
   const int lane = threadIdx.x & 31;
-  const int wglob = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
+  const int wglob = BX * (blockDim.x >> 5) + (threadIdx.x >> 5);
   const int N = S.n_bus;
   T* LU = (T*)D.lu + (size_t)g * S.n_slots * 32u;
   T* OFF = (T*)D.off + (size_t)g * S.n_off * 32u;
@@ -533,6 +545,10 @@ __global__ void __launch_bounds__(256) k_fill(SchedDev S, BatchDev D, int tw, in
       fill_store(LU, OFF, S.n_slots, dst[u].w, lane, l);
     }
   }
+}
+template <typename T, bool OUTAGE>
+__global__ void __launch_bounds__(256) k_fill(SchedDev S, BatchDev D, int tw, int per_warp) {
+  fill_body<T, OUTAGE>(S, D, tw, per_warp, blockIdx.x, blockIdx.y);
 }
 
 // Bulk (TMA) copy global -> shared with mbarrier completion, and a bounded
@@ -866,9 +882,10 @@ struct Rf {
 // malformed command, sets the error flag; the warp then drains its copies
 // and still takes every remaining barrier.
 template <typename T>
-__global__ void __launch_bounds__(sizeof(T) == 4 ? 32 * kMaxRefactorWarps : 256, 1) k_refactor(StreamDev P, SchedDev S, BatchDev D) {
+__device__ __forceinline__ void refactor_body(const StreamDev& P, const SchedDev& S, const BatchDev& D,
+                                              int BX, int NW) {
   using R = Rf<T>;
-  const int g = blockIdx.x;
+  const int g = BX;
   if (!D.gact[g]) return;
   extern __shared__ __align__(128) unsigned char smem_raw[];
   __shared__ __align__(8) uint64_t mbar[kMaxRefactorWarps][2];
@@ -876,7 +893,7 @@ __global__ void __launch_bounds__(sizeof(T) == 4 ? 32 * kMaxRefactorWarps : 256,
   __shared__ int prog[kMaxRefactorWarps];  // levels each warp has published (progress flags)
   __shared__ volatile int timed_out;
   constexpr uint32_t RB = R::RB;
-  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = NW;
   const int CW = P.chunk_words;
   int32_t* cbuf = reinterpret_cast<int32_t*>(smem_raw) + (size_t)warp * 2 * CW;
   const uint32_t ring_s = smem_u32(smem_raw + (size_t)nw * 2 * CW * 4);
@@ -901,18 +918,22 @@ __global__ void __launch_bounds__(sizeof(T) == 4 ? 32 * kMaxRefactorWarps : 256,
   if (warp == 0) sts(ring_lane + (uint32_t)P.rows_total * RB, (T)0);
   __syncthreads();
 
-  const int32_t* gw = P.words + (size_t)P.chunk0[warp] * CW;
-  const int nch = P.nchunks[warp];
-  if (lane == 0) {
+  // warps beyond the plan's (a CTA sized for another topology's larger
+  // plan, in a launch over several topologies) run no stream: they only
+  // take the plan's barriers
+  const bool runs = warp < nw;
+  const int32_t* gw = runs ? P.words + (size_t)P.chunk0[warp] * CW : P.words;
+  const int nch = runs ? P.nchunks[warp] : 0;
+  if (runs && lane == 0) {
     bulk_load(cbuf, gw, (unsigned)CW * 4u, &mbar[warp][0]);
     if (nch > 1) bulk_load(cbuf + CW, gw + CW, (unsigned)CW * 4u, &mbar[warp][1]);
   }
   // bulk copies issued into / completions waited for, per chunk buffer (warp
   // uniform): a warp that stops early waits for the copies still in flight
   // before the CTA can exit
-  int issued0 = 1, issued1 = nch > 1 ? 1 : 0, waited0 = 0, waited1 = 0;
+  int issued0 = runs ? 1 : 0, issued1 = nch > 1 ? 1 : 0, waited0 = 0, waited1 = 0;
   unsigned par0 = 0u, par1 = 0u;
-  bool ok = mbar_wait(&mbar[warp][0], par0);
+  bool ok = runs && mbar_wait(&mbar[warp][0], par0);
   if (ok) waited0++;
   par0 ^= 1u;
   int chunk = 0, buf = 0, pc = 0, bars = 0, lev = 0;
@@ -1085,7 +1106,9 @@ __global__ void __launch_bounds__(sizeof(T) == 4 ? 32 * kMaxRefactorWarps : 256,
     if (pc >= CW) ok = false;  // a command ran past its chunk
   }
 done:
-  if (!ok) {
+  if (!runs)
+    for (; bars < P.n_bars; bars++) __syncthreads();
+  if (!ok && runs) {
     if (lane == 0) atomicExch((int*)&timed_out, 1);
     asm volatile("cp.async.wait_all;\n" ::: "memory");
     // stream chunks still being copied into this warp's buffers: wait for
@@ -1104,6 +1127,11 @@ done:
     if (flags[1][lane]) D.piv_flag[s] = 1;
     if (lane == 0 && timed_out && D.err) atomicExch(D.err, 1);
   }
+}
+template <typename T>
+__global__ void __launch_bounds__(sizeof(T) == 4 ? 32 * kMaxRefactorWarps : 256, 1)
+    k_refactor(StreamDev P, SchedDev S, BatchDev D) {
+  refactor_body<T>(P, S, D, blockIdx.x, blockDim.x >> 5);
 }
 
 // ---------------------------------------------------------------------------
@@ -1124,12 +1152,12 @@ done:
 constexpr int kWideWarps = 4;  // warps per CTA of the wide kernels
 
 template <typename T>
-__global__ void __launch_bounds__(32 * kWideWarps) k_refactor_wide(SchedDev S, BatchDev D, int lev,
-                                                                   int groups) {
+__device__ __forceinline__ void refactor_wide_body(const SchedDev& S, const BatchDev& D, int lev,
+                                                   int groups, int BX) {
   extern __shared__ __align__(16) unsigned char wsm[];
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   const int q0 = S.lev_ptr[lev], ncol = S.lev_ptr[lev + 1] - q0;
-  const long long task = (long long)blockIdx.x * kWideWarps + warp;
+  const long long task = (long long)BX * kWideWarps + warp;
   if (task >= (long long)ncol * groups) return;
   const int g = (int)(task % groups), q = (int)(task / groups);
   if (!D.gact[g]) return;
@@ -1185,17 +1213,22 @@ __global__ void __launch_bounds__(32 * kWideWarps) k_refactor_wide(SchedDev S, B
   if (bad) D.sing[s] = 1;
   if (tiny) D.piv_flag[s] = 1;
 }
+template <typename T>
+__global__ void __launch_bounds__(32 * kWideWarps) k_refactor_wide(SchedDev S, BatchDev D, int lev,
+                                                                   int groups) {
+  refactor_wide_body<T>(S, D, lev, groups, blockIdx.x);
+}
 
 // The backward substitution of one wide refactor level's rows: x_k = (y_k -
 // sum U(k, j) x_j) / U(k, k), terms in the stream's order, one warp per
 // (row, group).  A row needs only rows of higher levels, so the levels run
 // from the last wide one down, after the stream kernel has solved the rest.
 template <typename T>
-__global__ void __launch_bounds__(32 * kWideWarps) k_solve_wide(SchedDev S, BatchDev D, int lev,
-                                                                int groups) {
+__device__ __forceinline__ void solve_wide_body(const SchedDev& S, const BatchDev& D, int lev,
+                                                int groups, int BX) {
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   const int q0 = S.lev_ptr[lev], nrow = S.lev_ptr[lev + 1] - q0;
-  const long long task = (long long)blockIdx.x * kWideWarps + warp;
+  const long long task = (long long)BX * kWideWarps + warp;
   if (task >= (long long)nrow * groups) return;
   const int g = (int)(task % groups), q = (int)(task / groups);
   if (!D.gact[g]) return;
@@ -1208,6 +1241,115 @@ __global__ void __launch_bounds__(32 * kWideWarps) k_solve_wide(SchedDev S, Batc
   const T x = v / LUr[(size_t)S.diag_slot[k] * 32];
   if (!isfinite(x)) D.sing[g * 32 + lane] = 1;
   Xg[(size_t)k * 32] = x;
+}
+template <typename T>
+__global__ void __launch_bounds__(32 * kWideWarps) k_solve_wide(SchedDev S, BatchDev D, int lev,
+                                                                int groups) {
+  solve_wide_body<T>(S, D, lev, groups, blockIdx.x);
+}
+
+// ---------------------------------------------------------------------------
+// Many topologies in one launch per phase.  A job is one topology's batch:
+// its schedule, batch buffers and refactor stream.  A launch covers a list
+// of jobs: off[k] .. off[k+1] are the CTAs of the list's k-th job (its
+// blocks of every group, group-major), so a CTA finds its job by binary
+// search over the n + 1 offsets, copies the job's descriptors into shared
+// memory and runs the same body as the single-topology kernel on them:
+// every scenario's arithmetic is the same.  The refactor's list names the
+// largest jobs first, so the block scheduler starts the longest dependency
+// chains first.
+struct __align__(16) MultiJob {
+  SchedDev S;
+  BatchDev D;
+  StreamDev P;
+  int nw;  // warps of the job's refactor plan
+};
+static_assert(sizeof(MultiJob) % 16 == 0, "jobs are copied as int4");
+
+struct MultiList {
+  const int32_t* off;  // [n + 1] first CTA of each listed job
+  const int32_t* job;  // [n] job index
+  int n;
+};
+
+// the listed job of this CTA (its copy in J) and the CTA's index within it
+__device__ __forceinline__ int enter_job(MultiJob& J, const MultiJob* __restrict__ jobs,
+                                         const MultiList& L) {
+  const int b = blockIdx.x;
+  int lo = 0, hi = L.n;
+  while (hi - lo > 1) {
+    const int mid = (lo + hi) >> 1;
+    if (L.off[mid] <= b) lo = mid;
+    else hi = mid;
+  }
+  const int4* a = reinterpret_cast<const int4*>(jobs + L.job[lo]);
+  int4* d = reinterpret_cast<int4*>(&J);
+  for (int i = threadIdx.x; i < (int)(sizeof(MultiJob) / 16); i += blockDim.x) d[i] = a[i];
+  __syncthreads();
+  return b - L.off[lo];
+}
+
+// CTAs per group of each kernel (the single-topology grids' x extent)
+__device__ __host__ __forceinline__ int update_blocks(int n_bus) { return (n_bus + 7) / 8; }
+__device__ __host__ __forceinline__ int inject_blocks(int n_bus) { return (n_bus + 31) / 32; }
+__device__ __host__ __forceinline__ int fill_blocks(int n_ftask, int n_fzero) {
+  return ((n_ftask + 7) / 8 + (n_fzero + 31) / 32 + 7) / 8;
+}
+
+template <typename T>
+__global__ void __launch_bounds__(256) k_update_multi(const MultiJob* __restrict__ jobs,
+                                                      MultiList L, int it, int mode) {
+  __shared__ __align__(16) MultiJob J;
+  const int b = enter_job(J, jobs, L), nb = update_blocks(J.S.n_bus);
+  update_body<T>(J.S, J.D, it, mode, b % nb, b / nb);
+}
+template <typename T>
+__global__ void __launch_bounds__(256) k_inject_multi(const MultiJob* __restrict__ jobs,
+                                                      MultiList L, int it) {
+  __shared__ __align__(16) MultiJob J;
+  const int b = enter_job(J, jobs, L), nb = inject_blocks(J.S.n_bus);
+  inject_body<T, false, 4, false>(J.S, J.D, it, b % nb, b / nb);
+}
+__global__ void k_decide_multi(const MultiJob* __restrict__ jobs, MultiList L, int it, int mode) {
+  __shared__ __align__(16) MultiJob J;
+  const int b = enter_job(J, jobs, L);
+  decide_body(J.D, it, mode, b);
+}
+template <typename T>
+__global__ void __launch_bounds__(256) k_fill_multi(const MultiJob* __restrict__ jobs, MultiList L) {
+  __shared__ __align__(16) MultiJob J;
+  const int b = enter_job(J, jobs, L), nb = fill_blocks(J.S.n_ftask, J.S.n_fzero);
+  fill_body<T, false>(J.S, J.D, (J.S.n_ftask + 7) / 8, 8, b % nb, b / nb);
+}
+template <typename T>
+__global__ void __launch_bounds__(sizeof(T) == 4 ? 32 * kMaxRefactorWarps : 256, 1)
+    k_refactor_multi(const MultiJob* __restrict__ jobs, MultiList L) {
+  __shared__ __align__(16) MultiJob J;
+  const int b = enter_job(J, jobs, L);
+  refactor_body<T>(J.P, J.S, J.D, b, J.nw);
+}
+// one wide level `lev` of every listed job (each job's CTAs: its columns of
+// that level times its groups, kWideWarps tasks per CTA)
+template <typename T>
+__global__ void __launch_bounds__(32 * kWideWarps) k_refactor_wide_multi(
+    const MultiJob* __restrict__ jobs, MultiList L, int lev) {
+  __shared__ __align__(16) MultiJob J;
+  const int b = enter_job(J, jobs, L);
+  refactor_wide_body<T>(J.S, J.D, lev, J.D.G, b);
+}
+template <typename T>
+__global__ void __launch_bounds__(32 * kWideWarps) k_solve_wide_multi(
+    const MultiJob* __restrict__ jobs, MultiList L, int lev) {
+  __shared__ __align__(16) MultiJob J;
+  const int b = enter_job(J, jobs, L);
+  solve_wide_body<T>(J.S, J.D, lev, J.D.G, b);
+}
+// every job's running-group counter to zero / into one array (one read back)
+__global__ void k_multi_counts(const MultiJob* __restrict__ jobs, int n, int32_t* out, int zero) {
+  for (int j = blockIdx.x * blockDim.x + threadIdx.x; j < n; j += gridDim.x * blockDim.x) {
+    if (zero) *jobs[j].D.nactive = 0;
+    else out[j] = *jobs[j].D.nactive;
+  }
 }
 
 // ---------------------------------------------------------------------------

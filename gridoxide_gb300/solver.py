@@ -165,6 +165,41 @@ def set_refactor_sync(progress_flags: bool) -> None:
     check(_lib.load().gox_set_refactor_sync(1 if progress_flags else 0), "gox_set_refactor_sync")
 
 
+def multi_solve(jobs, tol=1e-8, max_iter=20, precision=GOX_PRECISION_MIXED) -> list:
+    """Many topologies' batches in one Newton loop (gox_multi_solve): each
+    phase of each iteration is one launch over every topology still
+    running.  `jobs`: (Topology, p_spec [B, N], q_spec [B, N], vm0, va0)
+    with vm0 / va0 [N] (shared) or [B, N]; each topology at most once.
+    Returns one BatchResult per job, equal bit for bit to Topology.solve on
+    that job alone."""
+    n = len(jobs)
+    keep, outs = [], []
+    topo_a = (C.c_void_p * n)()
+    arr = {k: (C.c_void_p * n)() for k in ("p", "q", "vm", "va", "ovm", "ova", "it", "st", "mm")}
+    batch = np.zeros(n, np.int32)
+    vstride = np.zeros(n, np.int32)
+    for j, (topo, p, q, vm0, va0) in enumerate(jobs):
+        p, q = _f64(p), _f64(q)
+        B, N = p.shape
+        vm0, va0 = _f64(vm0), _f64(va0)
+        batch[j] = B
+        vstride[j] = N if vm0.ndim == 2 else 0
+        res = BatchResult(np.zeros((B, N)), np.zeros((B, N)), np.zeros(B, np.int32),
+                          np.zeros(B, np.int32), np.zeros(B))
+        keep += [p, q, vm0, va0]
+        outs.append(res)
+        topo_a[j] = topo.handle.value
+        for k, a in (("p", p), ("q", q), ("vm", vm0), ("va", va0), ("ovm", res.voltage_mag),
+                     ("ova", res.voltage_ang), ("it", res.iterations), ("st", res.status),
+                     ("mm", res.max_mismatch)):
+            arr[k][j] = a.ctypes.data
+    check(_lib.load().gox_multi_solve(
+        n, topo_a, _p(batch, _lib.i32p), arr["p"], arr["q"], arr["vm"], arr["va"],
+        _p(vstride, _lib.i32p), float(tol), int(max_iter), int(precision), arr["ovm"], arr["ova"],
+        arr["it"], arr["st"], arr["mm"]), "gox_multi_solve")
+    return outs
+
+
 def set_refactor_wide(min_width: int) -> None:
     """The wide kernels in the default refactor plan of topologies analysed
     from now on: leading refactor levels / trailing backward phases with at
