@@ -108,7 +108,10 @@ def make_inputs(world: int = 1, rank: int = 0):
     global batch and cut into contiguous shards (replicas.shard_bounds)."""
     from gridoxide_gb300 import grids as G
     from gridoxide_gb300 import replicas
-    g = G.config_grid(WORKLOAD["grid"])
+    if WORKLOAD["grid"].startswith("fam"):  # profiling: a family grid of that many buses
+        g = G.family_grid(int(WORKLOAD["grid"][3:]), 77)
+    else:
+        g = G.config_grid(WORKLOAD["grid"])
     yb = G.build_ybus(g)
     total = WORKLOAD["scenarios"] * world
     p, q = G.load_scenarios(g, total, WORKLOAD["sigma"], WORKLOAD["seed"])
@@ -648,6 +651,13 @@ def main():
                     help="profiling: a smaller batch")
     ap.add_argument("--quick", action="store_true",
                     help="profiling: mixed-precision steps only (no FP64, e2e, CPU legs)")
+    ap.add_argument("--no-autotune", action="store_true",
+                    help="profiling: the default refactor plan, no candidate timing")
+    ap.add_argument("--wide", type=int, default=0,
+                    help="profiling: the default plan's wide split (narrowest wide level)")
+    ap.add_argument("--host-loop", action="store_true",
+                    help="profiling: host-driven Newton loop on one host thread (no graph, no "
+                         "split halves)")
     args = ap.parse_args()
     WORKLOAD["grid"] = args.grid
     WORKLOAD["scenarios"] = args.scenarios
@@ -668,10 +678,17 @@ def main():
     torch.cuda.set_device(local)
     dev = torch.device("cuda", local)
     gox.build.build()
+    if args.no_autotune:
+        from gridoxide_gb300 import solver as S
+        S.set_autotune(False)
+        S.set_refactor_wide(args.wide)
 
     g, yb, p, q = make_inputs(world, rank)
     B, N = p.shape
     topo = gox.Topology(yb, g.bus_type)
+    if args.host_loop:
+        topo.set_graph(False)
+        topo.set_split(1)
     stream = torch.cuda.Stream(device=dev)
     tp = torch.from_numpy(p).to(dev)
     tq = torch.from_numpy(q).to(dev)
@@ -856,15 +873,18 @@ def main():
         "kernels": kernels,
         "clocks": cl,
     }
-    if rank == 0 and args.serve_rate > 0 and not args.quick:
-        rates = sorted({r for r in (1000.0, 3000.0, 10000.0, 30000.0, args.serve_rate)
-                        if r <= args.serve_rate})
-        line["serving"] = serve(gox, rates, args.serve_seconds)
     if rank == 0 and args.many_rounds > 0 and not args.quick:
         line["n1_case10000"] = n1_case10000(gox, args.many_rounds)
         line["many_topologies"] = many_topologies(gox, args.many_rounds)
         line["pgm_batch"] = pgm_batch(gox, args.many_rounds)
         line["qlim_case2000"] = qlim_case2000(gox, args.many_rounds)
+    # serving last: its 16 grids' refactor plans (tuned on one-group batches)
+    # enter the process's plan cache, where later topologies of the same
+    # size, fill and batch bucket would take them untimed
+    if rank == 0 and args.serve_rate > 0 and not args.quick:
+        rates = sorted({r for r in (1000.0, 3000.0, 10000.0, 30000.0, args.serve_rate)
+                        if r <= args.serve_rate})
+        line["serving"] = serve(gox, rates, args.serve_seconds)
     if rank == 0 and not args.no_cpu_baseline:
         threads = os.cpu_count() or 1
         v, dt, passes, ref = cpu_baseline(g, yb, p, q, threads)
