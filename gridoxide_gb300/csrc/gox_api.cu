@@ -254,6 +254,7 @@ struct DevSchedule {
   size_t st_smem[2] = {0, 0};
   bool st_bwd[2] = {false, false};  // the stream runs the backward substitution too
   int st_wl[2] = {0, 0}, st_wp[2] = {0, 0};  // levels / phases the wide kernels run
+  int st_wr[2] = {0, 0};                      // their stage rows per warp
   std::vector<int32_t> lev_ptr_h;  // host copy: columns per refactor level
   // launches of one refactor (with both substitutions when the stream has them)
   int refactor_launches(int i) const { return 1 + st_wl[i] + st_wp[i]; }
@@ -277,6 +278,7 @@ struct DevSchedule {
       st_bwd[i] = ss[i]->has_bwd;
       st_wl[i] = ss[i]->plan.wide_levels;
       st_wp[i] = ss[i]->plan.wide_phases;
+      st_wr[i] = ss[i]->plan.wide_rows;
     }
   }
 
@@ -526,28 +528,31 @@ struct Iter {
   }
   static void refactor(const DevSchedule& ds, const BatchDev& D, cudaStream_t st) {
     const int i = sizeof(T) == 4 ? 0 : 1;
-    refactor_with(ds, ds.st[i], ds.st_nw[i], ds.st_smem[i], ds.st_wl[i], ds.st_wp[i], D, D.G, st);
+    refactor_with(ds, ds.st[i], ds.st_nw[i], ds.st_smem[i], ds.st_wl[i], ds.st_wp[i], ds.st_wr[i], D,
+                  D.G, st);
   }
   // the refactor with a given plan's stream over the first `groups` groups:
   // the wide kernels' levels (one launch each), the stream kernel, the wide
   // kernels' backward phases (one launch each)
   static void refactor_with(const DevSchedule& ds, const StreamDev& P, int nw, size_t smem, int wl,
-                            int wp, const BatchDev& D, int groups, cudaStream_t st) {
-    wide_pre(ds, wl, D, groups, st);
+                            int wp, int wr, const BatchDev& D, int groups, cudaStream_t st) {
+    wide_pre(ds, wl, wr, D, groups, st);
     stream_kernel(P, nw, smem, ds.d, D, groups, st);
     wide_post(ds, wp, D, groups, st);
   }
   // the wide kernels' refactor levels (before the stream kernel) and their
   // backward-substitution levels (after it)
-  static void wide_pre(const DevSchedule& ds, int wl, const BatchDev& D, int groups,
+  static void wide_pre(const DevSchedule& ds, int wl, int wr, const BatchDev& D, int groups,
                        cudaStream_t st) {
     for (int L = 0; L < wl; L++) {
       const long long tasks = (long long)(ds.lev_ptr_h[L + 1] - ds.lev_ptr_h[L]) * groups;
       const unsigned blocks = (unsigned)((tasks + kWideWarps - 1) / kWideWarps);
       wide_attr();
-      k_refactor_wide<T><<<blocks, 32 * kWideWarps, kWideSmem, st>>>(ds.d, D, L, groups);
+      k_refactor_wide<T><<<blocks, 32 * kWideWarps, wide_smem(wr), st>>>(ds.d, D, L, groups, wr);
     }
   }
+  // shared memory of a wide-kernel CTA whose warps stage `rows` rows
+  static size_t wide_smem(int rows) { return (size_t)kWideWarps * rows * 32 * sizeof(T); }
   static void wide_post(const DevSchedule& ds, int wp, const BatchDev& D, int groups,
                         cudaStream_t st) {
     for (int L = wp - 1; L >= 0; L--) {
@@ -948,6 +953,7 @@ static std::vector<unsigned char> loop_key(const gox_topo* t, const BatchDev& D,
   put(&t->dsched.st[i], sizeof(StreamDev)); put(&t->dsched.st_nw[i], sizeof(int));
   put(&t->dsched.st_smem[i], sizeof(size_t)); put(&t->dsched.st_bwd[i], sizeof(bool));
   put(&t->dsched.st_wl[i], sizeof(int)); put(&t->dsched.st_wp[i], sizeof(int));
+  put(&t->dsched.st_wr[i], sizeof(int));
   return key;
 }
 
@@ -1073,7 +1079,7 @@ static void pivot_run(gox_topo* t, BatchDev& D, cudaStream_t st) {
 // (the most warps that fit).
 
 static std::mutex g_tune_mu;
-// key -> {warps, chunk words, sync, wide split (0/1: at kWideMinWidth, per topology)}
+// key -> {warps, chunk words, sync, wide split (0 none, else its narrowest level width)}
 static std::map<std::array<int, 4>, std::array<int, 4>> g_tune;
 static bool g_tune_loaded = false;
 static std::atomic<int> g_autotune{1};
@@ -1100,7 +1106,7 @@ static void tune_cache_load() {
 }
 
 static void tune_cache_store(const std::array<int, 4>& k, const StreamPlan& p) {
-  const int nw = p.nw, cw = p.chunk_words, sy = p.sync, wd = p.wide_levels + p.wide_phases > 0;
+  const int nw = p.nw, cw = p.chunk_words, sy = p.sync, wd = p.wide_levels > 0 ? p.wide_min : 0;
   g_tune[k] = {nw, cw, sy, wd};
   const char* path = std::getenv("GOX_TUNE_CACHE");
   if (!path || !*path) return;
@@ -1167,7 +1173,7 @@ static void autotune(gox_topo* t, const BatchDev& D, cudaStream_t st) {
       const Stream& cur = i == 0 ? t->s32 : t->s64;
       auto same = [&](const StreamPlan& p) {
         return p.nw == it->second[0] && p.chunk_words == it->second[1] && p.sync == it->second[2] &&
-               (p.wide_levels + p.wide_phases > 0 ? 1 : 0) == it->second[3];
+               (p.wide_levels > 0 ? p.wide_min : 0) == it->second[3];
       };
       if (same(cur.plan)) {
         TU.source = 2;
@@ -1230,7 +1236,7 @@ static void autotune(gox_topo* t, const BatchDev& D, cudaStream_t st) {
       GOX_CK(cudaMemcpyAsync(D.lu, bak.p, img_bytes, cudaMemcpyDeviceToDevice, st));
       GOX_CK(cudaEventRecord(e0, st));
       Iter<T>::refactor_with(t->dsched, P, s.plan.nw, stream_smem_bytes(s.plan), s.plan.wide_levels,
-                             s.plan.wide_phases, D, Gt, st);
+                             s.plan.wide_phases, s.plan.wide_rows, D, Gt, st);
       GOX_CK(cudaEventRecord(e1, st));
       GOX_CK(cudaEventSynchronize(e1));
       GOX_CK(cudaEventElapsedTime(&ms, e0, e1));
@@ -2047,9 +2053,11 @@ static void run_multi(const std::vector<gox_topo*>& ts, std::vector<BatchRun>& r
       J = jobs.as<MultiJob>();
     }
     rec();
+    int wr = 1;
+    for (int j : act) wr = std::max(wr, ts[j]->dsched.st_wr[i]);
     for (size_t L = 0; L < M.wide.size(); L++)
       launch(M.wide[L], [&](unsigned c, MultiList l) {
-        k_refactor_wide_multi<T><<<c, 32 * kWideWarps, Iter<T>::kWideSmem, st>>>(J, l, (int)L);
+        k_refactor_wide_multi<T><<<c, 32 * kWideWarps, Iter<T>::wide_smem(wr), st>>>(J, l, (int)L, wr);
       });
     rec();
     launch(M.rf, [&](unsigned c, MultiList l) {

@@ -1142,7 +1142,8 @@ __global__ void __launch_bounds__(sizeof(T) == 4 ? 32 * kMaxRefactorWarps : 256,
 // (column or row, group of 32 scenarios), so a level's work spreads over
 // every SM whatever the batch size, where the per-group stream kernel would
 // give it one SM per group.  A column's values are staged in shared memory
-// private to its warp's lanes (row r of lane l at stage[r * 32 + l]); its
+// private to its warp's lanes (row r of lane l at stage[r * 32 + l], `rows`
+// rows per warp: the plan's longest wide column); its
 // inputs -- the A image the fill wrote into the factor, the L values and y
 // of earlier columns -- come from global memory, where earlier launches
 // left them.  The arithmetic is the stream kernel's, in the same order per
@@ -1153,7 +1154,7 @@ constexpr int kWideWarps = 4;  // warps per CTA of the wide kernels
 
 template <typename T>
 __device__ __forceinline__ void refactor_wide_body(const SchedDev& S, const BatchDev& D, int lev,
-                                                   int groups, int BX) {
+                                                   int groups, int BX, int rows) {
   extern __shared__ __align__(16) unsigned char wsm[];
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   const int q0 = S.lev_ptr[lev], ncol = S.lev_ptr[lev + 1] - q0;
@@ -1161,7 +1162,7 @@ __device__ __forceinline__ void refactor_wide_body(const SchedDev& S, const Batc
   if (task >= (long long)ncol * groups) return;
   const int g = (int)(task % groups), q = (int)(task / groups);
   if (!D.gact[g]) return;
-  T* stg = reinterpret_cast<T*>(wsm) + (size_t)warp * kWideCap * 32 + lane;
+  T* stg = reinterpret_cast<T*>(wsm) + (size_t)warp * rows * 32 + lane;
   const int k = S.lev_cols[q0 + q];
   const int base = S.c_base[k], ulen = S.c_ulen[k], len = ulen + 1 + S.c_llen[k];
   const T* LUr = (const T*)D.lu + (size_t)g * S.n_slots * 32u + lane;
@@ -1215,8 +1216,8 @@ __device__ __forceinline__ void refactor_wide_body(const SchedDev& S, const Batc
 }
 template <typename T>
 __global__ void __launch_bounds__(32 * kWideWarps) k_refactor_wide(SchedDev S, BatchDev D, int lev,
-                                                                   int groups) {
-  refactor_wide_body<T>(S, D, lev, groups, blockIdx.x);
+                                                                   int groups, int rows) {
+  refactor_wide_body<T>(S, D, lev, groups, blockIdx.x, rows);
 }
 
 // The backward substitution of one wide refactor level's rows: x_k = (y_k -
@@ -1332,10 +1333,10 @@ __global__ void __launch_bounds__(sizeof(T) == 4 ? 32 * kMaxRefactorWarps : 256,
 // that level times its groups, kWideWarps tasks per CTA)
 template <typename T>
 __global__ void __launch_bounds__(32 * kWideWarps) k_refactor_wide_multi(
-    const MultiJob* __restrict__ jobs, MultiList L, int lev) {
+    const MultiJob* __restrict__ jobs, MultiList L, int lev, int rows) {
   __shared__ __align__(16) MultiJob J;
   const int b = enter_job(J, jobs, L);
-  refactor_wide_body<T>(J.S, J.D, lev, J.D.G, b);
+  refactor_wide_body<T>(J.S, J.D, lev, J.D.G, b, rows);
 }
 template <typename T>
 __global__ void __launch_bounds__(32 * kWideWarps) k_solve_wide_multi(

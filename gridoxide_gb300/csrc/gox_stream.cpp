@@ -898,7 +898,8 @@ struct Builder {
     // finished in global memory when it starts: level -1 here) and backward
     // phases they run after it
     const int S0 = P.wide_levels, PW = P.wide_phases;
-    if (S0 < 0 || S0 >= sc.n_levels || PW != S0 || (S0 > 0 && !(sc.fuse_fwd && with_bwd))) {
+    if (S0 < 0 || S0 >= sc.n_levels || PW != S0 || (S0 > 0 && !(sc.fuse_fwd && with_bwd)) ||
+        (S0 > 0 && (P.wide_rows <= 0 || P.wide_rows > kWideCap))) {
       err = "bad wide split";
       return false;
     }
@@ -1240,7 +1241,8 @@ struct Builder {
 }  // namespace
 
 static bool choose_stream_1(const Schedule& sc, int elem, size_t smem_budget, Stream& out,
-                            std::string& why, bool with_bwd, int sync, int wl, int wp);
+                            std::string& why, bool with_bwd, int sync, int wl, int wp, int wr,
+                            int wmin);
 
 using WaitLists = std::vector<std::vector<std::vector<int32_t>>>;
 static std::string interpret(const Schedule& sc, const Stream& st, std::vector<double>& lu,
@@ -1286,12 +1288,12 @@ bool choose_stream(const Schedule& sc, int elem, size_t smem_budget, Stream& out
   // with the wide kernels' split when asked and the schedule has one, then
   // with the backward substitution in the stream when the schedule allows
   // it (no off-diagonal BTF entries), else (or when no plan holds it) without
-  int wl = 0, wp = 0;
-  wide_split(sc, wide_min, wl, wp);
-  if (wl + wp > 0 && choose_stream_1(sc, elem, smem_budget, out, why, true, sync, wl, wp))
+  int wl = 0, wp = 0, wr = 0;
+  wide_split(sc, wide_min, wl, wp, wr);
+  if (wl + wp > 0 && choose_stream_1(sc, elem, smem_budget, out, why, true, sync, wl, wp, wr, wide_min))
     return true;
   for (bool bwd : {sc.fuse_fwd, false}) {
-    if (choose_stream_1(sc, elem, smem_budget, out, why, bwd, sync, 0, 0)) return true;
+    if (choose_stream_1(sc, elem, smem_budget, out, why, bwd, sync, 0, 0, 0, 0)) return true;
     if (!bwd) break;
   }
   return false;
@@ -1325,35 +1327,42 @@ static bool plan_for(const Schedule& sc, int elem, size_t smem_budget, int nw, i
   return true;
 }
 
-void wide_split(const Schedule& sc, int min_width, int& levels, int& phases) {
-  levels = phases = 0;
+void wide_split(const Schedule& sc, int min_width, int& levels, int& phases, int& rows) {
+  levels = phases = rows = 0;
   if (!sc.fuse_fwd || min_width <= 0) return;
   for (; levels < sc.n_levels - 1; levels++) {
     if (sc.lev_ptr[levels + 1] - sc.lev_ptr[levels] < min_width) break;
-    bool fits = true;
-    for (int q = sc.lev_ptr[levels]; q < sc.lev_ptr[levels + 1] && fits; q++) {
+    int longest = 0;
+    for (int q = sc.lev_ptr[levels]; q < sc.lev_ptr[levels + 1]; q++) {
       const int k = sc.lev_cols[q];
-      fits = sc.c_ulen[k] + 1 + sc.c_llen[k] <= kWideCap;
+      longest = std::max(longest, sc.c_ulen[k] + 1 + sc.c_llen[k]);
     }
-    if (!fits) break;
+    if (longest > kWideCap) break;
+    rows = std::max(rows, longest);
   }
   phases = levels;  // the rows of those columns, in reverse level order
 }
 
 std::vector<StreamPlan> candidate_plans(const Schedule& sc, int elem, size_t smem_budget) {
   std::vector<StreamPlan> out;
-  int wl = 0, wp = 0;
-  wide_split(sc, kWideMinWidth, wl, wp);
+  int wl[2], wp[2], wr[2];
+  wide_split(sc, kWideMinWidth, wl[0], wp[0], wr[0]);
+  wide_split(sc, kWideMinWidthDeep, wl[1], wp[1], wr[1]);
   for (int nw : {12, 10, 8, 7, 6, 5}) {
     if (nw > (elem == 4 ? kMaxRefactorWarps : 8)) continue;
     for (int cw : {320, 512}) {
       StreamPlan p;
       if (!plan_for(sc, elem, smem_budget, nw, cw, p)) continue;
-      for (int wide : {0, 1}) {
-        if (wide && wl + wp == 0) continue;
-        p.wide_levels = wide ? wl : 0;
-        p.wide_phases = wide ? wp : 0;
+      for (int wide : {0, 1, 2}) {
+        const int v = wide - 1;
+        if (wide && wl[v] == 0) continue;
+        if (wide == 2 && wl[1] == wl[0]) continue;  // the same split
+        p.wide_levels = wide ? wl[v] : 0;
+        p.wide_phases = wide ? wp[v] : 0;
+        p.wide_rows = wide ? wr[v] : 0;
+        p.wide_min = wide == 0 ? 0 : wide == 1 ? kWideMinWidth : kWideMinWidthDeep;
         for (int sync : {0, 1}) {
+          if (wide == 2 && sync == 1) continue;  // the deep split with barriers only
           p.sync = sync;
           out.push_back(p);
         }
@@ -1373,7 +1382,8 @@ bool build_plan(const Schedule& sc, const StreamPlan& p, Stream& out, std::strin
 }
 
 static bool choose_stream_1(const Schedule& sc, int elem, size_t smem_budget, Stream& out,
-                            std::string& why, bool with_bwd, int sync, int wl, int wp) {
+                            std::string& why, bool with_bwd, int sync, int wl, int wp, int wr,
+                            int wmin) {
   bool found = false;
   std::string last;
   for (int nw : {12, 10, 8, 6, 4, 3, 2, 1}) {
@@ -1383,6 +1393,8 @@ static bool choose_stream_1(const Schedule& sc, int elem, size_t smem_budget, St
     p.sync = sync;
     p.wide_levels = wl;
     p.wide_phases = wp;
+    p.wide_rows = wr;
+    p.wide_min = wl > 0 ? wmin : 0;
     Stream s;
     std::string w;
     if (!build_stream(sc, p, s, w, with_bwd)) {
@@ -1441,7 +1453,7 @@ static std::string interpret(const Schedule& sc, const Stream& st, std::vector<d
     for (int q = sc.lev_ptr[L]; q < sc.lev_ptr[L + 1]; q++) {
       const int k = sc.lev_cols[q], base = sc.c_base[k], ulen = sc.c_ulen[k];
       const int len = ulen + 1 + sc.c_llen[k];
-      if (len > kWideCap) return "a wide-kernel column longer than its stage";
+      if (len > P.wide_rows || len > kWideCap) return "a wide-kernel column longer than its stage";
       std::vector<double> stg(lu.begin() + base, lu.begin() + base + len);
       for (int p = 0; p < ulen; p++) {
         const int e = sc.cu_ptr[k] + p, j = sc.cu_j[e];

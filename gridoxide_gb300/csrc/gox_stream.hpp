@@ -137,15 +137,20 @@ struct StreamPlan {
   // values reach the stream, and the stream's reach them, through global
   // memory.  wide_phases equals wide_levels (the backward launches).
   int wide_levels = 0, wide_phases = 0;
+  int wide_min = 0;   // the narrowest level the split takes (0: no split)
+  int wide_rows = 0;  // rows of a wide-kernel warp's stage: the longest wide column
 };
-// Columns the wide kernels stage at once (per warp and lane, in shared memory).
-constexpr int kWideCap = 64;
-// Narrowest level / phase the autotuner's wide candidates give the wide kernels.
-constexpr int kWideMinWidth = 64;
+// Longest column the wide kernels stage (per warp and lane, in shared memory).
+constexpr int kWideCap = 128;
+// Narrowest levels the autotuner's wide candidates give the wide kernels:
+// the split for batches of many groups, and the deeper one for one or two
+// groups of a big grid (the serving shape).
+constexpr int kWideMinWidth = 64, kWideMinWidthDeep = 16;
 // The wide split of a schedule: the leading refactor levels with at least
 // min_width columns each, all columns at most kWideCap long (none when the
-// forward substitution is not fused); phases = levels.
-void wide_split(const Schedule& sc, int min_width, int& levels, int& phases);
+// forward substitution is not fused); phases = levels; rows = the longest
+// of those columns.
+void wide_split(const Schedule& sc, int min_width, int& levels, int& phases, int& rows);
 // The rings in the row space: warp 0's first, then the others'.
 inline int ring_size(const StreamPlan& p, int w) {
   return w == 0 && p.big_rows > p.ring_rows ? p.big_rows : p.ring_rows;

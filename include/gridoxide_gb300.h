@@ -372,12 +372,13 @@ int gox_set_refactor_sync(int32_t flags);
 
 /* The wide kernels in the default refactor plan: min_width > 0 hands the
  * leading refactor levels with at least min_width columns each (columns of
- * at most 64 entries) and the trailing backward-substitution phases with
- * at least min_width rows each to kernels that run one level / phase per
- * launch with one warp per (column or row, group of 32 scenarios) across
- * every SM; the per-group refactor kernel runs the levels between.  0
- * (default) keeps every level in the per-group kernel.  The results are
- * bit-identical either way; the autotuner times both (at min_width 64).
+ * at most 128 entries), and afterwards the backward-substitution rows of
+ * those columns (from the last such level down), to kernels that run one
+ * level per launch with one warp per (column or row, group of 32
+ * scenarios) across every SM; the per-group refactor kernel runs the rest.
+ * 0 (default) keeps every level in the per-group kernel.  The results are
+ * bit-identical either way; the autotuner times the plans without the
+ * split and with it at min_width 64 and 16.
  * Applies to topologies analysed afterwards; GOX_E_INVALID for < 0.  (No
  * counterpart in the reference: KLU's refactor is one sequential sweep per
  * scenario, src/klu_native/kernel.rs:476-524, solve.rs:56-102.) */
