@@ -74,6 +74,7 @@ SIGNATURES = {
     "gox_batch_solve_qlim": (C.c_int, [vp, C.c_int32, f64p, f64p, f64p, f64p, C.c_int32, f64p, f64p,
                                        C.c_double, C.c_int32, C.c_int32, C.c_int32, f64p, f64p, i32p,
                                        i32p, f64p, i32p, C.POINTER(C.c_uint8), i32p]),
+    "gox_set_multi_persistent": (C.c_int, [C.c_int32]),
     "gox_multi_solve": (C.c_int, [C.c_int32, vpp, i32p, vpp, vpp, vpp, vpp, i32p, C.c_double,
                                   C.c_int32, C.c_int32, vpp, vpp, vpp, vpp, vpp]),
     "gox_batch_solve_scaled": (C.c_int, [vp, C.c_int32, f64p, f64p, f64p, f64p, f64p, C.c_double,

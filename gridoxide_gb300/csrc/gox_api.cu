@@ -676,6 +676,17 @@ struct gox_topo {
   Timing timing;
   int64_t launches = 0;
   int device = 0;
+  // the refactor plans of the persistent many-topology kernel, per precision
+  // (at most 8 warps, no wide split: its CTA runs every phase of a group's
+  // Newton loop with the mismatch kernels' 8 warps); built on first use
+  struct PersistPlan {
+    bool built = false;
+    Stream s;
+    DevMem words, c0, nc;
+    StreamDev d{};
+    int nw = 0;
+    size_t smem = 0;
+  } persist[2];
   // device staging of gox_batch_solve's host arrays (grow-only)
   IoStage io;
   // mixed path: pivot-ratio threshold |u_kk| < piv_tol * max|L(:, k)| that
@@ -2109,6 +2120,125 @@ static void run_multi(const std::vector<gox_topo*>& ts, std::vector<BatchRun>& r
   }
 }
 
+// The persistent form (k_newton_persistent): each group's whole Newton loop
+// in one CTA taking (topology, group) items from a queue, largest topology
+// first, in one launch for the whole call.  Each topology runs a plan
+// without the wide split (FP32 up to 12 warps, FP64 8), compiled and checked
+// once.  gox_set_multi_persistent chooses it (default) or the lockstep loop
+// above; a topology for which no such plan fits sends the call to the
+// lockstep loop.
+static std::atomic<int> g_multi_persistent{1};
+// dynamic shared memory a persistent plan may use (the kernel's static
+// shared memory -- the job, the injections' reduction row, the refactor's
+// barriers and flags -- takes the rest of the 227 KB)
+static constexpr size_t kPersistSmem = 223 * 1024;
+
+// The persistent kernel's plan of a topology in precision i (built once);
+// false when none fits.
+static bool persist_plan(gox_topo* t, int i) {
+  gox_topo::PersistPlan& PP = t->persist[i];
+  if (PP.built) return PP.nw > 0;
+  PP.built = true;
+  const int elem = i == 0 ? 4 : 8;
+  bool ok = false;
+  for (const StreamPlan& p : candidate_plans(t->sc, elem, kPersistSmem)) {
+    if (p.sync != 0 || p.wide_levels != 0) continue;
+    if (compile_checked(t->sc, p, PP.s) && PP.s.has_bwd) {
+      ok = true;
+      break;
+    }
+  }
+  if (!ok) {
+    PP.nw = 0;
+    return false;
+  }
+  upload(PP.words, PP.s.words);
+  upload(PP.c0, PP.s.chunk0);
+  upload(PP.nc, PP.s.nchunks);
+  PP.d = StreamDev{};
+  PP.d.words = PP.words.as<int32_t>();
+  PP.d.chunk0 = PP.c0.as<int32_t>();
+  PP.d.nchunks = PP.nc.as<int32_t>();
+  PP.d.ring_rows = PP.s.plan.ring_rows;
+  PP.d.rows_total = ring_total(PP.s.plan);
+  PP.d.chunk_words = PP.s.plan.chunk_words;
+  PP.d.n_bars = PP.s.n_bars;
+  PP.d.sync = PP.s.plan.sync;
+  PP.nw = PP.s.plan.nw;
+  PP.smem = stream_smem_bytes(PP.s.plan);
+  return true;
+}
+
+template <typename T>
+static void run_persistent(const std::vector<gox_topo*>& ts, std::vector<BatchRun>& runs,
+                           int max_iter, cudaStream_t st, int64_t& launches) {
+  const int nj = (int)ts.size(), i = sizeof(T) == 4 ? 0 : 1;
+  std::vector<MultiJob> jobs(nj);
+  size_t smem = 0;
+  int nw = 8;
+  for (int j = 0; j < nj; j++) {
+    jobs[j].S = ts[j]->dsched.d;
+    jobs[j].D = runs[j].D;
+    jobs[j].P = ts[j]->persist[i].d;
+    jobs[j].nw = ts[j]->persist[i].nw;
+    smem = std::max(smem, ts[j]->persist[i].smem);
+    nw = std::max(nw, ts[j]->persist[i].nw);
+  }
+  // items: every group of every job, the longest jobs first
+  std::vector<int> order(nj);
+  for (int j = 0; j < nj; j++) order[j] = j;
+  std::stable_sort(order.begin(), order.end(), [&](int a, int b) {
+    return ts[a]->persist[i].s.est_cycles > ts[b]->persist[i].s.est_cycles;
+  });
+  std::vector<int2> items;
+  for (int j : order)
+    for (int g = 0; g < runs[j].D.G; g++) items.push_back(make_int2(j, g));
+  DevMem djobs, ditems, dnext;
+  djobs.ensure(jobs.size() * sizeof(MultiJob));
+  ditems.ensure(items.size() * sizeof(int2));
+  dnext.ensure(sizeof(int));
+  GOX_CK(cudaMemcpyAsync(djobs.p, jobs.data(), jobs.size() * sizeof(MultiJob), cudaMemcpyHostToDevice,
+                         st));
+  GOX_CK(cudaMemcpyAsync(ditems.p, items.data(), items.size() * sizeof(int2), cudaMemcpyHostToDevice,
+                         st));
+  GOX_CK(cudaMemsetAsync(dnext.p, 0, sizeof(int), st));
+  int dev = 0, sms = 0;
+  GOX_CK(cudaGetDevice(&dev));
+  GOX_CK(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+  {
+    static std::once_flag once[64];
+    std::call_once(once[dev & 63], [] {
+      GOX_CK(cudaFuncSetAttribute(k_newton_persistent<T>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                  (int)kPersistSmem));
+    });
+  }
+  const int grid = (int)std::min<size_t>(items.size(), (size_t)sms);
+  cudaEvent_t e0 = nullptr, e1 = nullptr;
+  const bool timing = ts[0]->timing.on;
+  if (timing) {
+    GOX_CK(cudaEventCreate(&e0));
+    GOX_CK(cudaEventCreate(&e1));
+    GOX_CK(cudaEventRecord(e0, st));
+  }
+  k_newton_persistent<T><<<grid, 32 * nw, smem, st>>>(
+      djobs.as<MultiJob>(), ditems.as<int2>(), (int)items.size(), dnext.as<int>(), max_iter);
+  launches++;
+  if (timing) GOX_CK(cudaEventRecord(e1, st));
+  GOX_CK(cudaStreamSynchronize(st));  // the host vectors go out of scope
+  GOX_CK(cudaGetLastError());
+  if (timing) {
+    float ms = 0;
+    GOX_CK(cudaEventElapsedTime(&ms, e0, e1));
+    Timing& T_ = ts[0]->timing;
+    T_.total = ms;
+    T_.k1 = T_.k2 = T_.k4 = 0;
+    T_.k3 = ms;  // one launch: every phase of every group
+    T_.iters = 0;
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+  }
+}
+
 // ---------------------------------------------------------------------------
 // Q-limit enforcement (newton_raphson_enforcing_q_limits, src/solver.rs:545-618)
 // over a batch: scenarios are grouped by the set of PV buses they have
@@ -2763,8 +2893,18 @@ int gox_multi_solve(int32_t n_topo, gox_topo* const* topos, const int32_t* batch
     }
     int64_t launches = 0;
     if (!ts.empty()) {
-      if (precision == GOX_PRECISION_FP64) run_multi<double>(ts, runs, max_iter, st, launches);
-      else run_multi<float>(ts, runs, max_iter, st, launches);
+      // the persistent kernel needs every schedule's forward substitution
+      // fused (no off-diagonal BTF blocks: no separate solve launch)
+      bool persistent = g_multi_persistent.load() != 0;
+      const int pi = precision == GOX_PRECISION_FP64 ? 1 : 0;
+      for (gox_topo* t : ts) persistent = persistent && t->sc.fuse_fwd && persist_plan(t, pi);
+      if (persistent) {
+        if (precision == GOX_PRECISION_FP64) run_persistent<double>(ts, runs, max_iter, st, launches);
+        else run_persistent<float>(ts, runs, max_iter, st, launches);
+      } else {
+        if (precision == GOX_PRECISION_FP64) run_multi<double>(ts, runs, max_iter, st, launches);
+        else run_multi<float>(ts, runs, max_iter, st, launches);
+      }
     }
     for (size_t k = 0; k < ts.size(); k++) {
       const int j = of[k];
@@ -3320,6 +3460,11 @@ int gox_set_autotune(int32_t on) {
 
 int gox_set_refactor_sync(int32_t flags) {
   g_refactor_sync.store(flags ? 1 : 0);
+  return GOX_OK;
+}
+
+int gox_set_multi_persistent(int32_t on) {
+  g_multi_persistent.store(on ? 1 : 0);
   return GOX_OK;
 }
 

@@ -148,7 +148,8 @@ __device__ __forceinline__ void update_body(const SchedDev& S, const BatchDev& D
   const int lane = threadIdx.x & 31;
   const int i = BX * 8 + (threadIdx.x >> 5);
   const int N = S.n_bus;
-  if (i >= N) return;
+  // a block is 8 warps (a wider CTA's other warps take no part)
+  if (i >= N || (threadIdx.x >> 5) >= 8) return;
   const int s = g * 32 + lane;
   const bool upd = D.status[s] == ST_RUNNING && (it > 0 || mode == 1) && D.sing[s] == 0;
   const size_t x = gidx(g, N, i, lane);
@@ -269,7 +270,9 @@ __device__ __forceinline__ void inject_body(const SchedDev& S, const BatchDev& D
   int obf = -1, obt = -1;
   if (OUTAGE) { obf = D.o_bf[s]; obt = D.o_bt[s]; }
   unsigned long long mx = 0ull;
-  const int i0 = (BX * 8 + warp) * BPW;
+  // a block is 8 warps; a wider CTA's other warps only take its barrier
+  const bool in_block = warp < 8;
+  const int i0 = in_block ? (BX * 8 + warp) * BPW : N;
   for (int i = i0; i < min(N, i0 + BPW); i++) {
     double ir = 0.0, ii = 0.0;
     int p = __ldg(S.yp + i);
@@ -347,7 +350,7 @@ __device__ __forceinline__ void inject_body(const SchedDev& S, const BatchDev& D
       ((T*)D.qT)[x] = (T)qc;
     }
   }
-  red[warp][lane] = mx;
+  if (in_block) red[warp][lane] = mx;
   __syncthreads();
   if (warp == 0) {
     unsigned long long m = 0ull;
@@ -433,9 +436,9 @@ template <typename T, bool OUTAGE>
 __device__ __forceinline__ void fill_body(const SchedDev& S, const BatchDev& D, int tw, int per_warp,
                                           int BX, int BY) {
   const int g = BY;
-  if (!D.gact[g]) return;
+  if (!D.gact[g] || (threadIdx.x >> 5) >= 8) return;  // a block is 8 warps
   const int lane = threadIdx.x & 31;
-  const int wglob = BX * (blockDim.x >> 5) + (threadIdx.x >> 5);
+  const int wglob = BX * 8 + (threadIdx.x >> 5);
   const int N = S.n_bus;
   T* LU = (T*)D.lu + (size_t)g * S.n_slots * 32u;
   T* OFF = (T*)D.off + (size_t)g * S.n_off * 32u;
@@ -559,6 +562,9 @@ __device__ __forceinline__ unsigned smem_u32(const void* p) {
 }
 __device__ __forceinline__ void mbar_init(uint64_t* bar) {
   asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;\n" ::"r"(smem_u32(bar)) : "memory");
+}
+__device__ __forceinline__ void mbar_inval(uint64_t* bar) {
+  asm volatile("mbarrier.inval.shared::cta.b64 [%0];\n" ::"r"(smem_u32(bar)) : "memory");
 }
 __device__ __forceinline__ void bulk_load(void* dst, const void* src, unsigned bytes, uint64_t* bar) {
   asm volatile(
@@ -1127,6 +1133,13 @@ done:
     if (flags[1][lane]) D.piv_flag[s] = 1;
     if (lane == 0 && timed_out && D.err) atomicExch(D.err, 1);
   }
+  // every copy into this warp's chunk buffers has completed (waited for, or
+  // drained on an error): the barriers may be initialized again by the next
+  // refactor a persistent CTA runs
+  if (lane == 0) {
+    mbar_inval(&mbar[warp][0]);
+    mbar_inval(&mbar[warp][1]);
+  }
 }
 template <typename T>
 __global__ void __launch_bounds__(sizeof(T) == 4 ? 32 * kMaxRefactorWarps : 256, 1)
@@ -1345,6 +1358,73 @@ __global__ void __launch_bounds__(32 * kWideWarps) k_solve_wide_multi(
   const int b = enter_job(J, jobs, L);
   solve_wide_body<T>(J.S, J.D, lev, J.D.G, b);
 }
+// ---------------------------------------------------------------------------
+// The persistent many-topology Newton kernel.  Each CTA (one per SM, as
+// many warps as the largest refactor plan; the mismatch and fill phases use
+// its first 8, the kernels' block) takes work items {job, group} from a device-side queue (listed largest
+// job first) and runs that group's whole Newton loop: update, injections,
+// decision, fill and refactor, one after the other with CTA barriers between
+// them, until its scenarios have converged or failed, then takes the next
+// item.  The phases are the single-topology kernels' bodies with the same
+// block coordinates (a loop over the blocks a group has in each kernel), so
+// every scenario's arithmetic is that of its single solve; a group that
+// leaves early skips only iterations that would leave its values unchanged
+// (no lane running: the update moves nothing, the rotation by a zero step
+// returns the same cos / sin).
+// the CTA: as wide as the largest plan it runs (FP32 up to 12 warps, FP64 8)
+template <typename T>
+constexpr int persist_threads() { return sizeof(T) == 4 ? 32 * kMaxRefactorWarps : 256; }
+template <typename T>
+__device__ __forceinline__ void newton_group(const MultiJob& J, int g, int max_iter) {
+  const SchedDev& S = J.S;
+  const BatchDev& D = J.D;
+  const int nbu = update_blocks(S.n_bus), nbi = inject_blocks(S.n_bus);
+  const int nbf = fill_blocks(S.n_ftask, S.n_fzero), tw = (S.n_ftask + 7) / 8;
+  int it = 0;
+  for (; it < max_iter; it++) {
+    for (int b = 0; b < nbu; b++) update_body<T>(S, D, it, 0, b, g);
+    __syncthreads();
+    for (int b = 0; b < nbi; b++) {
+      inject_body<T, false, 4, false>(S, D, it, b, g);
+      __syncthreads();  // its block reduction's shared row is reused by the next block
+    }
+    if (threadIdx.x < 32) decide_body(D, it, 0, g);
+    __syncthreads();
+    if (!D.gact[g]) break;
+    for (int b = 0; b < nbf; b++) fill_body<T, false>(S, D, tw, 8, b, g);
+    __syncthreads();
+    refactor_body<T>(J.P, S, D, g, J.nw);
+    __syncthreads();
+  }
+  if (it == max_iter) {
+    // the budget ran out with lanes running: their MaxIterations step
+    for (int b = 0; b < nbu; b++) update_body<T>(S, D, max_iter, 1, b, g);
+    __syncthreads();
+    if (threadIdx.x < 32) decide_body(D, max_iter, 1, g);
+    __syncthreads();
+  }
+}
+template <typename T>
+__global__ void __launch_bounds__(persist_threads<T>(), 1)
+    k_newton_persistent(const MultiJob* __restrict__ jobs, const int2* __restrict__ items,
+                        int n_items, int* __restrict__ next, int max_iter) {
+  __shared__ __align__(16) MultiJob J;
+  __shared__ int item;
+  for (;;) {
+    if (threadIdx.x == 0) item = atomicAdd(next, 1);
+    __syncthreads();
+    const int q = item;
+    if (q >= n_items) return;
+    const int2 w = items[q];
+    const int4* a = reinterpret_cast<const int4*>(jobs + w.x);
+    int4* d = reinterpret_cast<int4*>(&J);
+    for (int i = threadIdx.x; i < (int)(sizeof(MultiJob) / 16); i += blockDim.x) d[i] = a[i];
+    __syncthreads();
+    newton_group<T>(J, w.y, max_iter);
+    __syncthreads();  // every thread is done with J and `item` before the next item
+  }
+}
+
 // every job's running-group counter to zero / into one array (one read back)
 __global__ void k_multi_counts(const MultiJob* __restrict__ jobs, int n, int32_t* out, int zero) {
   for (int j = blockIdx.x * blockDim.x + threadIdx.x; j < n; j += gridDim.x * blockDim.x) {

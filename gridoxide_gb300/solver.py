@@ -165,13 +165,21 @@ def set_refactor_sync(progress_flags: bool) -> None:
     check(_lib.load().gox_set_refactor_sync(1 if progress_flags else 0), "gox_set_refactor_sync")
 
 
+def set_multi_persistent(on: bool) -> None:
+    """multi_solve's form: one persistent launch in which each CTA runs whole
+    Newton loops of (topology, group) items from a queue (default), or one
+    loop whose phases are one launch each over every topology still running."""
+    check(_lib.load().gox_set_multi_persistent(1 if on else 0), "gox_set_multi_persistent")
+
+
 def multi_solve(jobs, tol=1e-8, max_iter=20, precision=GOX_PRECISION_MIXED) -> list:
-    """Many topologies' batches in one Newton loop (gox_multi_solve): each
-    phase of each iteration is one launch over every topology still
-    running.  `jobs`: (Topology, p_spec [B, N], q_spec [B, N], vm0, va0)
-    with vm0 / va0 [N] (shared) or [B, N]; each topology at most once.
-    Returns one BatchResult per job, equal bit for bit to Topology.solve on
-    that job alone."""
+    """Many topologies' batches solved together (gox_multi_solve): one
+    persistent launch whose CTAs run whole Newton loops of (topology, group)
+    items, or (set_multi_persistent(False)) one loop with one launch per
+    phase.  `jobs`: (Topology, p_spec [B, N], q_spec [B, N], vm0, va0) with
+    vm0 / va0 [N] (shared) or [B, N]; each topology at most once.  Returns
+    one BatchResult per job, equal bit for bit to Topology.solve on that job
+    alone."""
     n = len(jobs)
     keep, outs = [], []
     topo_a = (C.c_void_p * n)()

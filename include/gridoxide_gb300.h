@@ -178,19 +178,26 @@ int gox_batch_solve_scaled(gox_topo *t, int32_t B, const double *scales, const d
                            double *va_out, int32_t *iterations, int32_t *status,
                            double *max_mismatch, double *history);
 
-/* Many topologies' batches in one Newton loop: the reference's BatchSolver
+/* Many topologies' batches solved together: the reference's BatchSolver
  * work queue over scenarios of uneven cost (src/batch.rs:230-281), here for
- * n_topo topologies at once.  Each iteration runs the update, injection,
- * decision, fill and refactor kernels once each over the work items of
- * every topology still running (the refactor's CTAs largest topology
- * first); a topology leaves the loop when its last scenario has converged
- * or failed.  Per topology j the arguments are gox_batch_solve's: batch[j]
+ * n_topo topologies at once.  By default (gox_set_multi_persistent(1)) one
+ * persistent kernel launch solves everything: each CTA takes (topology,
+ * group of 32 scenarios) items from a device-side queue, largest topology
+ * first, and runs that group's whole Newton loop (update, injections,
+ * decision, fill, refactor with both substitutions) until its scenarios
+ * have converged or failed; each topology then runs a refactor plan of at
+ * most 8 warps without the wide split (compiled once).  With
+ * gox_set_multi_persistent(0) -- or when a topology's BTF form has
+ * off-diagonal blocks -- one Newton loop runs the phases as one launch each
+ * over every topology still running (the refactor's CTAs largest topology
+ * first).  Per topology j the arguments are gox_batch_solve's: batch[j]
  * scenarios, p_spec[j] / q_spec[j] [batch[j]][n_bus], vm0[j] / va0[j] with
  * v_stride[j], outputs vm_out[j], va_out[j], iterations[j], status[j],
  * max_mismatch[j] (host arrays); tol, max_iter and precision are shared.
  * The results equal gox_batch_solve's on each topology alone, bit for bit.
  * No outages and no ZIP terms (GOX_E_INVALID), each topology at most once,
  * max_iter >= 1. */
+int gox_set_multi_persistent(int32_t on);
 int gox_multi_solve(int32_t n_topo, gox_topo *const *topos, const int32_t *batch,
                     const double *const *p_spec, const double *const *q_spec,
                     const double *const *vm0, const double *const *va0, const int32_t *v_stride,

@@ -1,12 +1,13 @@
-"""GPU: many topologies in one Newton loop (gox_multi_solve).
+"""GPU: many topologies solved together (gox_multi_solve).
 
-Each phase of each iteration is one launch over every topology still
-running; a topology leaves at the iteration its own solve would.  Every
-scenario's result must equal, bit for bit, the same batch solved alone by
-Topology.solve -- on three family grids of uneven size and batch (one of
-them with several groups and stragglers), in both precisions -- and the
-FP64 results must match the oracle (the reference's algorithm) within
-1e-9 with equal iteration counts."""
+Two forms: one persistent launch whose CTAs each run a (topology, group)
+item's whole Newton loop, taken from a queue; and one Newton loop whose
+phases are one launch each over every topology still running.  In both,
+every scenario's result must equal, bit for bit, the same batch solved
+alone by Topology.solve -- on three family grids of uneven size and batch
+(one of them with several groups and stragglers), in both precisions --
+and the FP64 results must match the oracle (the reference's algorithm)
+within 1e-9 with equal iteration counts."""
 import numpy as np
 import pytest
 
@@ -37,20 +38,34 @@ def _same(a, b):
     np.testing.assert_array_equal(a.max_mismatch, b.max_mismatch)
 
 
+@pytest.mark.parametrize("persistent", [True, False])
 @pytest.mark.parametrize("precision", [0, 1])
-def test_multi_equals_alone(gox, precision):
+def test_multi_equals_alone(gox, precision, persistent):
+    from gridoxide_gb300 import solver as S
     data = _jobs(gox)
     kw = dict(tol=1e-8, max_iter=20, precision=precision)
     alone = [gox.Topology(yb, g.bus_type).solve(p, q, g.vm, g.va, **kw) for g, yb, p, q in data]
     topos = [gox.Topology(yb, g.bus_type) for g, yb, _, _ in data]
-    mixed = gox.multi_solve([(t, p, q, g.vm, g.va) for t, (g, yb, p, q) in zip(topos, data)], **kw)
-    for a, m in zip(alone, mixed):
-        assert np.all(a.status == gox.GOX_CONVERGED)
-        _same(a, m)
-    # the same topologies again (fixed pivot orders, tuned plans): same bits
-    again = gox.multi_solve([(t, p, q, g.vm, g.va) for t, (g, yb, p, q) in zip(topos, data)], **kw)
-    for a, m in zip(alone, again):
-        _same(a, m)
+    S.set_multi_persistent(persistent)
+    try:
+        jobs = [(t, p, q, g.vm, g.va) for t, (g, yb, p, q) in zip(topos, data)]
+        mixed = gox.multi_solve(jobs, **kw)
+        for a, m in zip(alone, mixed):
+            assert np.all(a.status == gox.GOX_CONVERGED)
+            _same(a, m)
+        # the same topologies again (fixed pivot orders, tuned plans): same bits
+        again = gox.multi_solve(jobs, **kw)
+        for a, m in zip(alone, again):
+            _same(a, m)
+        # a budget that runs out: MaxIterations reported as alone
+        short = dict(kw, max_iter=2)
+        alone2 = [gox.Topology(yb, g.bus_type).solve(p, q, g.vm, g.va, **short)
+                  for g, yb, p, q in data]
+        for a, m in zip(alone2, gox.multi_solve(jobs, **short)):
+            assert np.any(a.status == gox.GOX_MAX_ITERATIONS)
+            _same(a, m)
+    finally:
+        S.set_multi_persistent(True)
 
 
 def test_multi_fp64_matches_oracle(gox, oracle_mod):
