@@ -2124,10 +2124,11 @@ static void run_multi(const std::vector<gox_topo*>& ts, std::vector<BatchRun>& r
 // in one CTA taking (topology, group) items from a queue, largest topology
 // first, in one launch for the whole call.  Each topology runs a plan
 // without the wide split (FP32 up to 12 warps, FP64 8), compiled and checked
-// once.  gox_set_multi_persistent chooses it (default) or the lockstep loop
-// above; a topology for which no such plan fits sends the call to the
-// lockstep loop.
-static std::atomic<int> g_multi_persistent{1};
+// once.  gox_set_multi_persistent(1) chooses it over the lockstep loop above
+// (the default, faster on the many-topology workload: its big grids keep
+// their wide kernels); a topology for which no such plan fits sends the
+// call to the lockstep loop.
+static std::atomic<int> g_multi_persistent{0};
 // dynamic shared memory a persistent plan may use (the kernel's static
 // shared memory -- the job, the injections' reduction row, the refactor's
 // barriers and flags -- takes the rest of the 227 KB)
@@ -2860,39 +2861,68 @@ int gox_multi_solve(int32_t n_topo, gox_topo* const* topos, const int32_t* batch
   }
   if (jobs.empty()) return GOX_OK;
   if (int r = require_device()) return r;
-  return guard_impl([&]() -> int {
-    cudaStream_t st = thread_stream();
-    AllocStreamScope alloc_scope(st);
-    std::vector<gox_topo*> ts;
-    std::vector<BatchRun> runs;
-    std::vector<int> of;  // job -> argument index
-    for (int j : jobs) {
-      gox_topo* t = topos[j];
-      const int B = batch[j], n = t->n_bus;
-      const size_t bn = (size_t)B * n, nv = (size_t)(v_stride[j] ? B : 1) * n;
-      IoStage& io = t->io;
-      io.p.ensure(bn * 8); io.q.ensure(bn * 8); io.vm.ensure(nv * 8); io.va.ensure(nv * 8);
-      io.ovm.ensure(bn * 8); io.ova.ensure(bn * 8); io.it.ensure((size_t)B * 4);
-      io.st.ensure((size_t)B * 4); io.mm.ensure((size_t)B * 8);
-      GOX_CK(cudaMemcpyAsync(io.p.p, p_spec[j], bn * 8, cudaMemcpyHostToDevice, st));
-      GOX_CK(cudaMemcpyAsync(io.q.p, q_spec[j], bn * 8, cudaMemcpyHostToDevice, st));
-      GOX_CK(cudaMemcpyAsync(io.vm.p, vm0[j], nv * 8, cudaMemcpyHostToDevice, st));
-      GOX_CK(cudaMemcpyAsync(io.va.p, va0[j], nv * 8, cudaMemcpyHostToDevice, st));
-      BatchRun R;
-      const int rc = batch_prepare(
-          t, B, io.p.as<double>(), io.q.as<double>(), io.vm.as<double>(), io.va.as<double>(),
-          v_stride[j], nullptr, nullptr, nullptr, tol, max_iter, precision, io.ovm.as<double>(),
-          io.ova.as<double>(), io.it.as<int32_t>(), io.st.as<int32_t>(), io.mm.as<double>(),
-          nullptr, st, p_spec[j], q_spec[j], vm0[j], va0[j], nullptr, nullptr, nullptr, R);
-      if (rc != GOX_OK) return rc;
-      if (!R.resolved) {
-        ts.push_back(t);
-        runs.push_back(R);
-        of.push_back(j);
-      }
+  // each job's set-up and results on up to 8 host threads (each its own
+  // stream), the solve itself on the calling thread's stream
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess) return GOX_E_CUDA;
+  auto parallel = [&](size_t n, const std::function<int(size_t)>& fn) -> int {
+    const size_t nt = std::min<size_t>(n, 8);
+    std::vector<int> rc(nt, GOX_OK);
+    std::vector<std::thread> th;
+    for (size_t w = 0; w < nt; w++)
+      th.emplace_back([&, w] {
+        rc[w] = guard_impl([&]() -> int {
+          GOX_CK(cudaSetDevice(dev));
+          cudaStream_t ws = thread_stream();
+          AllocStreamScope scope(ws);
+          for (size_t k = w; k < n; k += nt)
+            if (int r = fn(k)) return r;
+          return GOX_OK;
+        });
+      });
+    for (auto& x : th) x.join();
+    for (int r : rc)
+      if (r != GOX_OK) return r;
+    return GOX_OK;
+  };
+  std::vector<BatchRun> all(jobs.size());
+  int rc = parallel(jobs.size(), [&](size_t k) -> int {
+    const int j = jobs[k];
+    gox_topo* t = topos[j];
+    cudaStream_t ws = thread_stream();
+    const int B = batch[j], n = t->n_bus;
+    const size_t bn = (size_t)B * n, nv = (size_t)(v_stride[j] ? B : 1) * n;
+    IoStage& io = t->io;
+    io.p.ensure(bn * 8); io.q.ensure(bn * 8); io.vm.ensure(nv * 8); io.va.ensure(nv * 8);
+    io.ovm.ensure(bn * 8); io.ova.ensure(bn * 8); io.it.ensure((size_t)B * 4);
+    io.st.ensure((size_t)B * 4); io.mm.ensure((size_t)B * 8);
+    GOX_CK(cudaMemcpyAsync(io.p.p, p_spec[j], bn * 8, cudaMemcpyHostToDevice, ws));
+    GOX_CK(cudaMemcpyAsync(io.q.p, q_spec[j], bn * 8, cudaMemcpyHostToDevice, ws));
+    GOX_CK(cudaMemcpyAsync(io.vm.p, vm0[j], nv * 8, cudaMemcpyHostToDevice, ws));
+    GOX_CK(cudaMemcpyAsync(io.va.p, va0[j], nv * 8, cudaMemcpyHostToDevice, ws));
+    const int r = batch_prepare(
+        t, B, io.p.as<double>(), io.q.as<double>(), io.vm.as<double>(), io.va.as<double>(),
+        v_stride[j], nullptr, nullptr, nullptr, tol, max_iter, precision, io.ovm.as<double>(),
+        io.ova.as<double>(), io.it.as<int32_t>(), io.st.as<int32_t>(), io.mm.as<double>(),
+        nullptr, ws, p_spec[j], q_spec[j], vm0[j], va0[j], nullptr, nullptr, nullptr, all[k]);
+    GOX_CK(cudaStreamSynchronize(ws));  // set up before the solve's stream uses it
+    return r;
+  });
+  if (rc != GOX_OK) return rc;
+  std::vector<gox_topo*> ts;
+  std::vector<BatchRun> runs;
+  std::vector<int> of;  // solved job -> argument index
+  for (size_t k = 0; k < jobs.size(); k++)
+    if (!all[k].resolved) {
+      ts.push_back(topos[jobs[k]]);
+      runs.push_back(all[k]);
+      of.push_back(jobs[k]);
     }
-    int64_t launches = 0;
-    if (!ts.empty()) {
+  int64_t launches = 0;
+  if (!ts.empty()) {
+    rc = guard_impl([&]() -> int {
+      cudaStream_t st = thread_stream();
+      AllocStreamScope alloc_scope(st);
       // the persistent kernel needs every schedule's forward substitution
       // fused (no off-diagonal BTF blocks: no separate solve launch)
       bool persistent = g_multi_persistent.load() != 0;
@@ -2905,32 +2935,35 @@ int gox_multi_solve(int32_t n_topo, gox_topo* const* topos, const int32_t* batch
         if (precision == GOX_PRECISION_FP64) run_multi<double>(ts, runs, max_iter, st, launches);
         else run_multi<float>(ts, runs, max_iter, st, launches);
       }
-    }
-    for (size_t k = 0; k < ts.size(); k++) {
-      const int j = of[k];
-      gox_topo* t = ts[k];
-      IoStage& io = t->io;
-      const int rc = batch_finish(
-          t, batch[j], io.p.as<double>(), io.q.as<double>(), io.vm.as<double>(),
-          io.va.as<double>(), v_stride[j], nullptr, nullptr, nullptr, tol, max_iter, precision,
-          io.ovm.as<double>(), io.ova.as<double>(), io.it.as<int32_t>(), io.st.as<int32_t>(),
-          io.mm.as<double>(), nullptr, st, p_spec[j], q_spec[j], vm0[j], va0[j], nullptr, nullptr,
-          nullptr, runs[k]);
-      if (rc != GOX_OK) return rc;
+      return GOX_OK;
+    });
+    if (rc != GOX_OK) return rc;
+  }
+  std::vector<int> run_of(n_topo, -1);
+  for (size_t k = 0; k < of.size(); k++) run_of[of[k]] = (int)k;
+  return parallel(jobs.size(), [&](size_t k) -> int {
+    const int j = jobs[k];
+    gox_topo* t = topos[j];
+    cudaStream_t ws = thread_stream();
+    IoStage& io = t->io;
+    const int B = batch[j];
+    if (run_of[j] >= 0) {
+      const int r = batch_finish(
+          t, B, io.p.as<double>(), io.q.as<double>(), io.vm.as<double>(), io.va.as<double>(),
+          v_stride[j], nullptr, nullptr, nullptr, tol, max_iter, precision, io.ovm.as<double>(),
+          io.ova.as<double>(), io.it.as<int32_t>(), io.st.as<int32_t>(), io.mm.as<double>(),
+          nullptr, ws, p_spec[j], q_spec[j], vm0[j], va0[j], nullptr, nullptr, nullptr,
+          runs[run_of[j]]);
+      if (r != GOX_OK) return r;
       t->launches += launches / (int64_t)ts.size();
     }
-    for (int j : jobs) {
-      gox_topo* t = topos[j];
-      const int B = batch[j];
-      const size_t bn = (size_t)B * t->n_bus;
-      IoStage& io = t->io;
-      GOX_CK(cudaMemcpyAsync(vm_out[j], io.ovm.p, bn * 8, cudaMemcpyDeviceToHost, st));
-      GOX_CK(cudaMemcpyAsync(va_out[j], io.ova.p, bn * 8, cudaMemcpyDeviceToHost, st));
-      GOX_CK(cudaMemcpyAsync(iterations[j], io.it.p, (size_t)B * 4, cudaMemcpyDeviceToHost, st));
-      GOX_CK(cudaMemcpyAsync(status[j], io.st.p, (size_t)B * 4, cudaMemcpyDeviceToHost, st));
-      GOX_CK(cudaMemcpyAsync(max_mismatch[j], io.mm.p, (size_t)B * 8, cudaMemcpyDeviceToHost, st));
-    }
-    GOX_CK(cudaStreamSynchronize(st));
+    const size_t bn = (size_t)B * t->n_bus;
+    GOX_CK(cudaMemcpyAsync(vm_out[j], io.ovm.p, bn * 8, cudaMemcpyDeviceToHost, ws));
+    GOX_CK(cudaMemcpyAsync(va_out[j], io.ova.p, bn * 8, cudaMemcpyDeviceToHost, ws));
+    GOX_CK(cudaMemcpyAsync(iterations[j], io.it.p, (size_t)B * 4, cudaMemcpyDeviceToHost, ws));
+    GOX_CK(cudaMemcpyAsync(status[j], io.st.p, (size_t)B * 4, cudaMemcpyDeviceToHost, ws));
+    GOX_CK(cudaMemcpyAsync(max_mismatch[j], io.mm.p, (size_t)B * 8, cudaMemcpyDeviceToHost, ws));
+    GOX_CK(cudaStreamSynchronize(ws));
     return GOX_OK;
   });
 }
