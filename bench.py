@@ -233,7 +233,9 @@ def serve(gox, rates, seconds: float) -> dict:
     threads, mixed precision, host buffers).  Latency = submit to completion
     of each request.  The rates run in increasing order until one
     saturates (completed < 0.95 x offered, counting the drain after the last
-    arrival); that rate and every one before it are in `sweep`, with p50 and
+    arrival; `completed_in_window_rps` counts only the completions while
+    requests were arriving, `drain_ms` the time after the last arrival until
+    the last completion); that rate and every one before it are in `sweep`, with p50 and
     p99 latency by grid size; `saturation_rps` is the highest offered rate
     the server kept up with.  Each grid's requests draw their load vectors
     from 32 seeded samples of the grid's distribution (the per-request host
@@ -281,7 +283,7 @@ def serve(gox, rates, seconds: float) -> dict:
             g = grids[t][0]
             srv.wait(srv.submit(ids[t], g.p_spec, g.q_spec, *v0[t]), g.n_bus)
         st0 = srv.stats()
-        tickets = []
+        tickets, sub_t = [], []
         t0 = time.perf_counter()
         due = t0
         for i, (t, p, q, out) in enumerate(reqs):
@@ -289,6 +291,8 @@ def serve(gox, rates, seconds: float) -> dict:
             while time.perf_counter() < due:
                 pass
             tickets.append(srv.submit(ids[t], p, q, *v0[t], outage=out))
+            sub_t.append(time.perf_counter())
+        t_last = time.perf_counter()
         lat, conv = [], 0
         for (t, _, _, _), tk in zip(reqs, tickets):
             r = srv.wait(tk, grids[t][0].n_bus)
@@ -309,9 +313,14 @@ def serve(gox, rates, seconds: float) -> dict:
         dq = (st["queue_us"] - st0["queue_us"]) / 1000.0 / n_req
         ds = (st["solve_us"] - st0["solve_us"]) / 1000.0 / n_req
         done_rps = n_req / (t1 - t0)
+        # completions while requests were arriving, per second of arrivals
+        finished = np.array(sub_t) + lat / 1000.0
+        steady_rps = float(np.sum(finished <= t_last)) / max(t_last - t0, 1e-9)
         sweep.append({"offered_rps": rate, "requests": n_req,
                       "mean_queued_ms": round(dq, 3), "mean_in_solve_ms": round(ds, 3),
                       "completed_rps": round(done_rps, 1),
+                      "completed_in_window_rps": round(steady_rps, 1),
+                      "drain_ms": round(1000.0 * (t1 - t_last), 1),
                       "p50_ms": round(float(np.percentile(lat, 50)), 3),
                       "p99_ms": round(float(np.percentile(lat, 99)), 3), "batches": nb,
                       "mean_batch": round(n_req / max(nb, 1), 1), "converged": conv,
