@@ -232,12 +232,15 @@ def serve(gox, rates, seconds: float) -> dict:
     through the library's serving loop (continuous batching on worker
     threads, mixed precision, host buffers).  Latency = submit to completion
     of each request.  The rates run in increasing order until one
-    saturates (completed < 0.95 x offered, counting the drain after the last
-    arrival; `completed_in_window_rps` counts only the completions while
-    requests were arriving, `drain_ms` the time after the last arrival until
-    the last completion); that rate and every one before it are in `sweep`, with p50 and
-    p99 latency by grid size; `saturation_rps` is the highest offered rate
-    the server kept up with.  Each grid's requests draw their load vectors
+    saturates: fewer than 0.95 x offered requests per second completed while
+    requests were arriving (`completed_in_window_rps`; a server that keeps up
+    leaves only the requests of its last latency in flight, one that does not
+    a growing queue).  `completed_rps` divides by the time until the last
+    completion instead (the window plus `drain_ms`, which is the latency of
+    the slowest grids' last batches); `submitted_rps` is the rate the client
+    thread actually reached.  That rate and every one before it are in
+    `sweep`, with p50 and p99 latency by grid size; `saturation_rps` is the
+    highest offered rate the server kept up with.  Each grid's requests draw their load vectors
     from 32 seeded samples of the grid's distribution (the per-request host
     copies are the grid's size whatever the sample)."""
     from gridoxide_gb300 import grids as G
@@ -317,6 +320,7 @@ def serve(gox, rates, seconds: float) -> dict:
         finished = np.array(sub_t) + lat / 1000.0
         steady_rps = float(np.sum(finished <= t_last)) / max(t_last - t0, 1e-9)
         sweep.append({"offered_rps": rate, "requests": n_req,
+                      "submitted_rps": round(n_req / max(t_last - t0, 1e-9), 1),
                       "mean_queued_ms": round(dq, 3), "mean_in_solve_ms": round(ds, 3),
                       "completed_rps": round(done_rps, 1),
                       "completed_in_window_rps": round(steady_rps, 1),
@@ -325,7 +329,7 @@ def serve(gox, rates, seconds: float) -> dict:
                       "p99_ms": round(float(np.percentile(lat, 99)), 3), "batches": nb,
                       "mean_batch": round(n_req / max(nb, 1), 1), "converged": conv,
                       "p50_ms_by_buses": by_size, "p99_ms_by_buses": by_size99})
-        if done_rps < 0.95 * rate:
+        if steady_rps < 0.95 * rate:
             break
         saturation = rate
     out = dict(sweep[-1])
@@ -672,7 +676,7 @@ def main():
                     help="serving leg: highest Poisson arrival rate of the sweep (0 = skip)")
     ap.add_argument("--many-rounds", type=int, default=3,
                     help="N-1 10,000-bus and many-topology legs: timed rounds (0 = skip)")
-    ap.add_argument("--serve-seconds", type=float, default=2.0)
+    ap.add_argument("--serve-seconds", type=float, default=4.0)
     ap.add_argument("--grid", default=WORKLOAD["grid"], help="profiling: another grid")
     ap.add_argument("--scenarios", type=int, default=WORKLOAD["scenarios"],
                     help="profiling: a smaller batch")

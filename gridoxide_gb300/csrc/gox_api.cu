@@ -1158,11 +1158,12 @@ static void install_stream(gox_topo* t, int i, Stream&& s) {
   (i == 0 ? t->s32 : t->s64) = std::move(s);
   t->dsched.load_streams(t->s32, t->s64);
   drop_loops(t, i);
-  if (t->twin) {
-    t->twin->s32 = t->s32;
-    t->twin->s64 = t->s64;
-    if (t->twin->uploaded) t->twin->dsched.load_streams(t->twin->s32, t->twin->s64);
-    drop_loops(t->twin.get(), i);
+  // the split solves' twins (a chain: the twin of part k solves part k + 1)
+  for (gox_topo* tw = t->twin.get(); tw; tw = tw->twin.get()) {
+    tw->s32 = t->s32;
+    tw->s64 = t->s64;
+    if (tw->uploaded) tw->dsched.load_streams(tw->s32, tw->s64);
+    drop_loops(tw, i);
   }
 }
 
@@ -2522,10 +2523,10 @@ static int batch_any(gox_topo* t, int B, const double* p_spec, const double* q_s
   return GOX_OK;
 }
 
-// The twin of a factored topology: the same pattern, pivot order, schedule
-// and settings; its own device state
-static gox_topo* split_twin(gox_topo* t) {
-  if (t->twin) return t->twin.get();
+// A second instance of a factored topology: the same pattern, pivot order,
+// schedule, plans and settings; its own device state (it runs the streams its
+// topology chose, so its results are its topology's bit for bit)
+static std::unique_ptr<gox_topo> clone_factored(const gox_topo* t) {
   std::unique_ptr<gox_topo> v(new gox_topo());
   v->n_bus = t->n_bus;
   v->yp = t->yp; v->yi = t->yi; v->yre = t->yre; v->yim = t->yim; v->bus_type = t->bus_type;
@@ -2538,18 +2539,23 @@ static gox_topo* split_twin(gox_topo* t) {
   v->graphs_wanted = t->graphs_wanted;
   v->zip = t->zip;
   if (!v->zip.empty()) upload(v->dzip, v->zip);
-  // the twin runs the streams its topology chose (install_stream updates it)
   v->tune[0].done = v->tune[1].done = true;
-  t->twin = std::move(v);
+  return v;
+}
+
+// The twin a split solve's next part runs on (install_stream keeps its
+// streams the topology's)
+static gox_topo* split_twin(gox_topo* t) {
+  if (!t->twin) t->twin = clone_factored(t);
   return t->twin.get();
 }
 
 static constexpr int kSplitMinScenarios = 4096;
 
 // Holds a stream for `ns` nanoseconds (global timer; ns is capped by the
-// caller): the second half of a split solve starts this much later, so that
-// its mismatch and fill fall on the first half's refactor instead of running
-// beside the first half's own mismatch.
+// caller): part k of a split solve starts k offsets later, so that its
+// mismatch and fill fall on the other parts' refactors instead of running
+// beside their own mismatch.
 __global__ void k_delay(unsigned long long ns) {
   unsigned long long t0, t;
   asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t0));
@@ -2558,7 +2564,7 @@ __global__ void k_delay(unsigned long long ns) {
   } while (t - t0 < ns);
 }
 
-// The offset: about two thirds of one half's mismatch and fill, estimated per
+// The offset: about two thirds of one part's mismatch and fill, estimated per
 // bus and scenario (measured on the 2,000-bus grid: 0.29 ms for halves of
 // 2,048 scenarios), at most 5 ms
 static unsigned long long split_offset_ns(int n_bus, int scenarios) {
@@ -2567,10 +2573,10 @@ static unsigned long long split_offset_ns(int n_bus, int scenarios) {
 }
 
 // batch_any, or -- when the topology is set to split, its pivot order is
-// fixed, the start is given and the batch is large -- its two halves (split
-// at a multiple of 32 scenarios, so every group and result is the same)
-// solved concurrently, the first on `st` and the second by the twin on its
-// own stream from a second host thread
+// fixed, the start is given and the batch is large -- its parts (split at
+// multiples of 32 scenarios, so every group and result is the same) solved
+// concurrently, the first on `st` and each other one by a twin on its own
+// stream from its own host thread
 static int batch_split(gox_topo* t, int B, const double* p_spec, const double* q_spec,
                        const double* vm0, const double* va0, int v_stride, const int32_t* o_slot,
                        const double* o_dre, const double* o_dim, double tol, int max_iter,
@@ -2587,51 +2593,68 @@ static int batch_split(gox_topo* t, int B, const double* p_spec, const double* q
     return batch_any(t, B, p_spec, q_spec, vm0, va0, v_stride, o_slot, o_dre, o_dim, tol, max_iter,
                      precision, vm_out, va_out, iters, status, max_mis, hist, st, h_p, h_q, h_vm,
                      h_va, h_oslot, h_odre, h_odim);
-  gox_topo* tw = split_twin(t);
-  if (!tw->own_stream) GOX_CK(cudaStreamCreateWithFlags(&tw->own_stream, cudaStreamNonBlocking));
+  // parts of whole groups (every group and result is the one the whole
+  // batch would have), part k solved by the k-th twin on its own stream from
+  // its own host thread, started k offsets later
   const int n = t->n_bus;
-  const int B1 = ((B / 2 + 31) / 32) * 32, B2 = B - B1;
-  const size_t off = (size_t)B1 * n, voff = v_stride ? off : 0;
+  const int parts = std::min(t->split_parts, (B + 31) / 32);
+  const int G = (B + 31) / 32;
+  std::vector<int> first(parts + 1, 0);
+  for (int k = 0; k < parts; k++) first[k + 1] = first[k] + (G / parts + (k < G % parts ? 1 : 0)) * 32;
+  first[parts] = B;
+  std::vector<gox_topo*> tw(parts, t);
+  for (int k = 1; k < parts; k++) {
+    tw[k] = split_twin(tw[k - 1]);
+    if (!tw[k]->own_stream) GOX_CK(cudaStreamCreateWithFlags(&tw[k]->own_stream, cudaStreamNonBlocking));
+  }
   cudaEvent_t ready;
   GOX_CK(cudaEventCreateWithFlags(&ready, cudaEventDisableTiming));
   GOX_CK(cudaEventRecord(ready, st));  // the inputs, as the caller's stream has them
-  int r2 = GOX_OK;
-  std::thread second([&] {
-    r2 = guard_impl([&]() -> int {
-      GOX_CK(cudaSetDevice(t->device));
-      cudaStream_t s2 = tw->own_stream;
-      AllocStreamScope scope(s2);
-      GOX_CK(cudaStreamWaitEvent(s2, ready, 0));
-      k_delay<<<1, 1, 0, s2>>>(split_offset_ns(n, B2));
-      GOX_CK(cudaGetLastError());
-      return batch_any(tw, B2, p_spec + off, q_spec + off, vm0 + voff, va0 + voff, v_stride,
-                       o_slot ? o_slot + 4 * (size_t)B1 : nullptr,
-                       o_dre ? o_dre + 4 * (size_t)B1 : nullptr,
-                       o_dim ? o_dim + 4 * (size_t)B1 : nullptr, tol, max_iter, precision,
-                       vm_out + off, va_out + off, iters + B1, status + B1, max_mis + B1,
-                       hist ? hist + (size_t)B1 * max_iter : nullptr, s2,
-                       h_p ? h_p + off : nullptr, h_q ? h_q + off : nullptr,
-                       h_vm ? h_vm + voff : nullptr, h_va ? h_va + voff : nullptr,
-                       h_oslot ? h_oslot + 4 * (size_t)B1 : nullptr,
-                       h_odre ? h_odre + 4 * (size_t)B1 : nullptr,
-                       h_odim ? h_odim + 4 * (size_t)B1 : nullptr);
+  std::vector<int> rk(parts, GOX_OK);
+  auto part = [&](int k, cudaStream_t sk) -> int {
+    const int Bk = first[k + 1] - first[k];
+    const size_t off = (size_t)first[k] * n, voff = v_stride ? off : 0;
+    const size_t o4 = 4 * (size_t)first[k];
+    return batch_any(tw[k], Bk, p_spec + off, q_spec + off, vm0 + voff, va0 + voff, v_stride,
+                     o_slot ? o_slot + o4 : nullptr, o_dre ? o_dre + o4 : nullptr,
+                     o_dim ? o_dim + o4 : nullptr, tol, max_iter, precision, vm_out + off,
+                     va_out + off, iters + first[k], status + first[k], max_mis + first[k],
+                     hist ? hist + (size_t)first[k] * max_iter : nullptr, sk,
+                     h_p ? h_p + off : nullptr, h_q ? h_q + off : nullptr,
+                     h_vm ? h_vm + voff : nullptr, h_va ? h_va + voff : nullptr,
+                     h_oslot ? h_oslot + o4 : nullptr, h_odre ? h_odre + o4 : nullptr,
+                     h_odim ? h_odim + o4 : nullptr);
+  };
+  std::vector<std::thread> th;
+  for (int k = 1; k < parts; k++)
+    th.emplace_back([&, k] {
+      rk[k] = guard_impl([&]() -> int {
+        GOX_CK(cudaSetDevice(t->device));
+        cudaStream_t sk = tw[k]->own_stream;
+        AllocStreamScope scope(sk);
+        GOX_CK(cudaStreamWaitEvent(sk, ready, 0));
+        k_delay<<<1, 1, 0, sk>>>((unsigned long long)k *
+                                 split_offset_ns(n, first[k + 1] - first[k]));
+        GOX_CK(cudaGetLastError());
+        return part(k, sk);
+      });
     });
-  });
-  int r1 = GOX_OK;
   try {
-    r1 = batch_any(t, B1, p_spec, q_spec, vm0, va0, v_stride, o_slot, o_dre, o_dim, tol, max_iter,
-                   precision, vm_out, va_out, iters, status, max_mis, hist, st, h_p, h_q, h_vm,
-                   h_va, h_oslot, h_odre, h_odim);
+    rk[0] = part(0, st);
   } catch (...) {
-    second.join();
+    for (auto& x : th) x.join();
     cudaEventDestroy(ready);
     throw;
   }
-  second.join();
+  for (auto& x : th) x.join();
   cudaEventDestroy(ready);
-  t->launches += tw->launches + 1;
-  t->fallbacks += tw->fallbacks;
-  return r1 != GOX_OK ? r1 : r2;
+  for (int k = 1; k < parts; k++) {
+    t->launches += tw[k]->launches + 1;
+    t->fallbacks += tw[k]->fallbacks;
+  }
+  for (int r : rk)
+    if (r != GOX_OK) return r;
+  return GOX_OK;
 }
 
 extern "C" {
@@ -3608,7 +3631,7 @@ int64_t gox_last_launches(const gox_topo* t) { return t ? t->launches : -1; }
 int gox_set_pivot_tolerance(gox_topo* t, double tol) {
   if (!t || !(tol >= 0.0) || !std::isfinite(tol)) return GOX_E_INVALID;
   t->piv_tol = tol;
-  if (t->twin) t->twin->piv_tol = tol;
+  for (gox_topo* tw = t->twin.get(); tw; tw = tw->twin.get()) tw->piv_tol = tol;
   return GOX_OK;
 }
 
@@ -3638,7 +3661,7 @@ int gox_topo_set_zip(gox_topo* t, const double* zi_re, const double* zi_im, cons
 }
 
 int gox_topo_set_split(gox_topo* t, int32_t parts) {
-  if (!t || parts < 1 || parts > 2) return GOX_E_INVALID;
+  if (!t || parts < 1 || parts > 8) return GOX_E_INVALID;
   t->split_parts = parts;
   return GOX_OK;
 }
@@ -3646,7 +3669,7 @@ int gox_topo_set_split(gox_topo* t, int32_t parts) {
 int gox_topo_set_graph(gox_topo* t, int32_t on) {
   if (!t) return GOX_E_INVALID;
   t->graphs_wanted = on != 0;
-  if (t->twin) t->twin->graphs_wanted = on != 0;
+  for (gox_topo* tw = t->twin.get(); tw; tw = tw->twin.get()) tw->graphs_wanted = on != 0;
   return GOX_OK;
 }
 
@@ -3932,9 +3955,13 @@ extern "C" int gox_ls_factor_solve_values_static(gox_ls* h, const double* vals,
 // ---- serving -----------------------------------------------------------------
 // Worker threads batch queued single-scenario requests per topology
 // (continuous batching: while a batch runs, new requests queue; a free
-// worker takes the oldest request whose topology is not being solved and up
-// to max_batch of that topology's requests in arrival order) and solve each
-// batch with gox_batch_solve on the GPU.
+// worker takes the oldest request whose topology has a free lane and up to
+// max_batch of that topology's requests in arrival order) and solve each
+// batch with gox_batch_solve on the GPU.  A topology's lanes are instances
+// of it with their own device state: the topology itself and, once its
+// pivot order and plan are fixed, clones of it, so that requests arriving
+// while a long batch runs start on another instance instead of waiting for
+// it; every instance gives the same result bit for bit.
 
 #include <chrono>
 #include <condition_variable>
@@ -3982,12 +4009,44 @@ struct gox_server {
     for (int64_t v : reserved) r += v;
     return r;
   }
+  // Lanes: instance j of topology tp is inst[tp][j] (0: the topology; the
+  // others clones made on first use, owned here), busy while a worker
+  // solves a batch on it
+  static constexpr int kMaxLanes = 8;
+  int lanes = 1;
+  std::vector<std::array<gox_topo*, kMaxLanes>> inst;
+  std::vector<std::array<char, kMaxLanes>> lane_busy;
+  std::vector<int> inflight;  // per topology: batches being solved
+  // per topology: its pivot order and plan are fixed (recorded by the
+  // worker that ran its first batch), so clones of it may be made
+  std::vector<char> settled;
+  std::vector<std::unique_ptr<gox_topo>> owned;
+  int64_t clones = 0;
+  // A free lane of topology c (-1: none).  Existing instances first; a new
+  // clone only once the topology is settled and without an HBM budget (whose
+  // accounting admits one batch per topology).
+  int free_lane(int c) const {
+    if (!lane_busy[c][0]) return 0;
+    const bool grow = budget <= 0 && settled[c];
+    for (int j = 1; j < std::min(lanes, kMaxLanes); j++) {
+      if (lane_busy[c][j]) continue;
+      if (inst[c][j] || grow) return j;
+    }
+    return -1;
+  }
+  int64_t held(int tp) const {
+    int64_t b = 0;
+    for (gox_topo* x : inst[tp])
+      if (x) b += held_bytes(x);
+    return b;
+  }
   // Device bytes a topology's per-batch buffers hold now: its batch and
   // staging buffers, its split twin's, the linear guess system's and the
   // FP64 re-solve staging
   static int64_t held_bytes(gox_topo* t) {
     int64_t b = (int64_t)(t->batch.bytes() + t->io.bytes());
-    if (t->twin) b += (int64_t)(t->twin->batch.bytes() + t->twin->io.bytes());
+    for (gox_topo* tw = t->twin.get(); tw; tw = tw->twin.get())
+      b += (int64_t)(tw->batch.bytes() + tw->io.bytes());
     for (const gox::DevMem* m : {&t->guess.lu, &t->guess.off, &t->guess.rhs, &t->guess.sol,
                                  &t->guess.sing, &t->guess.piv, &t->guess.gact, &t->guess.err,
                                  &t->guess.gvm, &t->guess.gva, &t->fb.idx, &t->fb.p, &t->fb.q,
@@ -3999,9 +4058,9 @@ struct gox_server {
   static void release_buffers(gox_topo* t) {
     t->batch.release();
     t->io.release();
-    if (t->twin) {
-      t->twin->batch.release();
-      t->twin->io.release();
+    for (gox_topo* tw = t->twin.get(); tw; tw = tw->twin.get()) {
+      tw->batch.release();
+      tw->io.release();
     }
     for (gox::DevMem* m : {&t->guess.lu, &t->guess.off, &t->guess.rhs, &t->guess.sol,
                            &t->guess.gvm, &t->guess.gva, &t->fb.idx, &t->fb.p, &t->fb.q, &t->fb.vm,
@@ -4020,8 +4079,9 @@ struct gox_server {
     const int64_t per = scenario_bytes(topos[tp]);
     auto others = [&]() { return reserved_total() - reserved[tp]; };
     for (size_t o = 0; o < topos.size() && others() + 32 * per > budget; o++)
-      if ((int)o != tp && !busy[o] && reserved[o] > 0) {
-        release_buffers(topos[o]);
+      if ((int)o != tp && inflight[o] == 0 && reserved[o] > 0) {
+        for (gox_topo* x : inst[o])
+          if (x) release_buffers(x);
         reserved[o] = 0;
       }
     const int64_t groups = (budget - others()) / (32 * per);
@@ -4035,20 +4095,19 @@ struct gox_server {
     const int64_t slots = t->factored ? (int64_t)t->sc.n_slots + (int64_t)t->sc.n_off : 4 * na;
     return 8 * (8 * n + 5 * n + na + slots + 2 * nu) + 8 * 8 * n + 8 * 64 + 128;
   }
-  // Workers: each takes the oldest queued request whose topology no other
-  // worker is solving, with up to max_batch queued requests of that
-  // topology, so batches of different topologies run concurrently (each
-  // solve has its own stream) while one topology's state is used by one
-  // worker at a time.
+  // Workers: each takes the oldest queued request whose topology has a free
+  // lane, with up to max_batch queued requests of that topology, so batches
+  // of different topologies, and of one topology on its lanes, run
+  // concurrently (each solve has its own stream) while each instance's state
+  // is used by one worker at a time.
   static constexpr int kWorkers = 16;
   std::vector<std::thread> workers;
-  std::vector<char> busy;  // per topology
 
   void run() {
     cudaSetDevice(device);
     for (;;) {
       std::vector<std::shared_ptr<gox::ServerReq>> batch;
-      int tp = -1;
+      int tp = -1, ln = -1;
       gox_topo* t = nullptr;
       {
         std::unique_lock<std::mutex> lk(mu);
@@ -4057,20 +4116,23 @@ struct gox_server {
           cv.wait(lk, [&] {
             if (stop && queue.empty()) return true;
             for (const auto& r : queue)
-              if (!busy[r->topo]) return true;
+              if (free_lane(r->topo) >= 0) return true;
             return false;
           });
           if (stop && queue.empty()) return;
           // topologies in the order of their oldest queued request; the
-          // first whose batch fits the budget now
+          // first with a free lane whose batch fits the budget now
           std::vector<char> tried(topos.size(), 0);
           for (const auto& r : queue) {
             const int c = r->topo;
-            if (busy[c] || tried[c]) continue;
+            if (tried[c]) continue;
             tried[c] = 1;
+            const int j = free_lane(c);
+            if (j < 0) continue;
             cap = admit_cap(c);
             if (cap > 0) {
               tp = c;
+              ln = j;
               break;
             }
           }
@@ -4080,8 +4142,9 @@ struct gox_server {
           const int64_t seen = batches;
           cv.wait(lk, [&] { return stop || batches != seen; });
         }
-        busy[tp] = 1;
-        t = topos[tp];
+        lane_busy[tp][ln] = 1;
+        inflight[tp]++;
+        t = inst[tp][ln];
         for (auto it = queue.begin(); it != queue.end() && (int)batch.size() < cap;) {
           if ((*it)->topo == tp) {
             batch.push_back(*it);
@@ -4096,20 +4159,47 @@ struct gox_server {
         if (budget > 0) reserved[tp] = std::max(reserved[tp], groups * 32 * scenario_bytes(t));
       }
       const auto t_pick = std::chrono::steady_clock::now();
+      if (!t) {  // a new lane: clone the topology (outside the lock)
+        std::unique_ptr<gox_topo> c;
+        try {
+          c = clone_factored(topos[tp]);
+        } catch (...) {
+        }
+        std::lock_guard<std::mutex> lk(mu);
+        if (c) {
+          t = c.get();
+          inst[tp][ln] = t;
+          owned.push_back(std::move(c));
+          clones++;
+        } else {  // (no memory for a clone: the batch goes back to the queue)
+          for (auto it = batch.rbegin(); it != batch.rend(); ++it) queue.push_front(*it);
+          lane_busy[tp][ln] = 0;
+          inflight[tp]--;
+          lanes = std::max(1, ln);
+          cv.notify_all();
+          continue;
+        }
+      }
       solve(t, batch);
       // the topology's refactor plan was timed on its first batch (when the
       // autotuner is on); later batches keep it or a cached plan: no
       // timing inside the serving loop
       t->tune_cache_only = true;
+      // (read by the worker that solved on the topology itself: no other
+      // thread writes it now)
+      const bool fixed = ln == 0 && t->factored && t->guess_mode == 0 && !t->timing.on &&
+                         t->tune[precision == GOX_PRECISION_FP64 ? 1 : 0].done;
       const auto t_done = std::chrono::steady_clock::now();
       {
         std::lock_guard<std::mutex> lk(mu);
+        if (fixed) settled[tp] = 1;
         for (const auto& r : batch)
           queue_s += std::chrono::duration<double>(t_pick - r->t_submit).count();
         solve_s += std::chrono::duration<double>(t_done - t_pick).count() * (double)batch.size();
-        reserved[tp] = held_bytes(t);
+        reserved[tp] = held(tp);
         peak_reserved = std::max(peak_reserved, reserved_total());
-        busy[tp] = 0;
+        lane_busy[tp][ln] = 0;
+        inflight[tp]--;
         batches++;
         solved += (int64_t)batch.size();
       }
@@ -4198,7 +4288,12 @@ int gox_server_add_topology(gox_server* s, gox_topo* t, int32_t* topo_id) {
   if (!s || !t || !topo_id) return GOX_E_INVALID;
   std::lock_guard<std::mutex> lk(s->mu);
   s->topos.push_back(t);
-  s->busy.push_back(0);
+  std::array<gox_topo*, gox_server::kMaxLanes> in{};
+  in[0] = t;
+  s->inst.push_back(in);
+  s->lane_busy.push_back({});
+  s->inflight.push_back(0);
+  s->settled.push_back(0);
   s->reserved.push_back(0);
   *topo_id = (int32_t)s->topos.size() - 1;
   return GOX_OK;
@@ -4279,6 +4374,14 @@ int gox_server_stats(gox_server* s, int64_t* out) {
   out[4] = s->peak_reserved;
   out[5] = (int64_t)(s->queue_s * 1e6);
   out[6] = (int64_t)(s->solve_s * 1e6);
+  out[7] = s->clones;
+  return GOX_OK;
+}
+
+int gox_server_set_lanes(gox_server* s, int32_t lanes) {
+  if (!s || lanes < 1 || lanes > gox_server::kMaxLanes) return GOX_E_INVALID;
+  std::lock_guard<std::mutex> lk(s->mu);
+  s->lanes = lanes;
   return GOX_OK;
 }
 

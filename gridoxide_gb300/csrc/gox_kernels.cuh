@@ -629,6 +629,14 @@ __device__ __forceinline__ void sts(uint32_t a, float v) {
 __device__ __forceinline__ void sts(uint32_t a, double v) {
   asm volatile("st.shared.f64 [%0], %1;\n" ::"r"(a), "d"(v) : "memory");
 }
+__device__ __forceinline__ uint4 lds128(uint32_t a) {
+  uint4 v;
+  asm volatile("ld.shared.v4.b32 {%0, %1, %2, %3}, [%4];\n"
+               : "=r"(v.x), "=r"(v.y), "=r"(v.z), "=r"(v.w)
+               : "r"(a)
+               : "memory");
+  return v;
+}
 __device__ __forceinline__ void cp_async16(uint32_t smem, const void* gmem) {
   asm volatile("cp.async.ca.shared.global [%0], [%1], 16;\n" ::"r"(smem), "l"(gmem) : "memory");
 }
@@ -833,8 +841,10 @@ struct Rf {
     *xg = x;
   }
 
-  // pivot, scale L in place, write the column (and y_k) back; rows in
-  // blocks of 8, the last block clamped to the column's end
+  // pivot, scale L in place (each lane its scenario's rows, in blocks of 8,
+  // the last block clamped to the column's end), then the column's rows to
+  // its slots: a row of 32 values is contiguous both in the stage and in the
+  // factor image, so each lane moves 16 bytes of one row per instruction
   static __device__ __forceinline__ void finish(int k, int base, int ulen, int llen, uint32_t st_lane,
                                                 T* LUg, T* Xg, int lane, bool fuse, float ptol,
                                                 bool& bad, bool& tiny) {
@@ -842,14 +852,6 @@ struct Rf {
     const T piv = lds<T>(st_lane + (uint32_t)ulen * RB);
     bad |= (piv == (T)0);
     const T inv = rcp_rn(piv);
-    T* dst = LUg + (size_t)base * 32u + lane;
-    for (int p0 = 0; p0 <= ulen; p0 += 8) {
-      T v[8];
-#pragma unroll
-      for (int t = 0; t < 8; t++) v[t] = lds<T>(st_lane + (uint32_t)min(p0 + t, ulen) * RB);
-#pragma unroll
-      for (int t = 0; t < 8; t++) dst[(size_t)min(p0 + t, ulen) * 32u] = v[t];
-    }
     T colmax = fabs(piv);
     for (int p0 = ulen + 1; p0 < len; p0 += 8) {
       T v[8];
@@ -860,14 +862,25 @@ struct Rf {
 #pragma unroll
       for (int t = 0; t < 8; t++) {
         if (sizeof(T) == 8 && p0 + t >= len) break;  // FP64: no duplicate multiplies
-        const int r = min(p0 + t, len - 1);
         v[t] *= inv;
-        sts(st_lane + (uint32_t)r * RB, v[t]);
-        dst[(size_t)r * 32u] = v[t];
+        sts(st_lane + (uint32_t)min(p0 + t, len - 1) * RB, v[t]);
       }
     }
     tiny |= (ptol > 0.0f) && ((float)fabs(piv) < ptol * (float)colmax);
     if (fuse) Xg[(size_t)k * 32u + lane] = lds<T>(st_lane + (uint32_t)len * RB);
+    __syncwarp();
+    const int sub = lane % LPR, rsel = lane / LPR;
+    const uint32_t blk = st_lane - (uint32_t)lane * (uint32_t)sizeof(T) + (uint32_t)sub * 16u;
+    char* dst = reinterpret_cast<char*>(LUg + (size_t)base * 32u) + sub * 16;
+    for (int r0 = rsel; r0 < len + rsel; r0 += 4 * RPI) {
+      uint4 v[4];
+#pragma unroll
+      for (int u = 0; u < 4; u++) v[u] = lds128(blk + (uint32_t)min(r0 + u * RPI, len - 1) * RB);
+#pragma unroll
+      for (int u = 0; u < 4; u++)
+        *reinterpret_cast<uint4*>(dst + (size_t)min(r0 + u * RPI, len - 1) * RB) = v[u];
+    }
+    __syncwarp();
   }
 };
 

@@ -794,11 +794,15 @@ class Server:
             time.sleep(1e-4)
 
     def stats(self) -> dict:
-        a = np.zeros(7, np.int64)
+        a = np.zeros(8, np.int64)
         check(_lib.load().gox_server_stats(self._h, _p(a, _lib.i64p)), "gox_server_stats")
         return dict(batches=int(a[0]), solved=int(a[1]), queued=int(a[2]),
                     reserved_bytes=int(a[3]), peak_reserved_bytes=int(a[4]),
-                    queue_us=int(a[5]), solve_us=int(a[6]))
+                    queue_us=int(a[5]), solve_us=int(a[6]), clones=int(a[7]))
+
+    def set_lanes(self, lanes: int) -> None:
+        """Batches of one topology solved at the same time, 1..8 (gox_server_set_lanes)."""
+        check(_lib.load().gox_server_set_lanes(self._h, int(lanes)), "gox_server_set_lanes")
 
     def set_budget(self, nbytes: int) -> None:
         """Admit batches by an HBM budget in bytes (0: none)."""

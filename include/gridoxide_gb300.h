@@ -500,12 +500,15 @@ const char *gox_version(void);
 /* ---- serving --------------------------------------------------------------
  * Continuous batching of single-scenario requests over registered
  * topologies: each of 16 worker threads takes the oldest queued request
- * whose topology no other worker is solving and up to max_batch of that
- * topology's requests (arrival order), solves them with gox_batch_solve on
- * its own stream (batches of different topologies overlap on the GPU), and
- * publishes each result with its latency (submit to completion).  Lanes
- * are independent, so a request's result does not depend on the batch it
- * ran in.  A topology added to a server is used by the server's workers
+ * whose topology has a free lane and up to max_batch of that topology's
+ * requests (arrival order), solves them with gox_batch_solve on its own
+ * stream (batches of different topologies, and of one topology on its
+ * lanes, overlap on the GPU), and publishes each result with its latency
+ * (submit to completion).  A topology's lanes are the topology itself and,
+ * after its first batch has fixed its pivot order and plan, clones of it
+ * with their own device state (gox_server_set_lanes); every lane gives the
+ * same results bit for bit.  Scenarios are independent, so a request's
+ * result does not depend on the batch it ran in.  A topology added to a server is used by the server's workers
  * only: do not call it directly while the server runs.  Its refactor plan
  * is timed by the autotuner on its first batch at most; later batches keep
  * that plan (or a cached one), so no timing runs inside the serving loop.
@@ -529,11 +532,16 @@ int gox_server_submit(gox_server *s, int32_t topo_id, const double *p_spec, cons
  * pointers may be NULL. */
 int gox_server_poll(gox_server *s, int64_t ticket, double *vm, double *va, int32_t *iterations,
                     int32_t *status, double *max_mismatch, double *latency_s);
-/* [0] batches run, [1] requests solved, [2] requests queued, [3] device
- * bytes the topologies' batch buffers hold now, [4] their peak, [5] / [6]
- * microseconds summed over the solved requests spent queued / in their
- * batch's solve. */
+/* out[8]: [0] batches run, [1] requests solved, [2] requests queued, [3]
+ * device bytes the topologies' batch buffers hold now, [4] their peak, [5] /
+ * [6] microseconds summed over the solved requests spent queued / in their
+ * batch's solve, [7] topology clones made for lanes. */
 int gox_server_stats(gox_server *s, int64_t *out);
+/* Lanes per topology, 1..8 (default 1): how many batches of one topology
+ * may be solved at the same time.  Lanes beyond the first are clones made
+ * on first use (host copies of the topology's analysis and plans, device
+ * buffers of their own); with an HBM budget set, one lane per topology. */
+int gox_server_set_lanes(gox_server *s, int32_t lanes);
 /* Admission by HBM budget (bytes; 0, the default: none).  A worker admits
  * at most the batch whose buffers fit in the budget beside the other
  * topologies' buffers (by each topology's per-scenario device bytes),

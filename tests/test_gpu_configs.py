@@ -83,6 +83,10 @@ def test_case2000_full_batch_graph_and_split_match_oracle(gox, oracle_mod):
     # concurrent halves; the first mixed call captures its graphs, the next
     # ones run them
     rm = [solve(gox.GOX_PRECISION_MIXED) for _ in range(3)]
+    # four staggered parts of 1,024 scenarios, then five uneven ones
+    for parts in (4, 5):
+        topo.set_split(parts)
+        rm.append(solve(gox.GOX_PRECISION_MIXED))
     topo.set_split(1)
     topo.set_graph(False)
     plain = solve(gox.GOX_PRECISION_MIXED)

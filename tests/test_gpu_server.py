@@ -1,10 +1,12 @@
 """GPU: the serving loop (gox_server_*).  Requests arrive one scenario at a
 time (Poisson arrivals from a client thread) over three topologies, some
 with an N-1 outage; the workers batch them per topology, with or without
-an HBM budget (the buffers held then stay within it).  Every report
-must equal, bit for bit, a direct batched solve of the same scenario on the
-same topology (lanes are independent, so the batch a request ran in does
-not change its result), and carry a positive latency."""
+an HBM budget (the buffers held then stay within it), with one or several
+server lanes per topology (clones solving batches of one topology at the
+same time).  Every report must equal, bit for bit, a direct batched solve
+of the same scenario on the same topology (scenarios are independent, so
+neither the batch nor the clone a request ran on changes its result), and
+carry a positive latency."""
 import threading
 import time
 
@@ -27,8 +29,9 @@ def _grids():
 
 # 2 MB is below one group of 32 scenarios of the two larger grids: such a
 # batch waits until no other topology holds buffers, then runs alone
-@pytest.mark.parametrize("precision,budget", [(0, 0), (1, 0), (1, 16 << 20), (1, 2 << 20)])
-def test_server_reports_equal_direct_solves(gox, precision, budget):
+@pytest.mark.parametrize("precision,budget,lanes", [(0, 0, 2), (1, 0, 1), (1, 0, 4),
+                                                    (1, 16 << 20, 2), (1, 2 << 20, 2)])
+def test_server_reports_equal_direct_solves(gox, precision, budget, lanes):
     grids = _grids()
     topos = [gox.Topology(yb, g.bus_type) for g, yb in grids]
     rng = np.random.default_rng(40)
@@ -42,10 +45,16 @@ def test_server_reports_equal_direct_solves(gox, precision, budget):
             br = rng.choice(np.flatnonzero(~G.bridges(g)), size=1)
             out = tuple(a[0] for a in G.outage_deltas(g, yb, br))
         reqs.append((t, p[0], q[0], out))
-    srv = gox.Server(max_batch=64, precision=precision)
+    # (batches of at most 8 with several lanes: a topology's queued requests
+    # then take several batches, which run on its clones at the same time)
+    srv = gox.Server(max_batch=64 if lanes == 1 or budget else 8, precision=precision)
     ids = [srv.add_topology(tp) for tp in topos]
     if budget:
         srv.set_budget(budget)
+    srv.set_lanes(lanes)
+    if lanes > 1:  # each topology's first batch fixes its pivot order and plan
+        for t, (g, _) in enumerate(grids):
+            srv.wait(srv.submit(ids[t], g.p_spec, g.q_spec, g.vm, g.va), g.n_bus)
     tickets = [None] * len(reqs)
 
     def client():
@@ -60,9 +69,16 @@ def test_server_reports_equal_direct_solves(gox, precision, budget):
     reports = [srv.wait(tickets[i], grids[reqs[i][0]][0].n_bus) for i in range(len(reqs))]
     st = srv.stats()
     srv.close()
-    assert st["solved"] == len(reqs) and st["queued"] == 0 and st["batches"] >= 3
+    warm = 3 if lanes > 1 else 0
+    assert st["solved"] == len(reqs) + warm and st["queued"] == 0 and st["batches"] >= 3
     if budget >= 16 << 20:  # admitted batches kept the topologies' buffers within the budget
         assert 0 < st["peak_reserved_bytes"] <= budget
+    if budget:  # one lane per topology under a budget
+        assert st["clones"] == 0
+    elif lanes == 1:
+        assert st["clones"] == 0
+    else:  # requests arriving while a topology's batch runs start on a clone
+        assert 1 <= st["clones"] <= 3 * (lanes - 1)
     lat = np.array([r["latency_s"] for r in reports])
     assert np.all(lat > 0)
     # the same scenarios solved directly on the same topologies
@@ -103,4 +119,7 @@ def test_server_rejects_bad_requests(gox):
     assert r["status"] == gox.GOX_CONVERGED
     with pytest.raises(Exception):
         srv.poll(t, g.n_bus)  # a retired ticket
+    for bad in (0, 9):
+        with pytest.raises(Exception):
+            srv.set_lanes(bad)
     srv.close()
