@@ -2129,7 +2129,7 @@ static void run_multi(const std::vector<gox_topo*>& ts, std::vector<BatchRun>& r
 // (the default, faster on the many-topology workload: its big grids keep
 // their wide kernels); a topology for which no such plan fits sends the
 // call to the lockstep loop.
-static std::atomic<int> g_multi_persistent{0};
+static std::atomic<int> g_multi_persistent{1};
 // dynamic shared memory a persistent plan may use (the kernel's static
 // shared memory -- the job, the injections' reduction row, the refactor's
 // barriers and flags -- takes the rest of the 227 KB)

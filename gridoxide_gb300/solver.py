@@ -166,21 +166,25 @@ def set_refactor_sync(progress_flags: bool) -> None:
 
 
 def set_multi_persistent(on: bool) -> None:
-    """multi_solve's form: one Newton loop whose phases are one launch each
-    over every topology still running (default), or one persistent launch
-    in which each CTA runs whole Newton loops of (topology, group) items."""
+    """multi_solve's form: one persistent launch in which each CTA runs whole
+    Newton loops of (topology, group) items (default), or one Newton loop
+    whose phases are one launch each over every topology still running."""
     check(_lib.load().gox_set_multi_persistent(1 if on else 0), "gox_set_multi_persistent")
 
 
-def multi_solve(jobs, tol=1e-8, max_iter=20, precision=GOX_PRECISION_MIXED) -> list:
+def multi_solve(jobs, tol=1e-8, max_iter=20, precision=GOX_PRECISION_MIXED,
+                out: Optional[list] = None) -> list:
     """Many topologies' batches solved together (gox_multi_solve): one
-    Newton loop with one launch per phase over every topology still running,
-    or (set_multi_persistent(True)) one persistent launch whose CTAs run
-    whole Newton loops of (topology, group) items.  `jobs`: (Topology, p_spec [B, N], q_spec [B, N], vm0, va0) with
+    persistent launch whose CTAs run whole Newton loops of (topology, group)
+    items, or (set_multi_persistent(False)) one Newton loop with one launch
+    per phase over every topology still running.  `jobs`: (Topology, p_spec [B, N], q_spec [B, N], vm0, va0) with
     vm0 / va0 [N] (shared) or [B, N]; each topology at most once.  Returns
     one BatchResult per job, equal bit for bit to Topology.solve on that job
-    alone."""
+    alone.  out: one BatchResult per job to write into (e.g. over pinned
+    memory, reused across calls) instead of fresh arrays."""
     n = len(jobs)
+    if out is not None and len(out) != n:
+        raise ValueError("out must hold one BatchResult per job")
     keep, outs = [], []
     topo_a = (C.c_void_p * n)()
     arr = {k: (C.c_void_p * n)() for k in ("p", "q", "vm", "va", "ovm", "ova", "it", "st", "mm")}
@@ -192,8 +196,21 @@ def multi_solve(jobs, tol=1e-8, max_iter=20, precision=GOX_PRECISION_MIXED) -> l
         vm0, va0 = _f64(vm0), _f64(va0)
         batch[j] = B
         vstride[j] = N if vm0.ndim == 2 else 0
-        res = BatchResult(np.zeros((B, N)), np.zeros((B, N)), np.zeros(B, np.int32),
-                          np.zeros(B, np.int32), np.zeros(B))
+        if out is not None:
+            res = out[j]
+            ok = (res.voltage_mag.shape == (B, N) and res.voltage_ang.shape == (B, N) and
+                  res.iterations.shape == (B,) and res.status.shape == (B,) and
+                  res.max_mismatch.shape == (B,) and res.voltage_mag.dtype == np.float64 and
+                  res.voltage_ang.dtype == np.float64 and res.iterations.dtype == np.int32 and
+                  res.status.dtype == np.int32 and res.max_mismatch.dtype == np.float64 and
+                  all(a.flags.c_contiguous for a in (res.voltage_mag, res.voltage_ang,
+                                                     res.iterations, res.status,
+                                                     res.max_mismatch)))
+            if not ok:
+                raise ValueError("out arrays do not match the batch")
+        else:
+            res = BatchResult(np.empty((B, N)), np.empty((B, N)), np.zeros(B, np.int32),
+                              np.zeros(B, np.int32), np.zeros(B))
         keep += [p, q, vm0, va0]
         outs.append(res)
         topo_a[j] = topo.handle.value

@@ -53,9 +53,15 @@ def test_multi_equals_alone(gox, precision, persistent):
         for a, m in zip(alone, mixed):
             assert np.all(a.status == gox.GOX_CONVERGED)
             _same(a, m)
-        # the same topologies again (fixed pivot orders, tuned plans): same bits
-        again = gox.multi_solve(jobs, **kw)
-        for a, m in zip(alone, again):
+        # the same topologies again (fixed pivot orders, tuned plans), into
+        # caller-given result arrays (filled with NaN first): same bits
+        bufs = [gox.BatchResult(np.full(p.shape, np.nan), np.full(p.shape, np.nan),
+                                np.full(p.shape[0], -7, np.int32),
+                                np.full(p.shape[0], -7, np.int32),
+                                np.full(p.shape[0], np.nan)) for g, yb, p, q in data]
+        again = gox.multi_solve(jobs, out=bufs, **kw)
+        for a, m, b in zip(alone, again, bufs):
+            assert m is b
             _same(a, m)
         # a budget that runs out: MaxIterations reported as alone
         short = dict(kw, max_iter=2)
@@ -65,7 +71,7 @@ def test_multi_equals_alone(gox, precision, persistent):
             assert np.any(a.status == gox.GOX_MAX_ITERATIONS)
             _same(a, m)
     finally:
-        S.set_multi_persistent(False)  # the default
+        S.set_multi_persistent(True)  # the default
 
 
 def test_multi_fp64_matches_oracle(gox, oracle_mod):
