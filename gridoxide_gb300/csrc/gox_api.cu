@@ -4329,6 +4329,7 @@ int gox_server_submit(gox_server* s, int32_t topo_id, const double* p_spec, cons
       }
     }
     r->t_submit = std::chrono::steady_clock::now();
+    bool budgeted = false;
     {
       std::lock_guard<std::mutex> lk(s->mu);
       if (s->stop) return GOX_E_INVALID;
@@ -4336,8 +4337,13 @@ int gox_server_submit(gox_server* s, int32_t topo_id, const double* p_spec, cons
       s->all[r->ticket] = r;
       s->queue.push_back(r);
       *ticket = r->ticket;
+      budgeted = s->budget > 0;
     }
-    s->cv.notify_all();
+    // one idle worker takes the request (waking all 16 for every request
+    // makes them contend for the lock with the submitting thread); under a
+    // budget a worker may be waiting for a batch to finish instead, so all
+    if (budgeted) s->cv.notify_all();
+    else s->cv.notify_one();
     return GOX_OK;
   });
 }
