@@ -423,11 +423,12 @@ def many_topologies(gox, rounds: int) -> dict:
     batch of 8-1,024 scenarios each (loads x lognormal(0, 0.15), flat
     start); a round solves every grid's batch once; host buffers, mixed
     precision.  `value`: the round as one gox_multi_solve call in its
-    default form (one persistent launch whose CTAs run whole Newton loops of
-    (grid, group of 32) items from a device queue); beside it the same round
-    in the call's other form (`one_loop`: one launch per phase over every
-    grid still running) and as 48 independent solves issued from 8 host
-    threads (`threads`: each its own Newton loop and stream).  Every form
+    default form (one Newton loop, each phase one launch over every grid
+    still running); beside it the same round in the call's other form
+    (`one_launch`: one persistent launch whose CTAs run whole Newton loops of
+    (grid, group of 32) items from a device queue) and as 48 independent
+    solves issued from 8 host threads (`threads`: each its own Newton loop
+    and stream).  Every form
     reads its inputs from, and writes its results to, pinned host memory
     allocated once and reused every round (as a serving caller would), each
     form its own result buffers; the one-call forms' results must equal the
@@ -498,26 +499,26 @@ def many_topologies(gox, rounds: int) -> dict:
         same = all(np.array_equal(a.voltage_mag, b.voltage_mag) and
                    np.array_equal(a.iterations, b.iterations) for a, b in zip(res, mres))
         forms[persistent] = (float(np.median(mtimes)), same)
-    S.set_multi_persistent(True)  # the default
-    tm = forms[True][0]
+    S.set_multi_persistent(False)  # the default
+    tm = forms[False][0]
     return {"value": round(total / tm, 1), "unit": "solves/s", "grids": len(spec),
             "scenarios_per_round": total, "ms_per_round": round(1000 * tm, 2),
             "buses": [int(min(x[0] for x in spec)), int(max(x[0] for x in spec))],
             "converged": conv, "rounds": rounds,
-            "equal_to_threads_bitwise": forms[True][1],
+            "equal_to_threads_bitwise": forms[False][1],
             "threads": {"value": round(total / t, 1), "unit": "solves/s",
                         "ms_per_round": round(1000 * t, 2),
                         "note": "the 48 grids' batches as independent solves issued from 8 host "
                                 "threads, each its own Newton loop and stream"},
-            "one_loop": {"value": round(total / forms[False][0], 1), "unit": "solves/s",
-                         "ms_per_round": round(1000 * forms[False][0], 2),
-                         "equal_to_threads_bitwise": forms[False][1],
-                         "note": "gox_multi_solve's loop form: one Newton loop, each phase one "
-                                 "launch over every grid still running"},
-            "note": "one gox_multi_solve call per round, default form: one persistent launch "
-                    "whose CTAs run whole Newton loops of (grid, group of 32) items from a "
-                    "device queue, largest grid first; host buffers (pinned, allocated once), "
-                    "mixed precision, flat start"}
+            "one_launch": {"value": round(total / forms[True][0], 1), "unit": "solves/s",
+                           "ms_per_round": round(1000 * forms[True][0], 2),
+                           "equal_to_threads_bitwise": forms[True][1],
+                           "note": "gox_multi_solve's persistent form: one launch whose CTAs run "
+                                   "whole Newton loops of (grid, group of 32) items from a device "
+                                   "queue, largest grid first"},
+            "note": "one gox_multi_solve call per round, default form: one Newton loop, each "
+                    "phase one launch over every grid still running; host buffers (pinned, "
+                    "allocated once), mixed precision, flat start"}
 
 
 def pgm_batch(gox, rounds: int, batch: int = 4096) -> dict:

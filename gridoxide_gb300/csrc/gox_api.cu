@@ -1197,10 +1197,14 @@ static void autotune(gox_topo* t, const BatchDev& D, cudaStream_t st) {
           if (compile_checked(sc, p, s)) {
             install_stream(t, i, std::move(s));
             TU.source = 2;
+            return;
           }
-          return;
+          break;
         }
-      return;
+      // the cached plan does not fit this topology (another topology of the
+      // same size and fill bucket, e.g. one whose first level can go to the
+      // wide kernels): time the candidates, unless timing is not allowed
+      if (t->tune_cache_only) return;
     }
   }
   // compile and check every candidate (host threads in parallel)
@@ -2127,9 +2131,10 @@ static void run_multi(const std::vector<gox_topo*>& ts, std::vector<BatchRun>& r
 // without the wide split (FP32 up to 12 warps, FP64 8), compiled and checked
 // once.  gox_set_multi_persistent(1) chooses it over the lockstep loop above
 // (the default, faster on the many-topology workload: its big grids keep
-// their wide kernels); a topology for which no such plan fits sends the
-// call to the lockstep loop.
-static std::atomic<int> g_multi_persistent{1};
+// their wide kernels, while a persistent CTA runs a big grid's group alone on
+// its SM); a topology for which no such plan fits sends the call to the
+// lockstep loop.
+static std::atomic<int> g_multi_persistent{0};
 // dynamic shared memory a persistent plan may use (the kernel's static
 // shared memory -- the job, the injections' reduction row, the refactor's
 // barriers and flags -- takes the rest of the 227 KB)

@@ -166,18 +166,18 @@ def set_refactor_sync(progress_flags: bool) -> None:
 
 
 def set_multi_persistent(on: bool) -> None:
-    """multi_solve's form: one persistent launch in which each CTA runs whole
-    Newton loops of (topology, group) items (default), or one Newton loop
-    whose phases are one launch each over every topology still running."""
+    """multi_solve's form: one Newton loop whose phases are one launch each
+    over every topology still running (default), or one persistent launch
+    in which each CTA runs whole Newton loops of (topology, group) items."""
     check(_lib.load().gox_set_multi_persistent(1 if on else 0), "gox_set_multi_persistent")
 
 
 def multi_solve(jobs, tol=1e-8, max_iter=20, precision=GOX_PRECISION_MIXED,
                 out: Optional[list] = None) -> list:
     """Many topologies' batches solved together (gox_multi_solve): one
-    persistent launch whose CTAs run whole Newton loops of (topology, group)
-    items, or (set_multi_persistent(False)) one Newton loop with one launch
-    per phase over every topology still running.  `jobs`: (Topology, p_spec [B, N], q_spec [B, N], vm0, va0) with
+    Newton loop with one launch per phase over every topology still running,
+    or (set_multi_persistent(True)) one persistent launch whose CTAs run
+    whole Newton loops of (topology, group) items.  `jobs`: (Topology, p_spec [B, N], q_spec [B, N], vm0, va0) with
     vm0 / va0 [N] (shared) or [B, N]; each topology at most once.  Returns
     one BatchResult per job, equal bit for bit to Topology.solve on that job
     alone.  out: one BatchResult per job to write into (e.g. over pinned

@@ -180,17 +180,17 @@ int gox_batch_solve_scaled(gox_topo *t, int32_t B, const double *scales, const d
 
 /* Many topologies' batches solved together: the reference's BatchSolver
  * work queue over scenarios of uneven cost (src/batch.rs:230-281), here for
- * n_topo topologies at once.  By default one persistent kernel launch
- * solves everything: each CTA takes (topology, group of 32 scenarios) items
- * from a device-side queue, largest topology first, and runs that group's
- * whole Newton loop, each topology on a refactor plan without the wide
- * split (compiled once; a topology whose BTF form has off-diagonal blocks,
- * or for which no such plan fits, sends the call to the loop form).  With
- * gox_set_multi_persistent(0) one Newton loop runs each phase as one launch
- * over every topology still running instead (update, injections, decision,
- * fill, one launch per wide level, the refactor's CTAs largest topology
- * first); a topology leaves the loop when its last scenario has converged
- * or failed.  Each topology's set-up and results run on up to 8 host
+ * n_topo topologies at once.  By default one Newton loop runs each phase
+ * as one launch over every topology still running (update, injections,
+ * decision, fill, one launch per wide level, the refactor's CTAs largest
+ * topology first); a topology leaves the loop when its last scenario has
+ * converged or failed.  With gox_set_multi_persistent(1) one persistent
+ * kernel launch solves everything instead: each CTA takes (topology, group
+ * of 32 scenarios) items from a device-side queue, largest topology first,
+ * and runs that group's whole Newton loop, each topology on a refactor plan
+ * without the wide split (compiled once; a topology whose BTF form has
+ * off-diagonal blocks, or for which no such plan fits, sends the call to
+ * the loop).  Each topology's set-up and results run on up to 8 host
  * threads.  Per topology j the arguments are gox_batch_solve's: batch[j]
  * scenarios, p_spec[j] / q_spec[j] [batch[j]][n_bus], vm0[j] / va0[j] with
  * v_stride[j], outputs vm_out[j], va_out[j], iterations[j], status[j],

@@ -71,7 +71,7 @@ def test_multi_equals_alone(gox, precision, persistent):
             assert np.any(a.status == gox.GOX_MAX_ITERATIONS)
             _same(a, m)
     finally:
-        S.set_multi_persistent(True)  # the default
+        S.set_multi_persistent(False)  # the default
 
 
 def test_multi_fp64_matches_oracle(gox, oracle_mod):
