@@ -64,11 +64,19 @@ class ClockSampler:
         self.proc = None
 
     def start(self):
+        """Starts the sampler and returns once it has printed its first
+        sample (its NVML start-up, which can hold the driver for a moment,
+        is then over before the timed region begins; at most 10 s)."""
+        import select
+        self.first = ""
         try:
             self.proc = subprocess.Popen(
                 ["nvidia-smi", "-i", str(self.index), f"--query-gpu={self.Q}",
                  "--format=csv,noheader,nounits", "-lms", "200"],
                 stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            ready, _, _ = select.select([self.proc.stdout], [], [], 10.0)
+            if ready:
+                self.first = self.proc.stdout.readline()
         except Exception:
             self.proc = None
 
@@ -82,6 +90,7 @@ class ClockSampler:
         except Exception:
             self.proc.kill()
             out = ""
+        out = self.first + (out or "")
         sm, mx, reasons = [], 0.0, set()
         names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
         for line in out.strip().splitlines():
@@ -843,10 +852,16 @@ def main():
             torch.distributed.barrier()
         return np.array(ms), kern, launches, iters_run, cl
 
-    for _ in range(args.warmup):
-        step(gox.GOX_PRECISION_MIXED)
-        if not args.quick:
+    # warm-up (pivot orders, plan timing, captured loops), each step after an
+    # L2 flush as in the timed loop: FP64 first, so the timed mixed steps
+    # follow mixed ones
+    if not args.quick:
+        for _ in range(args.warmup):
+            flush.zero_()
             step(gox.GOX_PRECISION_FP64)
+    for _ in range(args.warmup):
+        flush.zero_()
+        step(gox.GOX_PRECISION_MIXED)
     torch.cuda.synchronize()
     # correctness of the timed configuration
     its = oit.cpu().numpy()
@@ -869,6 +884,7 @@ def main():
                           "iterations": iters_mx, "graph_solves": topo.info()["graph_solves"]}),
               flush=True)
         return
+    step(gox.GOX_PRECISION_FP64)  # untimed: the switch back to the FP64 loop
     ms_64, kern_64, launches_64, iters_64, _ = timed(gox.GOX_PRECISION_FP64,
                                                      max(3, args.steps // 2))
     it_64 = oit.cpu().numpy().copy()
