@@ -55,3 +55,46 @@ def test_autotuner_times_candidates_caches_and_keeps_results(gox):
         np.testing.assert_array_equal(r.voltage_mag, ref.voltage_mag)
         np.testing.assert_array_equal(r.voltage_ang, ref.voltage_ang)
         np.testing.assert_array_equal(r.iterations, ref.iterations)
+
+
+_STALE_CACHE_CHILD = r"""
+import sys
+sys.path.insert(0, sys.argv[1]); sys.path.insert(0, sys.argv[1] + "/tests")
+import numpy as np
+import gridoxide_gb300 as gox
+from gridoxide_gb300 import grids as G
+from helpers import grid_from_fixture, load_fixture, ybus_from_fixture
+fx = load_fixture("case118")
+g, yb = grid_from_fixture(fx), ybus_from_fixture(fx)
+p, q = G.load_scenarios(g, 64, 0.15, 77)
+t = gox.Topology(yb, g.bus_type)
+r = t.solve(p, q, g.vm, g.va, tol=1e-8, max_iter=20, precision=gox.GOX_PRECISION_MIXED)
+assert np.all(r.status == 0)
+print(t.tuning()["source"], t.tuning()["warps"])
+"""
+
+
+def test_cached_plan_that_does_not_fit_is_not_taken(tmp_path):
+    """A plan cached under a topology's key that is not among its candidates
+    (another topology of the same size and fill bucket chose it: here 11
+    warps, which no candidate list holds) sends the topology to timing its
+    own candidates, not to the untimed default plan.  The cache file is read
+    once per process, so the check runs in a child process."""
+    import math
+    import os
+    import subprocess
+    import sys
+    root = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+    n = 118
+    bb = int(round(2.0 * math.log2(n)))
+    cache = tmp_path / "tune.txt"
+    with open(cache, "w") as f:  # every fill tenth and batch bucket of the key
+        for fill in range(0, 400):
+            for gb in range(5):
+                f.write(f"gox-tune-3 0 {bb} {fill} {gb} 11 320 0 0\n")
+    env = dict(os.environ, GOX_TUNE_CACHE=str(cache))
+    out = subprocess.run([sys.executable, "-c", _STALE_CACHE_CHILD, root], env=env,
+                         capture_output=True, text=True, timeout=600)
+    assert out.returncode == 0, out.stderr[-2000:]
+    source, warps = out.stdout.split()[-2:]
+    assert source == "measured" and int(warps) != 11
