@@ -1741,9 +1741,11 @@ static int batch_finish(gox_topo* t, int B, const double* p_spec, const double* 
                         const int32_t* o_slot, const double* o_dre, const double* o_dim,
                         double tol, int max_iter, int precision, double* vm_out,
                         double* va_out, int32_t* iters, int32_t* status, double* max_mis,
-                        double* hist, cudaStream_t st, const double* h_p, const double* h_q,
-                        const double* h_vm, const double* h_va, const int32_t* h_oslot,
-                        const double* h_odre, const double* h_odim, BatchRun& R) {
+                        double* hist, cudaStream_t st, const double* /*h_p*/,
+                        const double* /*h_q*/, const double* /*h_vm*/, const double* /*h_va*/,
+                        const int32_t* /*h_oslot*/, const double* /*h_odre*/,
+                        const double* /*h_odim*/, BatchRun& R) {
+  // (the host copies of the inputs, batch_prepare's, are not read here)
   const int n = t->n_bus;
   const int G = (B + 31) / 32;
   const BatchDev& D = R.D;
