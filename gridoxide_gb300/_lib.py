@@ -116,6 +116,8 @@ SIGNATURES = {
     "gox_server_add_topology": (C.c_int, [vp, vp, i32p]),
     "gox_server_submit": (C.c_int, [vp, C.c_int32, f64p, f64p, f64p, f64p, i32p, f64p, f64p, i64p]),
     "gox_server_poll": (C.c_int, [vp, C.c_int64, f64p, f64p, i32p, i32p, f64p, f64p]),
+    "gox_server_submit_many": (C.c_int, [vp, C.c_int32, i32p, vpp, vpp, vpp, vpp, vpp, vpp, vpp,
+                                         i64p]),
     "gox_server_set_budget": (C.c_int, [vp, C.c_int64]),
     "gox_server_set_lanes": (C.c_int, [vp, C.c_int32]),
     "gox_server_stats": (C.c_int, [vp, i64p]),

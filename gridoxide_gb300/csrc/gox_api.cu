@@ -4355,6 +4355,69 @@ int gox_server_submit(gox_server* s, int32_t topo_id, const double* p_spec, cons
   });
 }
 
+int gox_server_submit_many(gox_server* s, int32_t count, const int32_t* topo_ids,
+                           const double* const* p_spec, const double* const* q_spec,
+                           const double* const* vm0, const double* const* va0,
+                           const int32_t* const* out_slot, const double* const* out_dre,
+                           const double* const* out_dim, int64_t* tickets) {
+  if (!s || count < 0 || (count > 0 && (!topo_ids || !p_spec || !q_spec || !vm0 || !va0 || !tickets)))
+    return GOX_E_INVALID;
+  if ((out_slot != nullptr) != (out_dre != nullptr) || (out_slot != nullptr) != (out_dim != nullptr))
+    return GOX_E_INVALID;
+  if (count == 0) return GOX_OK;
+  return guard_impl([&]() -> int {
+    std::vector<int> nb(count);
+    {
+      // every request is checked before any is queued
+      std::lock_guard<std::mutex> lk(s->mu);
+      for (int k = 0; k < count; k++) {
+        const int32_t id = topo_ids[k];
+        if (id < 0 || id >= (int32_t)s->topos.size() || !p_spec[k] || !q_spec[k] || !vm0[k] ||
+            !va0[k])
+          return GOX_E_INVALID;
+        if (out_slot && ((out_slot[k] != nullptr) != (out_dre[k] != nullptr) ||
+                         (out_slot[k] != nullptr) != (out_dim[k] != nullptr)))
+          return GOX_E_INVALID;
+        nb[k] = s->topos[id]->n_bus;
+      }
+    }
+    std::vector<std::shared_ptr<gox::ServerReq>> rs(count);
+    for (int k = 0; k < count; k++) {
+      auto r = std::make_shared<gox::ServerReq>();
+      const int n = nb[k];
+      r->topo = topo_ids[k];
+      r->p.assign(p_spec[k], p_spec[k] + n);
+      r->q.assign(q_spec[k], q_spec[k] + n);
+      r->vm0.assign(vm0[k], vm0[k] + n);
+      r->va0.assign(va0[k], va0[k] + n);
+      if (out_slot && out_slot[k]) {
+        r->outage = true;
+        for (int c = 0; c < 4; c++) {
+          r->slot[c] = out_slot[k][c];
+          r->dre[c] = out_dre[k][c];
+          r->dim[c] = out_dim[k][c];
+        }
+      }
+      rs[k] = std::move(r);
+    }
+    const auto now = std::chrono::steady_clock::now();
+    {
+      std::lock_guard<std::mutex> lk(s->mu);
+      if (s->stop) return GOX_E_INVALID;
+      for (int k = 0; k < count; k++) {
+        rs[k]->t_submit = now;
+        rs[k]->ticket = s->next_ticket++;
+        s->all[rs[k]->ticket] = rs[k];
+        s->queue.push_back(rs[k]);
+        tickets[k] = rs[k]->ticket;
+      }
+    }
+    if (count == 1 && s->budget <= 0) s->cv.notify_one();
+    else s->cv.notify_all();
+    return GOX_OK;
+  });
+}
+
 int gox_server_poll(gox_server* s, int64_t ticket, double* vm, double* va, int32_t* iterations,
                     int32_t* status, double* max_mismatch, double* latency_s) {
   if (!s) return GOX_E_INVALID;

@@ -787,6 +787,32 @@ class Server:
                                             *op, C.byref(t)), "gox_server_submit")
         return int(t.value)
 
+    def submit_many(self, topo_ids, p_ptrs, q_ptrs, vm_ptrs, va_ptrs, out_ptrs=None) -> np.ndarray:
+        """Queues len(topo_ids) requests in one call (gox_server_submit_many),
+        the inputs by address: uint64 arrays holding, per request, the
+        address of its contiguous float64 [n_bus] p_spec, q_spec, vm0, va0;
+        out_ptrs = (slot, dre, dim) uint64 address arrays (0: no outage) or
+        None.  The caller keeps the addressed arrays alive during the call
+        (the library copies them).  Returns the tickets."""
+        ids = _i32(topo_ids)
+        m = len(ids)
+        cols = [np.ascontiguousarray(a, dtype=np.uint64) for a in (p_ptrs, q_ptrs, vm_ptrs, va_ptrs)]
+        if any(c.shape != (m,) for c in cols) or m == 0 or any(np.any(c == 0) for c in cols):
+            raise ValueError("one non-null address per request and array")
+        if np.any(ids < 0) or np.any(ids >= len(self._n)):
+            raise ValueError("unknown topology id")
+        if out_ptrs is not None:
+            outs = [np.ascontiguousarray(a, dtype=np.uint64) for a in out_ptrs]
+            if len(outs) != 3 or any(o.shape != (m,) for o in outs):
+                raise ValueError("out_ptrs: three address arrays, one entry per request")
+        tickets = np.zeros(m, np.int64)
+        vpp = _lib.vpp
+        args = [c.ctypes.data_as(vpp) for c in cols]
+        oargs = [o.ctypes.data_as(vpp) for o in outs] if out_ptrs is not None else [None] * 3
+        check(_lib.load().gox_server_submit_many(self._h, m, _p(ids, _lib.i32p), *args, *oargs,
+                                                 _p(tickets, _lib.i64p)), "gox_server_submit_many")
+        return tickets
+
     def poll(self, ticket: int, n_bus: int) -> Optional[dict]:
         vm, va = np.zeros(n_bus), np.zeros(n_bus)
         it, st = C.c_int32(), C.c_int32()

@@ -527,6 +527,18 @@ int gox_server_add_topology(gox_server *s, gox_topo *t, int32_t *topo_id);
 int gox_server_submit(gox_server *s, int32_t topo_id, const double *p_spec, const double *q_spec,
                       const double *vm0, const double *va0, const int32_t *out_slot,
                       const double *out_dre, const double *out_dim, int64_t *ticket);
+/* Queues `count` requests in one call, each as gox_server_submit would
+ * (request k: topo_ids[k], p_spec[k], q_spec[k], vm0[k], va0[k] [n_bus of
+ * its topology]; out_slot / out_dre / out_dim NULL for no outages, else
+ * arrays of count pointers, NULL for a request without one), all with the
+ * same submit time; their tickets in tickets[count].  Every request is
+ * checked first: GOX_E_INVALID queues none.  A front end that drains its
+ * receive queue periodically submits what arrived at once. */
+int gox_server_submit_many(gox_server *s, int32_t count, const int32_t *topo_ids,
+                           const double *const *p_spec, const double *const *q_spec,
+                           const double *const *vm0, const double *const *va0,
+                           const int32_t *const *out_slot, const double *const *out_dre,
+                           const double *const *out_dim, int64_t *tickets);
 /* GOX_PENDING until the request is solved; then GOX_OK (the outputs are
  * written and the ticket is retired) or the batch's error code.  Output
  * pointers may be NULL. */

@@ -123,3 +123,53 @@ def test_server_rejects_bad_requests(gox):
         with pytest.raises(Exception):
             srv.set_lanes(bad)
     srv.close()
+
+
+def test_submit_many_equals_single_submits(gox):
+    """Requests queued in one call (gox_server_submit_many) report what the
+    same requests queued one by one report, bit for bit; a batch with an
+    unknown topology id queues nothing."""
+    grids = _grids()
+    topos = [gox.Topology(yb, g.bus_type) for g, yb in grids]
+    rng = np.random.default_rng(41)
+    reqs = []
+    for i in range(40):
+        t = int(rng.integers(0, 3))
+        g, yb = grids[t]
+        p, q = G.load_scenarios(g, 1, 0.1, 2000 + i)
+        out = None
+        if i % 5 == 0:
+            br = rng.choice(np.flatnonzero(~G.bridges(g)), size=1)
+            sl, dr, di = G.outage_deltas(g, yb, br)
+            out = (np.ascontiguousarray(sl[0], np.int32), np.ascontiguousarray(dr[0]),
+                   np.ascontiguousarray(di[0]))
+        reqs.append((t, np.ascontiguousarray(p[0]), np.ascontiguousarray(q[0]), out))
+    reports = {}
+    for mode in ("single", "many"):
+        srv = gox.Server(max_batch=16)
+        ids = [srv.add_topology(tp) for tp in topos]
+        if mode == "single":
+            tk = [srv.submit(ids[t], p, q, grids[t][0].vm, grids[t][0].va, outage=o)
+                  for t, p, q, o in reqs]
+        else:
+            vms = [np.ascontiguousarray(g.vm) for g, _ in grids]
+            vas = [np.ascontiguousarray(g.va) for g, _ in grids]
+            addr = lambda a: a.ctypes.data
+            with pytest.raises(ValueError):
+                srv.submit_many([0, 7], [addr(reqs[0][1])] * 2, [addr(reqs[0][2])] * 2,
+                                [addr(vms[0])] * 2, [addr(vas[0])] * 2)
+            assert srv.stats()["queued"] == 0
+            tk = srv.submit_many(
+                [ids[t] for t, _, _, _ in reqs], [addr(p) for _, p, _, _ in reqs],
+                [addr(q) for _, _, q, _ in reqs], [addr(vms[t]) for t, _, _, _ in reqs],
+                [addr(vas[t]) for t, _, _, _ in reqs],
+                out_ptrs=[[addr(o[c]) if o is not None else 0 for _, _, _, o in reqs]
+                          for c in range(3)])
+        reports[mode] = [srv.wait(int(k), grids[reqs[i][0]][0].n_bus) for i, k in enumerate(tk)]
+        srv.close()
+    for a, b in zip(reports["single"], reports["many"]):
+        np.testing.assert_array_equal(a["vm"], b["vm"])
+        np.testing.assert_array_equal(a["va"], b["va"])
+        assert (a["iterations"], a["status"], a["max_mismatch"]) == \
+            (b["iterations"], b["status"], b["max_mismatch"])
+    assert any(b["status"] == gox.GOX_CONVERGED for b in reports["many"])
