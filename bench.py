@@ -780,7 +780,7 @@ def main():
                     help="profiling: the default plan's wide split (narrowest wide level)")
     ap.add_argument("--host-loop", action="store_true",
                     help="profiling: host-driven Newton loop on one host thread (no graph, no "
-                         "split halves)")
+                         "split parts)")
     args = ap.parse_args()
     WORKLOAD["grid"] = args.grid
     WORKLOAD["scenarios"] = args.scenarios

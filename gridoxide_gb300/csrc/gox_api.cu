@@ -2572,7 +2572,7 @@ __global__ void k_delay(unsigned long long ns) {
 }
 
 // The offset: about two thirds of one part's mismatch and fill, estimated per
-// bus and scenario (measured on the 2,000-bus grid: 0.29 ms for halves of
+// bus and scenario (measured on the 2,000-bus grid: 0.29 ms for parts of
 // 2,048 scenarios), at most 5 ms
 static unsigned long long split_offset_ns(int n_bus, int scenarios) {
   const double ns = 0.07 * (double)n_bus * (double)scenarios;
@@ -2592,7 +2592,7 @@ static int batch_split(gox_topo* t, int B, const double* p_spec, const double* q
                        const double* h_p, const double* h_q, const double* h_vm, const double* h_va,
                        const int32_t* h_oslot, const double* h_odre, const double* h_odim) {
   // (FP64 solves stay whole: their refactor is bound by the FP64 pipe, which
-  // the halves would share; measured slower split)
+  // the parts would share; measured slower split)
   // (and not before the topology's plan for this precision is tuned: the
   // tuning installs streams the twin shares)
   if (t->split_parts < 2 || !t->factored || t->guess_mode != 0 || t->timing.on ||

@@ -8,7 +8,7 @@
   within 1e-7 pu of it (angles: 1e-7 of the grid's angle spread).
 * The 2,000-bus x 4,096-scenario batch through the paths the benchmark
   times: the Newton loop as a captured CUDA graph (second solve of a
-  configuration) and, for the mixed path, two concurrent halves.  FP64
+  configuration) and, for the mixed path, concurrent parts (two, four, five).  FP64
   matches the oracle as above; mixed converges, stays within 1e-7 of the
   oracle, and equals its first (unsplit, host-driven) solve bit for bit.
 """
@@ -80,7 +80,7 @@ def test_case2000_full_batch_graph_and_split_match_oracle(gox, oracle_mod):
         assert np.max(np.abs(r.voltage_mag - ref["vm"])) < TOL_V
         assert np.max(np.abs(r.voltage_ang - ref["va"])) < TOL_V
     # mixed: with the pivot order fixed, 4,096 scenarios run as two
-    # concurrent halves; the first mixed call captures its graphs, the next
+    # concurrent parts; the first mixed call captures its graphs, the next
     # ones run them
     rm = [solve(gox.GOX_PRECISION_MIXED) for _ in range(3)]
     # four staggered parts of 1,024 scenarios, then five uneven ones

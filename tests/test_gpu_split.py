@@ -1,7 +1,8 @@
 """GPU: split solves (gox_topo_set_split).  A batch of 4,096+ scenarios solved
-as two concurrent halves (the second by a twin instance of the topology on
-its own stream) gives the unsplit results bit for bit: mixed precision, with
-outages, through the host and the device entries."""
+as concurrent parts of whole groups (part k by the k-th clone of the topology
+on its own stream) gives the unsplit results bit for bit: mixed precision,
+with outages, 2, 3 (uneven parts) and 8 parts, through the host and the
+device entries."""
 import numpy as np
 import pytest
 
@@ -11,11 +12,12 @@ from helpers import grid_from_fixture, load_fixture, ybus_from_fixture
 pytestmark = pytest.mark.gpu
 
 
-@pytest.mark.parametrize("prec,outage", [("mixed", False), ("mixed", True)])
-def test_split_equals_unsplit(gox, prec, outage):
+@pytest.mark.parametrize("prec,outage,parts", [("mixed", False, 2), ("mixed", True, 2),
+                                               ("mixed", True, 3), ("mixed", False, 8)])
+def test_split_equals_unsplit(gox, prec, outage, parts):
     fx = load_fixture("case118")
     g, yb = grid_from_fixture(fx), ybus_from_fixture(fx)
-    B = 4096 + 96  # halves of 2,112 and 2,080 scenarios
+    B = 4096 + 96  # 131 groups, the last one of 32: two parts of 2,112 and 2,080 scenarios
     p, q = G.load_scenarios(g, B, 0.15, 51)
     out = None
     if outage:
@@ -26,7 +28,7 @@ def test_split_equals_unsplit(gox, prec, outage):
     topo.set_split(1)
     ref = topo.solve(p, q, g.vm, g.va, precision=precision, outage=out, history=True)
     ref = topo.solve(p, q, g.vm, g.va, precision=precision, outage=out, history=True)
-    topo.set_split(2)
+    topo.set_split(parts)
     for _ in range(2):
         res = topo.solve(p, q, g.vm, g.va, precision=precision, outage=out, history=True)
         for a, b in ((res.voltage_mag, ref.voltage_mag), (res.voltage_ang, ref.voltage_ang),
