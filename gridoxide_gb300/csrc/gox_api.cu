@@ -730,10 +730,10 @@ struct gox_topo {
     std::vector<std::array<double, 7>> table;  // timed candidates: warps, chunk words, ring rows, ms,
                                                // sync, wide levels, wide phases
   } tune[2];
-  // split solves: a second instance of this topology (same pivot order, own
-  // device buffers and stream) that solves the second half of a large batch
-  // concurrently with the first
-  int split_parts = 2;
+  // split solves: the parts a large batch is solved in (0: by batch size),
+  // and the next instance of this topology (same pivot order, own device
+  // buffers and stream) that solves the next part concurrently
+  int split_parts = 0;
   std::unique_ptr<gox_topo> twin;
   cudaStream_t own_stream = nullptr;
   bool graphs_off = false;   // a capture failed: the host-driven loop only
@@ -2595,7 +2595,11 @@ static int batch_split(gox_topo* t, int B, const double* p_spec, const double* q
   // the parts would share; measured slower split)
   // (and not before the topology's plan for this precision is tuned: the
   // tuning installs streams the twin shares)
-  if (t->split_parts < 2 || !t->factored || t->guess_mode != 0 || t->timing.on ||
+  // by batch size: two parts, four from 8,192 scenarios (measured on the
+  // 10,000-bus N-1 batch of 8,192: 4 parts 117-121 ms, 2 parts 122-124 ms
+  // with host buffers; the 2,000-bus batch of 4,096 alike for 2, 4 and 8)
+  const int want = t->split_parts > 0 ? t->split_parts : (B >= 8192 ? 4 : 2);
+  if (want < 2 || !t->factored || t->guess_mode != 0 || t->timing.on ||
       B < kSplitMinScenarios || precision != GOX_PRECISION_MIXED || !t->tune[0].done)
     return batch_any(t, B, p_spec, q_spec, vm0, va0, v_stride, o_slot, o_dre, o_dim, tol, max_iter,
                      precision, vm_out, va_out, iters, status, max_mis, hist, st, h_p, h_q, h_vm,
@@ -2604,7 +2608,7 @@ static int batch_split(gox_topo* t, int B, const double* p_spec, const double* q
   // batch would have), part k solved by the k-th twin on its own stream from
   // its own host thread, started k offsets later
   const int n = t->n_bus;
-  const int parts = std::min(t->split_parts, (B + 31) / 32);
+  const int parts = std::min(want, (B + 31) / 32);
   const int G = (B + 31) / 32;
   std::vector<int> first(parts + 1, 0);
   for (int k = 0; k < parts; k++) first[k + 1] = first[k] + (G / parts + (k < G % parts ? 1 : 0)) * 32;
@@ -3668,7 +3672,7 @@ int gox_topo_set_zip(gox_topo* t, const double* zi_re, const double* zi_im, cons
 }
 
 int gox_topo_set_split(gox_topo* t, int32_t parts) {
-  if (!t || parts < 1 || parts > 8) return GOX_E_INVALID;
+  if (!t || parts < 0 || parts > 8) return GOX_E_INVALID;
   t->split_parts = parts;
   return GOX_OK;
 }

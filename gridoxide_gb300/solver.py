@@ -551,7 +551,7 @@ class Topology:
         check(L.gox_topo_set_zip(self._h, *[_p(x, _lib.f64p) for x in a]), "gox_topo_set_zip")
 
     def set_split(self, parts: int) -> None:
-        """Solve large batches as 1 to 8 concurrent parts (gox_topo_set_split)."""
+        """Solve large batches as 1 to 8 concurrent parts, 0 by batch size (gox_topo_set_split)."""
         check(_lib.load().gox_topo_set_split(self._h, int(parts)), "gox_topo_set_split")
 
     def set_graph(self, on: bool) -> None:

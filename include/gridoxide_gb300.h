@@ -456,9 +456,10 @@ int gox_topo_set_zip(gox_topo *t, const double *zi_re, const double *zi_im, cons
  * topology on the host-driven loop. */
 int gox_topo_set_graph(gox_topo *t, int32_t on);
 
-/* Split solves (parts 1..8, default 2): once the pivot order is fixed, a
- * mixed-precision batch of 4,096+ scenarios with the given start is solved
- * as `parts` parts of whole groups of 32 scenarios at the same time, part k
+/* Split solves (parts 1..8, or 0, the default: two parts, four from 8,192
+ * scenarios): once the pivot order is fixed, a mixed-precision batch of
+ * 4,096+ scenarios with the given start is solved as `parts` parts of whole
+ * groups of 32 scenarios at the same time, part k
  * by the k-th instance of the topology (a chain of clones) on its own stream
  * from its own host thread, started k fractions of an iteration later so
  * that one part's mismatch and fill overlap the others' refactors.  Every

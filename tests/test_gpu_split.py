@@ -28,14 +28,17 @@ def test_split_equals_unsplit(gox, prec, outage, parts):
     topo.set_split(1)
     ref = topo.solve(p, q, g.vm, g.va, precision=precision, outage=out, history=True)
     ref = topo.solve(p, q, g.vm, g.va, precision=precision, outage=out, history=True)
-    topo.set_split(parts)
-    for _ in range(2):
+    for k in (parts, 0):  # the given parts, then parts by batch size (the default)
+        topo.set_split(k)
         res = topo.solve(p, q, g.vm, g.va, precision=precision, outage=out, history=True)
         for a, b in ((res.voltage_mag, ref.voltage_mag), (res.voltage_ang, ref.voltage_ang),
                      (res.iterations, ref.iterations), (res.status, ref.status),
                      (res.max_mismatch, ref.max_mismatch), (res.history, ref.history)):
             np.testing.assert_array_equal(a, b)
     assert np.all(ref.status == gox.GOX_CONVERGED)
+    for bad in (-1, 9):
+        with pytest.raises(gox.GoxError):
+            topo.set_split(bad)
 
 
 def test_split_device_entry(gox):
