@@ -20,7 +20,7 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 LIB = os.path.join(HERE, "liboracle.so")
 REF_LIB = os.path.join(HERE, "_ref", "libklu_ref.so")
 # The reference checkout the recipe compiles from (its vendored SuiteSparse):
-# $GRIDOXIDE_REFERENCE, else the read-only mount of this build environment.
+# $GRIDOXIDE_REFERENCE, else its default checkout location.
 REF_ROOT = os.environ.get("GRIDOXIDE_REFERENCE", "/root/reference")
 REF_SRC = os.path.join(REF_ROOT, "vendor", "suitesparse")
 
