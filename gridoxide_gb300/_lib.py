@@ -103,6 +103,8 @@ SIGNATURES = {
     "gox_set_timing": (C.c_int, [vp, C.c_int32]),
     "gox_last_timing": (C.c_int, [vp, f64p]),
     "gox_last_launches": (C.c_int64, [vp]),
+    "gox_topo_repacks": (C.c_int64, [vp]),
+    "gox_set_repack": (C.c_int, [C.c_int32]),
     "gox_set_pivot_tolerance": (C.c_int, [vp, C.c_double]),
     "gox_topo_set_initial_guess": (C.c_int, [vp, C.c_int32]),
     "gox_topo_set_graph": (C.c_int, [vp, C.c_int32]),

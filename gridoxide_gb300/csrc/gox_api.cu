@@ -5,6 +5,7 @@
 
 #include <algorithm>
 #include <array>
+#include <type_traits>
 #include <atomic>
 #include <cmath>
 #include <functional>
@@ -129,6 +130,63 @@ __global__ void k_gather_rows(const double* __restrict__ src, int B, int N, int 
     int g = s >> 5, l = s & 31;
     dst[t] = src[((size_t)g * N + i) * 32 + l];
   }
+}
+
+// Re-packing: the running scenarios of a batch (from[k], k < R) moved into
+// the first lanes of a smaller batch of Gp groups, and back.  Slots from R
+// up to whole groups copy scenario from[R - 1] and are marked unused.
+// Interleaved arrays [G][rows][32] of 4- or 8-byte words:
+template <typename W>
+__global__ void k_pack_rows(const W* __restrict__ src, W* __restrict__ dst, int rows,
+                            const int32_t* __restrict__ from, int R, int Gp) {
+  const size_t total = (size_t)Gp * rows * 32;
+  for (size_t t = blockIdx.x * (size_t)blockDim.x + threadIdx.x; t < total;
+       t += (size_t)gridDim.x * blockDim.x) {
+    const size_t gr = t >> 5;  // packed group * rows + row
+    const int k = (int)(gr / rows) * 32 + (int)(t & 31);
+    const int r = (int)(gr % rows);
+    const int s = from[min(k, R - 1)];
+    dst[t] = src[((size_t)(s >> 5) * rows + r) * 32 + (s & 31)];
+  }
+}
+template <typename W>
+__global__ void k_unpack_rows(const W* __restrict__ src, W* __restrict__ dst, int rows,
+                              const int32_t* __restrict__ from, int R) {
+  const size_t total = (size_t)R * rows;
+  for (size_t t = blockIdx.x * (size_t)blockDim.x + threadIdx.x; t < total;
+       t += (size_t)gridDim.x * blockDim.x) {
+    const int r = (int)(t / R), k = (int)(t % R), s = from[k];
+    dst[((size_t)(s >> 5) * rows + r) * 32 + (s & 31)] =
+        src[((size_t)(k >> 5) * rows + r) * 32 + (k & 31)];
+  }
+}
+// Per-scenario arrays of `width` words (scenario s at s * width):
+template <typename W>
+__global__ void k_pack_flat(const W* __restrict__ src, W* __restrict__ dst, int width,
+                            const int32_t* __restrict__ from, int R, int K) {
+  const size_t total = (size_t)K * width;
+  for (size_t t = blockIdx.x * (size_t)blockDim.x + threadIdx.x; t < total;
+       t += (size_t)gridDim.x * blockDim.x) {
+    const int k = (int)(t / width), c = (int)(t % width);
+    dst[t] = src[(size_t)from[min(k, R - 1)] * width + c];
+  }
+}
+template <typename W>
+__global__ void k_unpack_flat(const W* __restrict__ src, W* __restrict__ dst, int width,
+                              const int32_t* __restrict__ from, int R) {
+  const size_t total = (size_t)R * width;
+  for (size_t t = blockIdx.x * (size_t)blockDim.x + threadIdx.x; t < total;
+       t += (size_t)gridDim.x * blockDim.x) {
+    const int k = (int)(t / width), c = (int)(t % width);
+    dst[(size_t)from[k] * width + c] = src[t];
+  }
+}
+// The packed batch's padding slots do not run; every packed group runs.
+__global__ void k_pack_mark(int32_t* __restrict__ status, int32_t* __restrict__ gact, int R,
+                            int Gp) {
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t < Gp * 32 && t >= R) status[t] = ST_UNUSED;
+  if (t < Gp) gact[t] = 1;
 }
 
 // Uniformly scaled injections: p[s][i] = p_base[i] * scale[s] (and q), the
@@ -658,6 +716,9 @@ struct LoopGraph {
   std::vector<unsigned char> key;
   cudaGraphExec_t exec = nullptr;
   int uses = 0;
+  // a configuration whose host-driven solve re-packed its running scenarios
+  // stays on the host-driven loop, where re-packing can run
+  bool packs = false;
 };
 
 struct gox_topo {
@@ -673,6 +734,11 @@ struct gox_topo {
   Stream s32, s64;
   DevSchedule dsched;
   DevBatch batch;
+  // re-packing: the smaller batch the running scenarios move to, and their
+  // scenario indices in the batch
+  DevBatch pack;
+  DevMem pack_from;
+  int64_t repacks = 0;
   Timing timing;
   int64_t launches = 0;
   int device = 0;
@@ -993,6 +1059,7 @@ static bool run_loop_graph(gox_topo* t, const BatchDev& D, int max_iter, bool ou
     remember_loop(t, key);
     return false;
   }
+  if (lg->packs) return false;
   if (!lg->exec) {
     try {
       lg->exec = build_loop_graph<T>(t, D, max_iter, outage, st);
@@ -1287,6 +1354,108 @@ static void autotune(gox_topo* t, const BatchDev& D, cudaStream_t st) {
   tune_cache_store(key, bestp);
 }
 
+// Re-packing of the running scenarios (host-driven loop).  After an
+// iteration's decision, when the scenarios still running fit in at most half
+// of the groups still active, they move into the first lanes of a smaller
+// batch (t->pack) and the remaining iterations run there; at the end their
+// results go back to their own lanes.  Every kernel's arithmetic is per
+// lane, so a scenario's result is the same in either batch, bit for bit.
+// Fewer groups mean fewer mismatch and fill blocks and, when the batch spans
+// more than one wave of refactor CTAs, fewer waves.
+static constexpr int kPackMinGroups = 16;
+static std::atomic<int> g_repack{1};  // gox_set_repack
+
+template <typename T>
+static bool repack(gox_topo* t, const BatchDev& D, bool outage, int active_groups,
+                   cudaStream_t st, BatchDev& P, int& R, int64_t& launches) {
+  const int G = D.G;
+  std::vector<int32_t> status((size_t)G * 32);
+  GOX_CK(cudaMemcpyAsync(status.data(), D.status, status.size() * 4, cudaMemcpyDeviceToHost, st));
+  GOX_CK(cudaStreamSynchronize(st));
+  std::vector<int32_t> from;
+  for (int s = 0; s < G * 32; s++)
+    if (status[s] == ST_RUNNING) from.push_back(s);
+  R = (int)from.size();
+  const int Gp = (R + 31) / 32;
+  if (R == 0 || 2 * Gp > active_groups) return false;
+  const SchedDev& S = t->dsched.d;
+  const int prec = sizeof(T) == 4 ? GOX_PRECISION_MIXED : GOX_PRECISION_FP64;
+  const bool hist = D.hist != nullptr;
+  DevBatch& PB = t->pack;
+  PB.ensure(S, Gp, prec, D.max_iter, hist);
+  P = PB.view(hist, outage, D.tol, 0.0);
+  P.piv_tol = D.piv_tol;
+  P.err = D.err;  // one error flag for the solve
+  upload(t->pack_from, from);
+  const int32_t* fr = t->pack_from.as<int32_t>();
+  using U8 = unsigned long long;
+  using W = typename std::conditional<sizeof(T) == 4, uint32_t, U8>::type;
+  const int n = S.n_bus, nu = S.n_u, K = Gp * 32;
+  auto rows8 = [&](const double* a, double* b, int rows) {
+    k_pack_rows<U8><<<grid1d((size_t)K * rows), 256, 0, st>>>((const U8*)a, (U8*)b, rows, fr, R, Gp);
+    launches++;
+  };
+  auto rowsT = [&](const void* a, void* b, int rows) {
+    k_pack_rows<W><<<grid1d((size_t)K * rows), 256, 0, st>>>((const W*)a, (W*)b, rows, fr, R, Gp);
+    launches++;
+  };
+  auto flat4 = [&](const void* a, void* b, int width) {
+    k_pack_flat<uint32_t><<<grid1d((size_t)K * width), 256, 0, st>>>((const uint32_t*)a,
+                                                                       (uint32_t*)b, width, fr, R, K);
+    launches++;
+  };
+  auto flat8 = [&](const void* a, void* b, int width) {
+    k_pack_flat<U8><<<grid1d((size_t)K * width), 256, 0, st>>>((const U8*)a, (U8*)b, width, fr, R, K);
+    launches++;
+  };
+  // the state the rest of this iteration (fill, refactor) and the next ones read
+  rows8(D.vm, P.vm, n); rows8(D.va, P.va, n); rows8(D.cth, P.cth, n); rows8(D.sth, P.sth, n);
+  rows8(D.psp, P.psp, n); rows8(D.qsp, P.qsp, n);
+  rowsT(D.eT, P.eT, n); rowsT(D.fT, P.fT, n); rowsT(D.ivT, P.ivT, n);
+  rowsT(D.pT, P.pT, n); rowsT(D.qT, P.qT, n); rowsT(D.rhs, P.rhs, nu);
+  flat4(D.status, P.status, 1); flat4(D.iters, P.iters, 1); flat4(D.sing, P.sing, 1);
+  flat4(D.piv_flag, P.piv_flag, 1); flat8(D.maxmis, P.maxmis, 1);
+  if (hist) flat8(D.hist, P.hist, D.max_iter);
+  if (outage) {
+    flat4(D.o_slot, PB.o_slot.p, 4); flat4(D.o_bf, PB.o_bf.p, 1); flat4(D.o_bt, PB.o_bt.p, 1);
+    flat8(D.o_dre, PB.o_dre.p, 4); flat8(D.o_dim, PB.o_dim.p, 4);
+  }
+  GOX_CK(cudaMemsetAsync(P.maxacc, 0, (size_t)K * 8, st));
+  k_pack_mark<<<(K + 255) / 256, 256, 0, st>>>(P.status, P.gact, R, Gp);
+  launches++;
+  GOX_CK(cudaGetLastError());
+  t->repacks++;
+  return true;
+}
+
+// The packed scenarios' results back to their lanes of the batch.
+template <typename T>
+static void unpack(gox_topo* t, const BatchDev& P, const BatchDev& D, int R, cudaStream_t st,
+                   int64_t& launches) {
+  using U8 = unsigned long long;
+  const int n = t->dsched.d.n_bus;
+  const int32_t* fr = t->pack_from.as<int32_t>();
+  for (auto pr : {std::make_pair(P.vm, D.vm), std::make_pair(P.va, D.va)}) {
+    k_unpack_rows<U8><<<grid1d((size_t)R * n), 256, 0, st>>>((const U8*)pr.first, (U8*)pr.second,
+                                                             n, fr, R);
+    launches++;
+  }
+  for (auto pr : {std::make_pair(P.status, D.status), std::make_pair(P.iters, D.iters),
+                  std::make_pair(P.sing, D.sing), std::make_pair(P.piv_flag, D.piv_flag)}) {
+    k_unpack_flat<uint32_t><<<grid1d((size_t)R), 256, 0, st>>>((const uint32_t*)pr.first,
+                                                                (uint32_t*)pr.second, 1, fr, R);
+    launches++;
+  }
+  k_unpack_flat<U8><<<grid1d((size_t)R), 256, 0, st>>>((const U8*)P.maxmis, (U8*)D.maxmis, 1, fr, R);
+  launches++;
+  if (D.hist) {
+    k_unpack_flat<U8><<<grid1d((size_t)R * D.max_iter), 256, 0, st>>>(
+        (const U8*)P.hist, (U8*)D.hist, D.max_iter, fr, R);
+    launches++;
+  }
+  GOX_CK(cudaGetLastError());
+}
+
 template <typename T>
 static void run_iterations(gox_topo* t, BatchDev D, int max_iter, bool outage, cudaStream_t st,
                            int32_t* h_nactive) {
@@ -1318,6 +1487,9 @@ static void run_iterations(gox_topo* t, BatchDev D, int max_iter, bool outage, c
   int it = 0;
   bool tuned_now = false;
   std::vector<int> full;  // iterations that ran K2-K4
+  const BatchDev D0 = D;   // the batch (D becomes the packed one after a re-pack)
+  bool packed = false;
+  int R = 0;
   rec();
   for (it = 0; it < max_iter; it++) {
     GOX_CK(cudaMemsetAsync(D.nactive, 0, sizeof(int32_t), st));
@@ -1327,6 +1499,13 @@ static void run_iterations(gox_topo* t, BatchDev D, int max_iter, bool outage, c
     GOX_CK(cudaMemcpyAsync(h_nactive, D.nactive, sizeof(int32_t), cudaMemcpyDeviceToHost, st));
     GOX_CK(cudaStreamSynchronize(st));
     if (*h_nactive == 0) break;
+    if (!packed && !pivoting && it > 0 && *h_nactive >= kPackMinGroups && g_repack.load()) {
+      BatchDev P{};
+      if (repack<T>(t, D, outage, *h_nactive, st, P, R, t->launches)) {
+        D = P;
+        packed = true;
+      }
+    }
     Iter<T>::fill(S, D, outage, st);
     if (!pivoting && !t->tune[sizeof(T) == 4 ? 0 : 1].done) {
       autotune<T>(t, D, st);
@@ -1347,13 +1526,21 @@ static void run_iterations(gox_topo* t, BatchDev D, int max_iter, bool outage, c
     GOX_CK(cudaGetLastError());
   }
   if (it == max_iter) t->launches += Iter<T>::mismatch(S, D, max_iter, 1, outage, st);
+  if (packed) {
+    unpack<T>(t, D, D0, R, st, t->launches);
+    // this configuration stays on the host-driven loop
+    const std::vector<unsigned char> key = loop_key<T>(t, D0, max_iter, outage);
+    remember_loop(t, key);
+    for (auto& x : t->loop_graphs)
+      if (x.key == key) x.packs = true;
+  }
   rec();
   GOX_CK(cudaGetLastError());
   // the plan chosen during this solve changed the loop's key: remember the
   // new configuration, so that the next solve runs it as a graph
   if (tuned_now && !timing && !pivoting && !t->graphs_off && t->graphs_wanted &&
-      D.G >= kGraphMinGroups)
-    remember_loop(t, loop_key<T>(t, D, max_iter, outage));
+      D0.G >= kGraphMinGroups)
+    remember_loop(t, loop_key<T>(t, D0, max_iter, outage));
   if (timing) {
     GOX_CK(cudaEventSynchronize(ev.back()));
     auto el = [&](size_t a, size_t b) {
@@ -3639,6 +3826,18 @@ int gox_last_timing(const gox_topo* t, double* out) {
 
 int64_t gox_last_launches(const gox_topo* t) { return t ? t->launches : -1; }
 
+int gox_set_repack(int32_t on) {
+  g_repack.store(on ? 1 : 0);
+  return GOX_OK;
+}
+
+int64_t gox_topo_repacks(const gox_topo* t) {
+  if (!t) return -1;
+  int64_t r = t->repacks;
+  for (const gox_topo* tw = t->twin.get(); tw; tw = tw->twin.get()) r += tw->repacks;
+  return r;
+}
+
 int gox_set_pivot_tolerance(gox_topo* t, double tol) {
   if (!t || !(tol >= 0.0) || !std::isfinite(tol)) return GOX_E_INVALID;
   t->piv_tol = tol;
@@ -4055,7 +4254,8 @@ struct gox_server {
   // staging buffers, its split twin's, the linear guess system's and the
   // FP64 re-solve staging
   static int64_t held_bytes(gox_topo* t) {
-    int64_t b = (int64_t)(t->batch.bytes() + t->io.bytes());
+    int64_t b = (int64_t)(t->batch.bytes() + t->io.bytes() + t->pack.bytes() +
+                          t->pack_from.bytes);
     for (gox_topo* tw = t->twin.get(); tw; tw = tw->twin.get())
       b += (int64_t)(tw->batch.bytes() + tw->io.bytes());
     for (const gox::DevMem* m : {&t->guess.lu, &t->guess.off, &t->guess.rhs, &t->guess.sol,
@@ -4069,6 +4269,8 @@ struct gox_server {
   static void release_buffers(gox_topo* t) {
     t->batch.release();
     t->io.release();
+    t->pack.release();
+    t->pack_from.release();
     for (gox_topo* tw = t->twin.get(); tw; tw = tw->twin.get()) {
       tw->batch.release();
       tw->io.release();

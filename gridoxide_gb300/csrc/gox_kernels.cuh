@@ -175,15 +175,17 @@ __device__ __forceinline__ void update_body(const SchedDev& S, const BatchDev& D
   // from sincos; after a small step (|d| < 1/32) by rotating the previous
   // pair by d, with cos d and sin d from their Taylor series (the first
   // omitted terms are below 1e-19 there; the rotation adds about one
-  // rounding per iteration).  When every step of the warp is below 2^-10
-  // (the later iterations) two terms of each series suffice (the first
-  // omitted ones are below 2e-21).
+  // rounding per iteration).  After a step below 2^-10 (the later
+  // iterations) two terms of each series suffice (the first omitted ones are
+  // below 2e-21).  The choice is each lane's own, so a scenario's rounding
+  // does not depend on the other scenarios of its group (re-packing moves
+  // scenarios between groups).
   // (the FP32 path compares the step as solved: an FP32 compare)
   double sn, cs;
   const float ad = sizeof(T) == 4 ? fabsf(step) : 0.0f;
   const bool small = it > 0 && (sizeof(T) == 4 ? ad < 0.03125f : fabs(dth) < 0.03125);
   const bool tiny = it > 0 && (sizeof(T) == 4 ? ad < 0.0009765625f : fabs(dth) < 0.0009765625);
-  if (__all_sync(0xffffffffu, tiny)) {
+  if (tiny) {
     const double d2 = dth * dth;
     const double cd = 1.0 + d2 * (-1.0 / 2 + d2 * (1.0 / 24));
     const double sd = dth * (1.0 + d2 * (-1.0 / 6 + d2 * (1.0 / 120)));

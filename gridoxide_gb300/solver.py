@@ -225,6 +225,12 @@ def multi_solve(jobs, tol=1e-8, max_iter=20, precision=GOX_PRECISION_MIXED,
     return outs
 
 
+def set_repack(on: bool) -> None:
+    """Re-packing of running scenarios into fewer groups in the host-driven
+    Newton loop (default on; gox_set_repack); same results bit for bit."""
+    check(_lib.load().gox_set_repack(1 if on else 0), "gox_set_repack")
+
+
 def set_refactor_wide(min_width: int) -> None:
     """The wide kernels in the default refactor plan of topologies analysed
     from now on: leading refactor levels / trailing backward phases with at
@@ -526,6 +532,10 @@ class Topology:
 
     def last_launches(self) -> int:
         return int(_lib.load().gox_last_launches(self._h))
+
+    def repacks(self) -> int:
+        """Re-packs of running scenarios into fewer groups so far (gox_topo_repacks)."""
+        return int(_lib.load().gox_topo_repacks(self._h))
 
     def set_pivot_tolerance(self, tol: float) -> None:
         """Mixed path: scenarios whose FP32 refactor meets |u_kk| < tol *

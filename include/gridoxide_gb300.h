@@ -423,6 +423,16 @@ int gox_last_timing(const gox_topo *t, double *out);
 
 /* Kernel launches issued by the last gox_batch_solve* call. */
 int64_t gox_last_launches(const gox_topo *t);
+/* Re-packs so far by this topology's solves (its split parts' included):
+ * in the host-driven Newton loop, once the scenarios still running fit in at
+ * most half of the groups still active (16 or more), they move into the
+ * first lanes of a smaller batch for the remaining iterations and their
+ * results back at the end -- the same results bit for bit, fewer groups for
+ * the mismatch, fill and refactor launches.  A configuration whose solve
+ * re-packed stays on the host-driven loop (no captured graph). */
+int64_t gox_topo_repacks(const gox_topo *t);
+/* Re-packing on (1, the default) or off (0), process-wide. */
+int gox_set_repack(int32_t on);
 
 /* Start point of the batched solves.  GOX_GUESS_GIVEN (default): the
  * vm0/va0 passed to the call.  GOX_GUESS_LINEAR: the reference BatchSolver's
