@@ -258,6 +258,10 @@ def serve(gox, rates, seconds: float) -> dict:
     from 32 seeded samples of the grid's distribution (the per-request host
     copies are the grid's size whatever the sample)."""
     from gridoxide_gb300 import grids as G
+    import gc
+    # the earlier legs' pinned host buffers are freed now, not by a later
+    # collection inside a window (freeing pinned memory synchronizes the GPU)
+    gc.collect()
     spec = G.many_topologies(count=16, n_min=100, n_max=50000, seed=5)
     grids, topos, cand, v0 = [], [], [], []
     for (n, gs, _b, _ss) in spec:
