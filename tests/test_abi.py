@@ -88,3 +88,25 @@ def test_batch_solver_validation(gox):
     assert bs.solve(buses, yb, [], 1e-8, 20) == []
     sc = gox.uniform_load_scaling(g.p_spec, g.q_spec, 1.1)
     assert all(ov.p_spec == pytest.approx(g.p_spec[ov.bus] * 1.1) for ov in sc.bus_overrides)
+
+
+def test_loop_settings_validate_without_gpu(gox):
+    """Split parts (0 = by batch size, 1..8), re-packing and the other
+    process-wide loop and plan switches take their documented values and
+    reject the rest, without a GPU."""
+    from gridoxide_gb300 import solver as S
+    g = G.config_grid("case118")
+    topo = gox.Topology(G.build_ybus(g), g.bus_type)
+    for k in (0, 1, 2, 8):
+        topo.set_split(k)
+    for bad in (-1, 9):
+        with pytest.raises(gox.GoxError):
+            topo.set_split(bad)
+    L = _lib.load()
+    assert L.gox_topo_repacks(None) == -1
+    assert topo.repacks() == 0
+    for on in (False, True):  # True, the default, last
+        S.set_repack(on)
+    assert L.gox_topo_set_split(None, 2) == _lib.GOX_E_INVALID
+    assert L.gox_server_submit_many(None, 0, None, None, None, None, None, None, None, None,
+                                    None) == _lib.GOX_E_INVALID
