@@ -759,10 +759,11 @@ def factor_host(n: int, rows, cols, vals) -> Optional[dict]:
 
 class Server:
     """Continuous batching of single-scenario requests over registered
-    topologies (gox_server_*): a worker thread in the library batches the
-    queued requests of one topology at a time and solves them on the GPU;
-    ``poll`` returns a request's report (with its latency) once solved.
-    A registered Topology is used by the server's thread only."""
+    topologies (gox_server_*): worker threads in the library batch the
+    queued requests of a topology (one batch per topology at a time, or up
+    to ``set_lanes`` on clones of it) and solve them on the GPU; ``poll``
+    returns a request's report (with its latency) once solved.  A
+    registered Topology is used by the server's threads only."""
 
     def __init__(self, max_batch: int = 1024, precision: int = GOX_PRECISION_MIXED,
                  tol: float = 1e-8, max_iter: int = 20):
